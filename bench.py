@@ -1,0 +1,304 @@
+"""Benchmark of the GB300 LLG step: spin-steps/s of the stochastic Heun step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload: the large plain FP64 thermal run of the benchmark set, i.e. two-site cubic bcc 128^3
+(4,194,304 spins), periodic, shells 8+6+12 with per-bond full 3x3 tensors (isotropic 20/10/-1 meV,
+random symmetric anisotropic part at 1 %, random DMI |D| = 1 meV, J_ji = J_ij^T), uniaxial SIA
+K = 0.01 meV, B = (0, 0, 0.5) T, T = 300 K, alpha = 0.05, dt = 0.1 fs, Philox noise.  Synthetic,
+seeded; spins start uniform-random on the sphere.
+
+One "step" = one Heun step of the whole lattice (predictor + corrector kernel).  `value` times K
+steps with the spins resident in HBM (3 x 100 MB working set > 129 MB L2, so no L2 flush is needed);
+`e2e` times K calls of the public drop-in API `GB300LLG.step(e_host)` with pinned host spins
+(host->device copy, step, device->host copy per call).  Under torchrun each rank runs an
+independent replica (weak scaling, no collective on the data path).
+
+--impl reference times the reference's CPU algorithm (the C restatement of magex's fused numba
+kernels in oracle/, all host threads, its own ziggurat noise) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LLG spin-steps/s FP64 on 1×GB300 (%HBM roofline); batched vs plain; adjoint/fwd time"
+UNIT = "spin-steps/s"
+ALPHA, DT, TEMP, FIELD = 0.05, 1e-4, 300.0, (0.0, 0.0, 0.5)
+
+
+def workload_config(L):
+    return {"workload": f"bcc two-site {L}^3 ({2 * L ** 3:,} spins), 26 neighbours (8+6+12), full 3x3 tensors + DMI, "
+                        f"SIA K=0.01 meV, B=(0,0,0.5) T, T=300 K, alpha=0.05, dt=0.1 fs, Philox noise, Heun",
+            "spins": 2 * L ** 3, "neighbours": 26, "integrator": "heun", "noise": "philox",
+            "l2": "inputs larger than L2 (3 x 24 B x N = 302 MB working set)", "parallelism": "replicas"}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region (200 ms period)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        if self.proc is None:
+            return None
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------ CPU (oracle) timing
+def cpu_oracle_timing(L, min_seconds=10.0, max_steps=40, steps=None, warmup=1):
+    """The reference's CPU algorithm on the same workload: returns (spin-steps/s, steps, threads, seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=L, field=FIELD)
+    ora = oracle.OracleLLG(sc, ALPHA, DT, TEMP, seed=7, noise="ziggurat", csr="stencil")
+    e = sc.init_spins("random", seed=1)
+    for _ in range(warmup):
+        ora.step_inplace(e)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        ora.step_inplace(e)
+        n += 1
+        el = time.perf_counter() - t0
+        if steps is not None:
+            if n >= steps:
+                break
+        elif (el >= min_seconds and n >= 2) or n >= max_steps:
+            break
+    return sc.N * n / el, n, oracle.max_threads(), el
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    v, n, cores, el = cpu_oracle_timing(args.L, steps=args.steps, warmup=args.warmup)
+    sample = (f"{n} Heun steps of the full {args.L}^3 two-site bcc lattice ({2 * args.L ** 3:,} spins), "
+              f"C restatement of magex/fast.py _fused1/_fused2 with its ziggurat noise, OpenMP {cores} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": n,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / n, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(args.L),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------ GPU arm
+def fp64_flops_per_spin_step(z):
+    """Algorithmic FP64 flops of one Heun step per spin (FMA = 2): per stage 9 FMA per neighbour of the
+    full-tensor gather (18 z), on-site gradient 18, field assembly 12, thermal add 6, LLG rhs 27,
+    update + renormalisation 22 (predictor) / 25 (corrector)."""
+    return 2 * 18 * z + 2 * (18 + 12 + 6 + 27) + 22 + 25
+
+
+def read_ncu_traffic():
+    """Per-launch DRAM bytes of the LLG kernels from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            f = line.split()
+            if len(f) >= 3 and f[1] == "bytes_per_launch_per_spin":
+                out[f[0]] = float(f[2])
+    return out
+
+
+def run_gb300(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from magex_gb300 import _lib, build
+    build.build_library()
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    import ctypes as C
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    lib = _lib.load()
+    peak64 = C.c_double()
+    _lib.check(lib.mgx_measure_fp64_peak(C.byref(peak64)), "fp64 peak")
+
+    sc = bcc_two_site(L=args.L, field=FIELD)
+    N = sc.N
+    z = len(sc.bond_src) / sc.ns
+    e0 = sc.init_spins("random", seed=1 + rank)
+    sol = GB300LLG(sc, ALPHA, DT, TEMP, seed=1000 + rank)
+    lat = sol.model.to_lattice(e0)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        sol.stage_lattice(lat, 0)
+        sol.stage_lattice(lat, 1)
+    K = args.steps
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * K + 1)]
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev[0].record(stream)
+        for k in range(K):
+            sol.stage_lattice(lat, 0)
+            ev[2 * k + 1].record(stream)
+            sol.stage_lattice(lat, 1)
+            ev[2 * k + 2].record(stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+    total_ms = ev[0].elapsed_time(ev[2 * K])
+    pred_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(K)]
+    corr_ms = [ev[2 * k + 1].elapsed_time(ev[2 * k + 2]) for k in range(K)]
+    norm_err = float((torch.linalg.vector_norm(lat, dim=0) - 1).abs().max())
+    if not (norm_err < 1e-12):
+        raise RuntimeError(f"spins lost unit norm during the benchmark: {norm_err}")
+
+    # end to end through the public API with pinned host buffers
+    e_host = torch.from_numpy(e0).pin_memory()
+    out_host = torch.empty_like(e_host).pin_memory()
+    sol2 = GB300LLG(sc, ALPHA, DT, TEMP, seed=2000 + rank)
+    sol2.step(e_host, out=out_host)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    cur = e_host
+    for _ in range(K):
+        sol2.step(cur, out=out_host)
+        cur, out_host = out_host, cur
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    t_max = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
+    if ws > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    total_ms, e2e_s = float(t_max[0]), float(t_max[1])
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    value = N * K * ws / (total_ms * 1e-3)
+    pm, cm = statistics.mean(pred_ms), statistics.mean(corr_ms)
+    dominant, dom_ms = ("k_correct", cm) if cm >= pm else ("k_predict", pm)
+    # algorithmic HBM bytes per spin: predictor reads e, writes ep, k1; corrector reads ep, k1, e, writes e
+    bytes_per_spin = {"k_predict": 72.0, "k_correct": 96.0}[dominant]
+    hbm_peak = None
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        hbm_peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    else:
+        hbm_peak, peak_src = 6800.0, "fallback"
+    achieved = bytes_per_spin * N / (dom_ms * 1e-3) / 1e9
+    traffic = read_ncu_traffic().get(dominant)
+    flops_step = fp64_flops_per_spin_step(z)
+    fp64_achieved = flops_step * N * K / (total_ms * 1e-3)
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
+        "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded two-site bcc model, random initial spins)",
+        "config": workload_config(args.L),
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_source": peak_src,
+                     "traffic": None if traffic is None else traffic * N,
+                     "algorithmic_bytes_per_launch": bytes_per_spin * N, "launch_ms": dom_ms},
+        "fp64_roofline": {"achieved": fp64_achieved / 1e12, "peak": peak64.value / 1e12, "unit": "TFLOP/s",
+                          "frac": fp64_achieved / peak64.value, "flops_per_spin_step": flops_step,
+                          "peak_source": "measured live (mgx_measure_fp64_peak, DFMA loop)"},
+        "kernels_ms": {"k_predict": pm, "k_correct": cm},
+        "e2e": {"value": N * K * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
+                "api": "GB300LLG.step(pinned host (N,3) float64) -> pinned host (N,3)"},
+        "gpu_launches": 2 * K,
+        "clocks": clocks,
+    }
+    if ws == 1 and not args.no_cpu_baseline:
+        v, n, cores, el = cpu_oracle_timing(args.L)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{n} Heun steps of the full {args.L}^3 lattice ({N:,} spins), {el:.1f} s, "
+                                          "C restatement of magex's fused numba kernels + ziggurat noise (OpenMP)"}
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--L", type=int, default=128, help="bcc cells per side (default: the 128^3 workload)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,162 @@
+/*
+ * mgx.h -- C ABI of the GB300 (sm_103a) atomistic stochastic LLG step.
+ *
+ * This library replaces the kernel layer behind magex's LLG integrator:
+ *   - the NumPy Heun step         magex/llg.py:216-227 (LLGSolver.step, integrator "heun")
+ *   - its effective field          magex/spinmodel.py:454-473 (exchange_field, gradient, effective_field)
+ *   - the fused CPU kernels        magex/fast.py:336-390 (_fused1 predictor, _fused2 corrector)
+ *   - the numba.cuda kernels       magex/cuda_backend.py:144-218 (_k_pred, _k_corr)
+ *   - the kernel argument tuple    magex/fast.py:669-672 (FastModel.args)
+ *   - the observables of the run   magex/spinmodel.py:475-484,517-519, magex/llg.py:250-252
+ *
+ * Conventions
+ *   - Plain C types only.  Pointers documented "device" point to GPU memory owned by the caller;
+ *     "host" pointers are read during the call only.  A stream is a cudaStream_t passed as void*
+ *     (NULL = legacy default stream).  All device work of a call is enqueued on that stream;
+ *     no call synchronises the device unless it says so.
+ *   - Spins on the device use the lattice layout: component-major, then sublattice, then cell
+ *     (c0, c1, c2 row-major): x[c * N + s * ncell + cell].  mgx_pack_spins / mgx_unpack_spins
+ *     convert from / to magex's (N, 3) row-major array with site = cell * ns + s
+ *     (magex/spinmodel.py:197-204).
+ *   - Units as magex: time ps, field T, energy meV, moments mu_B.
+ *   - Every entry point returns an mgx_status; on failure mgx_last_error() gives a message.
+ *     No C++ exception crosses the ABI.  Objects are not thread-safe; distinct objects are.
+ */
+#ifndef MGX_H
+#define MGX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGX_VERSION 1
+
+#define MGX_MAX_SUBLATTICES 16
+#define MGX_MAX_BONDS 256          /* stencil couplings per unit cell after self-image folding */
+
+typedef int32_t mgx_status;
+enum {
+  MGX_OK = 0,
+  MGX_ERR_INVALID = 1,       /* bad argument (maps to ValueError) */
+  MGX_ERR_UNSUPPORTED = 2,   /* feature outside the kernels (maps to NotImplementedError) */
+  MGX_ERR_CUDA = 3,          /* CUDA runtime error (maps to RuntimeError) */
+  MGX_ERR_NOMEM = 4          /* device allocation failed (maps to MemoryError) */
+};
+
+enum { MGX_INTEGRATOR_HEUN = 0, MGX_INTEGRATOR_DEPONDT = 1 };
+enum { MGX_NOISE_NONE = 0, MGX_NOISE_HOST = 1, MGX_NOISE_PHILOX = 2 };
+
+typedef struct mgx_model mgx_model;
+typedef struct mgx_llg mgx_llg;
+
+/* Supercell of a unit-cell model, described by its per-cell coupling list ("stencil").
+ * Replaces the 3N x 3N CSR matrix of magex/spinmodel.py:240 and the per-site neighbour blocks of
+ * magex/fast.py:587-627: site (cell c, sublattice src) couples to (wrap(c + R), dst) with the
+ * coupling tensor of the bond.  Self-image couplings must already be folded into A_sub. */
+typedef struct mgx_lattice_desc {
+  int32_t ns;                /* sublattices per cell, 1..MGX_MAX_SUBLATTICES */
+  int32_t L[3];              /* supercell size in cells */
+  int32_t pbc[3];            /* 1 = periodic, 0 = open */
+  int32_t nbond;             /* couplings per cell, 0..MGX_MAX_BONDS */
+  const int32_t* bond_src;   /* host [nbond] sublattice of the site receiving the field */
+  const int32_t* bond_dst;   /* host [nbond] sublattice of the neighbour */
+  const int32_t* bond_R;     /* host [nbond*3] cell offset of the neighbour */
+  int32_t width;             /* doubles per coupling: 1 (J), 4 (J, Dx, Dy, Dz) or 9 (row-major 3x3) */
+  const double* bond_table;  /* host [nbond*width] */
+  const double* A_sub;       /* host [ns*9] single-ion tensors (row-major), or NULL for none */
+  const double* mu_sub;      /* host [ns] moments in mu_B */
+  const double* sign_sub;    /* host [ns] order-parameter signs (+-1), or NULL for all +1 */
+  double B[3];               /* external field (T) */
+} mgx_lattice_desc;
+
+/* Optional per-site overrides in magex site order (host arrays of N entries, or NULL).
+ * They mirror SpinSystem.A / mu / pinned after magex.structure edits
+ * (magex/structure.py:160-207).  Pinned sites keep their spin, as magex/fast.py:346-350. */
+typedef struct mgx_site_desc {
+  const double* A_site;      /* host [N*9] or NULL */
+  const double* mu_site;     /* host [N] or NULL */
+  const uint8_t* pinned;     /* host [N] (0/1) or NULL */
+} mgx_site_desc;
+
+/* Integrator parameters; mirror LLGSolver(alpha, dt, precession, integrator) of magex/llg.py:49-50. */
+typedef struct mgx_llg_params {
+  double dt;                 /* time step (ps) */
+  double alpha;              /* Gilbert damping, used when alpha_site == NULL */
+  const double* alpha_site;  /* host [N] per-site damping in magex order, or NULL */
+  int32_t precession;        /* 1: full LLG; 0: damping term only (magex/llg.py:21-28) */
+  int32_t integrator;        /* MGX_INTEGRATOR_HEUN or MGX_INTEGRATOR_DEPONDT */
+  int32_t noise;             /* MGX_NOISE_NONE / _HOST (caller supplies N(0,1) draws) / _PHILOX */
+  uint64_t seed;             /* Philox key (MGX_NOISE_PHILOX) */
+} mgx_llg_params;
+
+/* ---------------------------------------------------------------- library */
+int32_t mgx_version(void);
+/* Copy the last error message of the calling thread into buf (always NUL-terminated). */
+void mgx_last_error(char* buf, size_t len);
+
+/* ---------------------------------------------------------------- model
+ * mgx_model_create replaces FastModel(system) (magex/fast.py:630-657) and _Device (magex/cuda_backend.py:307-335):
+ * it validates the stencil and uploads tables and per-site arrays to the current device. */
+mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* sites, mgx_model** out);
+mgx_status mgx_model_destroy(mgx_model* m);
+mgx_status mgx_model_set_field(mgx_model* m, const double B[3]);   /* SpinSystem.set_field, magex/spinmodel.py:451-452 */
+int64_t mgx_model_nsites(const mgx_model* m);
+
+/* (N,3) magex-order device array <-> lattice-layout device array (3*N doubles each). */
+mgx_status mgx_pack_spins(const mgx_model* m, const double* aos, double* lat, void* stream);
+mgx_status mgx_unpack_spins(const mgx_model* m, const double* lat, double* aos, void* stream);
+
+/* ---------------------------------------------------------------- LLG plan
+ * Replaces LLGSolver's fast-path state (magex/llg.py:89-98) and CudaLLG.__init__ (magex/cuda_backend.py:341-360).
+ * Allocates the predictor scratch (6*N doubles) on the current device. */
+mgx_status mgx_llg_create(const mgx_model* m, const mgx_llg_params* p, mgx_llg** out);
+mgx_status mgx_llg_destroy(mgx_llg* plan);
+/* Thermal-field amplitude sigma_i = sqrt(2 alpha_i k_B T_i / (gamma mu_i mu_B dt)) (magex/llg.py:111):
+ * per sublattice (host [ns]) or per site (host [N] magex order, overrides).  Zero means no noise. */
+mgx_status mgx_llg_set_sigma(mgx_llg* plan, const double* sigma_sub, const double* sigma_site);
+
+/* One stochastic Heun step in place on e (device, lattice layout):
+ *   b = sigma * xi;  k1 = f(e, B(e) + b);  ep = |e + dt k1|^-1 (e + dt k1);
+ *   k2 = f(ep, B(ep) + b);  e <- normalise(e + dt/2 (k1 + k2))
+ * as magex/llg.py:216-227 and magex/fast.py:336-390.  xi is read from noise (device, lattice
+ * layout, 3*N N(0,1) draws) in MGX_NOISE_HOST mode, generated by Philox4x32-10 keyed by
+ * (seed, site, step) in MGX_NOISE_PHILOX mode, and ignored in MGX_NOISE_NONE mode. */
+mgx_status mgx_llg_step(mgx_llg* plan, double* e, const double* noise, uint64_t step, void* stream);
+/* nsteps Heun steps (noise NONE or PHILOX), steps step0 .. step0+nsteps-1. */
+mgx_status mgx_llg_run(mgx_llg* plan, double* e, int64_t nsteps, uint64_t step0, void* stream);
+/* One half of mgx_llg_step: stage 0 = predictor (reads e, writes the plan's ep and k1), stage 1 =
+ * corrector (reads ep, k1 and e, writes e).  For callers that exchange halos between the stages,
+ * as magex's slab decomposition does (magex/mpi_spin.py:160-174: _fused1, halo(ep), _fused2, halo(e)). */
+mgx_status mgx_llg_stage(mgx_llg* plan, int32_t stage, double* e, const double* noise, uint64_t step, void* stream);
+
+/* ---------------------------------------------------------------- observables
+ * Writes 8 doubles to out (device):
+ *   [0] E total (meV)  = sum_i e.A.e - e.h - mu_B mu e.B      (magex/spinmodel.py:475-484)
+ *   [1..3] sum_i e_i                                          (magex/llg.py:265, e.mean(0) * N)
+ *   [4..6] sum_i s_i e_i                                      (magex/spinmodel.py:517-519)
+ *   [7] max_i |e_i x B_eff,i| (T)                             (magex/llg.py:250-252)
+ * The sums are deterministic (fixed-shape tree reduction). */
+mgx_status mgx_observables(const mgx_model* m, const double* e, double* out, void* stream);
+/* Effective field B_eff (T) of spins e into B (device, lattice layout) (magex/spinmodel.py:471-473). */
+mgx_status mgx_effective_field(const mgx_model* m, const double* e, double* B, void* stream);
+
+/* Berg-Luscher topological charge over a triangle list (magex/texture.py:30-63):
+ * Q = hand/(4 pi) sum_t orient_t * 2 atan2(s1.(s2 x s3), 1 + s1.s2 + s2.s3 + s3.s1).
+ * tri: device [ntri*3] lattice-layout site indices; orient: device [ntri] (+-1, hand folded in).
+ * Writes Q to out (device, 1 double). */
+mgx_status mgx_topological_charge(const mgx_model* m, const double* e, const int32_t* tri,
+                                  const double* orient, int64_t ntri, double* out, void* stream);
+
+/* ---------------------------------------------------------------- diagnostics
+ * No counterpart in the reference.  Measures the device's sustained FP64 fused multiply-add rate
+ * (FLOP/s, 2 per FMA) with a register-resident DFMA loop on every SM; synchronises the device.
+ * The LLG kernels are bound by this rate on GB300, so it is the denominator of their roofline. */
+mgx_status mgx_measure_fp64_peak(double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MGX_H */

@@ -1,0 +1,118 @@
+"""ctypes binding of libmgx.so (declarations in include/mgx.h).
+
+The library is loaded from this package directory only (it is built in-tree by
+``magex_gb300.build``).  There is no fallback: if the library is missing or cannot load, every
+GPU entry point raises, so a run can never silently fall back to CPU code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmgx.so")
+
+MGX_OK, MGX_ERR_INVALID, MGX_ERR_UNSUPPORTED, MGX_ERR_CUDA, MGX_ERR_NOMEM = 0, 1, 2, 3, 4
+HEUN, DEPONDT = 0, 1
+NOISE_NONE, NOISE_HOST, NOISE_PHILOX = 0, 1, 2
+MAX_SUBLATTICES = 16
+MAX_BONDS = 256
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+_u8p = C.POINTER(C.c_uint8)
+
+
+class LatticeDesc(C.Structure):
+    _fields_ = [("ns", C.c_int32), ("L", C.c_int32 * 3), ("pbc", C.c_int32 * 3), ("nbond", C.c_int32),
+                ("bond_src", _ip), ("bond_dst", _ip), ("bond_R", _ip), ("width", C.c_int32),
+                ("bond_table", _dp), ("A_sub", _dp), ("mu_sub", _dp), ("sign_sub", _dp),
+                ("B", C.c_double * 3)]
+
+
+class SiteDesc(C.Structure):
+    _fields_ = [("A_site", _dp), ("mu_site", _dp), ("pinned", _u8p)]
+
+
+class LLGParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("alpha", C.c_double), ("alpha_site", _dp), ("precession", C.c_int32),
+                ("integrator", C.c_int32), ("noise", C.c_int32), ("seed", C.c_uint64)]
+
+
+#: every exported entry point with (restype, argtypes); the CPU tests check the export list against
+#: include/mgx.h
+SIGNATURES = {
+    "mgx_version": (C.c_int32, []),
+    "mgx_last_error": (None, [C.c_char_p, C.c_size_t]),
+    "mgx_model_create": (C.c_int32, [C.POINTER(LatticeDesc), C.POINTER(SiteDesc), C.POINTER(C.c_void_p)]),
+    "mgx_model_destroy": (C.c_int32, [C.c_void_p]),
+    "mgx_model_set_field": (C.c_int32, [C.c_void_p, _dp]),
+    "mgx_model_nsites": (C.c_int64, [C.c_void_p]),
+    "mgx_pack_spins": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_unpack_spins": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_llg_create": (C.c_int32, [C.c_void_p, C.POINTER(LLGParams), C.POINTER(C.c_void_p)]),
+    "mgx_llg_destroy": (C.c_int32, [C.c_void_p]),
+    "mgx_llg_set_sigma": (C.c_int32, [C.c_void_p, _dp, _dp]),
+    "mgx_llg_step": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "mgx_llg_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]),
+    "mgx_llg_stage": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "mgx_measure_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
+    "mgx_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_effective_field": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                           C.c_void_p, C.c_void_p]),
+}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load libmgx.so and attach signatures (cached).  Raises RuntimeError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libmgx.so not found at {path}: build it with `python -m magex_gb300.build` "
+                           "(the GB300 LLG path has no CPU fallback)")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    load().mgx_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status, what=""):
+    """Map an mgx_status to the exception magex raises in the same situation."""
+    if status == MGX_OK:
+        return
+    msg = f"{what}: {last_error()}" if what else last_error()
+    if status == MGX_ERR_INVALID:
+        raise ValueError(msg)
+    if status == MGX_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if status == MGX_ERR_NOMEM:
+        raise MemoryError(msg)
+    raise RuntimeError(msg)
+
+
+def dptr(a):
+    """ctypes double* of a C-contiguous float64 numpy array (or None)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+def u8ptr(a):
+    return None if a is None else a.ctypes.data_as(_u8p)

@@ -1,0 +1,200 @@
+// Internal declarations shared by the translation units of libmgx (GB300, sm_103a).
+//
+// Device data layout ("lattice layout"): for a supercell of ncell = L0*L1*L2 cells and ns
+// sublattices, site (s, cell) has lattice index q = s*ncell + cell and component c of a spin field
+// lives at x[c*N + q].  Threads of a warp therefore read consecutive cells of one sublattice, and
+// a neighbour at a fixed cell offset is again a consecutive run: every gather load is coalesced.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/mgx.h"
+
+namespace mgx {
+
+// ------------------------------------------------------------------ error reporting (host)
+mgx_status set_error(mgx_status code, const char* fmt, ...);
+mgx_status cuda_error(cudaError_t err, const char* where);
+
+#define MGX_CUDA_TRY(call)                                   \
+  do {                                                       \
+    cudaError_t err__ = (call);                              \
+    if (err__ != cudaSuccess) return ::mgx::cuda_error(err__, #call); \
+  } while (0)
+
+// ------------------------------------------------------------------ device-side lattice view
+struct DevLattice {
+  int ns;
+  int L0, L1, L2;
+  int ncell;
+  long long N;
+  int pbc0, pbc1, pbc2;
+  int width;                     // 1, 4 or 9 doubles per coupling
+  const int* bond_off;           // [ns+1] range of couplings per receiving sublattice
+  const int4* bond_geo;          // [nbond] (dst sublattice, d0, d1, d2); d = R mod L if periodic else R
+  const double* bond_J;          // [nbond*width]
+  int has_A;
+  const double* A_sub;           // [ns*9]
+  const double* inv_mu_sub;      // [ns] 1/(mu mu_B)
+  const double* mu_sub;          // [ns]
+  const double* sign_sub;        // [ns]
+  const double* A_site;          // [9][N] lattice layout, or nullptr
+  const double* inv_mu_site;     // [N] or nullptr
+  const double* mu_site;         // [N] or nullptr
+  const uint8_t* pinned;         // [N] or nullptr
+  double B0, B1, B2;
+};
+
+struct Model {
+  DevLattice d;
+  int nbond;
+  // device allocations owned by the model
+  void* dev_block = nullptr;     // tables and per-sublattice constants
+  double* A_site = nullptr;
+  double* inv_mu_site = nullptr;
+  double* mu_site = nullptr;
+  uint8_t* pinned = nullptr;
+  double* partials = nullptr;    // reduction scratch for observables
+  int partial_cap = 0;           // number of 8-double slots
+};
+
+// ------------------------------------------------------------------ small device helpers
+__device__ __forceinline__ void site_coords(const DevLattice& L, long long q, int& s, int& c0, int& c1, int& c2) {
+  s = (int)(q / L.ncell);
+  int cell = (int)(q - (long long)s * L.ncell);
+  c2 = cell % L.L2;
+  int t = cell / L.L2;
+  c1 = t % L.L1;
+  c0 = t / L.L1;
+}
+
+// Exchange field h = sum_j J_ij x_j at site (s, c0, c1, c2) of field x (lattice layout).
+// Couplings whose neighbour lies outside an open boundary are skipped, as magex drops them
+// when it builds the supercell (magex/spinmodel.py:218-223).
+template <int W>
+__device__ __forceinline__ void exchange_field(const DevLattice& L, const double* __restrict__ x, int s, int c0,
+                                               int c1, int c2, double& hx, double& hy, double& hz) {
+  hx = 0.0;
+  hy = 0.0;
+  hz = 0.0;
+  const long long N = L.N;
+  const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
+  for (int b = b0; b < b1; ++b) {
+    const int4 g = __ldg(L.bond_geo + b);
+    int n0 = c0 + g.y, n1 = c1 + g.z, n2 = c2 + g.w;
+    bool ok = true;
+    if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
+    if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
+    if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
+    if (!ok) continue;
+    const long long j = (long long)g.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
+    const double ex = __ldg(x + j), ey = __ldg(x + N + j), ez = __ldg(x + 2 * N + j);
+    const double* T = L.bond_J + (long long)b * W;
+    if (W == 1) {
+      const double J = __ldg(T);
+      hx = fma(J, ex, hx);
+      hy = fma(J, ey, hy);
+      hz = fma(J, ez, hz);
+    } else if (W == 4) {
+      // J e_j + e_j x D  (antisymmetric part with e_i.J^A.e_j = D.(e_i x e_j)), magex/fast.py:102-111
+      const double J = __ldg(T), Dx = __ldg(T + 1), Dy = __ldg(T + 2), Dz = __ldg(T + 3);
+      hx = fma(J, ex, hx); hx = fma(ey, Dz, hx); hx = fma(-ez, Dy, hx);
+      hy = fma(J, ey, hy); hy = fma(ez, Dx, hy); hy = fma(-ex, Dz, hy);
+      hz = fma(J, ez, hz); hz = fma(ex, Dy, hz); hz = fma(-ey, Dx, hz);
+    } else {
+      hx = fma(__ldg(T + 0), ex, hx); hx = fma(__ldg(T + 1), ey, hx); hx = fma(__ldg(T + 2), ez, hx);
+      hy = fma(__ldg(T + 3), ex, hy); hy = fma(__ldg(T + 4), ey, hy); hy = fma(__ldg(T + 5), ez, hy);
+      hz = fma(__ldg(T + 6), ex, hz); hz = fma(__ldg(T + 7), ey, hz); hz = fma(__ldg(T + 8), ez, hz);
+    }
+  }
+}
+
+// Effective field B = (2h - dE_onsite/de) / (mu mu_B) + B_ext (T) at lattice index q with spin (x,y,z):
+// magex/fast.py:309-317 and magex/spinmodel.py:458-473 (dE/de of e.A.e is 2 A e).
+template <int W>
+__device__ __forceinline__ void effective_field(const DevLattice& L, const double* __restrict__ x, long long q, int s,
+                                                int c0, int c1, int c2, double ex, double ey, double ez,
+                                                double& bx, double& by, double& bz) {
+  double hx, hy, hz;
+  exchange_field<W>(L, x, s, c0, c1, c2, hx, hy, hz);
+  double gx = 0.0, gy = 0.0, gz = 0.0;
+  if (L.has_A) {
+    double a[9];
+    if (L.A_site) {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a[k] = __ldg(L.A_site + (long long)k * L.N + q);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a[k] = __ldg(L.A_sub + s * 9 + k);
+    }
+    gx = 2.0 * fma(a[0], ex, fma(a[1], ey, a[2] * ez));
+    gy = 2.0 * fma(a[3], ex, fma(a[4], ey, a[5] * ez));
+    gz = 2.0 * fma(a[6], ex, fma(a[7], ey, a[8] * ez));
+  }
+  const double inv = L.inv_mu_site ? __ldg(L.inv_mu_site + q) : __ldg(L.inv_mu_sub + s);
+  bx = fma(fma(2.0, hx, -gx), inv, L.B0);
+  by = fma(fma(2.0, hy, -gy), inv, L.B1);
+  bz = fma(fma(2.0, hz, -gz), inv, L.B2);
+}
+
+// LLG right-hand side f = pre [e x B + alpha e x (e x B)], pre = -gamma / (1 + alpha^2)
+// (magex/llg.py:21-28, magex/fast.py:225-236); precession=false drops the e x B term.
+__device__ __forceinline__ void llg_rhs(double ex, double ey, double ez, double bx, double by, double bz, double a,
+                                        double pre, bool precession, double& fx, double& fy, double& fz) {
+  const double cx = ey * bz - ez * by;
+  const double cy = ez * bx - ex * bz;
+  const double cz = ex * by - ey * bx;
+  const double dx = ey * cz - ez * cy;
+  const double dy = ez * cx - ex * cz;
+  const double dz = ex * cy - ey * cx;
+  if (precession) {
+    fx = pre * fma(a, dx, cx);
+    fy = pre * fma(a, dy, cy);
+    fz = pre * fma(a, dz, cz);
+  } else {
+    fx = pre * (a * dx);
+    fy = pre * (a * dy);
+    fz = pre * (a * dz);
+  }
+}
+
+// ------------------------------------------------------------------ Philox4x32-10 (Salmon et al., SC'11)
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += W0;
+    k.y += W1;
+  }
+  return c;
+}
+
+// Three N(0,1) draws for (site, step) by Box-Muller on one Philox block.  The draws are computed
+// in fp32 (their statistical quality, not their rounding, matters) and widened to fp64.
+__device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uint64_t step, double& g0, double& g1,
+                                               double& g2) {
+  const uint4 r = philox4x32_10(make_uint4((uint32_t)site, (uint32_t)(site >> 32), (uint32_t)step,
+                                           (uint32_t)(step >> 32)),
+                                make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+  const float tw = 2.3283064365386963e-10f;                 // 2^-32
+  const float u1 = fmaf((float)r.x, tw, 0.5f * tw);          // (0, 1]
+  const float u3 = fmaf((float)r.z, tw, 0.5f * tw);
+  const float v1 = (float)r.y * tw, v3 = (float)r.w * tw;    // [0, 1)
+  const float m1 = sqrtf(-2.0f * logf(u1));
+  const float m3 = sqrtf(-2.0f * logf(u3));
+  float s1, c1;
+  sincospif(2.0f * v1, &s1, &c1);
+  g0 = (double)(m1 * c1);
+  g1 = (double)(m1 * s1);
+  g2 = (double)(m3 * cospif(2.0f * v3));
+}
+
+}  // namespace mgx

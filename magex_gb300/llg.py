@@ -1,0 +1,299 @@
+"""GB300 drop-in for magex's stochastic LLG integrator (``magex.llg.LLGSolver``, heun / depondt).
+
+    from magex_gb300 import LLGSolver            # or GB300LLG
+    sol = LLGSolver(system, alpha=0.1, dt=1e-4, temperature=300, seed=1)
+    e, table, snaps = sol.run(e0, steps=10000, output_every=100)
+
+Same constructor, ``step``, ``run``, ``max_torque``, ``time`` / ``T`` / ``dt`` attributes and table
+columns as magex ``magex/llg.py:48-283``.  The spins stay on the GPU for the whole ``run`` and every
+Heun step is two fused sm_103a kernels (libmgx: ``mgx_llg_step`` / ``mgx_llg_run``); observables
+rows are computed on the device by ``mgx_observables``.
+
+Thermal noise (``noise=``):
+  "philox"  counter-based Philox4x32-10 keyed by (seed, site, step), generated inside the kernels
+            (default; the trajectory differs from any magex backend, as magex's own numba and NumPy
+            backends differ from each other, but the statistics are those of magex/llg.py:106-122);
+  "host"    N(0,1) draws from ``numpy.random.default_rng(seed).normal(size=(N, 3))`` once per step,
+            exactly the stream of magex's NumPy path (magex/llg.py:69,119): trajectories then
+            reproduce magex's step for step.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time as _time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import GAMMA, K_B, MU_B
+from .device import DeviceModel, stream_ptr, supercell_from_system
+
+INTEGRATORS = ("heun", "rk4", "depondt", "sib", "euler")   # the names magex accepts (magex/llg.py:45)
+_SUPPORTED = {"heun": _lib.HEUN, "depondt": _lib.DEPONDT}
+
+
+def _philox_key(seed):
+    ss = np.random.SeedSequence(None if seed is None else int(seed))
+    return int(ss.generate_state(1, dtype=np.uint64)[0])
+
+
+class GB300LLG:
+    """Stochastic Heun / Depondt LLG on one GB300, with the API of magex ``LLGSolver``."""
+
+    def __init__(self, system, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
+                 thermostat="classical", integrator="heun", stt=None, sot=None, backend="gb300",
+                 noise="philox", device=None):
+        if integrator not in INTEGRATORS:
+            raise ValueError(f"integrator must be one of {INTEGRATORS}")
+        if integrator not in _SUPPORTED:
+            raise NotImplementedError(f"integrator '{integrator}' is not implemented by the GB300 kernels "
+                                      "(heun and depondt are)")
+        if thermostat != "classical":
+            raise NotImplementedError("the quantum thermostat is not implemented by the GB300 kernels")
+        if stt or sot:
+            raise NotImplementedError("spin-transfer / spin-orbit torques are not implemented by the GB300 kernels")
+        if backend not in ("gb300", "auto"):
+            raise ValueError("backend must be 'gb300'")
+        if noise not in ("philox", "host"):
+            raise ValueError("noise must be 'philox' or 'host'")
+        self.sys = system
+        self.sc = supercell_from_system(system)
+        self.model = DeviceModel(self.sc, device)
+        self.device = self.model.device
+        N = self.sc.N
+        a = getattr(self.sc, "alpha_site", None)
+        self.alpha = np.asarray(a if (a is not None and np.isscalar(alpha)) else alpha, float)
+        if self.alpha.ndim and a is not None and np.isscalar(alpha):
+            self.alpha = np.where(np.isnan(self.alpha), float(alpha), self.alpha)
+        self.dt = float(dt)
+        self.T = float(temperature)
+        self.seed = seed
+        self.rng = np.random.default_rng(seed)
+        self.precession = bool(precession)
+        self.thermostat = thermostat
+        self.integrator = integrator
+        self.noise = noise
+        self.time = 0.0
+        self.field_func = None
+        self.extra_field = None
+        self._step_index = 0
+        p = _lib.LLGParams()
+        p.dt = self.dt
+        if self.alpha.ndim:
+            if self.alpha.shape != (N,):
+                raise ValueError(f"alpha array must have shape ({N},)")
+            al = np.ascontiguousarray(self.alpha, np.float64)
+            p.alpha, p.alpha_site = 0.0, _lib.dptr(al)
+        else:
+            al = None
+            p.alpha = float(self.alpha)
+        p.precession = int(self.precession)
+        p.integrator = _SUPPORTED[integrator]
+        p.noise = _lib.NOISE_HOST if noise == "host" else _lib.NOISE_PHILOX
+        p.seed = _philox_key(seed)
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.model.lib.mgx_llg_create(self.model.handle, C.byref(p), C.byref(h)), "mgx_llg_create")
+        del al
+        self.handle = h
+        self._sigma_key = None
+        self._noisy = False
+        self._noise_lat = None
+        self._lat = None
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.model.lib.mgx_llg_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    # ------------------------------------------------------------------ thermal amplitude
+    def _site_T(self):
+        sT = getattr(self.sc, "site_T", None)
+        if sT is None:
+            return None
+        return np.where(np.isnan(sT), self.T, sT)
+
+    def _update_sigma(self):
+        """sigma_i = sqrt(2 alpha_i k_B T_i / (gamma mu_i mu_B dt)) (magex/llg.py:111), pushed to the plan
+        whenever T, dt or the site temperatures change."""
+        sT = getattr(self.sc, "site_T", None)
+        key = (self.T, id(sT), self.dt)
+        if key == self._sigma_key:
+            return
+        self._sigma_key = key
+        self._noisy = self.T > 0 or sT is not None
+        lib, sc = self.model.lib, self.sc
+        if not self._noisy:
+            _lib.check(lib.mgx_llg_set_sigma(self.handle, _lib.dptr(np.zeros(sc.ns)), None), "mgx_llg_set_sigma")
+            return
+        per_site = self.alpha.ndim or sT is not None or sc.mu_site is not None
+        if per_site:
+            T = self._site_T() if sT is not None else self.T
+            sig = np.sqrt(2.0 * self.alpha * K_B * T / (GAMMA * sc.mu * MU_B * self.dt))
+            sig = np.ascontiguousarray(np.broadcast_to(sig, (sc.N,)), np.float64)
+            _lib.check(lib.mgx_llg_set_sigma(self.handle, None, _lib.dptr(sig)), "mgx_llg_set_sigma")
+        else:
+            sig = np.sqrt(2.0 * self.alpha * K_B * self.T / (GAMMA * sc.mu_sub * MU_B * self.dt))
+            sig = np.ascontiguousarray(sig, np.float64)
+            _lib.check(lib.mgx_llg_set_sigma(self.handle, _lib.dptr(sig), None), "mgx_llg_set_sigma")
+
+    # ------------------------------------------------------------------ stepping on device
+    def _check_supported_callables(self):
+        if self.field_func is not None or self.extra_field is not None:
+            raise NotImplementedError("field_func / extra_field callables are not supported by the GB300 kernels")
+
+    def step_lattice(self, lat, stream=None):
+        """One step on device spins in the lattice layout ((3, N) float64, in place)."""
+        self._check_supported_callables()
+        self.model.sync_field()
+        self._update_sigma()
+        noise_ptr = None
+        if self.noise == "host" and self._noisy:
+            g = self.rng.normal(size=(self.sc.N, 3))
+            self._noise_lat = self.model.to_lattice(g, out=self._noise_lat, stream=stream)
+            noise_ptr = C.c_void_p(self._noise_lat.data_ptr())
+        elif self.noise == "host":
+            # T = 0: magex draws nothing (magex/llg.py:107-108); a zero field is added
+            if self._noise_lat is None:
+                self._noise_lat = torch.zeros((3, self.sc.N), dtype=torch.float64, device=self.device)
+            noise_ptr = C.c_void_p(self._noise_lat.data_ptr())
+        _lib.check(self.model.lib.mgx_llg_step(self.handle, C.c_void_p(lat.data_ptr()), noise_ptr,
+                                               C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_step")
+        self._step_index += 1
+        self.time += self.dt
+        return lat
+
+    def run_lattice(self, lat, nsteps, stream=None):
+        """nsteps steps on device lattice-layout spins; Philox noise only (one library call)."""
+        if self.noise == "host":
+            for _ in range(int(nsteps)):
+                self.step_lattice(lat, stream)
+            return lat
+        self._check_supported_callables()
+        self.model.sync_field()
+        self._update_sigma()
+        _lib.check(self.model.lib.mgx_llg_run(self.handle, C.c_void_p(lat.data_ptr()), C.c_int64(int(nsteps)),
+                                              C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_run")
+        self._step_index += int(nsteps)
+        self.time += self.dt * int(nsteps)
+        return lat
+
+    def stage_lattice(self, lat, stage, stream=None):
+        """Predictor (stage 0) or corrector (stage 1) half of a step on device lattice spins
+        (Philox or no noise); the step counter and the time advance after the corrector."""
+        if self.noise == "host":
+            raise ValueError("stage_lattice needs in-kernel (philox) noise")
+        self._check_supported_callables()
+        if stage == 0:
+            self.model.sync_field()
+            self._update_sigma()
+        _lib.check(self.model.lib.mgx_llg_stage(self.handle, C.c_int32(stage), C.c_void_p(lat.data_ptr()), None,
+                                                C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_stage")
+        if stage == 1:
+            self._step_index += 1
+            self.time += self.dt
+        return lat
+
+    # ------------------------------------------------------------------ magex API
+    def step(self, e, out=None):
+        """One integration step; returns new spins (magex/llg.py:216).
+
+        A numpy array in gives a new numpy array out (the input is not modified); an (N, 3) CUDA
+        tensor gives a CUDA tensor; an (N, 3) CPU tensor (pinned for asynchronous copies) gives a
+        CPU tensor, written into ``out`` when given."""
+        on_device = isinstance(e, torch.Tensor) and e.is_cuda
+        lat = self.model.to_lattice(e, out=self._lat)
+        self._lat = lat
+        self.step_lattice(lat)
+        dev = self.model.from_lattice(lat, out=getattr(self, "_aos", None))
+        self._aos = dev
+        if on_device:
+            return dev.clone() if out is None else out.copy_(dev)
+        if isinstance(e, torch.Tensor):
+            if out is None:
+                out = torch.empty((self.sc.N, 3), dtype=torch.float64, pin_memory=e.is_pinned())
+            out.copy_(dev, non_blocking=out.is_pinned())
+            torch.cuda.current_stream(self.device).synchronize()
+            return out
+        return dev.cpu().numpy()
+
+    def _row(self, lat):
+        obs = self.model.observables(lat).cpu().numpy()
+        N = self.sc.N
+        return [self.time, obs[0] / N, obs[1] / N, obs[2] / N, obs[3] / N,
+                float(np.linalg.norm(obs[4:7]) / N), float(obs[7])]
+
+    def max_torque(self, e):
+        """max_i |e_i x B_eff,i| (T) (magex/llg.py:250-252)."""
+        return float(self.model.observables(self.model.to_lattice(e))[7].item())
+
+    def effective_field(self, e):
+        """B_eff (N, 3) in tesla (magex/spinmodel.py:471-473), computed on the device."""
+        lat = self.model.to_lattice(e)
+        B = self.model.effective_field(lat)
+        out = self.model.from_lattice(B)
+        return out if (isinstance(e, torch.Tensor) and e.is_cuda) else out.cpu().numpy()
+
+    def energy(self, e, per_spin=False):
+        """Total energy (meV) (magex/spinmodel.py:475-484), computed on the device."""
+        E = float(self.model.observables(self.model.to_lattice(e))[0].item())
+        return E / self.sc.N if per_spin else E
+
+    def run(self, e, steps, output_every=100, snapshots=0, callback=None, torque_tol=None, log=None):
+        """Integrate ``steps`` steps; returns (spins, table, snapshots) as magex/llg.py:254-283.
+
+        table columns: t (ps), E/N (meV), <ex>, <ey>, <ez>, order parameter, max torque (T).
+        Between output rows the steps run back to back on the device (one library call per
+        interval when no callback or snapshot needs the spins on the host).
+        """
+        on_device = isinstance(e, torch.Tensor) and e.is_cuda
+        steps = int(steps)
+        output_every = max(1, int(output_every))
+        rows, snaps = [], []
+        snap_every = max(1, steps // snapshots) if snapshots else 0
+        lat = self.model.to_lattice(e)
+        t0 = _time.time()
+
+        def host_spins():
+            return self.model.from_lattice(lat).cpu().numpy()
+
+        n = 0
+        while n <= steps:
+            if n % output_every == 0 or n == steps:
+                rows.append(self._row(lat))
+                tq = rows[-1][6]
+                if log and (n % (output_every * 10) == 0 or n == steps):
+                    m = rows[-1][2:5]
+                    log(f"  step {n:8d}  t = {self.time:9.3f} ps  E/N = {rows[-1][1]: .6f} meV  "
+                        f"m = ({m[0]: .3f},{m[1]: .3f},{m[2]: .3f})  |torque|max = {tq:.2e} T")
+                if torque_tol is not None and self.T == 0 and tq < torque_tol and n > 0:
+                    if log:
+                        log(f"  converged: max torque {tq:.2e} T < {torque_tol:g} T after {n} steps")
+                    break
+            if snap_every and n % snap_every == 0:
+                snaps.append((self.time, host_spins()))
+            if callback:
+                callback(n, host_spins())
+            if n >= steps:
+                break
+            # advance to the next step at which the host needs something
+            nxt = min(steps, (n // output_every + 1) * output_every)
+            if snap_every:
+                nxt = min(nxt, (n // snap_every + 1) * snap_every)
+            if callback:
+                nxt = n + 1
+            self.run_lattice(lat, nxt - n)
+            n = nxt
+        if log:
+            torch.cuda.synchronize(self.device)
+            log(f"  LLG wall time {_time.time() - t0:.1f} s")
+        out = self.model.from_lattice(lat)
+        return (out if on_device else out.cpu().numpy()), np.array(rows), snaps
+
+
+LLGSolver = GB300LLG

@@ -1,0 +1,375 @@
+/*
+ * heun_ref.c -- CPU restatement of magex's LLG hot path.  TEST INFRASTRUCTURE ONLY.
+ *
+ * This file is the oracle the GB300 kernels are checked against and the CPU baseline that
+ * bench.py times.  Nothing in the product (magex_gb300/) loads it.
+ *
+ * What it restates (operation order of the reference's fused CPU kernels):
+ *   oracle_step         magex/fast.py:336-390  (_fused1 predictor, _fused2 corrector; Heun and
+ *                       Depondt), with the field of magex/fast.py:87-120,309-317 and the right-hand
+ *                       side of magex/fast.py:225-236; the thermal field b is an input (already
+ *                       scaled by sigma), as in magex's extras path magex/llg.py:200-208.
+ *   oracle_observables  magex/spinmodel.py:475-484 (energy), :517-519 (order parameter),
+ *                       magex/llg.py:250-252,265 (max torque, mean spin).
+ *   oracle_gauss3       magex/fast.py:123-200 (xorshift64* streams over 256 fixed chunks and the
+ *                       128-layer Marsaglia-Tsang ziggurat), the reference's multithreaded noise.
+ *
+ * Neighbour data is magex's per-site block list (magex/fast.py:587-627): ptr (N+1), nbr, typ and a
+ * coupling table of width 1 (J), 4 (J, D) or 9 (3x3 row-major), in magex site order.
+ * Build: see oracle/Makefile (gcc -O2 -fopenmp, plain C99, no target-specific flags).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MU_B 5.7883818060e-2
+#define GAMMA 0.1760859630
+
+typedef struct oracle_model {
+  int64_t N;
+  const int64_t* ptr;
+  const int32_t* nbr;
+  const int32_t* typ;
+  const double* table;
+  int32_t width;
+  const double* A;        /* N*9 or NULL (no on-site terms) */
+  const double* mu;       /* N */
+  double B[3];
+  const uint8_t* pinned;  /* N or NULL */
+} oracle_model;
+
+static void hfield(const oracle_model* m, int64_t i, const double* e, double* h) {
+  double hx = 0.0, hy = 0.0, hz = 0.0;
+  const int w = m->width;
+  for (int64_t k = m->ptr[i]; k < m->ptr[i + 1]; ++k) {
+    const int64_t j = m->nbr[k];
+    const double* T = m->table + (int64_t)m->typ[k] * w;
+    const double ex = e[3 * j], ey = e[3 * j + 1], ez = e[3 * j + 2];
+    if (w == 1) {
+      hx += T[0] * ex;
+      hy += T[0] * ey;
+      hz += T[0] * ez;
+    } else if (w == 4) {
+      hx += T[0] * ex + (ey * T[3] - ez * T[2]);
+      hy += T[0] * ey + (ez * T[1] - ex * T[3]);
+      hz += T[0] * ez + (ex * T[2] - ey * T[1]);
+    } else {
+      hx += T[0] * ex + T[1] * ey + T[2] * ez;
+      hy += T[3] * ex + T[4] * ey + T[5] * ez;
+      hz += T[6] * ex + T[7] * ey + T[8] * ez;
+    }
+  }
+  h[0] = hx;
+  h[1] = hy;
+  h[2] = hz;
+}
+
+static void onsite_grad(const oracle_model* m, int64_t i, const double* v, double* g) {
+  g[0] = g[1] = g[2] = 0.0;
+  if (!m->A) return;
+  const double* A = m->A + 9 * i;
+  g[0] = 2.0 * (A[0] * v[0] + A[1] * v[1] + A[2] * v[2]);
+  g[1] = 2.0 * (A[3] * v[0] + A[4] * v[1] + A[5] * v[2]);
+  g[2] = 2.0 * (A[6] * v[0] + A[7] * v[1] + A[8] * v[2]);
+}
+
+/* B_eff of site i for spins e (T) */
+static void bloc(const oracle_model* m, int64_t i, const double* e, double* B) {
+  double h[3], g[3];
+  hfield(m, i, e, h);
+  onsite_grad(m, i, e + 3 * i, g);
+  const double inv = 1.0 / (m->mu[i] * MU_B);
+  B[0] = (2 * h[0] - g[0]) * inv + m->B[0];
+  B[1] = (2 * h[1] - g[1]) * inv + m->B[1];
+  B[2] = (2 * h[2] - g[2]) * inv + m->B[2];
+}
+
+static void rhs(const double* e, const double* b, double a, int prec, double* f) {
+  const double cx = e[1] * b[2] - e[2] * b[1];
+  const double cy = e[2] * b[0] - e[0] * b[2];
+  const double cz = e[0] * b[1] - e[1] * b[0];
+  const double dx = e[1] * cz - e[2] * cy;
+  const double dy = e[2] * cx - e[0] * cz;
+  const double dz = e[0] * cy - e[1] * cx;
+  const double pre = -GAMMA / (1.0 + a * a);
+  if (prec) {
+    f[0] = pre * (cx + a * dx);
+    f[1] = pre * (cy + a * dy);
+    f[2] = pre * (cz + a * dz);
+  } else {
+    f[0] = pre * a * dx;
+    f[1] = pre * a * dy;
+    f[2] = pre * a * dz;
+  }
+}
+
+static void rot(double* v, double wx, double wy, double wz) {
+  const double th = sqrt(wx * wx + wy * wy + wz * wz);
+  if (th < 1e-14) return;
+  const double kx = wx / th, ky = wy / th, kz = wz / th;
+  const double c = cos(th), s = sin(th);
+  const double kd = kx * v[0] + ky * v[1] + kz * v[2];
+  const double cx = ky * v[2] - kz * v[1], cy = kz * v[0] - kx * v[2], cz = kx * v[1] - ky * v[0];
+  const double x = v[0] * c + cx * s + kx * kd * (1 - c);
+  const double y = v[1] * c + cy * s + ky * kd * (1 - c);
+  const double z = v[2] * c + cz * s + kz * kd * (1 - c);
+  v[0] = x;
+  v[1] = y;
+  v[2] = z;
+}
+
+static void set_threads(int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+}
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+/* One Heun (depondt = 0) or Depondt (depondt = 1) step in place on e (N*3, magex order).
+ * alpha: N damping values; b: N*3 thermal field (T) or NULL; ep, k1: N*3 scratch. */
+void oracle_step(const oracle_model* m, const double* alpha, double dt, int prec, int depondt, const double* b,
+                 double* e, double* ep, double* k1, int nthreads) {
+  const int64_t N = m->N;
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) {
+    if (m->pinned && m->pinned[i]) {
+      ep[3 * i] = e[3 * i];
+      ep[3 * i + 1] = e[3 * i + 1];
+      ep[3 * i + 2] = e[3 * i + 2];
+      k1[3 * i] = k1[3 * i + 1] = k1[3 * i + 2] = 0.0;
+      continue;
+    }
+    double B[3], f[3];
+    bloc(m, i, e, B);
+    if (b) {
+      B[0] += b[3 * i];
+      B[1] += b[3 * i + 1];
+      B[2] += b[3 * i + 2];
+    }
+    rhs(e + 3 * i, B, alpha[i], prec, f);
+    if (depondt) {
+      const double* v = e + 3 * i;
+      const double wx = v[1] * f[2] - v[2] * f[1], wy = v[2] * f[0] - v[0] * f[2], wz = v[0] * f[1] - v[1] * f[0];
+      k1[3 * i] = wx;
+      k1[3 * i + 1] = wy;
+      k1[3 * i + 2] = wz;
+      double r[3] = {v[0], v[1], v[2]};
+      rot(r, dt * wx, dt * wy, dt * wz);
+      ep[3 * i] = r[0];
+      ep[3 * i + 1] = r[1];
+      ep[3 * i + 2] = r[2];
+    } else {
+      k1[3 * i] = f[0];
+      k1[3 * i + 1] = f[1];
+      k1[3 * i + 2] = f[2];
+      const double x = e[3 * i] + dt * f[0], y = e[3 * i + 1] + dt * f[1], z = e[3 * i + 2] + dt * f[2];
+      const double q = 1.0 / sqrt(x * x + y * y + z * z);
+      ep[3 * i] = x * q;
+      ep[3 * i + 1] = y * q;
+      ep[3 * i + 2] = z * q;
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) {
+    if (m->pinned && m->pinned[i]) continue;
+    double B[3], f[3], x, y, z;
+    bloc(m, i, ep, B);
+    if (b) {
+      B[0] += b[3 * i];
+      B[1] += b[3 * i + 1];
+      B[2] += b[3 * i + 2];
+    }
+    rhs(ep + 3 * i, B, alpha[i], prec, f);
+    if (depondt) {
+      const double* p = ep + 3 * i;
+      const double wx = p[1] * f[2] - p[2] * f[1], wy = p[2] * f[0] - p[0] * f[2], wz = p[0] * f[1] - p[1] * f[0];
+      double r[3] = {e[3 * i], e[3 * i + 1], e[3 * i + 2]};
+      rot(r, 0.5 * dt * (k1[3 * i] + wx), 0.5 * dt * (k1[3 * i + 1] + wy), 0.5 * dt * (k1[3 * i + 2] + wz));
+      x = r[0];
+      y = r[1];
+      z = r[2];
+    } else {
+      x = e[3 * i] + 0.5 * dt * (k1[3 * i] + f[0]);
+      y = e[3 * i + 1] + 0.5 * dt * (k1[3 * i + 1] + f[1]);
+      z = e[3 * i + 2] + 0.5 * dt * (k1[3 * i + 2] + f[2]);
+    }
+    const double q = 1.0 / sqrt(x * x + y * y + z * z);
+    e[3 * i] = x * q;
+    e[3 * i + 1] = y * q;
+    e[3 * i + 2] = z * q;
+  }
+}
+
+/* out[8] = E, sum e (3), sum s e (3), max |e x B_eff| (pinned sites have zero field). */
+void oracle_observables(const oracle_model* m, const double* e, const double* signs, double* out, int nthreads) {
+  const int64_t N = m->N;
+  double E = 0, mx = 0, my = 0, mz = 0, ox = 0, oy = 0, oz = 0, tmax = 0;
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static) reduction(+ : E, mx, my, mz, ox, oy, oz) reduction(max : tmax)
+  for (int64_t i = 0; i < N; ++i) {
+    const double* v = e + 3 * i;
+    double h[3], g[3];
+    hfield(m, i, e, h);
+    onsite_grad(m, i, v, g);
+    E += 0.5 * (v[0] * g[0] + v[1] * g[1] + v[2] * g[2]) - (v[0] * h[0] + v[1] * h[1] + v[2] * h[2]) -
+         MU_B * m->mu[i] * (v[0] * m->B[0] + v[1] * m->B[1] + v[2] * m->B[2]);
+    mx += v[0];
+    my += v[1];
+    mz += v[2];
+    const double s = signs ? signs[i] : 1.0;
+    ox += s * v[0];
+    oy += s * v[1];
+    oz += s * v[2];
+    if (!(m->pinned && m->pinned[i])) {
+      const double inv = 1.0 / (m->mu[i] * MU_B);
+      const double bx = (2 * h[0] - g[0]) * inv + m->B[0];
+      const double by = (2 * h[1] - g[1]) * inv + m->B[1];
+      const double bz = (2 * h[2] - g[2]) * inv + m->B[2];
+      const double tx = v[1] * bz - v[2] * by, ty = v[2] * bx - v[0] * bz, tz = v[0] * by - v[1] * bx;
+      const double t = sqrt(tx * tx + ty * ty + tz * tz);
+      if (t > tmax) tmax = t;
+    }
+  }
+  out[0] = E;
+  out[1] = mx;
+  out[2] = my;
+  out[3] = mz;
+  out[4] = ox;
+  out[5] = oy;
+  out[6] = oz;
+  out[7] = tmax;
+}
+
+/* ---------------------------------------------------------------- reference noise generator */
+static double ZKN[128], ZWN[128], ZFN[128];
+static int zig_ready = 0;
+
+static void zig_tables(void) {
+  /* 128-layer ziggurat for the standard normal (Marsaglia & Tsang, J. Stat. Softw. 5(8), 2000),
+   * same right-tail point and layer area as magex/fast.py:137-158 */
+  double dn = 3.442619855899, tn = dn;
+  const double vn = 9.91256303526217e-3, m1 = 2147483648.0;
+  const double q = vn / exp(-0.5 * dn * dn);
+  ZKN[0] = (dn / q) * m1;
+  ZKN[1] = 0.0;
+  ZWN[0] = q / m1;
+  ZWN[127] = dn / m1;
+  ZFN[0] = 1.0;
+  ZFN[127] = exp(-0.5 * dn * dn);
+  for (int i = 126; i >= 1; --i) {
+    dn = sqrt(-2.0 * log(vn / dn + exp(-0.5 * dn * dn)));
+    ZKN[i + 1] = (dn / tn) * m1;
+    tn = dn;
+    ZFN[i] = exp(-0.5 * dn * dn);
+    ZWN[i] = dn / m1;
+  }
+  zig_ready = 1;
+}
+
+static inline uint64_t xs_next(uint64_t* s) {
+  uint64_t x = *s;
+  x ^= x >> 12;
+  x ^= x << 25;
+  x ^= x >> 27;
+  *s = x;
+  return x * 2685821657736338717ULL;
+}
+
+static inline double xs_unif(uint64_t* s) { return (double)(xs_next(s) >> 11) * (1.0 / 9007199254740992.0); }
+
+static inline int64_t xs_hz(uint64_t* s) { return (int64_t)(int32_t)(uint32_t)(xs_next(s) >> 32); }
+
+static double znorm(uint64_t* s) {
+  int64_t hz = xs_hz(s);
+  int64_t iz = hz & 127;
+  if ((double)llabs(hz) < ZKN[iz]) return (double)hz * ZWN[iz];
+  const double r = 3.442619855899;
+  for (;;) {
+    double x = (double)hz * ZWN[iz];
+    if (iz == 0) {
+      double y;
+      do {
+        double u = xs_unif(s);
+        x = -log(u > 1e-300 ? u : 1e-300) * 0.2904764;
+        u = xs_unif(s);
+        y = -log(u > 1e-300 ? u : 1e-300);
+      } while (!(y + y >= x * x));
+      return hz > 0 ? r + x : -r - x;
+    }
+    if (ZFN[iz] + xs_unif(s) * (ZFN[iz - 1] - ZFN[iz]) < exp(-0.5 * x * x)) return x;
+    hz = xs_hz(s);
+    iz = hz & 127;
+    if ((double)llabs(hz) < ZKN[iz]) return (double)hz * ZWN[iz];
+  }
+}
+
+/* out[i, c] = scale[i] * N(0,1) over nc fixed chunks (stream c owns chunk c), pinned sites 0:
+ * magex/fast.py:189-200.  The draws do not depend on the number of threads. */
+void oracle_gauss3(double* out, uint64_t* states, int nc, const double* scale, const uint8_t* pinned, int64_t N,
+                   int nthreads) {
+  if (!zig_ready) zig_tables();
+  const int64_t chunk = (N + nc - 1) / nc;
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < nc; ++c) {
+    const int64_t lo = (int64_t)c * chunk, hi = lo + chunk < N ? lo + chunk : N;
+    for (int64_t i = lo; i < hi; ++i)
+      for (int comp = 0; comp < 3; ++comp) {
+        const double g = znorm(&states[c]);
+        out[3 * i + comp] = (pinned && pinned[i]) ? 0.0 : scale[i] * g;
+      }
+  }
+}
+
+/* ---------------------------------------------------------------- neighbour list for a stencil */
+/* Per-site neighbour list of a periodic / open supercell in magex site order, neighbours in the
+ * given coupling order (cell offsets R, sublattices src -> dst, coupling type typ_of_bond).
+ * ptr must hold N+1 entries; nbr / typ hold ptr[N] entries (call once with nbr == NULL to size). */
+int64_t oracle_stencil_csr(int ns, const int32_t* L, const int32_t* pbc, int nbond, const int32_t* src,
+                           const int32_t* dst, const int32_t* R, const int32_t* typ_of_bond, int64_t* ptr,
+                           int32_t* nbr, int32_t* typ) {
+  const int64_t ncell = (int64_t)L[0] * L[1] * L[2], N = ncell * ns;
+  ptr[0] = 0;
+  for (int64_t site = 0; site < N; ++site) {
+    const int64_t cell = site / ns;
+    const int s = (int)(site - cell * ns);
+    const int c[3] = {(int)(cell / ((int64_t)L[1] * L[2])), (int)((cell / L[2]) % L[1]), (int)(cell % L[2])};
+    int64_t n = ptr[site];
+    for (int b = 0; b < nbond; ++b) {
+      if (src[b] != s) continue;
+      int t[3], ok = 1;
+      for (int a = 0; a < 3; ++a) {
+        int x = c[a] + R[3 * b + a];
+        if (pbc[a]) {
+          x %= L[a];
+          if (x < 0) x += L[a];
+        } else if (x < 0 || x >= L[a]) {
+          ok = 0;
+        }
+        t[a] = x;
+      }
+      if (!ok) continue;
+      if (nbr) {
+        nbr[n] = (int32_t)(((((int64_t)t[0] * L[1] + t[1]) * L[2]) + t[2]) * ns + dst[b]);
+        typ[n] = typ_of_bond[b];
+      }
+      ++n;
+    }
+    ptr[site + 1] = n;
+  }
+  return ptr[N];
+}

@@ -1,0 +1,212 @@
+"""Python side of the CPU oracle (liboracle.so, built from oracle/heun_ref.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg, never by the magex_gb300 package.
+
+``OracleLLG`` restates magex's LLG step on the CPU: the Heun / Depondt predictor-corrector of
+magex/fast.py:336-390 (operation order of the reference's fused kernels, which it shows to agree
+with the NumPy path magex/llg.py:216-227 to 1e-12), the thermal amplitude of magex/llg.py:106-122
+and the observables of magex/spinmodel.py:475-484,517-519 and magex/llg.py:250-252,265.
+
+Noise modes: "host" draws ``numpy.random.default_rng(seed).normal(size=(N, 3))`` per step exactly
+like magex's NumPy path; "ziggurat" ports magex's numba generator (xorshift64* + ziggurat,
+magex/fast.py:123-200,683-688), used to time the CPU baseline.
+
+Parity of this oracle with the reference is pinned by tests/test_oracle_golden.py against
+trajectories generated by the reference itself (tests/golden/make_golden.py).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+MU_B = 5.7883818060e-2
+K_B = 8.617333262e-2
+GAMMA = 0.1760859630
+
+_dp = C.POINTER(C.c_double)
+
+
+class _Model(C.Structure):
+    _fields_ = [("N", C.c_int64), ("ptr", C.POINTER(C.c_int64)), ("nbr", C.POINTER(C.c_int32)),
+                ("typ", C.POINTER(C.c_int32)), ("table", _dp), ("width", C.c_int32), ("A", _dp), ("mu", _dp),
+                ("B", C.c_double * 3), ("pinned", C.POINTER(C.c_uint8))]
+
+
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so with the Makefile next to this file (gcc, OpenMP)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "heun_ref.c")):
+        r = subprocess.run(["make", "-C", HERE, "-B" if force else "all"], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(LIB)
+        lib.oracle_step.argtypes = [C.POINTER(_Model), _dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
+        lib.oracle_step.restype = None
+        lib.oracle_observables.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, C.c_int]
+        lib.oracle_observables.restype = None
+        lib.oracle_gauss3.argtypes = [_dp, C.POINTER(C.c_uint64), C.c_int, _dp, C.POINTER(C.c_uint8), C.c_int64, C.c_int]
+        lib.oracle_gauss3.restype = None
+        lib.oracle_max_threads.restype = C.c_int
+        ip = C.POINTER(C.c_int32)
+        lib.oracle_stencil_csr.argtypes = [C.c_int, ip, ip, C.c_int, ip, ip, ip, ip, C.POINTER(C.c_int64), ip, ip]
+        lib.oracle_stencil_csr.restype = C.c_int64
+        _lib = lib
+    return _lib
+
+
+def max_threads():
+    return int(load().oracle_max_threads())
+
+
+def _p(a, t=_dp):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def stencil_csr(sc):
+    """magex-order per-site neighbour list of a Supercell built by the C helper (fast at 10^6-10^7
+    sites).  Every stencil coupling is its own table type; neighbours keep the coupling order."""
+    lib = load()
+    ip = C.POINTER(C.c_int32)
+    L = np.array(sc.L, np.int32)
+    pbc = np.array(sc.pbc, np.int32)
+    src = np.ascontiguousarray(sc.bond_src, np.int32)
+    dst = np.ascontiguousarray(sc.bond_dst, np.int32)
+    R = np.ascontiguousarray(sc.bond_R, np.int32).reshape(-1)
+    typ_of = np.arange(len(src), dtype=np.int32)
+    ptr = np.zeros(sc.N + 1, np.int64)
+    nnz = lib.oracle_stencil_csr(sc.ns, _p(L, ip), _p(pbc, ip), len(src), _p(src, ip), _p(dst, ip), _p(R, ip),
+                                 _p(typ_of, ip), _p(ptr, C.POINTER(C.c_int64)), None, None)
+    nbr = np.zeros(nnz, np.int32)
+    typ = np.zeros(nnz, np.int32)
+    lib.oracle_stencil_csr(sc.ns, _p(L, ip), _p(pbc, ip), len(src), _p(src, ip), _p(dst, ip), _p(R, ip),
+                           _p(typ_of, ip), _p(ptr, C.POINTER(C.c_int64)), _p(nbr, ip), _p(typ, ip))
+    return ptr, nbr, typ, np.ascontiguousarray(sc.table, np.float64), sc.width
+
+
+class OracleLLG:
+    """CPU restatement of magex LLGSolver (heun / depondt) on a Supercell.
+
+    csr="blocks" uses Supercell.neighbour_csr() (magex's sorted, merged block list: closest to the
+    reference summation order); csr="stencil" uses the C builder (for large supercells).
+    """
+
+    def __init__(self, sc, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
+                 integrator="heun", noise="host", threads=0, csr="blocks"):
+        self.lib = load()
+        self.sc = sc
+        N = sc.N
+        if csr == "blocks":
+            ptr, nbr, typ, table = sc.neighbour_csr()
+            width = 9
+        else:
+            ptr, nbr, typ, table, width = stencil_csr(sc)
+        self._arrays = dict(ptr=np.ascontiguousarray(ptr, np.int64), nbr=np.ascontiguousarray(nbr, np.int32),
+                            typ=np.ascontiguousarray(typ, np.int32), table=np.ascontiguousarray(table, np.float64))
+        A = sc.A if sc.has_A else None
+        self._arrays["A"] = None if A is None else np.ascontiguousarray(A, np.float64).reshape(-1)
+        self._arrays["mu"] = np.ascontiguousarray(sc.mu, np.float64)
+        pin = None if sc.pinned is None else np.ascontiguousarray(np.asarray(sc.pinned, bool), np.uint8)
+        self._arrays["pinned"] = pin
+        m = _Model()
+        m.N = N
+        m.ptr = _p(self._arrays["ptr"], C.POINTER(C.c_int64))
+        m.nbr = _p(self._arrays["nbr"], C.POINTER(C.c_int32))
+        m.typ = _p(self._arrays["typ"], C.POINTER(C.c_int32))
+        m.table = _p(self._arrays["table"])
+        m.width = width
+        m.A = _p(self._arrays["A"])
+        m.mu = _p(self._arrays["mu"])
+        m.B[:] = [float(x) for x in sc.B]
+        m.pinned = _p(pin, C.POINTER(C.c_uint8))
+        self._m = m
+        a = getattr(sc, "alpha_site", None)
+        al = np.asarray(a if (a is not None and np.isscalar(alpha)) else alpha, float)
+        if al.ndim and a is not None and np.isscalar(alpha):
+            al = np.where(np.isnan(al), float(alpha), al)
+        self.alpha = al
+        self._alpha_arr = np.ascontiguousarray(np.broadcast_to(al, (N,)), np.float64)
+        self.dt = float(dt)
+        self.T = float(temperature)
+        self.rng = np.random.default_rng(seed)
+        self.precession = bool(precession)
+        self.depondt = integrator == "depondt"
+        if integrator not in ("heun", "depondt"):
+            raise ValueError("oracle implements heun and depondt")
+        self.noise = noise
+        self.threads = int(threads)
+        self.time = 0.0
+        self._ep = np.empty((N, 3))
+        self._k1 = np.empty((N, 3))
+        self._b = np.empty((N, 3))
+        if noise == "ziggurat":
+            ss = np.random.SeedSequence(int(seed) if seed is not None else None)
+            st = ss.generate_state(256, dtype=np.uint64)
+            st[st == 0] = np.uint64(0x9E3779B97F4A7C15)
+            self._streams = np.ascontiguousarray(st)
+
+    def sigma(self):
+        sc = self.sc
+        sT = getattr(sc, "site_T", None)
+        T = self.T if sT is None else np.where(np.isnan(sT), self.T, sT)
+        return np.sqrt(2.0 * self.alpha * K_B * T / (GAMMA * sc.mu * MU_B * self.dt))
+
+    def noisy(self):
+        return self.T > 0 or getattr(self.sc, "site_T", None) is not None
+
+    def thermal_field(self):
+        """(N,3) b in tesla, or None at T = 0 (no draw), as magex/llg.py:106-122."""
+        if not self.noisy():
+            return None
+        sig = np.ascontiguousarray(np.broadcast_to(self.sigma(), (self.sc.N,)), np.float64)
+        if self.noise == "host":
+            b = sig[:, None] * self.rng.normal(size=(self.sc.N, 3))
+            if self.sc.pinned is not None:
+                b[np.asarray(self.sc.pinned, bool)] = 0.0
+            return np.ascontiguousarray(b)
+        pin = self._arrays["pinned"]
+        self.lib.oracle_gauss3(_p(self._b), self._streams.ctypes.data_as(C.POINTER(C.c_uint64)), 256, _p(sig),
+                               _p(pin, C.POINTER(C.c_uint8)), self.sc.N, self.threads)
+        return self._b
+
+    def step(self, e):
+        """One step; returns a new (N,3) array (the input is left unchanged)."""
+        out = np.array(e, dtype=np.float64, order="C", copy=True)
+        self.step_inplace(out)
+        return out
+
+    def step_inplace(self, e, b="draw"):
+        self._m.B[:] = [float(x) for x in self.sc.B]
+        if isinstance(b, str):
+            b = self.thermal_field()
+        self.lib.oracle_step(C.byref(self._m), _p(self._alpha_arr), self.dt, int(self.precession), int(self.depondt),
+                             _p(b), _p(e), _p(self._ep), _p(self._k1), self.threads)
+        self.time += self.dt
+        return e
+
+    def observables(self, e):
+        e = np.ascontiguousarray(e, np.float64)
+        out = np.zeros(8)
+        sg = np.ascontiguousarray(self.sc.signs, np.float64)
+        self._m.B[:] = [float(x) for x in self.sc.B]
+        self.lib.oracle_observables(C.byref(self._m), _p(e), _p(sg), _p(out), self.threads)
+        return out
+
+    def row(self, e):
+        o = self.observables(e)
+        N = self.sc.N
+        return [self.time, o[0] / N, o[1] / N, o[2] / N, o[3] / N, float(np.linalg.norm(o[4:7]) / N), float(o[7])]

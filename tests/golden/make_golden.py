@@ -1,0 +1,167 @@
+"""Generate the golden fixtures of the LLG path by running the reference (magex) itself.
+
+Run in a container where the reference source tree is available (read-only is fine):
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/magex
+
+It imports magex from that tree and writes, next to this file:
+  models.json      magex make_model dicts and the load_results coupling lists of a set of models
+  llg_golden.npz   LLGSolver trajectories (NumPy Heun / Depondt path, the reference's own stream of
+                   thermal noise), observables, run() tables and topological charges
+
+The fixtures are inputs and outputs of the reference, not data of any public benchmark; every model
+is a seeded synthetic lattice.  numpy / scipy versions are recorded in the npz.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))      # the repo, for the bcc model generator
+
+
+def main(ref_root):
+    sys.path.insert(0, ref_root)
+    import scipy
+    from magex import models as RM
+    from magex import spinmodel as RS
+    from magex import texture as RT
+    from magex.llg import LLGSolver
+    from magex.structure import apply_structure
+    from magex_gb300.workloads import bcc_two_site_model
+
+    tmp = tempfile.mkdtemp()
+    out = {"numpy_version": np.array(np.__version__), "scipy_version": np.array(scipy.__version__)}
+    models = {}
+
+    def uc_of(name, d):
+        p = os.path.join(tmp, name + ".json")
+        with open(p, "w") as f:
+            json.dump(d, f)
+        uc = RS.load_results(p)
+        models[name] = dict(
+            model=d,
+            couplings=[[int(i), int(j), [int(x) for x in R], np.asarray(J).tolist()] for i, j, R, J in uc.couplings],
+            A=np.asarray(uc.A).tolist(), moments=np.asarray(uc.moments).tolist(),
+            signs=np.asarray(uc.signs).tolist(),
+            info={k: uc.info[k] for k in ("rcut", "nn_distance", "shells", "ncouplings_per_cell", "J0_fraction")})
+        return uc
+
+    # ---------------------------------------------------------------- models (make_model kwargs)
+    kw_cases = {
+        "sc": dict(lattice="sc", a=3.0, J=[1.0], moment=2.0),
+        "sc_dmi": dict(lattice="sc", J=[1.0], D=0.1, K=0.05),
+        "sc_two_shell": dict(lattice="sc", J=[1.0, 0.3], D=0.1, K=0.05),
+        "sc_afm": dict(lattice="sc", J=[-1.0], order="afm"),
+        "sc_open": dict(lattice="sc", J=[1.0], D=0.2, K=0.1),
+        "tri": dict(lattice="triangular", a=3.0, J=[1.0], D=0.3, dmi="interfacial", K=0.05, moment=2.0),
+        "tri_two_shell": dict(lattice="triangular", J=[1.0, 0.2], D=0.3, K=0.1),
+        "honeycomb_bulk": dict(lattice="honeycomb", J=[1.0, 0.1, 0.05], D=0.2, dmi="bulk"),
+        "bcc1": dict(lattice="bcc", J=[1.0, 0.3]),
+        "fcc_jani": dict(lattice="fcc", J=[1.0], Jani=[[0.01, 0, 0], [0, 0.02, 0], [0, 0, -0.03]]),
+        "kagome": dict(lattice="kagome", J=[1.0], D=0.1),
+    }
+    ucs = {}
+    for name, kw in kw_cases.items():
+        models[name + "__kwargs"] = kw
+        ucs[name] = uc_of(name, RM.make_model(**kw))
+    ucs["bcc2"] = uc_of("bcc2", bcc_two_site_model(J=(20.0, 10.0, -1.0), seed=0))
+    ucs["bcc2_shell4"] = uc_of("bcc2_shell4", bcc_two_site_model(J=(20.0, 10.0, -1.0, 1.0), dmi_frac=0.05,
+                                                                 per="shell", seed=1))
+
+    # ---------------------------------------------------------------- trajectories
+    def traj(tag, uc, L, pbc, B, alpha, dt, T, seed, steps, keep, integrator="heun", init_seed=None,
+             structure=None, run_every=None):
+        s = RS.SpinSystem(uc, L, pbc, B)
+        if structure:
+            apply_structure(s, structure)
+        e = s.init_spins("random", seed=seed if init_seed is None else init_seed)
+        sol = LLGSolver(s, alpha, dt, T, seed, integrator=integrator)
+        out[f"{tag}/e0"] = e.copy()
+        for n in range(1, steps + 1):
+            e = sol.step(e)
+            if n in keep:
+                out[f"{tag}/e{n}"] = e.copy()
+        out[f"{tag}/energy"] = np.array(s.energy(e))
+        out[f"{tag}/order"] = np.array(s.order_parameter(e))
+        out[f"{tag}/torque"] = np.array(sol.max_torque(e))
+        out[f"{tag}/field"] = s.effective_field(e)
+        if run_every:
+            s2 = RS.SpinSystem(uc, L, pbc, B)
+            if structure:
+                apply_structure(s2, structure)
+            sol2 = LLGSolver(s2, alpha, dt, T, seed, integrator=integrator)
+            _, tab, _ = sol2.run(out[f"{tag}/e0"].copy(), steps, output_every=run_every)
+            out[f"{tag}/table"] = tab
+        meta = dict(L=list(L), pbc=[bool(x) for x in pbc], B=list(map(float, B)), alpha=alpha, dt=dt, T=T, seed=seed,
+                    steps=steps, keep=sorted(keep), integrator=integrator, structure=structure, run_every=run_every,
+                    init_seed=seed if init_seed is None else init_seed)
+        models["traj__" + tag] = meta
+
+    # config-1 workload: sc 16^3, J = 1 meV, mu = 2, alpha 0.1, dt 0.1 fs, T = 0, 1000 steps
+    traj("sc16", ucs["sc"], (16, 16, 16), (1, 1, 1), (0, 0, 0), 0.1, 1e-4, 0.0, 1, 1000, {1, 10, 100, 1000},
+         run_every=100)
+    # thermal, the reference's own noise stream (default_rng(seed).normal per step)
+    traj("sc6_thermal", ucs["sc_dmi"], (6, 6, 6), (1, 1, 1), (0.1, 0, 0.5), 0.2, 1e-3, 50.0, 5, 20, {1, 5, 20},
+         run_every=5)
+    # config-2 Hamiltonian on a 4^3 copy: full tensors, DMI, SIA, Zeeman, T = 300 K
+    traj("bcc2_thermal", ucs["bcc2"], (4, 4, 4), (1, 1, 1), (0, 0, 0.5), 0.05, 1e-4, 300.0, 7, 20, {1, 20})
+    traj("bcc2_T0", ucs["bcc2"], (4, 4, 4), (1, 1, 1), (0, 0, 0.5), 0.05, 1e-4, 0.0, 8, 100, {1, 100},
+         run_every=25)
+    traj("bcc2_shell4", ucs["bcc2_shell4"], (4, 4, 4), (1, 1, 1), (0, 0, 0.2), 0.05, 1e-4, 600.0, 9, 10, {10})
+    # config-4 Hamiltonian on a 16x16 copy (T = 0, alpha 0.3, B_z = 2 T)
+    traj("tri16", ucs["tri"], (16, 16, 1), (1, 1, 0), (0, 0, 2.0), 0.3, 1e-4, 0.0, 4, 200, {1, 200}, run_every=50)
+    # Depondt (magex tests/cuda_sim_check.py model), T = 0 and T > 0
+    traj("sc_depondt", ucs["sc_dmi"], (4, 4, 3), (1, 1, 1), (0.1, 0, 0.5), 0.2, 1e-3, 0.0, 1, 20, {1, 20},
+         integrator="depondt")
+    traj("tri_depondt_thermal", ucs["tri"], (8, 8, 1), (1, 1, 0), (0, 0, 2.0), 0.3, 1e-3, 10.0, 2, 20, {20},
+         integrator="depondt")
+    # edge cases: open boundaries, self-image folding and repeated neighbours, AFM two-sublattice cell
+    traj("sc_open", ucs["sc_open"], (5, 5, 4), (0, 0, 0), (0.2, 0, 2.0), 0.1, 1e-3, 0.0, 2, 20, {20})
+    traj("sc_tiny_fold", ucs["sc_two_shell"], (1, 2, 3), (1, 1, 1), (0, 0, 0.3), 0.1, 1e-3, 5.0, 2, 20, {20})
+    traj("sc_afm", ucs["sc_afm"], (3, 3, 3), (1, 1, 1), (0, 0, 0), 0.5, 2e-3, 0.0, 2, 50, {50}, run_every=10)
+    traj("honeycomb", ucs["honeycomb_bulk"], (6, 5, 1), (1, 1, 0), (0, 0.1, 0.3), 0.1, 1e-3, 3.0, 3, 10, {10})
+    # structure: per-material damping and temperature, pinned bottom layer, site temperature profile
+    st = dict(materials=[dict(name="bulk", alpha=0.3, T=40.0)], pinned=[dict(region="bottom", layers=1,
+                                                                                  direction=[0, 0, 1])],
+              temperature_profile=dict(axis="x", T0=5.0, T1=30.0))
+    traj("sc_structure", ucs["sc_dmi"], (6, 6, 4), (1, 1, 1), (0, 0, 0.5), 0.1, 1e-3, 10.0, 6, 10, {10},
+         structure=st)
+    # Larmor precession of one free spin (magex tests/test_spindyn.py:36-45)
+    s = RS.SpinSystem(uc_of("free", RM.make_model("sc", J=[0.0])), (1, 1, 1), field=(0, 0, 2.0))
+    sol = LLGSolver(s, alpha=0.0, dt=1e-3)
+    e = np.array([[1.0, 0, 0]])
+    ph = []
+    for _ in range(1000):
+        e = sol.step(e)
+        ph.append(np.arctan2(e[0, 1], e[0, 0]))
+    out["larmor/e1000"] = e
+    out["larmor/phase"] = np.unwrap(np.array(ph))
+
+    # ---------------------------------------------------------------- topological charge
+    s = RS.SpinSystem(ucs["tri"], (30, 30, 1), (1, 1, 0))
+    c = s.positions[:, :2].mean(0)
+    r = s.positions[:, :2] - c
+    R = np.linalg.norm(r, axis=1)
+    th = np.pi * np.exp(-(R / 8.0) ** 2)
+    ph = np.arctan2(r[:, 1], r[:, 0])
+    e = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)
+    out["topo/skyrmion_e"] = e
+    out["topo/skyrmion_Q"] = np.array(RT.topological_charge(s, e))
+    e2 = s.init_spins("random", seed=11)
+    out["topo/random_e"] = e2
+    out["topo/random_Q"] = np.array(RT.topological_charge(s, e2))
+
+    np.savez_compressed(os.path.join(HERE, "llg_golden.npz"), **out)
+    with open(os.path.join(HERE, "models.json"), "w") as f:
+        json.dump(models, f)
+    print("wrote", os.path.join(HERE, "llg_golden.npz"), os.path.join(HERE, "models.json"))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

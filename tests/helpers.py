@@ -1,0 +1,50 @@
+"""Shared helpers of the test-suite: rebuild the golden systems with the GB300 host model."""
+import numpy as np
+
+from magex_gb300.lattice import Supercell
+from magex_gb300.spinmodel import load_results
+
+
+def golden_supercell(golden_models, tag):
+    """Supercell + trajectory metadata of golden trajectory `tag` (structure edits applied)."""
+    meta = golden_models["traj__" + tag]
+    model_name = {
+        "sc16": "sc", "sc6_thermal": "sc_dmi", "bcc2_thermal": "bcc2", "bcc2_T0": "bcc2", "bcc2_shell4": "bcc2_shell4",
+        "tri16": "tri", "sc_depondt": "sc_dmi", "tri_depondt_thermal": "tri", "sc_open": "sc_open",
+        "sc_tiny_fold": "sc_two_shell", "sc_afm": "sc_afm", "honeycomb": "honeycomb_bulk", "sc_structure": "sc_dmi",
+    }[tag]
+    uc = load_results(golden_models[model_name]["model"])
+    sc = Supercell(uc, meta["L"], meta["pbc"], meta["B"])
+    if meta.get("structure"):
+        apply_structure_subset(sc, meta["structure"])
+    return sc, meta
+
+
+def apply_structure_subset(sc, st):
+    """The parts of magex.structure.apply_structure that the golden case uses (magex/structure.py):
+    one bulk material with alpha and T (:172-179), a pinned bottom layer with a direction (:198-207)
+    and a linear temperature profile along x that fills sites without a material T (:208-225)."""
+    for m in st.get("materials", []):
+        if "alpha" in m:
+            sc.alpha_site = np.full(sc.N, float(m["alpha"]))
+        if "T" in m:
+            sc.site_T = np.full(sc.N, float(m["T"]))
+    cells = np.repeat(np.stack(np.meshgrid(*[np.arange(n) for n in sc.L], indexing="ij"), -1).reshape(-1, 3), sc.ns, 0)
+    for p in st.get("pinned", []):
+        n = int(p.get("layers", 1))
+        z = cells[:, 2]
+        sel = z < z.min() + n
+        if sc.pinned is None:
+            sc.pinned = np.zeros(sc.N, bool)
+            sc.pinned_dir = sc.ref.copy()
+        sc.pinned |= sel
+        if "direction" in p:
+            d = np.asarray(p["direction"], float)
+            sc.pinned_dir[sel] = d / np.linalg.norm(d)
+    tp = st.get("temperature_profile")
+    if tp:
+        P = sc.positions
+        u = (P[:, 0] - P[:, 0].min()) / max(np.ptp(P[:, 0]), 1e-9)
+        prof = float(tp["T0"]) + (float(tp["T1"]) - float(tp["T0"])) * u
+        sc.site_T = prof if sc.site_T is None else np.where(np.isnan(sc.site_T), prof, sc.site_T)
+    return sc

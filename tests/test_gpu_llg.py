@@ -1,0 +1,171 @@
+"""GB300 LLG kernels (through the C ABI) against the reference's golden trajectories and the oracle.
+
+Tolerances: spins are unit vectors, so max |e_gpu - e_ref| is a relative error.  Per step the
+kernels may differ from the reference by 1e-12 (floating-point summation order and fused
+multiply-adds), accumulated linearly; after 1000 T = 0 steps by at most 1e-9.
+"""
+import numpy as np
+import pytest
+import torch
+
+from helpers import golden_supercell
+
+pytestmark = pytest.mark.gpu
+
+TRAJ = ["sc16", "sc6_thermal", "bcc2_thermal", "bcc2_T0", "bcc2_shell4", "tri16", "sc_depondt", "tri_depondt_thermal",
+        "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb", "sc_structure"]
+
+
+def _solver(golden_models, tag, noise="host"):
+    from magex_gb300.llg import GB300LLG
+    sc, meta = golden_supercell(golden_models, tag)
+    sol = GB300LLG(sc, meta["alpha"], meta["dt"], meta["T"], meta["seed"], integrator=meta["integrator"], noise=noise)
+    return sc, meta, sol
+
+
+@pytest.mark.parametrize("tag", TRAJ)
+def test_trajectory_matches_reference(cuda, golden, golden_models, tag):
+    sc, meta, sol = _solver(golden_models, tag)
+    e = golden[f"{tag}/e0"].copy()
+    for n in range(1, meta["steps"] + 1):
+        e = sol.step(e)
+        if n in meta["keep"]:
+            err = np.abs(e - golden[f"{tag}/e{n}"]).max()
+            assert err <= min(1e-9, 1e-12 * n + 1e-13), (tag, n, err)
+    assert abs(sol.energy(e) - float(golden[f"{tag}/energy"])) <= 1e-12 * max(1.0, abs(float(golden[f"{tag}/energy"])))
+    assert abs(sol.max_torque(e) - float(golden[f"{tag}/torque"])) <= 1e-10 * max(1.0, float(golden[f"{tag}/torque"]))
+    B = sol.effective_field(e)
+    ref_B = golden[f"{tag}/field"]
+    assert np.abs(B - ref_B).max() <= 1e-12 * max(1.0, np.abs(ref_B).max())
+
+
+def test_sc16_1000_steps_device_resident(cuda, golden, golden_models):
+    """Config-1 workload: 1000 T = 0 steps kept on the device (one library call), <= 1e-9."""
+    from magex_gb300.llg import GB300LLG
+    sc, meta = golden_supercell(golden_models, "sc16")
+    sol = GB300LLG(sc, meta["alpha"], meta["dt"], 0.0, meta["seed"])
+    lat = sol.model.to_lattice(golden["sc16/e0"])
+    sol.run_lattice(lat, 1000)
+    e = sol.model.from_lattice(lat).cpu().numpy()
+    assert np.abs(e - golden["sc16/e1000"]).max() <= 1e-9
+    assert abs(sol.time - 0.1) < 1e-12
+
+
+@pytest.mark.parametrize("tag", ["sc16", "sc6_thermal", "bcc2_T0", "tri16", "sc_afm"])
+def test_run_table_matches_reference(cuda, golden, golden_models, tag):
+    sc, meta, sol = _solver(golden_models, tag)
+    e, tab, snaps = sol.run(golden[f"{tag}/e0"].copy(), meta["steps"], output_every=meta["run_every"], snapshots=2)
+    ref = golden[f"{tag}/table"]
+    assert tab.shape == ref.shape
+    assert np.allclose(tab[:, :6], ref[:, :6], rtol=1e-11, atol=1e-12)
+    assert np.allclose(tab[:, 6], ref[:, 6], rtol=1e-9, atol=1e-10)
+    assert len(snaps) == 3 and snaps[0][1].shape == (sc.N, 3)
+
+
+def test_oracle_agrees_on_bcc_32cube_thermal_host_noise(cuda):
+    """Config-2 Hamiltonian at 32^3 (65,536 spins), T = 300 K, identical host noise: GPU vs oracle."""
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    from oracle import OracleLLG
+    sc = bcc_two_site(L=32)
+    e0 = sc.init_spins("random", seed=3)
+    gpu = GB300LLG(sc, 0.05, 1e-4, 300.0, 11, noise="host")
+    ora = OracleLLG(sc, 0.05, 1e-4, 300.0, 11, csr="stencil")
+    a, b = e0.copy(), e0.copy()
+    for n in range(1, 6):
+        a = gpu.step(a)
+        b = ora.step(b)
+        assert np.abs(a - b).max() <= 1e-12 * n
+    assert abs(gpu.energy(a) - ora.observables(b)[0]) <= 1e-12 * abs(ora.observables(b)[0])
+
+
+def test_full_size_bcc_128cube_properties(cuda):
+    """Config-2 lattice at full size (4,194,304 spins): parity with the oracle for 2 T = 0 steps, unit
+    norm after Philox steps, and bit-identical repeat of a seeded Philox run."""
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    from oracle import OracleLLG
+    sc = bcc_two_site(L=128)
+    e0 = sc.init_spins("random", seed=5)
+    gpu = GB300LLG(sc, 0.05, 1e-4, 0.0, 1)
+    ora = OracleLLG(sc, 0.05, 1e-4, 0.0, 1, csr="stencil")
+    a = gpu.step(gpu.step(e0))
+    b = ora.step(ora.step(e0))
+    assert np.abs(a - b).max() <= 2e-12
+    del ora
+    runs = []
+    for _ in range(2):
+        sol = GB300LLG(sc, 0.05, 1e-4, 300.0, 123)
+        lat = sol.model.to_lattice(e0)
+        sol.run_lattice(lat, 20)
+        runs.append(lat.clone())
+    assert torch.equal(runs[0], runs[1])
+    norm = torch.linalg.vector_norm(runs[0], dim=0)
+    assert float((norm - 1).abs().max()) < 1e-14
+
+
+def test_topological_charge(cuda, golden):
+    from magex_gb300.device import DeviceModel
+    from magex_gb300.workloads import triangle_list, triangular_film
+    sc = triangular_film(L=30, field=(0, 0, 0))
+    dm = DeviceModel(sc)
+    dm.set_triangles(*triangle_list(sc))
+    for key in ("skyrmion", "random"):
+        Q = float(dm.topological_charge(dm.to_lattice(golden[f"topo/{key}_e"])).item())
+        assert abs(Q - float(golden[f"topo/{key}_Q"])) < 1e-9, key
+
+
+def test_larmor_precession(cuda, golden, golden_models):
+    from magex_gb300.constants import GAMMA
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    sc = Supercell(load_results(golden_models["free"]["model"]), (1, 1, 1), field=(0, 0, 2.0))
+    sol = GB300LLG(sc, alpha=0.0, dt=1e-3)
+    e = np.array([[1.0, 0, 0]])
+    ph = []
+    for _ in range(1000):
+        e = sol.step(e)
+        ph.append(np.arctan2(e[0, 1], e[0, 0]))
+    assert np.abs(e - golden["larmor/e1000"]).max() < 1e-12
+    w = np.polyfit(np.arange(1, 1001) * 1e-3, np.unwrap(ph), 1)[0]
+    assert abs(abs(w) - GAMMA * 2.0) / (GAMMA * 2.0) < 1e-6
+
+
+def test_philox_thermal_equilibrium_langevin(cuda):
+    """Free spins in a field at T > 0 with in-kernel Philox noise relax to the classical Langevin
+    magnetisation <m_z> = coth(x) - 1/x, x = mu mu_B B / (k_B T) (the reference's test
+    tests/test_spindyn.py:77-89 checks the same law with Monte Carlo)."""
+    from magex_gb300.constants import K_B, MU_B
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results, make_model
+    sc = Supercell(load_results(make_model("sc", J=[0.0], moment=2.0)), (16, 16, 16), field=(0, 0, 5.0))
+    T = 5.0
+    sol = GB300LLG(sc, alpha=0.5, dt=1e-3, temperature=T, seed=9)
+    lat = sol.model.to_lattice(sc.init_spins("random", seed=1))
+    sol.run_lattice(lat, 8000)
+    ms = []
+    for _ in range(40):
+        sol.run_lattice(lat, 500)
+        ms.append(float(lat[2].mean()))
+    x = 2.0 * MU_B * 5.0 / (K_B * T)
+    assert abs(np.mean(ms) - (1 / np.tanh(x) - 1 / x)) < 0.01
+
+
+def test_invalid_inputs_raise(cuda, golden_models):
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    sc = Supercell(load_results(golden_models["sc"]["model"]), (4, 4, 4))
+    with pytest.raises(ValueError):
+        GB300LLG(sc, dt=-1.0)
+    with pytest.raises(ValueError):
+        GB300LLG(sc, integrator="leapfrog")
+    with pytest.raises(NotImplementedError):
+        GB300LLG(sc, integrator="rk4")
+    with pytest.raises(NotImplementedError):
+        GB300LLG(sc, thermostat="quantum")
+    sol = GB300LLG(sc)
+    with pytest.raises(ValueError):
+        sol.step(np.zeros((3, 3)))
