@@ -139,6 +139,7 @@ class DeviceModel:
         self._B = np.array(sc.B, float)
         self._obs = torch.empty(8, dtype=torch.float64, device=self.device)
         self._tri = None
+        self.field_owner = None
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -151,8 +152,10 @@ class DeviceModel:
 
     # ------------------------------------------------------------------ state sync
     def sync_field(self):
-        """Push a changed external field (SpinSystem.set_field) to the device model."""
-        B = np.asarray(self.sc.B, float)
+        """Push a changed external field (SpinSystem.set_field) to the device model.  The field is
+        read from ``field_owner`` (the magex SpinSystem a solver was built from) when set."""
+        owner = self.field_owner if self.field_owner is not None else self.sc
+        B = np.asarray(owner.B, float).reshape(3)
         if not np.array_equal(B, self._B):
             arr = (C.c_double * 3)(*[float(x) for x in B])
             _lib.check(self.lib.mgx_model_set_field(self.handle, arr), "mgx_model_set_field")
@@ -195,7 +198,11 @@ class DeviceModel:
     def set_triangles(self, tri_sites, orient):
         """Triangle list (magex site indices, (T, 3)) and orientation signs for topological charge."""
         sc = self.sc
-        tri = np.asarray(tri_sites, np.int64)
+        tri = np.asarray(tri_sites, np.int64).reshape(-1, 3)
+        if tri.size and (tri.min() < 0 or tri.max() >= sc.N):
+            raise ValueError("triangle vertices must be site indices in [0, N)")
+        if len(np.asarray(orient).reshape(-1)) != len(tri):
+            raise ValueError("one orientation sign per triangle")
         cell, s = tri // sc.ns, tri % sc.ns
         lat_idx = (s * sc.ncell + cell).astype(np.int32)
         self._tri = torch.as_tensor(np.ascontiguousarray(lat_idx.reshape(-1)), device=self.device)

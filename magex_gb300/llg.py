@@ -60,6 +60,8 @@ class GB300LLG:
         self.sys = system
         self.sc = supercell_from_system(system)
         self.model = DeviceModel(self.sc, device)
+        if system is not self.sc:
+            self.model.field_owner = system          # follow SpinSystem.set_field (magex/llg.py:327)
         self.device = self.model.device
         N = self.sc.N
         a = getattr(self.sc, "alpha_site", None)
