@@ -132,6 +132,27 @@ mgx_status mgx_llg_run(mgx_llg* plan, double* e, int64_t nsteps, uint64_t step0,
  * as magex's slab decomposition does (magex/mpi_spin.py:160-174: _fused1, halo(ep), _fused2, halo(e)). */
 mgx_status mgx_llg_stage(mgx_llg* plan, int32_t stage, double* e, const double* noise, uint64_t step, void* stream);
 
+/* ---------------------------------------------------------------- step without allocation
+ * No counterpart in the reference.  One Heun / Depondt step like mgx_llg_step, for callers that
+ * cannot allocate GPU memory while they step: a host framework that owns all device memory through
+ * its own pool and only hands the plugin its input and output buffers, a loop captured into a CUDA
+ * graph in global capture mode (where cudaMalloc is not allowed), or a real-time loop that must not
+ * wait on the allocator.  It needs no plan: the predictor scratch (ep, k1) and the per-sublattice
+ * constants live in one static device array of 64 + 6 * MGX_NOALLOC_MAX_SITES doubles (12 MiB) that
+ * every GPU loading the library holds until the process exits; the call itself allocates nothing.
+ *   - m: a model from mgx_model_create (created beforehand) with at most MGX_NOALLOC_MAX_SITES sites;
+ *     larger models are rejected with MGX_ERR_INVALID.
+ *   - p: dt, uniform alpha (p->alpha_site must be NULL), precession, integrator, noise mode, seed.
+ *   - sigma_sub: host [ns] thermal amplitudes (read during the call), required unless p->noise is
+ *     MGX_NOISE_NONE; e, noise and step as for mgx_llg_step.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress, with that
+ * device current); make that first call before any stream capture begins.  All calls on a device
+ * share the array, which keeps the last call's contents: calls whose GPU work overlaps (other
+ * streams or host threads) race on it and must be serialised by the caller. */
+#define MGX_NOALLOC_MAX_SITES 262144
+mgx_status mgx_llg_step_noalloc(const mgx_model* m, const mgx_llg_params* p, const double* sigma_sub, double* e,
+                                const double* noise, uint64_t step, void* stream);
+
 /* ---------------------------------------------------------------- observables
  * Writes 8 doubles to out (device):
  *   [0] E total (meV)  = sum_i e.A.e - e.h - mu_B mu e.B      (magex/spinmodel.py:475-484)

@@ -17,6 +17,7 @@ HEUN, DEPONDT = 0, 1
 NOISE_NONE, NOISE_HOST, NOISE_PHILOX = 0, 1, 2
 MAX_SUBLATTICES = 16
 MAX_BONDS = 256
+NOALLOC_MAX_SITES = 262144
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -57,6 +58,8 @@ SIGNATURES = {
     "mgx_llg_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]),
     "mgx_llg_stage": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "mgx_measure_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
+    "mgx_llg_step_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(LLGParams), _dp, C.c_void_p, C.c_void_p, C.c_uint64,
+                                         C.c_void_p]),
     "mgx_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_effective_field": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,

@@ -63,6 +63,35 @@ struct Model {
   int partial_cap = 0;           // number of 8-double slots
 };
 
+// ------------------------------------------------------------------ LLG plan (mgx_llg.cu)
+struct DevLLG {
+  double dt, half_dt;
+  int precession;
+  int noise;
+  int integrator;
+  uint64_t seed;
+  const double* alpha_sub;   // [ns]
+  const double* pre_sub;     // [ns]  -gamma / (1 + alpha^2)
+  const double* sigma_sub;   // [ns]
+  const double* alpha_site;  // [N] or nullptr
+  const double* pre_site;    // [N] or nullptr
+  const double* sigma_site;  // [N] or nullptr
+  double* ep;                // [3][N] predicted spins
+  double* k1;                // [3][N] predictor slope (Heun) or rotation rate (Depondt)
+};
+
+struct LLGPlan {
+  const Model* model;
+  DevLLG p;
+  void* sub_block = nullptr;     // alpha_sub | pre_sub | sigma_sub
+  double* site_block = nullptr;  // alpha_site | pre_site
+  double* sigma_site = nullptr;
+  double* scratch = nullptr;     // ep | k1
+};
+
+// Enqueue the predictor (stages & 1) and / or the corrector (stages & 2) of one step on st.
+void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
+
 // ------------------------------------------------------------------ small device helpers
 __device__ __forceinline__ void site_coords(const DevLattice& L, long long q, int& s, int& c0, int& c1, int& c2) {
   s = (int)(q / L.ncell);

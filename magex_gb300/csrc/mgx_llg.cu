@@ -12,31 +12,6 @@
 
 namespace mgx {
 
-struct DevLLG {
-  double dt, half_dt;
-  int precession;
-  int noise;
-  int integrator;
-  uint64_t seed;
-  const double* alpha_sub;   // [ns]
-  const double* pre_sub;     // [ns]  -gamma / (1 + alpha^2)
-  const double* sigma_sub;   // [ns]
-  const double* alpha_site;  // [N] or nullptr
-  const double* pre_site;    // [N] or nullptr
-  const double* sigma_site;  // [N] or nullptr
-  double* ep;                // [3][N] predicted spins
-  double* k1;                // [3][N] predictor slope (Heun) or rotation rate (Depondt)
-};
-
-struct LLGPlan {
-  const Model* model;
-  DevLLG p;
-  void* sub_block = nullptr;     // alpha_sub | pre_sub | sigma_sub
-  double* site_block = nullptr;  // alpha_site | pre_site
-  double* sigma_site = nullptr;
-  double* scratch = nullptr;     // ep | k1
-};
-
 // magex site number of lattice index q (layout-independent Philox counter)
 __device__ __forceinline__ uint64_t magex_site(const DevLattice& L, long long q, int s) {
   return (uint64_t)(q - (long long)s * L.ncell) * (uint64_t)L.ns + (uint64_t)s;
@@ -178,8 +153,8 @@ static void dispatch_noise(const LLGPlan* pl, double* e, const double* noise, ui
   }
 }
 
-static void enqueue_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st,
-                         int stages = 3) {
+void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st,
+                      int stages) {
   switch (pl->model->d.width) {
     case 1: dispatch_noise<1>(pl, e, noise, step, stages, st); break;
     case 4: dispatch_noise<4>(pl, e, noise, step, stages, st); break;
@@ -307,7 +282,7 @@ mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t st
   if (!pl || !e) return set_error(MGX_ERR_INVALID, "mgx_llg_step: null argument");
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step: host-noise plan needs a noise buffer");
-  enqueue_step(pl, e, noise, step, (cudaStream_t)stream);
+  enqueue_llg_step(pl, e, noise, step, (cudaStream_t)stream, 3);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }
@@ -318,7 +293,7 @@ mgx_status mgx_llg_stage(mgx_llg* pp, int32_t stage, double* e, const double* no
   if (stage != 0 && stage != 1) return set_error(MGX_ERR_INVALID, "stage %d is not 0 (predictor) or 1 (corrector)", stage);
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
     return set_error(MGX_ERR_INVALID, "mgx_llg_stage: host-noise plan needs a noise buffer");
-  enqueue_step(pl, e, noise, step, (cudaStream_t)stream, stage == 0 ? 1 : 2);
+  enqueue_llg_step(pl, e, noise, step, (cudaStream_t)stream, stage == 0 ? 1 : 2);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }
@@ -329,7 +304,7 @@ mgx_status mgx_llg_run(mgx_llg* pp, double* e, int64_t nsteps, uint64_t step0, v
   if (nsteps < 0) return set_error(MGX_ERR_INVALID, "nsteps must be >= 0");
   if (pl->p.noise == MGX_NOISE_HOST)
     return set_error(MGX_ERR_INVALID, "mgx_llg_run: host-noise plans step one at a time (mgx_llg_step)");
-  for (int64_t n = 0; n < nsteps; ++n) enqueue_step(pl, e, nullptr, step0 + (uint64_t)n, (cudaStream_t)stream);
+  for (int64_t n = 0; n < nsteps; ++n) enqueue_llg_step(pl, e, nullptr, step0 + (uint64_t)n, (cudaStream_t)stream, 3);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }
