@@ -27,6 +27,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -162,6 +164,60 @@ def read_ncu_traffic():
     return out
 
 
+def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None):
+    """Uneven-film ensemble: 256 triangular films L in {32, 48, ..., 256}, J1 = 1 meV, interfacial DMI
+    D/J = 0.3, K = 0.05 meV, B_z ~ U[0, 3] T, T ~ U[0, 20] K, alpha 0.1, dt 0.1 fs, Philox, seeded.
+    Times the batched form (one persistent launch per stage, graph replays, autotuned launch shape)
+    against per-system plain plans (one GB300LLG per film, each running its steps in one call)."""
+    import torch
+    from magex_gb300.batched import BatchedLLG
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import film_ensemble, triangle_list, triangular_film
+    spec = film_ensemble(n=nsys, seed=0)
+    films = [triangular_film(L=s["L"], field=s["B"]) for s in spec]
+    Ts = [s["T"] for s in spec]
+    seeds = list(range(1, nsys + 1))
+    e0 = [sc.init_spins("random", seed=k) for k, sc in enumerate(films)]
+    ens = BatchedLLG(films, 0.1, 1e-4, Ts, seeds)
+    ens.set_spins(e0)
+    ens.set_triangles([triangle_list(sc) for sc in films])
+    best, timings = ens.autotune(steps=3)
+    ntot = ens.ntot
+    stream = torch.cuda.current_stream()
+    ens.run(50, graph_chunk=50)                        # capture + warm-up
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    ens.run(K_batch, graph_chunk=50)
+    b.record(stream)
+    b.synchronize()
+    t_batch = a.elapsed_time(b) * 1e-3
+    rows = ens.rows()
+    Q = ens.topological_charge()
+    sols = [GB300LLG(sc, 0.1, 1e-4, Ts[k], seeds[k]) for k, sc in enumerate(films)]
+    lats = [sol.model.to_lattice(e0[k]) for k, sol in enumerate(sols)]
+    for sol, lat in zip(sols, lats):
+        sol.run_lattice(lat, 2)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for sol, lat in zip(sols, lats):
+        sol.run_lattice(lat, K_plain)
+    b.record(stream)
+    b.synchronize()
+    t_plain = a.elapsed_time(b) * 1e-3
+    v_batch = ntot * K_batch / t_batch
+    v_plain = ntot * K_plain / t_plain
+    return {"workload": f"{nsys} triangular films, L in {{32,48,...,256}} (uneven, {ntot:,} spins in total), "
+                        "J1=1 meV, interfacial DMI D/J=0.3, K=0.05 meV, B_z~U[0,3] T, T~U[0,20] K, alpha 0.1, "
+                        "dt 0.1 fs, Philox, FP64",
+            "value": v_batch, "unit": UNIT, "steps": K_batch, "plain_value": v_plain, "plain_steps": K_plain,
+            "speedup_vs_plain": v_batch / v_plain, "launch": {"threads": best[0], "ctas_per_sm": best[1]},
+            "autotune_ms_per_step": {f"{t}x{c}": round(v, 4) for (t, c), v in timings.items()},
+            "ms_per_step": 1e3 * t_batch / K_batch, "gpu_launches_per_step": 2,
+            "plain_gpu_launches_per_step": 2 * nsys,
+            "final_mean_E_per_spin": float(np.mean(rows[:, 1])), "Q_range": [float(Q.min()), float(Q.max())]}
+
+
 def run_gb300(args):
     import torch
     ws, rank, local = dist_env()
@@ -273,6 +329,8 @@ def run_gb300(args):
         "gpu_launches": 2 * K,
         "clocks": clocks,
     }
+    if ws == 1 and not args.no_batched:
+        line["batched"] = bench_batched()
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -291,6 +349,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--L", type=int, default=128, help="bcc cells per side (default: the 128^3 workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

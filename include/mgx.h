@@ -51,6 +51,7 @@ enum { MGX_NOISE_NONE = 0, MGX_NOISE_HOST = 1, MGX_NOISE_PHILOX = 2 };
 
 typedef struct mgx_model mgx_model;
 typedef struct mgx_llg mgx_llg;
+typedef struct mgx_batch mgx_batch;
 
 /* Supercell of a unit-cell model, described by its per-cell coupling list ("stencil").
  * Replaces the 3N x 3N CSR matrix of magex/spinmodel.py:240 and the per-site neighbour blocks of
@@ -131,6 +132,36 @@ mgx_status mgx_llg_run(mgx_llg* plan, double* e, int64_t nsteps, uint64_t step0,
  * corrector (reads ep, k1 and e, writes e).  For callers that exchange halos between the stages,
  * as magex's slab decomposition does (magex/mpi_spin.py:160-174: _fused1, halo(ep), _fused2, halo(e)). */
 mgx_status mgx_llg_stage(mgx_llg* plan, int32_t stage, double* e, const double* noise, uint64_t step, void* stream);
+
+/* ---------------------------------------------------------------- batched ensemble
+ * Many independent systems (replicas, temperature / field scans, different lattices, uneven sizes)
+ * stepped together: one persistent launch per Heun stage over a (system, first site) tile list,
+ * optionally replayed from a CUDA graph.  The reference steps one system per LLGSolver
+ * (magex/llg.py:216-227); a batch step equals nsys such steps (the kernels share the per-site
+ * code of mgx_llg_step, so each system's result is the same as its own plan's).
+ * Spins of system k are the (3, N_k) lattice-layout block at 3 * mgx_batch_offset(b, k) doubles of
+ * one device array of 3 * mgx_batch_nsites(b) doubles.  The models must outlive the batch. */
+mgx_status mgx_batch_create(const mgx_model* const* models, const mgx_llg_params* params, int32_t nsys,
+                            mgx_batch** out);   /* params[k]: per system; uniform alpha; one noise mode and integrator */
+mgx_status mgx_batch_destroy(mgx_batch* b);
+int64_t mgx_batch_nsites(const mgx_batch* b);
+int64_t mgx_batch_offset(const mgx_batch* b, int32_t sys);        /* site offset of system sys (sys = nsys: total) */
+mgx_status mgx_batch_set_sigma(mgx_batch* b, int32_t sys, const double* sigma_sub);   /* host [ns] */
+/* Re-read every model's field (after mgx_model_set_field) into the batch. */
+mgx_status mgx_batch_sync_models(mgx_batch* b);
+/* Launch shape: threads = sites per tile and threads per CTA (64, 128, 256, 512); ctas_per_sm = resident
+ * CTAs per SM of the persistent grid (0 = one CTA per tile).  Chosen by the autotuner of magex_gb300.batched. */
+mgx_status mgx_batch_set_launch(mgx_batch* b, int32_t threads, int32_t ctas_per_sm);
+mgx_status mgx_batch_step(mgx_batch* b, double* e, const double* noise, uint64_t step, void* stream);
+/* nsteps steps (noise NONE or PHILOX) from step index step0; graph_chunk > 0 captures graph_chunk steps
+ * into a CUDA graph once (per spin pointer and launch shape) and replays it. */
+mgx_status mgx_batch_run(mgx_batch* b, double* e, int64_t nsteps, uint64_t step0, int32_t graph_chunk, void* stream);
+/* Per-system observables: out (device) [nsys*8], 8 values per system as mgx_observables. */
+mgx_status mgx_batch_observables(mgx_batch* b, const double* e, double* out, void* stream);
+/* Per-system triangle lists for the topological charge: tri (host) [3*ntri] lattice indices local to each
+ * system, orient (host) [ntri], tri_off (host) [nsys+1] triangle offsets (tri_off[0] = 0). */
+mgx_status mgx_batch_set_triangles(mgx_batch* b, const int32_t* tri, const double* orient, const int64_t* tri_off);
+mgx_status mgx_batch_topological_charge(mgx_batch* b, const double* e, double* out, void* stream);  /* out [nsys] */
 
 /* ---------------------------------------------------------------- step without allocation
  * No counterpart in the reference.  One Heun / Depondt step like mgx_llg_step, for callers that

@@ -60,6 +60,18 @@ SIGNATURES = {
     "mgx_measure_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
     "mgx_llg_step_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(LLGParams), _dp, C.c_void_p, C.c_void_p, C.c_uint64,
                                          C.c_void_p]),
+    "mgx_batch_create": (C.c_int32, [C.POINTER(C.c_void_p), C.POINTER(LLGParams), C.c_int32, C.POINTER(C.c_void_p)]),
+    "mgx_batch_destroy": (C.c_int32, [C.c_void_p]),
+    "mgx_batch_nsites": (C.c_int64, [C.c_void_p]),
+    "mgx_batch_offset": (C.c_int64, [C.c_void_p, C.c_int32]),
+    "mgx_batch_set_sigma": (C.c_int32, [C.c_void_p, C.c_int32, _dp]),
+    "mgx_batch_sync_models": (C.c_int32, [C.c_void_p]),
+    "mgx_batch_set_launch": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32]),
+    "mgx_batch_step": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "mgx_batch_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_int32, C.c_void_p]),
+    "mgx_batch_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_batch_set_triangles": (C.c_int32, [C.c_void_p, _ip, _dp, C.POINTER(C.c_int64)]),
+    "mgx_batch_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_effective_field": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,

@@ -8,119 +8,22 @@
 #include <cmath>
 #include <vector>
 
-#include "mgx_internal.cuh"
+#include "mgx_step.cuh"
 
 namespace mgx {
-
-// magex site number of lattice index q (layout-independent Philox counter)
-__device__ __forceinline__ uint64_t magex_site(const DevLattice& L, long long q, int s) {
-  return (uint64_t)(q - (long long)s * L.ncell) * (uint64_t)L.ns + (uint64_t)s;
-}
-
-// Rodrigues rotation of (x,y,z) by the rotation vector w (angle |w|), magex/fast.py:271-282
-__device__ __forceinline__ void rotate(double& x, double& y, double& z, double wx, double wy, double wz) {
-  const double th = sqrt(wx * wx + wy * wy + wz * wz);
-  if (th < 1e-14) return;
-  const double kx = wx / th, ky = wy / th, kz = wz / th;
-  double s, c;
-  sincos(th, &s, &c);
-  const double kd = kx * x + ky * y + kz * z;
-  const double cx = ky * z - kz * y, cy = kz * x - kx * z, cz = kx * y - ky * x;
-  const double omc = 1.0 - c;
-  const double nx = x * c + cx * s + kx * kd * omc;
-  const double ny = y * c + cy * s + ky * kd * omc;
-  const double nz = z * c + cz * s + kz * kd * omc;
-  x = nx;
-  y = ny;
-  z = nz;
-}
-
-template <int NOISE>
-__device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P, const double* __restrict__ noise,
-                                            long long q, int s, uint64_t step, double& bx, double& by, double& bz) {
-  if (NOISE == MGX_NOISE_NONE) return;
-  const double sig = P.sigma_site ? __ldg(P.sigma_site + q) : __ldg(P.sigma_sub + s);
-  double g0, g1, g2;
-  if (NOISE == MGX_NOISE_HOST) {
-    g0 = __ldg(noise + q);
-    g1 = __ldg(noise + L.N + q);
-    g2 = __ldg(noise + 2 * L.N + q);
-  } else {
-    philox_normal3(P.seed, magex_site(L, q, s), step, g0, g1, g2);
-  }
-  bx = fma(sig, g0, bx);
-  by = fma(sig, g1, by);
-  bz = fma(sig, g2, bz);
-}
 
 template <int W, int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_predict(const DevLattice L, const DevLLG P, const double* __restrict__ e,
                                                  const double* __restrict__ noise, uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= L.N) return;
-  const long long N = L.N;
-  const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
-  if (L.pinned && L.pinned[q]) {
-    P.ep[q] = ex; P.ep[N + q] = ey; P.ep[2 * N + q] = ez;
-    P.k1[q] = 0.0; P.k1[N + q] = 0.0; P.k1[2 * N + q] = 0.0;
-    return;
-  }
-  int s, c0, c1, c2;
-  site_coords(L, q, s, c0, c1, c2);
-  double bx, by, bz;
-  effective_field<W>(L, e, q, s, c0, c1, c2, ex, ey, ez, bx, by, bz);
-  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
-  const double a = P.alpha_site ? __ldg(P.alpha_site + q) : __ldg(P.alpha_sub + s);
-  const double pre = P.pre_site ? __ldg(P.pre_site + q) : __ldg(P.pre_sub + s);
-  double fx, fy, fz;
-  llg_rhs(ex, ey, ez, bx, by, bz, a, pre, P.precession != 0, fx, fy, fz);
-  if (INTEG == MGX_INTEGRATOR_DEPONDT) {
-    // rotation rate w = e x f (de/dt = w x e for a tangent f); the rotated predictor is used
-    // without renormalisation, as magex/fast.py:284-288,359-362 and magex/llg.py:237-238
-    const double wx = ey * fz - ez * fy, wy = ez * fx - ex * fz, wz = ex * fy - ey * fx;
-    double x = ex, y = ey, z = ez;
-    rotate(x, y, z, P.dt * wx, P.dt * wy, P.dt * wz);
-    P.ep[q] = x; P.ep[N + q] = y; P.ep[2 * N + q] = z;
-    P.k1[q] = wx; P.k1[N + q] = wy; P.k1[2 * N + q] = wz;
-    return;
-  }
-  const double x = fma(P.dt, fx, ex);
-  const double y = fma(P.dt, fy, ey);
-  const double z = fma(P.dt, fz, ez);
-  const double r = rsqrt(x * x + y * y + z * z);
-  P.ep[q] = x * r; P.ep[N + q] = y * r; P.ep[2 * N + q] = z * r;
-  P.k1[q] = fx; P.k1[N + q] = fy; P.k1[2 * N + q] = fz;
+  if (q < L.N) predict_site<W, NOISE, INTEG>(L, P, e, noise, q, step);
 }
 
 template <int W, int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_correct(const DevLattice L, const DevLLG P, double* __restrict__ e,
                                                  const double* __restrict__ noise, uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= L.N) return;
-  if (L.pinned && L.pinned[q]) return;
-  const long long N = L.N;
-  int s, c0, c1, c2;
-  site_coords(L, q, s, c0, c1, c2);
-  const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
-  double bx, by, bz;
-  effective_field<W>(L, P.ep, q, s, c0, c1, c2, px, py, pz, bx, by, bz);
-  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
-  const double a = P.alpha_site ? __ldg(P.alpha_site + q) : __ldg(P.alpha_sub + s);
-  const double pre = P.pre_site ? __ldg(P.pre_site + q) : __ldg(P.pre_sub + s);
-  double fx, fy, fz;
-  llg_rhs(px, py, pz, bx, by, bz, a, pre, P.precession != 0, fx, fy, fz);
-  const double k1x = P.k1[q], k1y = P.k1[N + q], k1z = P.k1[2 * N + q];
-  double x = e[q], y = e[N + q], z = e[2 * N + q];
-  if (INTEG == MGX_INTEGRATOR_DEPONDT) {
-    const double wx = py * fz - pz * fy, wy = pz * fx - px * fz, wz = px * fy - py * fx;
-    rotate(x, y, z, P.half_dt * (k1x + wx), P.half_dt * (k1y + wy), P.half_dt * (k1z + wz));
-  } else {
-    x = fma(P.half_dt, k1x + fx, x);
-    y = fma(P.half_dt, k1y + fy, y);
-    z = fma(P.half_dt, k1z + fz, z);
-  }
-  const double r = rsqrt(x * x + y * y + z * z);
-  e[q] = x * r; e[N + q] = y * r; e[2 * N + q] = z * r;
+  if (q < L.N) correct_site<W, NOISE, INTEG>(L, P, e, noise, q, step);
 }
 
 // stages: bit 0 = predictor, bit 1 = corrector

@@ -3,23 +3,12 @@
 // block over the per-block partials), so the sums do not depend on scheduling.
 #include <cmath>
 
-#include "mgx_internal.cuh"
+#include "mgx_observe.cuh"
 
 namespace mgx {
 
 constexpr int OBS_TPB = 256;
-constexpr int OBS_NV = 8;
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ double warp_max(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
 
 // Per site: E_i = e.A.e - e.h - mu_B mu e.B (magex/spinmodel.py:475-484), e, s e, |e x B_eff|.
 template <int W>
@@ -27,46 +16,7 @@ __global__ void __launch_bounds__(OBS_TPB) k_observe(const DevLattice L, const d
                                                      double* __restrict__ partial) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v[OBS_NV] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (q < L.N) {
-    const long long N = L.N;
-    const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
-    int s, c0, c1, c2;
-    site_coords(L, q, s, c0, c1, c2);
-    double hx, hy, hz;
-    exchange_field<W>(L, e, s, c0, c1, c2, hx, hy, hz);
-    double Ae[3] = {0.0, 0.0, 0.0};
-    if (L.has_A) {
-      double a[9];
-      if (L.A_site) {
-        for (int k = 0; k < 9; ++k) a[k] = L.A_site[(long long)k * N + q];
-      } else {
-        for (int k = 0; k < 9; ++k) a[k] = L.A_sub[s * 9 + k];
-      }
-      Ae[0] = a[0] * ex + a[1] * ey + a[2] * ez;
-      Ae[1] = a[3] * ex + a[4] * ey + a[5] * ez;
-      Ae[2] = a[6] * ex + a[7] * ey + a[8] * ez;
-    }
-    const double mu = L.mu_site ? L.mu_site[q] : L.mu_sub[s];
-    const double inv = L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s];
-    const double eAe = ex * Ae[0] + ey * Ae[1] + ez * Ae[2];
-    const double eh = ex * hx + ey * hy + ez * hz;
-    const double eB = ex * L.B0 + ey * L.B1 + ez * L.B2;
-    v[0] = eAe - eh - 5.7883818060e-2 * mu * eB;
-    v[1] = ex;
-    v[2] = ey;
-    v[3] = ez;
-    const double sg = L.sign_sub[s];
-    v[4] = sg * ex;
-    v[5] = sg * ey;
-    v[6] = sg * ez;
-    if (!(L.pinned && L.pinned[q])) {
-      const double bx = (2.0 * hx - 2.0 * Ae[0]) * inv + L.B0;
-      const double by = (2.0 * hy - 2.0 * Ae[1]) * inv + L.B1;
-      const double bz = (2.0 * hz - 2.0 * Ae[2]) * inv + L.B2;
-      const double tx = ey * bz - ez * by, ty = ez * bx - ex * bz, tz = ex * by - ey * bx;
-      v[7] = sqrt(tx * tx + ty * ty + tz * tz);
-    }
-  }
+  if (q < L.N) observe_site<W>(L, e, q, v);
   __shared__ double red[OBS_TPB / 32][OBS_NV];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -122,7 +72,6 @@ __global__ void __launch_bounds__(256) k_field(const DevLattice L, const double*
   B[q] = bx; B[N + q] = by; B[2 * N + q] = bz;
 }
 
-// solid angle of each triangle, magex/texture.py:55-60
 __global__ void __launch_bounds__(OBS_TPB) k_solid_angle(long long N, const double* __restrict__ e,
                                                          const int* __restrict__ tri,
                                                          const double* __restrict__ orient, long long ntri,
@@ -130,13 +79,7 @@ __global__ void __launch_bounds__(OBS_TPB) k_solid_angle(long long N, const doub
   double acc = 0.0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ntri;
        t += (long long)gridDim.x * blockDim.x) {
-    const int a = tri[3 * t], b = tri[3 * t + 1], c = tri[3 * t + 2];
-    const double ax = e[a], ay = e[N + a], az = e[2 * N + a];
-    const double bx = e[b], by = e[N + b], bz = e[2 * N + b];
-    const double cx = e[c], cy = e[N + c], cz = e[2 * N + c];
-    const double num = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
-    const double den = 1.0 + (ax * bx + ay * by + az * bz) + (bx * cx + by * cy + bz * cz) + (cx * ax + cy * ay + cz * az);
-    acc += 2.0 * atan2(num, den) * orient[t];
+    acc += solid_angle(e, N, tri[3 * t], tri[3 * t + 1], tri[3 * t + 2]) * orient[t];
   }
   __shared__ double red[OBS_TPB / 32];
   acc = warp_sum(acc);
