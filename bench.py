@@ -218,6 +218,59 @@ def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None):
             "final_mean_E_per_spin": float(np.mean(rows[:, 1])), "Q_range": [float(Q.min()), float(Q.max())]}
 
 
+def bench_adjoint(L=128, nsteps=2000, seg=100):
+    """Differentiable-LLG workload: triangular 128 x 128, J1 = 1 meV, D/J = 0.3, K = 0.05 meV, B_z = 2 T,
+    T = 0, alpha 0.3, dt 0.1 fs, 2000 Heun steps, checkpoint every 100 steps; loss = sum |e(T) - target|^2.
+    Times the plain forward (GB300LLG), the checkpointed forward and the backward (recompute + adjoint)
+    of magex_gb300.adjoint.llg_trajectory."""
+    import torch
+    from magex_gb300.adjoint import AdjointLLG, llg_trajectory
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import film_parameter_basis, triangular_film, uniaxial_sia
+    sc = triangular_film(L=L, field=(0, 0, 2.0))
+    S = torch.as_tensor(film_parameter_basis(sc))
+    adj = AdjointLLG(sc, alpha=0.3, dt=1e-4, seg_steps=seg)
+    e0 = sc.init_spins("random", seed=1)
+    target = torch.as_tensor(sc.init_spins("random", seed=2), device=adj.device)
+    plain = GB300LLG(sc, 0.3, 1e-4, 0.0, 1)
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+
+    def once(record):
+        theta = torch.tensor([1.0, 0.3], dtype=torch.float64, requires_grad=True)
+        T = theta[0] * torch.eye(3, dtype=torch.float64)[None] + theta[1] * S
+        A = torch.as_tensor(uniaxial_sia(0.05))[None]
+        B = torch.tensor([0.0, 0.0, 2.0], dtype=torch.float64)
+        lat = plain.model.to_lattice(e0)
+        e = torch.as_tensor(e0, device=adj.device).requires_grad_(True)
+        torch.cuda.synchronize()
+        if record:
+            ev[0].record(stream)
+        plain.run_lattice(lat, nsteps)
+        if record:
+            ev[1].record(stream)
+        eT = llg_trajectory(adj, e, T, A, B, nsteps)
+        loss = ((eT - target) ** 2).sum()
+        if record:
+            ev[2].record(stream)
+        loss.backward()
+        if record:
+            ev[3].record(stream)
+        torch.cuda.synchronize()
+        return theta.grad
+
+    once(False)
+    g = once(True)
+    t_plain = ev[0].elapsed_time(ev[1])
+    t_fwd = ev[1].elapsed_time(ev[2])
+    t_bwd = ev[2].elapsed_time(ev[3])
+    return {"workload": f"triangular {L}x{L} film, J1=1 meV, D/J=0.3, K=0.05 meV, B_z=2 T, T=0, alpha 0.3, "
+                        f"dt 0.1 fs, {nsteps} Heun steps, checkpoint every {seg}, loss sum|e(T)-target|^2, FP64",
+            "forward_plain_ms": t_plain, "forward_checkpointed_ms": t_fwd, "backward_ms": t_bwd,
+            "adjoint_over_forward": t_bwd / t_plain, "gradient_total_over_forward": (t_fwd + t_bwd) / t_plain,
+            "grad_J1_D": [float(x) for x in g]}
+
+
 def run_gb300(args):
     import torch
     ws, rank, local = dist_env()
@@ -331,6 +384,8 @@ def run_gb300(args):
     }
     if ws == 1 and not args.no_batched:
         line["batched"] = bench_batched()
+    if ws == 1 and not args.no_adjoint:
+        line["adjoint"] = bench_adjoint()
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -350,6 +405,7 @@ def main():
     ap.add_argument("--L", type=int, default=128, help="bcc cells per side (default: the 128^3 workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

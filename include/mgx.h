@@ -52,6 +52,7 @@ enum { MGX_NOISE_NONE = 0, MGX_NOISE_HOST = 1, MGX_NOISE_PHILOX = 2 };
 typedef struct mgx_model mgx_model;
 typedef struct mgx_llg mgx_llg;
 typedef struct mgx_batch mgx_batch;
+typedef struct mgx_adjoint mgx_adjoint;
 
 /* Supercell of a unit-cell model, described by its per-cell coupling list ("stencil").
  * Replaces the 3N x 3N CSR matrix of magex/spinmodel.py:240 and the per-site neighbour blocks of
@@ -105,6 +106,11 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
 mgx_status mgx_model_destroy(mgx_model* m);
 mgx_status mgx_model_set_field(mgx_model* m, const double B[3]);   /* SpinSystem.set_field, magex/spinmodel.py:451-452 */
 int64_t mgx_model_nsites(const mgx_model* m);
+/* Replace the coupling tensors (host [nbond*width], the order given at creation) or the
+ * per-sublattice single-ion tensors (host [ns*9]); synchronous.  Used to evaluate a trajectory at new
+ * parameters (magex rebuilds FastModel after editing couplings, magex/fast.py:631). */
+mgx_status mgx_model_set_couplings(mgx_model* m, const double* bond_table);
+mgx_status mgx_model_set_onsite(mgx_model* m, const double* A_sub);
 
 /* (N,3) magex-order device array <-> lattice-layout device array (3*N doubles each). */
 mgx_status mgx_pack_spins(const mgx_model* m, const double* aos, double* lat, void* stream);
@@ -162,6 +168,33 @@ mgx_status mgx_batch_observables(mgx_batch* b, const double* e, double* out, voi
  * system, orient (host) [ntri], tri_off (host) [nsys+1] triangle offsets (tri_off[0] = 0). */
 mgx_status mgx_batch_set_triangles(mgx_batch* b, const int32_t* tri, const double* orient, const int64_t* tri_off);
 mgx_status mgx_batch_topological_charge(mgx_batch* b, const double* e, double* out, void* stream);  /* out [nsys] */
+
+/* ---------------------------------------------------------------- adjoint of the Heun step
+ * No counterpart in the reference (magex has no gradients).  Reverse-mode derivative of a Heun
+ * trajectory (noise NONE or PHILOX, uniform alpha, per-sublattice single-ion tensors):
+ *   mgx_adjoint_forward  recomputes nsteps (<= seg_steps) steps from e0 (device, lattice layout),
+ *                        storing e, ep and both total fields of every step (a checkpointed segment);
+ *                        writes the final spins to e_out when not NULL;
+ *   mgx_adjoint_backward maps ebar = dL/de(end of segment) to dL/de(start of segment) in place and adds
+ *                        the segment's parameter gradients to per-site accumulators;
+ *   mgx_adjoint_grads    sums the accumulators into out (device) [9*ngroups + 9*ns + 3]:
+ *                        dL/dT_g (row-major 3x3 per coupling group g), dL/dA (component-major:
+ *                        out[9G + k*ns + s] = dL/dA_s[k]), dL/dB.
+ * fwd is the forward stencil model (width 9); rev is the reverse stencil: for every forward coupling
+ * (i -> j, R, J) one coupling (j -> i, -R, J^T) of the same supercell, in an order grouped by receiving
+ * sublattice and then by (rev_group, rev_transposed).  rev_group[b] names the parameter tensor T_g that
+ * the forward coupling uses, rev_transposed[b] = 1 when that coupling is T_g^T.  */
+mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const int32_t* rev_group,
+                              const int32_t* rev_transposed, int32_t ngroups, const mgx_llg_params* p,
+                              int32_t seg_steps, mgx_adjoint** out);
+mgx_status mgx_adjoint_destroy(mgx_adjoint* a);
+mgx_status mgx_adjoint_set_sigma(mgx_adjoint* a, const double* sigma_sub);
+mgx_status mgx_adjoint_sync_models(mgx_adjoint* a);      /* after mgx_model_set_couplings / _set_onsite / _set_field */
+mgx_status mgx_adjoint_forward(mgx_adjoint* a, const double* e0, int32_t nsteps, uint64_t step0, double* e_out,
+                               void* stream);
+mgx_status mgx_adjoint_backward(mgx_adjoint* a, double* ebar, void* stream);
+mgx_status mgx_adjoint_zero_grads(mgx_adjoint* a, void* stream);
+mgx_status mgx_adjoint_grads(mgx_adjoint* a, double* out, void* stream);
 
 /* ---------------------------------------------------------------- step without allocation
  * No counterpart in the reference.  One Heun / Depondt step like mgx_llg_step, for callers that

@@ -72,6 +72,17 @@ SIGNATURES = {
     "mgx_batch_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_batch_set_triangles": (C.c_int32, [C.c_void_p, _ip, _dp, C.POINTER(C.c_int64)]),
     "mgx_batch_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_model_set_couplings": (C.c_int32, [C.c_void_p, _dp]),
+    "mgx_model_set_onsite": (C.c_int32, [C.c_void_p, _dp]),
+    "mgx_adjoint_create": (C.c_int32, [C.c_void_p, C.c_void_p, _ip, _ip, C.c_int32, C.POINTER(LLGParams), C.c_int32,
+                                       C.POINTER(C.c_void_p)]),
+    "mgx_adjoint_destroy": (C.c_int32, [C.c_void_p]),
+    "mgx_adjoint_set_sigma": (C.c_int32, [C.c_void_p, _dp]),
+    "mgx_adjoint_sync_models": (C.c_int32, [C.c_void_p]),
+    "mgx_adjoint_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_uint64, C.c_void_p, C.c_void_p]),
+    "mgx_adjoint_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_adjoint_zero_grads": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "mgx_adjoint_grads": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_effective_field": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,

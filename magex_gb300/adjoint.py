@@ -1,0 +1,237 @@
+"""Differentiable LLG trajectories: the hand-written adjoint of the Heun step behind torch.autograd.
+
+    adj = AdjointLLG(sc, groups, alpha=0.3, dt=1e-4, seg_steps=100)
+    eT = llg_trajectory(adj, e0, T, A, B, nsteps=2000)       # torch tensors, autograd-aware
+    loss = ((eT - target) ** 2).sum()
+    loss.backward()                                           # e0.grad, T.grad, A.grad, B.grad
+
+The couplings of the supercell stencil are parameterised by a few 3x3 tensors ``T[g]``: coupling
+``b`` uses ``T[group[b]]`` (or its transpose when ``transposed[b]``), so physical parameters (J shells,
+DMI, anisotropic exchange) map onto ``T`` with ordinary torch operations and autograd applies the
+chain rule.  ``A`` holds the per-sublattice single-ion tensors and ``B`` the external field.
+
+The forward pass runs the trajectory in segments of ``seg_steps`` steps and keeps only the spins at
+segment starts (checkpoints).  The backward pass recomputes each segment from its checkpoint,
+storing per step e, ep and both total fields, then runs the adjoint kernels (libmgx
+``mgx_adjoint_*``) back through the segment.  Thermal (Philox) noise is regenerated bit-identically
+from (seed, site, step), so the gradient is the pathwise derivative of the same noisy trajectory.
+magex itself has no gradients; parity of this module is pinned against central finite differences
+and against torch autograd of a dense FP64 restatement (tests/test_gpu_adjoint.py).
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import GAMMA, K_B, MU_B
+from .device import DeviceModel, stream_ptr
+from .lattice import WIDTH_FULL
+from .llg import _philox_key
+
+
+class CouplingGroups:
+    """group[b], transposed[b] for every stencil coupling b, and the number of groups."""
+
+    def __init__(self, group, transposed=None, ngroups=None):
+        self.group = np.asarray(group, np.int32)
+        self.transposed = np.zeros_like(self.group) if transposed is None else np.asarray(transposed, np.int32)
+        self.ngroups = int(self.group.max()) + 1 if ngroups is None else int(ngroups)
+
+    @classmethod
+    def per_bond(cls, sc):
+        """Every coupling its own tensor (dL/dJ_b for each coupling of the unit cell)."""
+        return cls(np.arange(len(sc.bond_src)))
+
+    @classmethod
+    def per_shell(cls, sc, ndigits=4):
+        """One tensor per neighbour shell on canonical bonds (src < dst, or src == dst and R > 0) and its
+        transpose on the reverse bonds: the shell-tensor parameterisation of the bcc workloads."""
+        uc = sc.uc
+        d = []
+        for i, j, R in zip(sc.bond_src, sc.bond_dst, sc.bond_R):
+            r = uc.positions[j] + R @ uc.cell - uc.positions[i]
+            d.append(round(float(np.linalg.norm(r)), ndigits))
+        shells = sorted(set(d))
+        group = np.array([shells.index(x) for x in d], np.int32)
+        trans = np.array([0 if (i < j or (i == j and tuple(R) > (0, 0, 0))) else 1
+                          for i, j, R in zip(sc.bond_src, sc.bond_dst, sc.bond_R)], np.int32)
+        return cls(group, trans, len(shells))
+
+    def tensors_from(self, sc):
+        """T (ngroups, 3, 3) consistent with the supercell's couplings (checked)."""
+        T = np.zeros((self.ngroups, 3, 3))
+        seen = np.zeros(self.ngroups, bool)
+        for b, J in enumerate(sc.bond_J):
+            g = self.group[b]
+            Jg = J.T if self.transposed[b] else J
+            if not seen[g]:
+                T[g], seen[g] = Jg, True
+            elif np.abs(T[g] - Jg).max() > 1e-12 * max(1.0, np.abs(Jg).max()):
+                raise ValueError(f"coupling {b} does not match the tensor of its group {g}")
+        return T
+
+    def bond_tensors(self, T):
+        """(nbond, 3, 3) coupling tensors of parameter tensors T (numpy)."""
+        Tb = np.asarray(T, float)[self.group]
+        return np.where(self.transposed[:, None, None] == 1, Tb.transpose(0, 2, 1), Tb)
+
+
+def _full_width(sc):
+    v = copy.copy(sc)
+    v.width = WIDTH_FULL
+    v.table = np.ascontiguousarray(sc.bond_J.reshape(-1, 9))
+    return v
+
+
+def _reverse(sc, groups):
+    """Reverse stencil: coupling (j -> i, -R, J^T) for every forward (i -> j, R, J), ordered by receiving
+    sublattice and then (group, transposed); returns (view, order) with order[k] = forward bond of k."""
+    order = sorted(range(len(sc.bond_src)),
+                   key=lambda b: (int(sc.bond_dst[b]), int(groups.group[b]), int(groups.transposed[b]), b))
+    order = np.array(order, np.int64)
+    v = copy.copy(sc)
+    v.bond_src = np.ascontiguousarray(sc.bond_dst[order], np.int32)
+    v.bond_dst = np.ascontiguousarray(sc.bond_src[order], np.int32)
+    v.bond_R = np.ascontiguousarray(-sc.bond_R[order], np.int32)
+    v.bond_J = np.ascontiguousarray(sc.bond_J[order].transpose(0, 2, 1))
+    v.width = WIDTH_FULL
+    v.table = np.ascontiguousarray(v.bond_J.reshape(-1, 9))
+    return v, order
+
+
+class AdjointLLG:
+    """Forward / adjoint engine of Heun trajectories on one supercell (uniform alpha per run)."""
+
+    def __init__(self, sc, groups=None, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
+                 seg_steps=100, device=None):
+        if sc.alpha_site is not None or sc.site_T is not None or sc.A_site is not None:
+            raise NotImplementedError("the adjoint supports uniform damping, temperature and per-sublattice A")
+        if sc.terms or sc.has_higher:
+            raise NotImplementedError("extra energy terms are not supported by the GB300 kernels")
+        self.sc = sc
+        self.groups = CouplingGroups.per_bond(sc) if groups is None else groups
+        self.T0 = self.groups.tensors_from(sc)
+        self.fwd = DeviceModel(_full_width(sc), device)
+        rev_view, self.rev_order = _reverse(sc, self.groups)
+        self.rev = DeviceModel(rev_view, device)
+        self.device = self.fwd.device
+        self.lib = self.fwd.lib
+        self.alpha, self.dt, self.T = float(alpha), float(dt), float(temperature)
+        self.seg_steps = int(seg_steps)
+        p = _lib.LLGParams()
+        p.dt, p.alpha, p.alpha_site = self.dt, self.alpha, None
+        p.precession = int(bool(precession))
+        p.integrator = _lib.HEUN
+        p.noise = _lib.NOISE_PHILOX if self.T > 0 else _lib.NOISE_NONE
+        p.seed = _philox_key(seed)
+        rg = np.ascontiguousarray(self.groups.group[self.rev_order], np.int32)
+        rt = np.ascontiguousarray(self.groups.transposed[self.rev_order], np.int32)
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.mgx_adjoint_create(self.fwd.handle, self.rev.handle, _lib.iptr(rg), _lib.iptr(rt),
+                                                   self.groups.ngroups, C.byref(p), self.seg_steps, C.byref(h)),
+                       "mgx_adjoint_create")
+        self.handle = h
+        if self.T > 0:
+            sig = np.ascontiguousarray(np.sqrt(2.0 * self.alpha * K_B * self.T / (GAMMA * sc.mu_sub * MU_B * self.dt)))
+            _lib.check(self.lib.mgx_adjoint_set_sigma(h, _lib.dptr(sig)), "mgx_adjoint_set_sigma")
+        ns, G = sc.ns, self.groups.ngroups
+        self._grads = torch.empty(9 * G + 9 * ns + 3, dtype=torch.float64, device=self.device)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.lib.mgx_adjoint_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    # ------------------------------------------------------------------ parameters
+    def set_params(self, T, A, B):
+        """Load parameter tensors T (G,3,3), A (ns,3,3) and field B (3) into both device stencils."""
+        T = np.asarray(T, float).reshape(self.groups.ngroups, 3, 3)
+        Jf = np.ascontiguousarray(self.groups.bond_tensors(T).reshape(-1))
+        Jr = np.ascontiguousarray(self.groups.bond_tensors(T)[self.rev_order].transpose(0, 2, 1).reshape(-1))
+        A = np.ascontiguousarray(np.asarray(A, float).reshape(self.sc.ns, 9))
+        _lib.check(self.lib.mgx_model_set_couplings(self.fwd.handle, _lib.dptr(Jf)), "set_couplings")
+        _lib.check(self.lib.mgx_model_set_couplings(self.rev.handle, _lib.dptr(Jr)), "set_couplings")
+        _lib.check(self.lib.mgx_model_set_onsite(self.fwd.handle, _lib.dptr(A)), "set_onsite")
+        _lib.check(self.lib.mgx_model_set_onsite(self.rev.handle, _lib.dptr(A)), "set_onsite")
+        Bv = (C.c_double * 3)(*[float(x) for x in np.asarray(B, float).reshape(3)])
+        _lib.check(self.lib.mgx_model_set_field(self.fwd.handle, Bv), "set_field")
+        self.fwd._B = np.array(list(Bv))
+        self.fwd.sc.B = np.array(list(Bv))
+        _lib.check(self.lib.mgx_adjoint_sync_models(self.handle), "sync_models")
+
+    # ------------------------------------------------------------------ trajectory
+    def _segments(self, nsteps):
+        out, n = [], 0
+        while n < nsteps:
+            k = min(self.seg_steps, nsteps - n)
+            out.append((n, k))
+            n += k
+        return out
+
+    def forward(self, e0_lat, nsteps):
+        """Run nsteps from lattice-layout spins; returns (e_T, checkpoints at segment starts)."""
+        ckpts = []
+        cur = e0_lat.contiguous()
+        for n0, k in self._segments(int(nsteps)):
+            ckpts.append(cur)
+            nxt = torch.empty_like(cur)
+            _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(cur.data_ptr()), k, n0,
+                                                    C.c_void_p(nxt.data_ptr()), stream_ptr()), "mgx_adjoint_forward")
+            cur = nxt
+        return cur, ckpts
+
+    def backward(self, ckpts, ebar_T_lat, nsteps):
+        """dL/de_0 (lattice layout) and (dL/dT, dL/dA, dL/dB) from dL/de_T."""
+        ebar = ebar_T_lat.clone().contiguous()
+        _lib.check(self.lib.mgx_adjoint_zero_grads(self.handle, stream_ptr()), "zero_grads")
+        segs = self._segments(int(nsteps))
+        for (n0, k), ck in zip(reversed(segs), reversed(ckpts)):
+            _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(ck.data_ptr()), k, n0, None, stream_ptr()),
+                       "mgx_adjoint_forward (recompute)")
+            _lib.check(self.lib.mgx_adjoint_backward(self.handle, C.c_void_p(ebar.data_ptr()), stream_ptr()),
+                       "mgx_adjoint_backward")
+        _lib.check(self.lib.mgx_adjoint_grads(self.handle, C.c_void_p(self._grads.data_ptr()), stream_ptr()),
+                   "mgx_adjoint_grads")
+        G, ns = self.groups.ngroups, self.sc.ns
+        g = self._grads
+        gT = g[:9 * G].view(G, 3, 3).clone()
+        gA = g[9 * G:9 * G + 9 * ns].view(9, ns).t().reshape(ns, 3, 3).clone()
+        gB = g[9 * G + 9 * ns:].clone()
+        return ebar, gT, gA, gB
+
+
+class _Trajectory(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, e0, T, A, B, adj, nsteps):
+        adj.set_params(T.detach().cpu().numpy(), A.detach().cpu().numpy(), B.detach().cpu().numpy())
+        lat0 = adj.fwd.to_lattice(e0.detach())
+        eT, ckpts = adj.forward(lat0, nsteps)
+        ctx.adj, ctx.nsteps, ctx.ckpts = adj, nsteps, ckpts
+        ctx.devs = (e0.device, T.device, A.device, B.device)
+        ctx.params = (T.detach().cpu().numpy(), A.detach().cpu().numpy(), B.detach().cpu().numpy())
+        out = adj.fwd.from_lattice(eT)
+        return out.to(e0.device)
+
+    @staticmethod
+    def backward(ctx, grad_eT):
+        adj = ctx.adj
+        adj.set_params(*ctx.params)                  # the parameters may have changed since the forward
+        ebar_T = adj.fwd.to_lattice(grad_eT.detach().contiguous())
+        ebar0, gT, gA, gB = adj.backward(ctx.ckpts, ebar_T, ctx.nsteps)
+        ge0 = adj.fwd.from_lattice(ebar0)
+        d0, dT, dA, dB = ctx.devs
+        return ge0.to(d0), gT.to(dT), gA.to(dA), gB.to(dB), None, None
+
+
+def llg_trajectory(adj, e0, T, A, B, nsteps):
+    """Spins after nsteps Heun steps from e0 ((N,3) tensor), differentiable in e0, T, A and B."""
+    return _Trajectory.apply(e0, T, A, B, adj, int(nsteps))

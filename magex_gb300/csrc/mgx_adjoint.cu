@@ -1,0 +1,559 @@
+// Adjoint (reverse-mode derivative) of the stochastic Heun step, with step checkpointing.
+//
+// Forward step (magex/llg.py:216-227), per site i, with H = B_eff + b:
+//   H1 = H(e), f1 = f(e, H1), x = e + dt f1, p = x / |x|,
+//   H2 = H(p), f2 = f(p, H2), y = e + dt/2 (f1 + f2), e' = y / |y|,
+//   H(v)_i = (2 sum_j J_ij v_j - 2 A_i v_i) / (mu_i mu_B) + B + b_i,
+//   f(e, H) = pre [e x H + alpha e x (e x H)].
+// The reference has no gradients; this file supplies d loss / d e and the parameter gradients for
+// a trajectory.  Given ebar' = dL/de' one backward step is three kernels:
+//   k_adj_local   (site-local) ybar, f1bar = f2bar = dt/2 ybar, H2bar and pbar from the rhs adjoint at
+//                 (p, H2), g2 = 2 H2bar / (mu mu_B), local A term; A and B gradients of stage 2;
+//   k_adj_mid     pbar += sum_rev J^T g2 (transposed stencil gather), xbar through the normalisation,
+//                 f1bar += dt xbar, H1bar and ebar from the rhs adjoint at (e, H1), g1; J gradients of
+//                 stage 2 (g2_i (x) p_j per coupling group); A and B gradients of stage 1;
+//   k_adj_final   ebar = acc + sum_rev J^T g1; J gradients of stage 1 (g1_i (x) e_j).
+// The transposed gather uses a second stencil (the reverse couplings j -> i with J_ij^T), so the
+// adjoint is exact also when a coupling set does not satisfy J_ji = J_ij^T.
+// Parameter gradients accumulate per site (deterministic, no atomics) and are summed at the end.
+// States of a segment of steps are recomputed from a checkpoint and stored (e, p, H1, H2).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mgx_observe.cuh"
+#include "mgx_step.cuh"
+
+namespace mgx {
+
+struct AdjDev {
+  DevLattice F;           // forward stencil
+  DevLattice R;           // reverse stencil (transposed tensors), bonds sorted by (src, group, transposed)
+  const int2* group;      // [nbond_rev] (parameter group, transposed flag) of the reverse couplings
+  int ngroups;
+  double dt, half_dt;
+  double pre, alpha;      // uniform damping
+  int precession;
+  double* PG;             // [ngroups*9][N] coupling-group gradients per site
+  double* PA;             // [9][N] single-ion gradients per site
+  double* PB;             // [3][N] field gradients per site
+};
+
+struct AdjPlan {
+  const Model* fwd = nullptr;
+  const Model* rev = nullptr;
+  AdjDev d;
+  DevLLG P;               // forward parameters; ep / k1 re-pointed per step
+  int seg_cap = 0;
+  int noise = MGX_NOISE_NONE;
+  double* seg = nullptr;  // [seg_cap][4][3N]
+  double* e_end = nullptr;
+  double* work = nullptr; // eacc | pbar | f1bar | g1 | g2 (5 x 3N)
+  double* k1 = nullptr;
+  double* grads = nullptr;  // reduction output on device
+  int2* d_group = nullptr;
+  void* sub = nullptr;
+  int seg_steps = 0;
+};
+
+__device__ __forceinline__ void cross3(double ax, double ay, double az, double bx, double by, double bz, double& cx,
+                                       double& cy, double& cz) {
+  cx = ay * bz - az * by;
+  cy = az * bx - ax * bz;
+  cz = ax * by - ay * bx;
+}
+
+// rhs adjoint: given fbar, Hbar = pre [fbar x e + a e x (e x fbar)],
+// ebar = pre [H x fbar + a (c x fbar - H x (e x fbar))] with c = e x H (precession);
+// without precession the e x H terms are dropped.
+__device__ __forceinline__ void rhs_adjoint(double ex, double ey, double ez, double Hx, double Hy, double Hz,
+                                            double fbx, double fby, double fbz, double a, double pre, bool prec,
+                                            double& Hbx, double& Hby, double& Hbz, double& ebx, double& eby,
+                                            double& ebz) {
+  double ux, uy, uz;   // e x fbar
+  cross3(ex, ey, ez, fbx, fby, fbz, ux, uy, uz);
+  double wx, wy, wz;   // e x (e x fbar)
+  cross3(ex, ey, ez, ux, uy, uz, wx, wy, wz);
+  double cx, cy, cz;   // c = e x H
+  cross3(ex, ey, ez, Hx, Hy, Hz, cx, cy, cz);
+  double t1x, t1y, t1z;   // c x fbar
+  cross3(cx, cy, cz, fbx, fby, fbz, t1x, t1y, t1z);
+  double t2x, t2y, t2z;   // H x (e x fbar)
+  cross3(Hx, Hy, Hz, ux, uy, uz, t2x, t2y, t2z);
+  Hbx = a * wx; Hby = a * wy; Hbz = a * wz;
+  ebx = a * (t1x - t2x); eby = a * (t1y - t2y); ebz = a * (t1z - t2z);
+  if (prec) {
+    double hx, hy, hz;   // H x fbar
+    cross3(Hx, Hy, Hz, fbx, fby, fbz, hx, hy, hz);
+    Hbx -= ux; Hby -= uy; Hbz -= uz;      // fbar x e = -(e x fbar)
+    ebx += hx; eby += hy; ebz += hz;
+  }
+  Hbx *= pre; Hby *= pre; Hbz *= pre;
+  ebx *= pre; eby *= pre; ebz *= pre;
+}
+
+__device__ __forceinline__ void onsite_tensor(const DevLattice& L, long long q, int s, double* a) {
+  if (L.A_site) {
+    for (int k = 0; k < 9; ++k) a[k] = L.A_site[(long long)k * L.N + q];
+  } else {
+    for (int k = 0; k < 9; ++k) a[k] = L.A_sub[s * 9 + k];
+  }
+}
+
+__device__ __forceinline__ void load3(const double* x, long long N, long long q, double& a, double& b, double& c) {
+  a = x[q];
+  b = x[N + q];
+  c = x[2 * N + q];
+}
+__device__ __forceinline__ void store3(double* x, long long N, long long q, double a, double b, double c) {
+  x[q] = a;
+  x[N + q] = b;
+  x[2 * N + q] = c;
+}
+
+// Transposed gather sum_rev J^T g_nbr at site q of the reverse stencil, with the parameter-gradient
+// outer products g_nbr (x) v (v = own p or e) summed per (group, transposed) run and added to PG.
+__device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __restrict__ g, long long q, int s,
+                                               int c0, int c1, int c2, double vx, double vy, double vz,
+                                               double& ox, double& oy, double& oz) {
+  const DevLattice& L = A.R;
+  const long long N = L.N;
+  ox = oy = oz = 0.0;
+  const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
+  int cur_g = -1, cur_t = 0;
+  double sx = 0.0, sy = 0.0, sz = 0.0;
+  auto flush = [&]() {
+    if (cur_g < 0) return;
+    double* P = A.PG + (long long)cur_g * 9 * N + q;
+    const double gv[3] = {sx, sy, sz}, vv[3] = {vx, vy, vz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const double m = cur_t ? vv[a] * gv[b] : gv[a] * vv[b];
+        P[(long long)(3 * a + b) * N] += m;
+      }
+  };
+  for (int b = b0; b < b1; ++b) {
+    const int2 gr = __ldg(A.group + b);
+    if (gr.x != cur_g || gr.y != cur_t) {
+      flush();
+      cur_g = gr.x;
+      cur_t = gr.y;
+      sx = sy = sz = 0.0;
+    }
+    const int4 geo = __ldg(L.bond_geo + b);
+    int n0 = c0 + geo.y, n1 = c1 + geo.z, n2 = c2 + geo.w;
+    bool ok = true;
+    if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
+    if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
+    if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
+    if (!ok) continue;
+    const long long j = (long long)geo.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
+    const double gx = g[j], gy = g[N + j], gz = g[2 * N + j];
+    const double* T = L.bond_J + (long long)b * 9;
+    ox = fma(__ldg(T + 0), gx, ox); ox = fma(__ldg(T + 1), gy, ox); ox = fma(__ldg(T + 2), gz, ox);
+    oy = fma(__ldg(T + 3), gx, oy); oy = fma(__ldg(T + 4), gy, oy); oy = fma(__ldg(T + 5), gz, oy);
+    oz = fma(__ldg(T + 6), gx, oz); oz = fma(__ldg(T + 7), gy, oz); oz = fma(__ldg(T + 8), gz, oz);
+    sx += gx;
+    sy += gy;
+    sz += gz;
+  }
+  flush();
+}
+
+// ---------------------------------------------------------------- forward recomputation (stores states)
+template <int NOISE>
+__global__ void __launch_bounds__(256) k_fwd_pred(const DevLattice L, const DevLLG P, const double* __restrict__ e,
+                                                  uint64_t step, double* __restrict__ H1) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < L.N) predict_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H1);
+}
+
+template <int NOISE>
+__global__ void __launch_bounds__(256) k_fwd_corr(const DevLattice L, const DevLLG P, double* __restrict__ e,
+                                                  uint64_t step, double* __restrict__ H2, double* __restrict__ eout) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < L.N) correct_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H2, eout);
+}
+
+// ---------------------------------------------------------------- backward kernels
+__global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double* __restrict__ E,
+                                                   const double* __restrict__ Pp, const double* __restrict__ H1,
+                                                   const double* __restrict__ H2, const double* __restrict__ ebar,
+                                                   double* __restrict__ eacc, double* __restrict__ pbar,
+                                                   double* __restrict__ f1bar, double* __restrict__ g2) {
+  const DevLattice& L = A.F;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= L.N) return;
+  const long long N = L.N;
+  double zbx, zby, zbz;
+  load3(ebar, N, q, zbx, zby, zbz);
+  if (L.pinned && L.pinned[q]) {
+    store3(eacc, N, q, zbx, zby, zbz);
+    store3(pbar, N, q, 0.0, 0.0, 0.0);
+    store3(f1bar, N, q, 0.0, 0.0, 0.0);
+    store3(g2, N, q, 0.0, 0.0, 0.0);
+    return;
+  }
+  const int s = (int)(q / L.ncell);
+  double ex, ey, ez, px, py, pz, h1x, h1y, h1z, h2x, h2y, h2z;
+  load3(E, N, q, ex, ey, ez);
+  load3(Pp, N, q, px, py, pz);
+  load3(H1, N, q, h1x, h1y, h1z);
+  load3(H2, N, q, h2x, h2y, h2z);
+  const bool prec = A.precession != 0;
+  double f1x, f1y, f1z, f2x, f2y, f2z;
+  llg_rhs(ex, ey, ez, h1x, h1y, h1z, A.alpha, A.pre, prec, f1x, f1y, f1z);
+  llg_rhs(px, py, pz, h2x, h2y, h2z, A.alpha, A.pre, prec, f2x, f2y, f2z);
+  const double yx = fma(A.half_dt, f1x + f2x, ex), yy = fma(A.half_dt, f1y + f2y, ey), yz = fma(A.half_dt, f1z + f2z, ez);
+  const double ny = sqrt(yx * yx + yy * yy + yz * yz), inv_ny = 1.0 / ny;
+  const double zx = yx * inv_ny, zy = yy * inv_ny, zz = yz * inv_ny;
+  const double zd = zx * zbx + zy * zby + zz * zbz;
+  const double ybx = (zbx - zx * zd) * inv_ny, yby = (zby - zy * zd) * inv_ny, ybz = (zbz - zz * zd) * inv_ny;
+  const double fbx = A.half_dt * ybx, fby = A.half_dt * yby, fbz = A.half_dt * ybz;
+  double Hbx, Hby, Hbz, pbx, pby, pbz;
+  rhs_adjoint(px, py, pz, h2x, h2y, h2z, fbx, fby, fbz, A.alpha, A.pre, prec, Hbx, Hby, Hbz, pbx, pby, pbz);
+  const double inv = L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s];
+  const double gx = 2.0 * Hbx * inv, gy = 2.0 * Hby * inv, gz = 2.0 * Hbz * inv;
+  if (L.has_A) {
+    double a[9];
+    onsite_tensor(L, q, s, a);
+    pbx -= a[0] * gx + a[3] * gy + a[6] * gz;     // -A^T g
+    pby -= a[1] * gx + a[4] * gy + a[7] * gz;
+    pbz -= a[2] * gx + a[5] * gy + a[8] * gz;
+  }
+  const double gv[3] = {gx, gy, gz}, pv[3] = {px, py, pz};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * pv[k % 3];
+  A.PB[q] += Hbx;
+  A.PB[N + q] += Hby;
+  A.PB[2 * N + q] += Hbz;
+  store3(eacc, N, q, ybx, yby, ybz);
+  store3(pbar, N, q, pbx, pby, pbz);
+  store3(f1bar, N, q, fbx, fby, fbz);
+  store3(g2, N, q, gx, gy, gz);
+}
+
+__global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* __restrict__ E,
+                                                 const double* __restrict__ Pp, const double* __restrict__ H1,
+                                                 double* __restrict__ eacc, const double* __restrict__ pbar,
+                                                 const double* __restrict__ f1bar, const double* __restrict__ g2,
+                                                 double* __restrict__ g1) {
+  const DevLattice& L = A.F;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= L.N) return;
+  const long long N = L.N;
+  int s, c0, c1, c2;
+  site_coords(L, q, s, c0, c1, c2);
+  double px, py, pz;
+  load3(Pp, N, q, px, py, pz);
+  double tx, ty, tz;
+  adjoint_gather(A, g2, q, s, c0, c1, c2, px, py, pz, tx, ty, tz);
+  double pbx, pby, pbz;
+  load3(pbar, N, q, pbx, pby, pbz);
+  pbx += tx;
+  pby += ty;
+  pbz += tz;
+  double ax, ay, az;
+  load3(eacc, N, q, ax, ay, az);
+  if (L.pinned && L.pinned[q]) {          // p = e on pinned sites
+    store3(eacc, N, q, ax + pbx, ay + pby, az + pbz);
+    store3(g1, N, q, 0.0, 0.0, 0.0);
+    return;
+  }
+  double ex, ey, ez, h1x, h1y, h1z;
+  load3(E, N, q, ex, ey, ez);
+  load3(H1, N, q, h1x, h1y, h1z);
+  const bool prec = A.precession != 0;
+  double f1x, f1y, f1z;
+  llg_rhs(ex, ey, ez, h1x, h1y, h1z, A.alpha, A.pre, prec, f1x, f1y, f1z);
+  const double xx = fma(A.dt, f1x, ex), xy = fma(A.dt, f1y, ey), xz = fma(A.dt, f1z, ez);
+  const double nx = sqrt(xx * xx + xy * xy + xz * xz), inv_nx = 1.0 / nx;
+  const double ux = xx * inv_nx, uy = xy * inv_nx, uz = xz * inv_nx;
+  const double ud = ux * pbx + uy * pby + uz * pbz;
+  const double xbx = (pbx - ux * ud) * inv_nx, xby = (pby - uy * ud) * inv_nx, xbz = (pbz - uz * ud) * inv_nx;
+  ax += xbx;
+  ay += xby;
+  az += xbz;
+  double fbx, fby, fbz;
+  load3(f1bar, N, q, fbx, fby, fbz);
+  fbx = fma(A.dt, xbx, fbx);
+  fby = fma(A.dt, xby, fby);
+  fbz = fma(A.dt, xbz, fbz);
+  double Hbx, Hby, Hbz, ebx, eby, ebz;
+  rhs_adjoint(ex, ey, ez, h1x, h1y, h1z, fbx, fby, fbz, A.alpha, A.pre, prec, Hbx, Hby, Hbz, ebx, eby, ebz);
+  const double inv = L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s];
+  const double gx = 2.0 * Hbx * inv, gy = 2.0 * Hby * inv, gz = 2.0 * Hbz * inv;
+  ax += ebx;
+  ay += eby;
+  az += ebz;
+  if (L.has_A) {
+    double a[9];
+    onsite_tensor(L, q, s, a);
+    ax -= a[0] * gx + a[3] * gy + a[6] * gz;
+    ay -= a[1] * gx + a[4] * gy + a[7] * gz;
+    az -= a[2] * gx + a[5] * gy + a[8] * gz;
+  }
+  const double gv[3] = {gx, gy, gz}, ev[3] = {ex, ey, ez};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * ev[k % 3];
+  A.PB[q] += Hbx;
+  A.PB[N + q] += Hby;
+  A.PB[2 * N + q] += Hbz;
+  store3(eacc, N, q, ax, ay, az);
+  store3(g1, N, q, gx, gy, gz);
+}
+
+__global__ void __launch_bounds__(256) k_adj_final(const AdjDev A, const double* __restrict__ E,
+                                                   const double* __restrict__ eacc, const double* __restrict__ g1,
+                                                   double* __restrict__ ebar) {
+  const DevLattice& L = A.F;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= L.N) return;
+  const long long N = L.N;
+  int s, c0, c1, c2;
+  site_coords(L, q, s, c0, c1, c2);
+  double ex, ey, ez;
+  load3(E, N, q, ex, ey, ez);
+  double tx, ty, tz;
+  adjoint_gather(A, g1, q, s, c0, c1, c2, ex, ey, ez, tx, ty, tz);
+  double ax, ay, az;
+  load3(eacc, N, q, ax, ay, az);
+  store3(ebar, N, q, ax + tx, ay + ty, az + tz);
+}
+
+// out[r] = sum of x[r*stride .. r*stride + len)  (one block per row, fixed-order tree)
+__global__ void __launch_bounds__(256) k_sum_rows(const double* __restrict__ x, long long len, long long stride,
+                                                  double* __restrict__ out) {
+  const double* row = x + (long long)blockIdx.x * stride;
+  double acc = 0.0;
+  for (long long i = threadIdx.x; i < len; i += blockDim.x) acc += row[i];
+  __shared__ double red[8];
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < 8; ++w) s += red[w];
+    out[blockIdx.x] = s;
+  }
+}
+
+static double* seg_ptr(const AdjPlan* a, int n, int k) {   // k: 0 E, 1 P, 2 H1, 3 H2
+  return a->seg + ((size_t)n * 4 + k) * 3 * (size_t)a->fwd->d.N;
+}
+
+}  // namespace mgx
+
+using namespace mgx;
+
+extern "C" {
+
+mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const int32_t* rev_group,
+                              const int32_t* rev_transposed, int32_t ngroups, const mgx_llg_params* p,
+                              int32_t seg_steps, mgx_adjoint** out) {
+  const Model* F = reinterpret_cast<const Model*>(fwd);
+  const Model* R = reinterpret_cast<const Model*>(rev);
+  if (!F || !R || !p || !out) return set_error(MGX_ERR_INVALID, "mgx_adjoint_create: null argument");
+  *out = nullptr;
+  if (F->d.width != 9 || R->d.width != 9)
+    return set_error(MGX_ERR_INVALID, "the adjoint needs full-tensor (width 9) forward and reverse models");
+  if (F->d.ns != R->d.ns || F->d.L0 != R->d.L0 || F->d.L1 != R->d.L1 || F->d.L2 != R->d.L2 ||
+      F->d.pbc0 != R->d.pbc0 || F->d.pbc1 != R->d.pbc1 || F->d.pbc2 != R->d.pbc2)
+    return set_error(MGX_ERR_INVALID, "forward and reverse models must describe the same supercell");
+  if (F->nbond != R->nbond) return set_error(MGX_ERR_INVALID, "the reverse stencil must have one coupling per forward coupling");
+  if (F->d.A_site) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint supports single-ion tensors per sublattice only");
+  if (ngroups < 1 || ngroups > 4096) return set_error(MGX_ERR_INVALID, "ngroups must be in 1..4096");
+  if (R->nbond > 0 && (!rev_group || !rev_transposed)) return set_error(MGX_ERR_INVALID, "group arrays are required");
+  if (p->alpha_site) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint supports a uniform damping only");
+  if (p->integrator != MGX_INTEGRATOR_HEUN) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint is implemented for heun");
+  if (p->noise == MGX_NOISE_HOST) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint recomputes noise: use none or philox");
+  if (!(p->dt > 0.0)) return set_error(MGX_ERR_INVALID, "dt must be positive");
+  if (seg_steps < 1) return set_error(MGX_ERR_INVALID, "seg_steps must be >= 1");
+  std::vector<int2> grp(std::max(R->nbond, 1));
+  for (int b = 0; b < R->nbond; ++b) {
+    if (rev_group[b] < 0 || rev_group[b] >= ngroups) return set_error(MGX_ERR_INVALID, "group of bond %d out of range", b);
+    grp[b] = make_int2(rev_group[b], rev_transposed[b] ? 1 : 0);
+  }
+  AdjPlan* a = new AdjPlan();
+  a->fwd = F;
+  a->rev = R;
+  a->seg_cap = seg_steps;
+  a->noise = p->noise;
+  const long long N = F->d.N;
+  const int ns = F->d.ns;
+  const double gamma = 0.1760859630;
+  const double pre = -gamma / (1.0 + p->alpha * p->alpha);
+  const size_t n3 = 3 * (size_t)N;
+  cudaError_t err = cudaMalloc(&a->seg, sizeof(double) * n3 * 4 * seg_steps);
+  if (err == cudaSuccess) err = cudaMalloc(&a->e_end, sizeof(double) * n3);
+  if (err == cudaSuccess) err = cudaMalloc(&a->work, sizeof(double) * n3 * 5);
+  if (err == cudaSuccess) err = cudaMalloc(&a->k1, sizeof(double) * n3);
+  if (err == cudaSuccess) err = cudaMalloc(&a->d_group, sizeof(int2) * grp.size());
+  if (err == cudaSuccess) err = cudaMalloc(&a->d.PG, sizeof(double) * 9 * (size_t)ngroups * N);
+  if (err == cudaSuccess) err = cudaMalloc(&a->d.PA, sizeof(double) * 9 * (size_t)N);
+  if (err == cudaSuccess) err = cudaMalloc(&a->d.PB, sizeof(double) * 3 * (size_t)N);
+  if (err == cudaSuccess) err = cudaMalloc(&a->grads, sizeof(double) * (9 * (size_t)ngroups + 9 * ns + 3));
+  if (err == cudaSuccess) err = cudaMalloc(&a->sub, sizeof(double) * 3 * ns);
+  if (err == cudaSuccess) err = cudaMemcpy(a->d_group, grp.data(), sizeof(int2) * grp.size(), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) {
+    std::vector<double> sub(3 * ns, 0.0);
+    for (int s = 0; s < ns; ++s) {
+      sub[s] = p->alpha;
+      sub[ns + s] = pre;
+    }
+    err = cudaMemcpy(a->sub, sub.data(), sizeof(double) * sub.size(), cudaMemcpyHostToDevice);
+  }
+  if (err == cudaSuccess) err = cudaMemset(a->d.PG, 0, sizeof(double) * 9 * (size_t)ngroups * N);
+  if (err == cudaSuccess) err = cudaMemset(a->d.PA, 0, sizeof(double) * 9 * (size_t)N);
+  if (err == cudaSuccess) err = cudaMemset(a->d.PB, 0, sizeof(double) * 3 * (size_t)N);
+  if (err != cudaSuccess) {
+    mgx_adjoint_destroy(reinterpret_cast<mgx_adjoint*>(a));
+    return cuda_error(err, "mgx_adjoint_create");
+  }
+  AdjDev& d = a->d;
+  d.F = F->d;
+  d.R = R->d;
+  d.group = a->d_group;
+  d.ngroups = ngroups;
+  d.dt = p->dt;
+  d.half_dt = 0.5 * p->dt;
+  d.alpha = p->alpha;
+  d.pre = pre;
+  d.precession = p->precession ? 1 : 0;
+  DevLLG& P = a->P;
+  P.dt = p->dt;
+  P.half_dt = 0.5 * p->dt;
+  P.precession = p->precession ? 1 : 0;
+  P.noise = p->noise;
+  P.integrator = MGX_INTEGRATOR_HEUN;
+  P.seed = p->seed;
+  P.alpha_sub = (const double*)a->sub;
+  P.pre_sub = P.alpha_sub + ns;
+  P.sigma_sub = P.alpha_sub + 2 * ns;
+  P.alpha_site = P.pre_site = P.sigma_site = nullptr;
+  P.ep = nullptr;
+  P.k1 = a->k1;
+  *out = reinterpret_cast<mgx_adjoint*>(a);
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_destroy(mgx_adjoint* aa) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a) return MGX_OK;
+  cudaFree(a->seg);
+  cudaFree(a->e_end);
+  cudaFree(a->work);
+  cudaFree(a->k1);
+  cudaFree(a->d_group);
+  cudaFree(a->d.PG);
+  cudaFree(a->d.PA);
+  cudaFree(a->d.PB);
+  cudaFree(a->grads);
+  cudaFree(a->sub);
+  delete a;
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_set_sigma(mgx_adjoint* aa, const double* sigma_sub) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a || !sigma_sub) return set_error(MGX_ERR_INVALID, "mgx_adjoint_set_sigma: null argument");
+  const int ns = a->fwd->d.ns;
+  for (int s = 0; s < ns; ++s)
+    if (!std::isfinite(sigma_sub[s]) || sigma_sub[s] < 0.0) return set_error(MGX_ERR_INVALID, "sigma must be finite and >= 0");
+  MGX_CUDA_TRY(cudaMemcpy((double*)a->sub + 2 * ns, sigma_sub, sizeof(double) * ns, cudaMemcpyHostToDevice));
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_sync_models(mgx_adjoint* aa) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_sync_models: null argument");
+  a->d.F = a->fwd->d;
+  a->d.R = a->rev->d;
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_forward(mgx_adjoint* aa, const double* e0, int32_t nsteps, uint64_t step0, double* e_out,
+                               void* stream) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a || !e0) return set_error(MGX_ERR_INVALID, "mgx_adjoint_forward: null argument");
+  if (nsteps < 1 || nsteps > a->seg_cap)
+    return set_error(MGX_ERR_INVALID, "nsteps = %d outside 1..%d (segment capacity)", nsteps, a->seg_cap);
+  cudaStream_t st = (cudaStream_t)stream;
+  const DevLattice& L = a->fwd->d;
+  const long long N = L.N;
+  const unsigned grid = (unsigned)((N + 255) / 256);
+  MGX_CUDA_TRY(cudaMemcpyAsync(seg_ptr(a, 0, 0), e0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
+  for (int n = 0; n < nsteps; ++n) {
+    DevLLG P = a->P;
+    P.ep = seg_ptr(a, n, 1);
+    double* E = seg_ptr(a, n, 0);
+    double* eout = (n + 1 < nsteps) ? seg_ptr(a, n + 1, 0) : a->e_end;
+    const uint64_t step = step0 + (uint64_t)n;
+    if (a->noise == MGX_NOISE_PHILOX) {
+      k_fwd_pred<MGX_NOISE_PHILOX><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 2));
+      k_fwd_corr<MGX_NOISE_PHILOX><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 3), eout);
+    } else {
+      k_fwd_pred<MGX_NOISE_NONE><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 2));
+      k_fwd_corr<MGX_NOISE_NONE><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 3), eout);
+    }
+  }
+  a->seg_steps = nsteps;
+  if (e_out) MGX_CUDA_TRY(cudaMemcpyAsync(e_out, a->e_end, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
+  MGX_CUDA_TRY(cudaGetLastError());
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_backward(mgx_adjoint* aa, double* ebar, void* stream) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a || !ebar) return set_error(MGX_ERR_INVALID, "mgx_adjoint_backward: null argument");
+  if (a->seg_steps < 1) return set_error(MGX_ERR_INVALID, "mgx_adjoint_backward: run mgx_adjoint_forward first");
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long N = a->fwd->d.N;
+  const size_t n3 = 3 * (size_t)N;
+  const unsigned grid = (unsigned)((N + 255) / 256);
+  double* eacc = a->work;
+  double* pbar = a->work + n3;
+  double* f1bar = a->work + 2 * n3;
+  double* g1 = a->work + 3 * n3;
+  double* g2 = a->work + 4 * n3;
+  for (int n = a->seg_steps - 1; n >= 0; --n) {
+    const double* E = seg_ptr(a, n, 0);
+    const double* Pp = seg_ptr(a, n, 1);
+    const double* H1 = seg_ptr(a, n, 2);
+    const double* H2 = seg_ptr(a, n, 3);
+    k_adj_local<<<grid, 256, 0, st>>>(a->d, E, Pp, H1, H2, ebar, eacc, pbar, f1bar, g2);
+    k_adj_mid<<<grid, 256, 0, st>>>(a->d, E, Pp, H1, eacc, pbar, f1bar, g2, g1);
+    k_adj_final<<<grid, 256, 0, st>>>(a->d, E, eacc, g1, ebar);
+  }
+  MGX_CUDA_TRY(cudaGetLastError());
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_zero_grads(mgx_adjoint* aa, void* stream) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_zero_grads: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long N = a->fwd->d.N;
+  MGX_CUDA_TRY(cudaMemsetAsync(a->d.PG, 0, sizeof(double) * 9 * (size_t)a->d.ngroups * N, st));
+  MGX_CUDA_TRY(cudaMemsetAsync(a->d.PA, 0, sizeof(double) * 9 * (size_t)N, st));
+  MGX_CUDA_TRY(cudaMemsetAsync(a->d.PB, 0, sizeof(double) * 3 * (size_t)N, st));
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_grads(mgx_adjoint* aa, double* out, void* stream) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a || !out) return set_error(MGX_ERR_INVALID, "mgx_adjoint_grads: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const DevLattice& L = a->fwd->d;
+  const long long N = L.N;
+  const int G = a->d.ngroups, ns = L.ns;
+  k_sum_rows<<<9 * G, 256, 0, st>>>(a->d.PG, N, N, out);
+  k_sum_rows<<<9 * ns, 256, 0, st>>>(a->d.PA, L.ncell, L.ncell, out + 9 * G);   // rows (component k, sublattice s)
+  k_sum_rows<<<3, 256, 0, st>>>(a->d.PB, N, N, out + 9 * G + 9 * ns);
+  MGX_CUDA_TRY(cudaGetLastError());
+  return MGX_OK;
+}
+
+}  // extern "C"

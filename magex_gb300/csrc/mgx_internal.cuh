@@ -61,6 +61,7 @@ struct Model {
   uint8_t* pinned = nullptr;
   double* partials = nullptr;    // reduction scratch for observables
   int partial_cap = 0;           // number of 8-double slots
+  int* slot_of_bond = nullptr;   // host [nbond]: position of input coupling b in the device table
 };
 
 // ------------------------------------------------------------------ LLG plan (mgx_llg.cu)

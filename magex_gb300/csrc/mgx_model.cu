@@ -105,11 +105,13 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
   }
   for (int s = 0; s < ns; ++s) off[s + 1] += off[s];
   std::vector<int> fill(off.begin(), off.end() - 1);
+  std::vector<int> slot_of(std::max(nb, 1), 0);
   std::vector<int4> geo(std::max(nb, 1));
   std::vector<double> J((size_t)std::max(nb, 1) * W, 0.0);
   for (int b = 0; b < nb; ++b) {
     const int i = lat->bond_src[b];
     const int slot = fill[i]++;
+    slot_of[b] = slot;
     int d[3];
     bool self = (lat->bond_dst[b] == i);
     for (int a = 0; a < 3; ++a) {
@@ -146,6 +148,8 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
   }
 
   Model* m = new Model();
+  m->slot_of_bond = new int[std::max(nb, 1)];
+  std::copy(slot_of.begin(), slot_of.end(), m->slot_of_bond);
   DevLattice& d = m->d;
   d.ns = ns;
   d.L0 = lat->L[0];
@@ -243,7 +247,38 @@ mgx_status mgx_model_destroy(mgx_model* mm) {
   cudaFree(m->mu_site);
   cudaFree(m->pinned);
   cudaFree(m->partials);
+  delete[] m->slot_of_bond;
   delete m;
+  return MGX_OK;
+}
+
+mgx_status mgx_model_set_couplings(mgx_model* mm, const double* bond_table) {
+  Model* m = reinterpret_cast<Model*>(mm);
+  if (!m || (!bond_table && m->nbond > 0)) return set_error(MGX_ERR_INVALID, "mgx_model_set_couplings: null argument");
+  const int W = m->d.width, nb = m->nbond;
+  std::vector<double> J((size_t)std::max(nb, 1) * W, 0.0);
+  for (int b = 0; b < nb; ++b)
+    for (int k = 0; k < W; ++k) {
+      const double v = bond_table[(size_t)b * W + k];
+      if (!std::isfinite(v)) return set_error(MGX_ERR_INVALID, "coupling %d is not finite", b);
+      J[(size_t)m->slot_of_bond[b] * W + k] = v;
+    }
+  if (nb > 0)
+    MGX_CUDA_TRY(cudaMemcpy(const_cast<double*>(m->d.bond_J), J.data(), sizeof(double) * nb * W, cudaMemcpyHostToDevice));
+  return MGX_OK;
+}
+
+mgx_status mgx_model_set_onsite(mgx_model* mm, const double* A_sub) {
+  Model* m = reinterpret_cast<Model*>(mm);
+  if (!m || !A_sub) return set_error(MGX_ERR_INVALID, "mgx_model_set_onsite: null argument");
+  if (m->d.A_site) return set_error(MGX_ERR_INVALID, "the model has per-site single-ion tensors");
+  bool has_A = false;
+  for (int k = 0; k < 9 * m->d.ns; ++k) {
+    if (!std::isfinite(A_sub[k])) return set_error(MGX_ERR_INVALID, "single-ion tensor is not finite");
+    has_A |= A_sub[k] != 0.0;
+  }
+  MGX_CUDA_TRY(cudaMemcpy(const_cast<double*>(m->d.A_sub), A_sub, sizeof(double) * 9 * m->d.ns, cudaMemcpyHostToDevice));
+  m->d.has_A = has_A ? 1 : 0;
   return MGX_OK;
 }
 

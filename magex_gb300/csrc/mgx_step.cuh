@@ -50,15 +50,20 @@ __device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P
   bz = fma(sig, g2, bz);
 }
 
-// Predictor of site q (0 <= q < L.N): writes P.ep and P.k1 at q.
+// Predictor of site q (0 <= q < L.N): writes P.ep and P.k1 at q.  With Hout != nullptr the total
+// field (effective + thermal) of the site is stored there too (adjoint recomputation).
 template <int W, int NOISE, int INTEG>
 __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& P, const double* __restrict__ e,
-                                             const double* __restrict__ noise, long long q, uint64_t step) {
+                                             const double* __restrict__ noise, long long q, uint64_t step,
+                                             double* __restrict__ Hout = nullptr) {
   const long long N = L.N;
   const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
   if (L.pinned && L.pinned[q]) {
     P.ep[q] = ex; P.ep[N + q] = ey; P.ep[2 * N + q] = ez;
     P.k1[q] = 0.0; P.k1[N + q] = 0.0; P.k1[2 * N + q] = 0.0;
+    if (Hout) {
+      Hout[q] = 0.0; Hout[N + q] = 0.0; Hout[2 * N + q] = 0.0;
+    }
     return;
   }
   int s, c0, c1, c2;
@@ -66,6 +71,9 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
   double bx, by, bz;
   effective_field<W>(L, e, q, s, c0, c1, c2, ex, ey, ez, bx, by, bz);
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
+  if (Hout) {
+    Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
+  }
   const double a = P.alpha_site ? __ldg(P.alpha_site + q) : __ldg(P.alpha_sub + s);
   const double pre = P.pre_site ? __ldg(P.pre_site + q) : __ldg(P.pre_sub + s);
   double fx, fy, fz;
@@ -88,11 +96,21 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
   P.k1[q] = fx; P.k1[N + q] = fy; P.k1[2 * N + q] = fz;
 }
 
-// Corrector of site q (0 <= q < L.N): reads P.ep (neighbours), P.k1 and e at q, writes e at q.
+// Corrector of site q (0 <= q < L.N): reads P.ep (neighbours), P.k1 and e at q, writes e at q
+// (or eout at q when given; the adjoint recomputation keeps e).  Hout as in predict_site.
 template <int W, int NOISE, int INTEG>
 __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& P, double* __restrict__ e,
-                                             const double* __restrict__ noise, long long q, uint64_t step) {
-  if (L.pinned && L.pinned[q]) return;
+                                             const double* __restrict__ noise, long long q, uint64_t step,
+                                             double* __restrict__ Hout = nullptr, double* __restrict__ eout = nullptr) {
+  if (L.pinned && L.pinned[q]) {
+    if (eout) {
+      eout[q] = e[q]; eout[L.N + q] = e[L.N + q]; eout[2 * L.N + q] = e[2 * L.N + q];
+    }
+    if (Hout) {
+      Hout[q] = 0.0; Hout[L.N + q] = 0.0; Hout[2 * L.N + q] = 0.0;
+    }
+    return;
+  }
   const long long N = L.N;
   int s, c0, c1, c2;
   site_coords(L, q, s, c0, c1, c2);
@@ -100,6 +118,9 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
   double bx, by, bz;
   effective_field<W>(L, P.ep, q, s, c0, c1, c2, px, py, pz, bx, by, bz);
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
+  if (Hout) {
+    Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
+  }
   const double a = P.alpha_site ? __ldg(P.alpha_site + q) : __ldg(P.alpha_sub + s);
   const double pre = P.pre_site ? __ldg(P.pre_site + q) : __ldg(P.pre_sub + s);
   double fx, fy, fz;
@@ -115,7 +136,8 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
     z = fma(P.half_dt, k1z + fz, z);
   }
   const double r = rsqrt(x * x + y * y + z * z);
-  e[q] = x * r; e[N + q] = y * r; e[2 * N + q] = z * r;
+  double* o = eout ? eout : e;
+  o[q] = x * r; o[N + q] = y * r; o[2 * N + q] = z * r;
 }
 
 }  // namespace mgx

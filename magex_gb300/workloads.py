@@ -131,3 +131,22 @@ def triangle_list(sc):
     t2 = np.stack([idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)], -1).reshape(-1, 3)
     tri = np.concatenate([t1, t2])
     return tri, np.ones(len(tri))
+
+
+def film_parameter_basis(sc, normal=(0.0, 0.0, 1.0)):
+    """For a one-shell film with interfacial DMI (make_model "triangular"/"square" with D): the constant
+    matrices S_b = skew(n x r_b / |r_b|) of every stencil coupling, so that J_b = J1 I + D S_b (exact
+    for the couplings make_model writes).  Returns (S (nbond, 3, 3))."""
+    uc = sc.uc
+    n = np.asarray(normal, float) / np.linalg.norm(normal)
+    S = []
+    for i, j, R in zip(sc.bond_src, sc.bond_dst, sc.bond_R):
+        r = uc.positions[j] + R @ uc.cell - uc.positions[i]
+        S.append(skew(np.cross(n, r / np.linalg.norm(r))))
+    return np.array(S)
+
+
+def uniaxial_sia(K, axis=(0.0, 0.0, 1.0)):
+    """Traceless single-ion tensor -K (n n^T - I/3) of magex/models.py:109."""
+    n = np.asarray(axis, float) / np.linalg.norm(axis)
+    return -K * (np.outer(n, n) - np.eye(3) / 3)
