@@ -218,7 +218,7 @@ def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None):
             "final_mean_E_per_spin": float(np.mean(rows[:, 1])), "Q_range": [float(Q.min()), float(Q.max())]}
 
 
-def bench_adjoint(L=128, nsteps=2000, seg=100):
+def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
     """Differentiable-LLG workload: triangular 128 x 128, J1 = 1 meV, D/J = 0.3, K = 0.05 meV, B_z = 2 T,
     T = 0, alpha 0.3, dt 0.1 fs, 2000 Heun steps, checkpoint every 100 steps; loss = sum |e(T) - target|^2.
     Times the plain forward (GB300LLG), the checkpointed forward and the backward (recompute + adjoint)
@@ -228,8 +228,12 @@ def bench_adjoint(L=128, nsteps=2000, seg=100):
     from magex_gb300.llg import GB300LLG
     from magex_gb300.workloads import film_parameter_basis, triangular_film, uniaxial_sia
     sc = triangular_film(L=L, field=(0, 0, 2.0))
-    S = torch.as_tensor(film_parameter_basis(sc))
-    adj = AdjointLLG(sc, alpha=0.3, dt=1e-4, seg_steps=seg)
+    adj = AdjointLLG(sc, alpha=0.3, dt=1e-4, seg_steps=seg, cache_bytes=cache_bytes)
+    S_bond = film_parameter_basis(sc)
+    S = torch.zeros((adj.groups.ngroups, 3, 3), dtype=torch.float64)
+    for b in range(len(S_bond)):
+        if not adj.groups.transposed[b]:
+            S[adj.groups.group[b]] = torch.as_tensor(S_bond[b])
     e0 = sc.init_spins("random", seed=1)
     target = torch.as_tensor(sc.init_spins("random", seed=2), device=adj.device)
     plain = GB300LLG(sc, 0.3, 1e-4, 0.0, 1)
@@ -266,6 +270,7 @@ def bench_adjoint(L=128, nsteps=2000, seg=100):
     t_bwd = ev[2].elapsed_time(ev[3])
     return {"workload": f"triangular {L}x{L} film, J1=1 meV, D/J=0.3, K=0.05 meV, B_z=2 T, T=0, alpha 0.3, "
                         f"dt 0.1 fs, {nsteps} Heun steps, checkpoint every {seg}, loss sum|e(T)-target|^2, FP64",
+            "resident_segments": len(adj._segments(nsteps)) if cache_bytes else 0,
             "forward_plain_ms": t_plain, "forward_checkpointed_ms": t_fwd, "backward_ms": t_bwd,
             "adjoint_over_forward": t_bwd / t_plain, "gradient_total_over_forward": (t_fwd + t_bwd) / t_plain,
             "grad_J1_D": [float(x) for x in g]}
@@ -386,6 +391,9 @@ def run_gb300(args):
         line["batched"] = bench_batched()
     if ws == 1 and not args.no_adjoint:
         line["adjoint"] = bench_adjoint()
+        # the same trajectory with every segment kept in HBM (2000 steps x 14 N doubles = 3.7 GB): no recompute
+        line["adjoint_resident"] = bench_adjoint(cache_bytes=8 << 30)
+        line["adjoint_large"] = bench_adjoint(L=1024, nsteps=200, seg=50)
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -406,9 +414,21 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
+    ap.add_argument("--only", choices=["adjoint", "batched"], default=None,
+                    help="run only one of the secondary measurements and print its JSON (for profiling)")
+    ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--adjoint-L", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.only:
+        import torch
+        torch.cuda.set_device(0)
+        from magex_gb300 import build
+        build.build_library()
+        out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps) if args.only == "adjoint" else bench_batched()
+        print(json.dumps(out), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -103,6 +103,26 @@ void mgx_last_error(char* buf, size_t len);
  * mgx_model_create replaces FastModel(system) (magex/fast.py:630-657) and _Device (magex/cuda_backend.py:307-335):
  * it validates the stencil and uploads tables and per-site arrays to the current device. */
 mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* sites, mgx_model** out);
+
+/* Arbitrary lattice (carved shapes, vacancies, edited exchange): per-site neighbour lists in magex site
+ * order, the argument list of magex's fused kernels (FastModel.args, magex/fast.py:669-672: ptr, nbr,
+ * (typ, table), A, mu, B, pinned) built by neighbour_blocks (magex/fast.py:587-627).  Spins of such a
+ * model use the identity layout: x[c * N + site]. */
+typedef struct mgx_csr_desc {
+  int64_t nsites;
+  const int64_t* ptr;        /* host [N+1] */
+  const int32_t* nbr;        /* host [ptr[N]] */
+  const int32_t* typ;        /* host [ptr[N]] coupling type of each neighbour */
+  int32_t ntypes;
+  int32_t width;             /* 1, 4 or 9 doubles per type (as mgx_lattice_desc) */
+  const double* table;       /* host [ntypes*width] */
+  const double* A_site;      /* host [N*9] or NULL */
+  const double* mu_site;     /* host [N] */
+  const double* sign_site;   /* host [N] or NULL */
+  const uint8_t* pinned;     /* host [N] or NULL */
+  double B[3];
+} mgx_csr_desc;
+mgx_status mgx_model_create_csr(const mgx_csr_desc* csr, mgx_model** out);
 mgx_status mgx_model_destroy(mgx_model* m);
 mgx_status mgx_model_set_field(mgx_model* m, const double B[3]);   /* SpinSystem.set_field, magex/spinmodel.py:451-452 */
 int64_t mgx_model_nsites(const mgx_model* m);
@@ -182,7 +202,7 @@ mgx_status mgx_batch_topological_charge(mgx_batch* b, const double* e, double* o
  *                        out[9G + k*ns + s] = dL/dA_s[k]), dL/dB.
  * fwd is the forward stencil model (width 9); rev is the reverse stencil: for every forward coupling
  * (i -> j, R, J) one coupling (j -> i, -R, J^T) of the same supercell, in an order grouped by receiving
- * sublattice and then by (rev_group, rev_transposed).  rev_group[b] names the parameter tensor T_g that
+ * sublattice and then by rev_group.  rev_group[b] names the parameter tensor T_g that
  * the forward coupling uses, rev_transposed[b] = 1 when that coupling is T_g^T.  */
 mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const int32_t* rev_group,
                               const int32_t* rev_transposed, int32_t ngroups, const mgx_llg_params* p,
@@ -190,9 +210,15 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
 mgx_status mgx_adjoint_destroy(mgx_adjoint* a);
 mgx_status mgx_adjoint_set_sigma(mgx_adjoint* a, const double* sigma_sub);
 mgx_status mgx_adjoint_sync_models(mgx_adjoint* a);      /* after mgx_model_set_couplings / _set_onsite / _set_field */
+/* Segment storage: mgx_adjoint_storage_doubles(a) doubles per segment (14 N per step + 3 N).  By default
+ * the adjoint uses one storage it owns; mgx_adjoint_set_storage switches to caller storage (device,
+ * 16-byte aligned; NULL = the own one), so that segments kept resident need no recomputation. */
+int64_t mgx_adjoint_storage_doubles(const mgx_adjoint* a);
+mgx_status mgx_adjoint_set_storage(mgx_adjoint* a, double* storage);
 mgx_status mgx_adjoint_forward(mgx_adjoint* a, const double* e0, int32_t nsteps, uint64_t step0, double* e_out,
                                void* stream);
-mgx_status mgx_adjoint_backward(mgx_adjoint* a, double* ebar, void* stream);
+/* nsteps: the length of the segment held by the current storage. */
+mgx_status mgx_adjoint_backward(mgx_adjoint* a, double* ebar, int32_t nsteps, void* stream);
 mgx_status mgx_adjoint_zero_grads(mgx_adjoint* a, void* stream);
 mgx_status mgx_adjoint_grads(mgx_adjoint* a, double* out, void* stream);
 

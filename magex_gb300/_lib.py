@@ -40,6 +40,12 @@ class LLGParams(C.Structure):
                 ("integrator", C.c_int32), ("noise", C.c_int32), ("seed", C.c_uint64)]
 
 
+class CSRDesc(C.Structure):
+    _fields_ = [("nsites", C.c_int64), ("ptr", C.POINTER(C.c_int64)), ("nbr", _ip), ("typ", _ip),
+                ("ntypes", C.c_int32), ("width", C.c_int32), ("table", _dp), ("A_site", _dp), ("mu_site", _dp),
+                ("sign_site", _dp), ("pinned", _u8p), ("B", C.c_double * 3)]
+
+
 #: every exported entry point with (restype, argtypes); the CPU tests check the export list against
 #: include/mgx.h
 SIGNATURES = {
@@ -47,6 +53,7 @@ SIGNATURES = {
     "mgx_last_error": (None, [C.c_char_p, C.c_size_t]),
     "mgx_model_create": (C.c_int32, [C.POINTER(LatticeDesc), C.POINTER(SiteDesc), C.POINTER(C.c_void_p)]),
     "mgx_model_destroy": (C.c_int32, [C.c_void_p]),
+    "mgx_model_create_csr": (C.c_int32, [C.POINTER(CSRDesc), C.POINTER(C.c_void_p)]),
     "mgx_model_set_field": (C.c_int32, [C.c_void_p, _dp]),
     "mgx_model_nsites": (C.c_int64, [C.c_void_p]),
     "mgx_pack_spins": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -80,7 +87,9 @@ SIGNATURES = {
     "mgx_adjoint_set_sigma": (C.c_int32, [C.c_void_p, _dp]),
     "mgx_adjoint_sync_models": (C.c_int32, [C.c_void_p]),
     "mgx_adjoint_forward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_uint64, C.c_void_p, C.c_void_p]),
-    "mgx_adjoint_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_adjoint_backward": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "mgx_adjoint_storage_doubles": (C.c_int64, [C.c_void_p]),
+    "mgx_adjoint_set_storage": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mgx_adjoint_zero_grads": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mgx_adjoint_grads": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

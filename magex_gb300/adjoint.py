@@ -10,10 +10,12 @@ The couplings of the supercell stencil are parameterised by a few 3x3 tensors ``
 DMI, anisotropic exchange) map onto ``T`` with ordinary torch operations and autograd applies the
 chain rule.  ``A`` holds the per-sublattice single-ion tensors and ``B`` the external field.
 
-The forward pass runs the trajectory in segments of ``seg_steps`` steps and keeps only the spins at
+The forward pass runs the trajectory in segments of ``seg_steps`` steps and keeps the spins at
 segment starts (checkpoints).  The backward pass recomputes each segment from its checkpoint,
-storing per step e, ep and both total fields, then runs the adjoint kernels (libmgx
-``mgx_adjoint_*``) back through the segment.  Thermal (Philox) noise is regenerated bit-identically
+storing per step e, ep, both total fields and the two normalisation factors, then runs the adjoint
+kernels (libmgx ``mgx_adjoint_*``) back through the segment.  With ``cache_bytes`` > 0 the last
+segments that fit keep their states from the forward pass and are not recomputed (checkpointing
+sized to the memory one grants it).  Thermal (Philox) noise is regenerated bit-identically
 from (seed, site, step), so the gradient is the pathwise derivative of the same noisy trajectory.
 magex itself has no gradients; parity of this module is pinned against central finite differences
 and against torch autograd of a dense FP64 restatement (tests/test_gpu_adjoint.py).
@@ -45,6 +47,28 @@ class CouplingGroups:
     def per_bond(cls, sc):
         """Every coupling its own tensor (dL/dJ_b for each coupling of the unit cell)."""
         return cls(np.arange(len(sc.bond_src)))
+
+    @classmethod
+    def symmetric_pairs(cls, sc):
+        """One tensor per pair of mutually reverse couplings (i -> j, R) and (j -> i, -R) whose tensors
+        are transposes of each other (J_ji = J_ij^T, true for every model built here): the reverse
+        coupling uses the transposed group tensor.  Couplings without such a partner get their own
+        group.  Half as many groups as per_bond, so half the gradient bookkeeping per site."""
+        n = len(sc.bond_src)
+        key = {(int(sc.bond_src[b]), int(sc.bond_dst[b]), tuple(int(x) for x in sc.bond_R[b])): b for b in range(n)}
+        group = -np.ones(n, np.int32)
+        trans = np.zeros(n, np.int32)
+        g = 0
+        for b in range(n):
+            if group[b] >= 0:
+                continue
+            group[b] = g
+            rb = key.get((int(sc.bond_dst[b]), int(sc.bond_src[b]), tuple(-int(x) for x in sc.bond_R[b])))
+            if rb is not None and rb != b and group[rb] < 0 and np.array_equal(sc.bond_J[rb], sc.bond_J[b].T):
+                group[rb] = g
+                trans[rb] = 1
+            g += 1
+        return cls(group, trans, g)
 
     @classmethod
     def per_shell(cls, sc, ndigits=4):
@@ -89,9 +113,8 @@ def _full_width(sc):
 
 def _reverse(sc, groups):
     """Reverse stencil: coupling (j -> i, -R, J^T) for every forward (i -> j, R, J), ordered by receiving
-    sublattice and then (group, transposed); returns (view, order) with order[k] = forward bond of k."""
-    order = sorted(range(len(sc.bond_src)),
-                   key=lambda b: (int(sc.bond_dst[b]), int(groups.group[b]), int(groups.transposed[b]), b))
+    sublattice and then group; returns (view, order) with order[k] = forward bond of k."""
+    order = sorted(range(len(sc.bond_src)), key=lambda b: (int(sc.bond_dst[b]), int(groups.group[b]), b))
     order = np.array(order, np.int64)
     v = copy.copy(sc)
     v.bond_src = np.ascontiguousarray(sc.bond_dst[order], np.int32)
@@ -107,13 +130,13 @@ class AdjointLLG:
     """Forward / adjoint engine of Heun trajectories on one supercell (uniform alpha per run)."""
 
     def __init__(self, sc, groups=None, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
-                 seg_steps=100, device=None):
+                 seg_steps=100, cache_bytes=0, device=None):
         if sc.alpha_site is not None or sc.site_T is not None or sc.A_site is not None:
             raise NotImplementedError("the adjoint supports uniform damping, temperature and per-sublattice A")
         if sc.terms or sc.has_higher:
             raise NotImplementedError("extra energy terms are not supported by the GB300 kernels")
         self.sc = sc
-        self.groups = CouplingGroups.per_bond(sc) if groups is None else groups
+        self.groups = CouplingGroups.symmetric_pairs(sc) if groups is None else groups
         self.T0 = self.groups.tensors_from(sc)
         self.fwd = DeviceModel(_full_width(sc), device)
         rev_view, self.rev_order = _reverse(sc, self.groups)
@@ -141,6 +164,8 @@ class AdjointLLG:
             _lib.check(self.lib.mgx_adjoint_set_sigma(h, _lib.dptr(sig)), "mgx_adjoint_set_sigma")
         ns, G = sc.ns, self.groups.ngroups
         self._grads = torch.empty(9 * G + 9 * ns + 3, dtype=torch.float64, device=self.device)
+        self.storage_doubles = int(self.lib.mgx_adjoint_storage_doubles(h))
+        self.cache_bytes = int(cache_bytes)
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -178,27 +203,51 @@ class AdjointLLG:
         return out
 
     def forward(self, e0_lat, nsteps):
-        """Run nsteps from lattice-layout spins; returns (e_T, checkpoints at segment starts)."""
+        """Run nsteps from lattice-layout spins; returns (e_T, checkpoints, resident segments).
+
+        A checkpoint (the spins) is kept at the start of every segment of seg_steps steps.  When
+        cache_bytes allows, the last segments also keep their full states (a resident segment costs
+        mgx_adjoint_storage_doubles doubles), so the backward pass does not recompute them."""
+        segs = self._segments(int(nsteps))
+        ncache = min(len(segs), self.cache_bytes // (8 * self.storage_doubles))
+        cache = [torch.empty(self.storage_doubles, dtype=torch.float64, device=self.device) for _ in range(ncache)]
+        first_cached = len(segs) - ncache
         ckpts = []
         cur = e0_lat.contiguous()
-        for n0, k in self._segments(int(nsteps)):
-            ckpts.append(cur)
-            nxt = torch.empty_like(cur)
-            _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(cur.data_ptr()), k, n0,
-                                                    C.c_void_p(nxt.data_ptr()), stream_ptr()), "mgx_adjoint_forward")
-            cur = nxt
-        return cur, ckpts
+        try:
+            for k, (n0, m) in enumerate(segs):
+                ckpts.append(cur)
+                store = cache[k - first_cached] if k >= first_cached else None
+                _lib.check(self.lib.mgx_adjoint_set_storage(self.handle, None if store is None else
+                                                            C.c_void_p(store.data_ptr())), "set_storage")
+                nxt = torch.empty_like(cur)
+                _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(cur.data_ptr()), m, n0,
+                                                        C.c_void_p(nxt.data_ptr()), stream_ptr()), "mgx_adjoint_forward")
+                cur = nxt
+        finally:
+            self.lib.mgx_adjoint_set_storage(self.handle, None)
+        return cur, ckpts, cache
 
-    def backward(self, ckpts, ebar_T_lat, nsteps):
+    def backward(self, ckpts, ebar_T_lat, nsteps, cache=()):
         """dL/de_0 (lattice layout) and (dL/dT, dL/dA, dL/dB) from dL/de_T."""
         ebar = ebar_T_lat.clone().contiguous()
         _lib.check(self.lib.mgx_adjoint_zero_grads(self.handle, stream_ptr()), "zero_grads")
         segs = self._segments(int(nsteps))
-        for (n0, k), ck in zip(reversed(segs), reversed(ckpts)):
-            _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(ck.data_ptr()), k, n0, None, stream_ptr()),
-                       "mgx_adjoint_forward (recompute)")
-            _lib.check(self.lib.mgx_adjoint_backward(self.handle, C.c_void_p(ebar.data_ptr()), stream_ptr()),
-                       "mgx_adjoint_backward")
+        first_cached = len(segs) - len(cache)
+        try:
+            for k in range(len(segs) - 1, -1, -1):
+                n0, m = segs[k]
+                if k >= first_cached:
+                    _lib.check(self.lib.mgx_adjoint_set_storage(self.handle, C.c_void_p(cache[k - first_cached].data_ptr())),
+                               "set_storage")
+                else:
+                    _lib.check(self.lib.mgx_adjoint_set_storage(self.handle, None), "set_storage")
+                    _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(ckpts[k].data_ptr()), m, n0, None,
+                                                            stream_ptr()), "mgx_adjoint_forward (recompute)")
+                _lib.check(self.lib.mgx_adjoint_backward(self.handle, C.c_void_p(ebar.data_ptr()), m, stream_ptr()),
+                           "mgx_adjoint_backward")
+        finally:
+            self.lib.mgx_adjoint_set_storage(self.handle, None)
         _lib.check(self.lib.mgx_adjoint_grads(self.handle, C.c_void_p(self._grads.data_ptr()), stream_ptr()),
                    "mgx_adjoint_grads")
         G, ns = self.groups.ngroups, self.sc.ns
@@ -214,8 +263,8 @@ class _Trajectory(torch.autograd.Function):
     def forward(ctx, e0, T, A, B, adj, nsteps):
         adj.set_params(T.detach().cpu().numpy(), A.detach().cpu().numpy(), B.detach().cpu().numpy())
         lat0 = adj.fwd.to_lattice(e0.detach())
-        eT, ckpts = adj.forward(lat0, nsteps)
-        ctx.adj, ctx.nsteps, ctx.ckpts = adj, nsteps, ckpts
+        eT, ckpts, cache = adj.forward(lat0, nsteps)
+        ctx.adj, ctx.nsteps, ctx.ckpts, ctx.cache = adj, nsteps, ckpts, cache
         ctx.devs = (e0.device, T.device, A.device, B.device)
         ctx.params = (T.detach().cpu().numpy(), A.detach().cpu().numpy(), B.detach().cpu().numpy())
         out = adj.fwd.from_lattice(eT)
@@ -226,7 +275,8 @@ class _Trajectory(torch.autograd.Function):
         adj = ctx.adj
         adj.set_params(*ctx.params)                  # the parameters may have changed since the forward
         ebar_T = adj.fwd.to_lattice(grad_eT.detach().contiguous())
-        ebar0, gT, gA, gB = adj.backward(ctx.ckpts, ebar_T, ctx.nsteps)
+        ebar0, gT, gA, gB = adj.backward(ctx.ckpts, ebar_T, ctx.nsteps, ctx.cache)
+        ctx.cache = ()
         ge0 = adj.fwd.from_lattice(ebar0)
         d0, dT, dA, dB = ctx.devs
         return ge0.to(d0), gT.to(dT), gA.to(dA), gB.to(dB), None, None

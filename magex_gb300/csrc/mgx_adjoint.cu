@@ -6,7 +6,8 @@
 //   H(v)_i = (2 sum_j J_ij v_j - 2 A_i v_i) / (mu_i mu_B) + B + b_i,
 //   f(e, H) = pre [e x H + alpha e x (e x H)].
 // The reference has no gradients; this file supplies d loss / d e and the parameter gradients for
-// a trajectory.  Given ebar' = dL/de' one backward step is three kernels:
+// a trajectory.  Given ebar' = dL/de' one backward step is three kernel bodies (the last one of a
+// step and the first one of the step before it run as one kernel):
 //   k_adj_local   (site-local) ybar, f1bar = f2bar = dt/2 ybar, H2bar and pbar from the rhs adjoint at
 //                 (p, H2), g2 = 2 H2bar / (mu mu_B), local A term; A and B gradients of stage 2;
 //   k_adj_mid     pbar += sum_rev J^T g2 (transposed stencil gather), xbar through the normalisation,
@@ -16,7 +17,9 @@
 // The transposed gather uses a second stencil (the reverse couplings j -> i with J_ij^T), so the
 // adjoint is exact also when a coupling set does not satisfy J_ji = J_ij^T.
 // Parameter gradients accumulate per site (deterministic, no atomics) and are summed at the end.
-// States of a segment of steps are recomputed from a checkpoint and stored (e, p, H1, H2).
+// States of a segment of steps are recomputed from a checkpoint and stored (e, p, H1, H2 and the two
+// inverse norms); a caller may keep several segments resident (mgx_adjoint_set_storage) and skip
+// their recomputation.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -46,8 +49,8 @@ struct AdjPlan {
   DevLLG P;               // forward parameters; ep / k1 re-pointed per step
   int seg_cap = 0;
   int noise = MGX_NOISE_NONE;
-  double* seg = nullptr;  // [seg_cap][4][3N]
-  double* e_end = nullptr;
+  double* seg = nullptr;  // current segment storage (own_seg or caller storage)
+  double* own_seg = nullptr;
   double* work = nullptr; // eacc | pbar | f1bar | g1 | g2 (5 x 3N)
   double* k1 = nullptr;
   double* grads = nullptr;  // reduction output on device
@@ -63,29 +66,30 @@ __device__ __forceinline__ void cross3(double ax, double ay, double az, double b
   cz = ax * by - ay * bx;
 }
 
-// rhs adjoint: given fbar, Hbar = pre [fbar x e + a e x (e x fbar)],
-// ebar = pre [H x fbar + a (c x fbar - H x (e x fbar))] with c = e x H (precession);
-// without precession the e x H terms are dropped.
+// rhs adjoint for f = pre [e x H + a e x (e x H)]: given fbar,
+//   Hbar = pre [fbar x e + a e x (e x fbar)] = pre [-(e x fbar) + a (e (e.fbar) - fbar)],
+//   ebar = pre [H x fbar + a ((e x H) x fbar - H x (e x fbar))]
+//        = pre [H x fbar + a (H (e.fbar) + fbar (H.e) - 2 e (H.fbar))],
+// using the triple-product identities and |e| = 1 (e and p are unit vectors to rounding);
+// without precession the e x H terms (H x fbar, e x fbar) are dropped.
 __device__ __forceinline__ void rhs_adjoint(double ex, double ey, double ez, double Hx, double Hy, double Hz,
                                             double fbx, double fby, double fbz, double a, double pre, bool prec,
                                             double& Hbx, double& Hby, double& Hbz, double& ebx, double& eby,
                                             double& ebz) {
-  double ux, uy, uz;   // e x fbar
-  cross3(ex, ey, ez, fbx, fby, fbz, ux, uy, uz);
-  double wx, wy, wz;   // e x (e x fbar)
-  cross3(ex, ey, ez, ux, uy, uz, wx, wy, wz);
-  double cx, cy, cz;   // c = e x H
-  cross3(ex, ey, ez, Hx, Hy, Hz, cx, cy, cz);
-  double t1x, t1y, t1z;   // c x fbar
-  cross3(cx, cy, cz, fbx, fby, fbz, t1x, t1y, t1z);
-  double t2x, t2y, t2z;   // H x (e x fbar)
-  cross3(Hx, Hy, Hz, ux, uy, uz, t2x, t2y, t2z);
-  Hbx = a * wx; Hby = a * wy; Hbz = a * wz;
-  ebx = a * (t1x - t2x); eby = a * (t1y - t2y); ebz = a * (t1z - t2z);
+  const double ef = ex * fbx + ey * fby + ez * fbz;
+  const double He = Hx * ex + Hy * ey + Hz * ez;
+  const double m2Hf = -2.0 * (Hx * fbx + Hy * fby + Hz * fbz);
+  Hbx = a * fma(ex, ef, -fbx);
+  Hby = a * fma(ey, ef, -fby);
+  Hbz = a * fma(ez, ef, -fbz);
+  ebx = a * fma(ex, m2Hf, fma(fbx, He, Hx * ef));
+  eby = a * fma(ey, m2Hf, fma(fby, He, Hy * ef));
+  ebz = a * fma(ez, m2Hf, fma(fbz, He, Hz * ef));
   if (prec) {
-    double hx, hy, hz;   // H x fbar
-    cross3(Hx, Hy, Hz, fbx, fby, fbz, hx, hy, hz);
-    Hbx -= ux; Hby -= uy; Hbz -= uz;      // fbar x e = -(e x fbar)
+    double ux, uy, uz, hx, hy, hz;
+    cross3(ex, ey, ez, fbx, fby, fbz, ux, uy, uz);     // e x fbar
+    cross3(Hx, Hy, Hz, fbx, fby, fbz, hx, hy, hz);     // H x fbar
+    Hbx -= ux; Hby -= uy; Hbz -= uz;
     ebx += hx; eby += hy; ebz += hz;
   }
   Hbx *= pre; Hby *= pre; Hbz *= pre;
@@ -112,7 +116,9 @@ __device__ __forceinline__ void store3(double* x, long long N, long long q, doub
 }
 
 // Transposed gather sum_rev J^T g_nbr at site q of the reverse stencil, with the parameter-gradient
-// outer products g_nbr (x) v (v = own p or e) summed per (group, transposed) run and added to PG.
+// outer products added to PG once per group run: a forward coupling with tensor T_g contributes
+// g_nbr (x) v, one with T_g^T contributes v (x) g_nbr (v = own p or e), so each run keeps the sums of
+// g_nbr over its plain and its transposed couplings and flushes 9 values per group.
 __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __restrict__ g, long long q, int s,
                                                int c0, int c1, int c2, double vx, double vy, double vz,
                                                double& ox, double& oy, double& oz) {
@@ -120,27 +126,29 @@ __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __
   const long long N = L.N;
   ox = oy = oz = 0.0;
   const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
-  int cur_g = -1, cur_t = 0;
-  double sx = 0.0, sy = 0.0, sz = 0.0;
+  int cur_g = -1;
+  double sx = 0.0, sy = 0.0, sz = 0.0;      // sum of g over couplings with tensor T_g
+  double tx = 0.0, ty = 0.0, tz = 0.0;      // sum of g over couplings with tensor T_g^T
+  const double vv[3] = {vx, vy, vz};
   auto flush = [&]() {
     if (cur_g < 0) return;
     double* P = A.PG + (long long)cur_g * 9 * N + q;
-    const double gv[3] = {sx, sy, sz}, vv[3] = {vx, vy, vz};
+    const double gs[3] = {sx, sy, sz}, gt[3] = {tx, ty, tz};
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int b = 0; b < 3; ++b) {
-        const double m = cur_t ? vv[a] * gv[b] : gv[a] * vv[b];
-        P[(long long)(3 * a + b) * N] += m;
+        double* cell = P + (long long)(3 * a + b) * N;
+        *cell = fma(vv[a], gt[b], fma(gs[a], vv[b], *cell));
       }
   };
   for (int b = b0; b < b1; ++b) {
     const int2 gr = __ldg(A.group + b);
-    if (gr.x != cur_g || gr.y != cur_t) {
+    if (gr.x != cur_g) {
       flush();
       cur_g = gr.x;
-      cur_t = gr.y;
       sx = sy = sz = 0.0;
+      tx = ty = tz = 0.0;
     }
     const int4 geo = __ldg(L.bond_geo + b);
     int n0 = c0 + geo.y, n1 = c1 + geo.z, n2 = c2 + geo.w;
@@ -150,14 +158,16 @@ __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __
     if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
     if (!ok) continue;
     const long long j = (long long)geo.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
-    const double gx = g[j], gy = g[N + j], gz = g[2 * N + j];
+    const double gx = __ldg(g + j), gy = __ldg(g + N + j), gz = __ldg(g + 2 * N + j);
     const double* T = L.bond_J + (long long)b * 9;
     ox = fma(__ldg(T + 0), gx, ox); ox = fma(__ldg(T + 1), gy, ox); ox = fma(__ldg(T + 2), gz, ox);
     oy = fma(__ldg(T + 3), gx, oy); oy = fma(__ldg(T + 4), gy, oy); oy = fma(__ldg(T + 5), gz, oy);
     oz = fma(__ldg(T + 6), gx, oz); oz = fma(__ldg(T + 7), gy, oz); oz = fma(__ldg(T + 8), gz, oz);
-    sx += gx;
-    sy += gy;
-    sz += gz;
+    if (gr.y) {
+      tx += gx; ty += gy; tz += gz;
+    } else {
+      sx += gx; sy += gy; sz += gz;
+    }
   }
   flush();
 }
@@ -165,30 +175,30 @@ __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __
 // ---------------------------------------------------------------- forward recomputation (stores states)
 template <int NOISE>
 __global__ void __launch_bounds__(256) k_fwd_pred(const DevLattice L, const DevLLG P, const double* __restrict__ e,
-                                                  uint64_t step, double* __restrict__ H1) {
+                                                  uint64_t step, double* __restrict__ H1, double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) predict_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H1);
+  if (q < L.N) predict_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H1, R);
 }
 
 template <int NOISE>
 __global__ void __launch_bounds__(256) k_fwd_corr(const DevLattice L, const DevLLG P, double* __restrict__ e,
-                                                  uint64_t step, double* __restrict__ H2, double* __restrict__ eout) {
+                                                  uint64_t step, double* __restrict__ H2, double* __restrict__ eout,
+                                                  double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) correct_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H2, eout);
+  if (q < L.N) correct_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H2, eout, nullptr, R + L.N);
 }
 
 // ---------------------------------------------------------------- backward kernels
-__global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double* __restrict__ E,
-                                                   const double* __restrict__ Pp, const double* __restrict__ H1,
-                                                   const double* __restrict__ H2, const double* __restrict__ ebar,
-                                                   double* __restrict__ eacc, double* __restrict__ pbar,
-                                                   double* __restrict__ f1bar, double* __restrict__ g2) {
+// Site-local part of the backward step (first kernel body of step n): ybar from zbar = dL/de' through
+// the corrector normalisation (e' = y |y|^-1 and |y|^-1 are stored), the rhs adjoint at (p, H2), g2
+// and the stage-2 single-ion and field gradients.
+__device__ __forceinline__ void adj_local_site(const AdjDev& A, long long q, const double* __restrict__ Z,
+                                               const double* __restrict__ Pp, const double* __restrict__ H2,
+                                               const double* __restrict__ R, double zbx, double zby, double zbz,
+                                               double* __restrict__ eacc, double* __restrict__ pbar,
+                                               double* __restrict__ f1bar, double* __restrict__ g2) {
   const DevLattice& L = A.F;
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= L.N) return;
   const long long N = L.N;
-  double zbx, zby, zbz;
-  load3(ebar, N, q, zbx, zby, zbz);
   if (L.pinned && L.pinned[q]) {
     store3(eacc, N, q, zbx, zby, zbz);
     store3(pbar, N, q, 0.0, 0.0, 0.0);
@@ -197,35 +207,29 @@ __global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double*
     return;
   }
   const int s = (int)(q / L.ncell);
-  double ex, ey, ez, px, py, pz, h1x, h1y, h1z, h2x, h2y, h2z;
-  load3(E, N, q, ex, ey, ez);
+  double zx, zy, zz, px, py, pz, h2x, h2y, h2z;
+  load3(Z, N, q, zx, zy, zz);
   load3(Pp, N, q, px, py, pz);
-  load3(H1, N, q, h1x, h1y, h1z);
   load3(H2, N, q, h2x, h2y, h2z);
+  const double inv_ny = R[N + q];
   const bool prec = A.precession != 0;
-  double f1x, f1y, f1z, f2x, f2y, f2z;
-  llg_rhs(ex, ey, ez, h1x, h1y, h1z, A.alpha, A.pre, prec, f1x, f1y, f1z);
-  llg_rhs(px, py, pz, h2x, h2y, h2z, A.alpha, A.pre, prec, f2x, f2y, f2z);
-  const double yx = fma(A.half_dt, f1x + f2x, ex), yy = fma(A.half_dt, f1y + f2y, ey), yz = fma(A.half_dt, f1z + f2z, ez);
-  const double ny = sqrt(yx * yx + yy * yy + yz * yz), inv_ny = 1.0 / ny;
-  const double zx = yx * inv_ny, zy = yy * inv_ny, zz = yz * inv_ny;
   const double zd = zx * zbx + zy * zby + zz * zbz;
-  const double ybx = (zbx - zx * zd) * inv_ny, yby = (zby - zy * zd) * inv_ny, ybz = (zbz - zz * zd) * inv_ny;
+  const double ybx = fma(-zx, zd, zbx) * inv_ny, yby = fma(-zy, zd, zby) * inv_ny, ybz = fma(-zz, zd, zbz) * inv_ny;
   const double fbx = A.half_dt * ybx, fby = A.half_dt * yby, fbz = A.half_dt * ybz;
   double Hbx, Hby, Hbz, pbx, pby, pbz;
   rhs_adjoint(px, py, pz, h2x, h2y, h2z, fbx, fby, fbz, A.alpha, A.pre, prec, Hbx, Hby, Hbz, pbx, pby, pbz);
-  const double inv = L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s];
-  const double gx = 2.0 * Hbx * inv, gy = 2.0 * Hby * inv, gz = 2.0 * Hbz * inv;
+  const double inv2 = 2.0 * (L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s]);
+  const double gx = Hbx * inv2, gy = Hby * inv2, gz = Hbz * inv2;
   if (L.has_A) {
     double a[9];
     onsite_tensor(L, q, s, a);
     pbx -= a[0] * gx + a[3] * gy + a[6] * gz;     // -A^T g
     pby -= a[1] * gx + a[4] * gy + a[7] * gz;
     pbz -= a[2] * gx + a[5] * gy + a[8] * gz;
-  }
-  const double gv[3] = {gx, gy, gz}, pv[3] = {px, py, pz};
+    const double gv[3] = {gx, gy, gz}, pv[3] = {px, py, pz};
 #pragma unroll
-  for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * pv[k % 3];
+    for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * pv[k % 3];
+  }
   A.PB[q] += Hbx;
   A.PB[N + q] += Hby;
   A.PB[2 * N + q] += Hbz;
@@ -235,11 +239,26 @@ __global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double*
   store3(g2, N, q, gx, gy, gz);
 }
 
+__global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double* __restrict__ Z,
+                                                   const double* __restrict__ Pp, const double* __restrict__ H2,
+                                                   const double* __restrict__ R, const double* __restrict__ ebar,
+                                                   double* __restrict__ eacc, double* __restrict__ pbar,
+                                                   double* __restrict__ f1bar, double* __restrict__ g2) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= A.F.N) return;
+  double zbx, zby, zbz;
+  load3(ebar, A.F.N, q, zbx, zby, zbz);
+  adj_local_site(A, q, Z, Pp, H2, R, zbx, zby, zbz, eacc, pbar, f1bar, g2);
+}
+
+// Second kernel of step n: pbar += sum_rev J^T g2, xbar through the predictor normalisation
+// (p = x |x|^-1, both stored), the rhs adjoint at (e, H1), g1; stage-2 coupling and stage-1 single-ion
+// and field gradients.
 __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* __restrict__ E,
                                                  const double* __restrict__ Pp, const double* __restrict__ H1,
-                                                 double* __restrict__ eacc, const double* __restrict__ pbar,
-                                                 const double* __restrict__ f1bar, const double* __restrict__ g2,
-                                                 double* __restrict__ g1) {
+                                                 const double* __restrict__ R, double* __restrict__ eacc,
+                                                 const double* __restrict__ pbar, const double* __restrict__ f1bar,
+                                                 const double* __restrict__ g2, double* __restrict__ g1) {
   const DevLattice& L = A.F;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
@@ -265,14 +284,10 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
   double ex, ey, ez, h1x, h1y, h1z;
   load3(E, N, q, ex, ey, ez);
   load3(H1, N, q, h1x, h1y, h1z);
+  const double inv_nx = R[q];
   const bool prec = A.precession != 0;
-  double f1x, f1y, f1z;
-  llg_rhs(ex, ey, ez, h1x, h1y, h1z, A.alpha, A.pre, prec, f1x, f1y, f1z);
-  const double xx = fma(A.dt, f1x, ex), xy = fma(A.dt, f1y, ey), xz = fma(A.dt, f1z, ez);
-  const double nx = sqrt(xx * xx + xy * xy + xz * xz), inv_nx = 1.0 / nx;
-  const double ux = xx * inv_nx, uy = xy * inv_nx, uz = xz * inv_nx;
-  const double ud = ux * pbx + uy * pby + uz * pbz;
-  const double xbx = (pbx - ux * ud) * inv_nx, xby = (pby - uy * ud) * inv_nx, xbz = (pbz - uz * ud) * inv_nx;
+  const double ud = px * pbx + py * pby + pz * pbz;
+  const double xbx = fma(-px, ud, pbx) * inv_nx, xby = fma(-py, ud, pby) * inv_nx, xbz = fma(-pz, ud, pbz) * inv_nx;
   ax += xbx;
   ay += xby;
   az += xbz;
@@ -283,8 +298,8 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
   fbz = fma(A.dt, xbz, fbz);
   double Hbx, Hby, Hbz, ebx, eby, ebz;
   rhs_adjoint(ex, ey, ez, h1x, h1y, h1z, fbx, fby, fbz, A.alpha, A.pre, prec, Hbx, Hby, Hbz, ebx, eby, ebz);
-  const double inv = L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s];
-  const double gx = 2.0 * Hbx * inv, gy = 2.0 * Hby * inv, gz = 2.0 * Hbz * inv;
+  const double inv2 = 2.0 * (L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s]);
+  const double gx = Hbx * inv2, gy = Hby * inv2, gz = Hbz * inv2;
   ax += ebx;
   ay += eby;
   az += ebz;
@@ -294,10 +309,10 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
     ax -= a[0] * gx + a[3] * gy + a[6] * gz;
     ay -= a[1] * gx + a[4] * gy + a[7] * gz;
     az -= a[2] * gx + a[5] * gy + a[8] * gz;
-  }
-  const double gv[3] = {gx, gy, gz}, ev[3] = {ex, ey, ez};
+    const double gv[3] = {gx, gy, gz}, ev[3] = {ex, ey, ez};
 #pragma unroll
-  for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * ev[k % 3];
+    for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * ev[k % 3];
+  }
   A.PB[q] += Hbx;
   A.PB[N + q] += Hby;
   A.PB[2 * N + q] += Hbz;
@@ -305,9 +320,16 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
   store3(g1, N, q, gx, gy, gz);
 }
 
+// Last kernel of step n: ebar_n = acc + sum_rev J^T g1 (and the stage-1 coupling gradients).  With
+// FUSE the site-local body of step n - 1 follows in the same thread on ebar_n, which is then never
+// stored; otherwise ebar_n is written out.
+template <bool FUSE>
 __global__ void __launch_bounds__(256) k_adj_final(const AdjDev A, const double* __restrict__ E,
-                                                   const double* __restrict__ eacc, const double* __restrict__ g1,
-                                                   double* __restrict__ ebar) {
+                                                   double* __restrict__ eacc, const double* __restrict__ g1,
+                                                   double* __restrict__ ebar, const double* __restrict__ Pprev,
+                                                   const double* __restrict__ H2prev, const double* __restrict__ Rprev,
+                                                   double* __restrict__ pbar, double* __restrict__ f1bar,
+                                                   double* __restrict__ g2) {
   const DevLattice& L = A.F;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
@@ -320,7 +342,12 @@ __global__ void __launch_bounds__(256) k_adj_final(const AdjDev A, const double*
   adjoint_gather(A, g1, q, s, c0, c1, c2, ex, ey, ez, tx, ty, tz);
   double ax, ay, az;
   load3(eacc, N, q, ax, ay, az);
-  store3(ebar, N, q, ax + tx, ay + ty, az + tz);
+  if (FUSE) {
+    // step n - 1 ends in e(n) = E: its corrector output z is this step's input spins
+    adj_local_site(A, q, E, Pprev, H2prev, Rprev, ax + tx, ay + ty, az + tz, eacc, pbar, f1bar, g2);
+  } else {
+    store3(ebar, N, q, ax + tx, ay + ty, az + tz);
+  }
 }
 
 // out[r] = sum of x[r*stride .. r*stride + len)  (one block per row, fixed-order tree)
@@ -340,8 +367,17 @@ __global__ void __launch_bounds__(256) k_sum_rows(const double* __restrict__ x, 
   }
 }
 
-static double* seg_ptr(const AdjPlan* a, int n, int k) {   // k: 0 E, 1 P, 2 H1, 3 H2
-  return a->seg + ((size_t)n * 4 + k) * 3 * (size_t)a->fwd->d.N;
+constexpr int SEG_E = 0, SEG_P = 1, SEG_H1 = 2, SEG_H2 = 3, SEG_R = 4;
+
+// Segment storage: per step [e | ep | H1 | H2] (3N doubles each) and [1/|x| | 1/|y|] (2N) of the
+// predictor and corrector normalisations, then one more e slot for the spins after the last step.
+static size_t seg_stride(const AdjPlan* a) { return 14 * (size_t)a->fwd->d.N; }
+static size_t seg_doubles(const AdjPlan* a) { return seg_stride(a) * a->seg_cap + 3 * (size_t)a->fwd->d.N; }
+
+static double* seg_ptr(const AdjPlan* a, int n, int k) {
+  const size_t N = (size_t)a->fwd->d.N;
+  if (k == SEG_E && n == a->seg_cap) return a->seg + seg_stride(a) * a->seg_cap;   // tail slot
+  return a->seg + seg_stride(a) * n + (size_t)k * 3 * N;
 }
 
 }  // namespace mgx
@@ -357,6 +393,8 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   const Model* R = reinterpret_cast<const Model*>(rev);
   if (!F || !R || !p || !out) return set_error(MGX_ERR_INVALID, "mgx_adjoint_create: null argument");
   *out = nullptr;
+  if (F->d.layout != 0 || R->d.layout != 0)
+    return set_error(MGX_ERR_UNSUPPORTED, "the adjoint is implemented for lattice stencils, not neighbour lists");
   if (F->d.width != 9 || R->d.width != 9)
     return set_error(MGX_ERR_INVALID, "the adjoint needs full-tensor (width 9) forward and reverse models");
   if (F->d.ns != R->d.ns || F->d.L0 != R->d.L0 || F->d.L1 != R->d.L1 || F->d.L2 != R->d.L2 ||
@@ -386,8 +424,8 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   const double gamma = 0.1760859630;
   const double pre = -gamma / (1.0 + p->alpha * p->alpha);
   const size_t n3 = 3 * (size_t)N;
-  cudaError_t err = cudaMalloc(&a->seg, sizeof(double) * n3 * 4 * seg_steps);
-  if (err == cudaSuccess) err = cudaMalloc(&a->e_end, sizeof(double) * n3);
+  cudaError_t err = cudaMalloc(&a->own_seg, sizeof(double) * seg_doubles(a));
+  a->seg = a->own_seg;
   if (err == cudaSuccess) err = cudaMalloc(&a->work, sizeof(double) * n3 * 5);
   if (err == cudaSuccess) err = cudaMalloc(&a->k1, sizeof(double) * n3);
   if (err == cudaSuccess) err = cudaMalloc(&a->d_group, sizeof(int2) * grp.size());
@@ -442,8 +480,7 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
 mgx_status mgx_adjoint_destroy(mgx_adjoint* aa) {
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
   if (!a) return MGX_OK;
-  cudaFree(a->seg);
-  cudaFree(a->e_end);
+  cudaFree(a->own_seg);
   cudaFree(a->work);
   cudaFree(a->k1);
   cudaFree(a->d_group);
@@ -474,6 +511,19 @@ mgx_status mgx_adjoint_sync_models(mgx_adjoint* aa) {
   return MGX_OK;
 }
 
+int64_t mgx_adjoint_storage_doubles(const mgx_adjoint* aa) {
+  const AdjPlan* a = reinterpret_cast<const AdjPlan*>(aa);
+  return a ? (int64_t)seg_doubles(a) : -1;
+}
+
+mgx_status mgx_adjoint_set_storage(mgx_adjoint* aa, double* storage) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_set_storage: null adjoint");
+  if (storage && ((uintptr_t)storage % 16) != 0) return set_error(MGX_ERR_INVALID, "storage must be 16-byte aligned");
+  a->seg = storage ? storage : a->own_seg;
+  return MGX_OK;
+}
+
 mgx_status mgx_adjoint_forward(mgx_adjoint* aa, const double* e0, int32_t nsteps, uint64_t step0, double* e_out,
                                void* stream) {
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
@@ -483,49 +533,58 @@ mgx_status mgx_adjoint_forward(mgx_adjoint* aa, const double* e0, int32_t nsteps
   cudaStream_t st = (cudaStream_t)stream;
   const DevLattice& L = a->fwd->d;
   const long long N = L.N;
-  const unsigned grid = (unsigned)((N + 255) / 256);
-  MGX_CUDA_TRY(cudaMemcpyAsync(seg_ptr(a, 0, 0), e0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
+  const int tpb = site_block_size(N);
+  const unsigned grid = (unsigned)((N + tpb - 1) / tpb);
+  if (e0 != seg_ptr(a, 0, SEG_E))
+    MGX_CUDA_TRY(cudaMemcpyAsync(seg_ptr(a, 0, SEG_E), e0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
   for (int n = 0; n < nsteps; ++n) {
     DevLLG P = a->P;
-    P.ep = seg_ptr(a, n, 1);
-    double* E = seg_ptr(a, n, 0);
-    double* eout = (n + 1 < nsteps) ? seg_ptr(a, n + 1, 0) : a->e_end;
+    P.ep = seg_ptr(a, n, SEG_P);
+    double* E = seg_ptr(a, n, SEG_E);
+    double* R = seg_ptr(a, n, SEG_R);
     const uint64_t step = step0 + (uint64_t)n;
     if (a->noise == MGX_NOISE_PHILOX) {
-      k_fwd_pred<MGX_NOISE_PHILOX><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 2));
-      k_fwd_corr<MGX_NOISE_PHILOX><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 3), eout);
+      k_fwd_pred<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
+      k_fwd_corr<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
     } else {
-      k_fwd_pred<MGX_NOISE_NONE><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 2));
-      k_fwd_corr<MGX_NOISE_NONE><<<grid, 256, 0, st>>>(L, P, E, step, seg_ptr(a, n, 3), eout);
+      k_fwd_pred<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
+      k_fwd_corr<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
     }
   }
-  a->seg_steps = nsteps;
-  if (e_out) MGX_CUDA_TRY(cudaMemcpyAsync(e_out, a->e_end, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
+  if (e_out)
+    MGX_CUDA_TRY(cudaMemcpyAsync(e_out, seg_ptr(a, nsteps, SEG_E), sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }
 
-mgx_status mgx_adjoint_backward(mgx_adjoint* aa, double* ebar, void* stream) {
+mgx_status mgx_adjoint_backward(mgx_adjoint* aa, double* ebar, int32_t nsteps, void* stream) {
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
   if (!a || !ebar) return set_error(MGX_ERR_INVALID, "mgx_adjoint_backward: null argument");
-  if (a->seg_steps < 1) return set_error(MGX_ERR_INVALID, "mgx_adjoint_backward: run mgx_adjoint_forward first");
+  if (nsteps < 1 || nsteps > a->seg_cap)
+    return set_error(MGX_ERR_INVALID, "nsteps = %d outside 1..%d (segment capacity)", nsteps, a->seg_cap);
   cudaStream_t st = (cudaStream_t)stream;
   const long long N = a->fwd->d.N;
   const size_t n3 = 3 * (size_t)N;
-  const unsigned grid = (unsigned)((N + 255) / 256);
+  const int tpb = site_block_size(N);
+  const unsigned grid = (unsigned)((N + tpb - 1) / tpb);
   double* eacc = a->work;
   double* pbar = a->work + n3;
   double* f1bar = a->work + 2 * n3;
   double* g1 = a->work + 3 * n3;
   double* g2 = a->work + 4 * n3;
-  for (int n = a->seg_steps - 1; n >= 0; --n) {
-    const double* E = seg_ptr(a, n, 0);
-    const double* Pp = seg_ptr(a, n, 1);
-    const double* H1 = seg_ptr(a, n, 2);
-    const double* H2 = seg_ptr(a, n, 3);
-    k_adj_local<<<grid, 256, 0, st>>>(a->d, E, Pp, H1, H2, ebar, eacc, pbar, f1bar, g2);
-    k_adj_mid<<<grid, 256, 0, st>>>(a->d, E, Pp, H1, eacc, pbar, f1bar, g2, g1);
-    k_adj_final<<<grid, 256, 0, st>>>(a->d, E, eacc, g1, ebar);
+  const int last = nsteps - 1;
+  k_adj_local<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, last + 1, SEG_E), seg_ptr(a, last, SEG_P),
+                                    seg_ptr(a, last, SEG_H2), seg_ptr(a, last, SEG_R), ebar, eacc, pbar, f1bar, g2);
+  for (int n = last; n >= 0; --n) {
+    k_adj_mid<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
+                                    seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
+    if (n > 0) {
+      k_adj_final<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr, seg_ptr(a, n - 1, SEG_P),
+                                              seg_ptr(a, n - 1, SEG_H2), seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
+    } else {
+      k_adj_final<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr, nullptr,
+                                               nullptr, nullptr, nullptr);
+    }
   }
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;

@@ -48,6 +48,13 @@ struct DevLattice {
   const double* mu_site;         // [N] or nullptr
   const uint8_t* pinned;         // [N] or nullptr
   double B0, B1, B2;
+  // neighbour-list layout (arbitrary lattices): ns = 1, ncell = N, site q has couplings
+  // csr_ptr[q] .. csr_ptr[q+1] to csr_nbr[k] with tensor bond_J[csr_typ[k]]
+  int layout;                    // 0 stencil, 1 csr
+  const long long* csr_ptr;      // [N+1]
+  const int* csr_nbr;            // [nnz]
+  const int* csr_typ;            // [nnz]
+  const double* sign_site;       // [N] order-parameter signs, or nullptr
 };
 
 struct Model {
@@ -62,6 +69,8 @@ struct Model {
   double* partials = nullptr;    // reduction scratch for observables
   int partial_cap = 0;           // number of 8-double slots
   int* slot_of_bond = nullptr;   // host [nbond]: position of input coupling b in the device table
+  void* csr_block = nullptr;     // ptr | nbr | typ (neighbour-list layout)
+  double* sign_site = nullptr;
 };
 
 // ------------------------------------------------------------------ LLG plan (mgx_llg.cu)
@@ -84,11 +93,20 @@ struct DevLLG {
 struct LLGPlan {
   const Model* model;
   DevLLG p;
+  bool sigma_zero = true;        // every thermal amplitude is 0: the noise-free kernels are used
   void* sub_block = nullptr;     // alpha_sub | pre_sub | sigma_sub
   double* site_block = nullptr;  // alpha_site | pre_site
   double* sigma_site = nullptr;
   double* scratch = nullptr;     // ep | k1
 };
+
+// Threads per block of the one-site-per-thread kernels: 256, or fewer for small lattices so that the
+// grid still spreads over every SM (a 16k-site film gives 256 blocks of 64 instead of 64 of 256).
+inline int site_block_size(long long N) {
+  if (N >= 152LL * 8 * 256) return 256;
+  if (N >= 152LL * 4 * 128) return 128;
+  return 64;
+}
 
 // Enqueue the predictor (stages & 1) and / or the corrector (stages & 2) of one step on st.
 void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
@@ -113,6 +131,32 @@ __device__ __forceinline__ void exchange_field(const DevLattice& L, const double
   hy = 0.0;
   hz = 0.0;
   const long long N = L.N;
+  if (L.layout == 1) {
+    // per-site neighbour list (magex/fast.py:87-120 layout): q = c2 when ns = 1 and ncell = N
+    const long long q = c2;
+    const long long k1 = __ldg(L.csr_ptr + q + 1);
+    for (long long k = __ldg(L.csr_ptr + q); k < k1; ++k) {
+      const long long j = __ldg(L.csr_nbr + k);
+      const double ex = __ldg(x + j), ey = __ldg(x + N + j), ez = __ldg(x + 2 * N + j);
+      const double* T = L.bond_J + (long long)__ldg(L.csr_typ + k) * W;
+      if (W == 1) {
+        const double J = __ldg(T);
+        hx = fma(J, ex, hx);
+        hy = fma(J, ey, hy);
+        hz = fma(J, ez, hz);
+      } else if (W == 4) {
+        const double J = __ldg(T), Dx = __ldg(T + 1), Dy = __ldg(T + 2), Dz = __ldg(T + 3);
+        hx = fma(J, ex, hx); hx = fma(ey, Dz, hx); hx = fma(-ez, Dy, hx);
+        hy = fma(J, ey, hy); hy = fma(ez, Dx, hy); hy = fma(-ex, Dz, hy);
+        hz = fma(J, ez, hz); hz = fma(ex, Dy, hz); hz = fma(-ey, Dx, hz);
+      } else {
+        hx = fma(__ldg(T + 0), ex, hx); hx = fma(__ldg(T + 1), ey, hx); hx = fma(__ldg(T + 2), ez, hx);
+        hy = fma(__ldg(T + 3), ex, hy); hy = fma(__ldg(T + 4), ey, hy); hy = fma(__ldg(T + 5), ez, hy);
+        hz = fma(__ldg(T + 6), ex, hz); hz = fma(__ldg(T + 7), ey, hz); hz = fma(__ldg(T + 8), ez, hz);
+      }
+    }
+    return;
+  }
   const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
   for (int b = b0; b < b1; ++b) {
     const int4 g = __ldg(L.bond_geo + b);

@@ -31,7 +31,7 @@ template <int W, int NOISE, int INTEG>
 static void launch_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages,
                         cudaStream_t st) {
   const DevLattice& L = pl->model->d;
-  const int tpb = 256;
+  const int tpb = site_block_size(L.N);
   const unsigned grid = (unsigned)((L.N + tpb - 1) / tpb);
   if (stages & 1) k_predict<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step);
   if (stages & 2) k_correct<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step);
@@ -49,7 +49,9 @@ static void dispatch_integ(const LLGPlan* pl, double* e, const double* noise, ui
 template <int W>
 static void dispatch_noise(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages,
                            cudaStream_t st) {
-  switch (pl->p.noise) {
+  // sigma = 0 everywhere: the thermal field is exactly zero, skip generating it
+  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
+  switch (mode) {
     case MGX_NOISE_HOST: dispatch_integ<W, MGX_NOISE_HOST>(pl, e, noise, step, stages, st); break;
     case MGX_NOISE_PHILOX: dispatch_integ<W, MGX_NOISE_PHILOX>(pl, e, noise, step, stages, st); break;
     default: dispatch_integ<W, MGX_NOISE_NONE>(pl, e, noise, step, stages, st); break;
@@ -161,22 +163,32 @@ mgx_status mgx_llg_set_sigma(mgx_llg* pp, const double* sigma_sub, const double*
   if (!pl) return set_error(MGX_ERR_INVALID, "mgx_llg_set_sigma: null plan");
   const int ns = pl->model->d.ns;
   const long long N = pl->model->d.N;
+  bool zero = true;
   if (sigma_sub) {
-    for (int s = 0; s < ns; ++s)
+    for (int s = 0; s < ns; ++s) {
       if (!std::isfinite(sigma_sub[s]) || sigma_sub[s] < 0.0)
         return set_error(MGX_ERR_INVALID, "sigma_sub must be finite and >= 0");
+      zero &= sigma_sub[s] == 0.0;
+    }
     MGX_CUDA_TRY(cudaMemcpy((double*)pl->sub_block + 2 * ns, sigma_sub, sizeof(double) * ns, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<double> cur(ns);
+    MGX_CUDA_TRY(cudaMemcpy(cur.data(), (double*)pl->sub_block + 2 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+    for (double x : cur) zero &= x == 0.0;
   }
   if (sigma_site) {
     std::vector<double> v = site_to_lattice(sigma_site, ns, pl->model->d.ncell);
-    for (double x : v)
+    for (double x : v) {
       if (!std::isfinite(x) || x < 0.0) return set_error(MGX_ERR_INVALID, "sigma_site must be finite and >= 0");
+      zero &= x == 0.0;
+    }
     if (!pl->sigma_site) MGX_CUDA_TRY(cudaMalloc(&pl->sigma_site, sizeof(double) * N));
     MGX_CUDA_TRY(cudaMemcpy(pl->sigma_site, v.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
     pl->p.sigma_site = pl->sigma_site;
   } else {
     pl->p.sigma_site = nullptr;
   }
+  pl->sigma_zero = zero;
   return MGX_OK;
 }
 

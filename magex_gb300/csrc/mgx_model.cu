@@ -238,6 +238,121 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
   return MGX_OK;
 }
 
+mgx_status mgx_model_create_csr(const mgx_csr_desc* c, mgx_model** out) {
+  if (!c || !out) return set_error(MGX_ERR_INVALID, "mgx_model_create_csr: null argument");
+  *out = nullptr;
+  const long long N = c->nsites;
+  if (N < 1 || N > 0x7fffffffLL) return set_error(MGX_ERR_INVALID, "nsites = %lld outside 1..2^31-1", N);
+  const int W = c->width;
+  if (W != 1 && W != 4 && W != 9) return set_error(MGX_ERR_INVALID, "coupling width %d must be 1, 4 or 9", W);
+  if (!c->ptr || !c->mu_site) return set_error(MGX_ERR_INVALID, "ptr and mu_site must not be null");
+  if (c->ptr[0] != 0) return set_error(MGX_ERR_INVALID, "ptr[0] must be 0");
+  for (long long i = 0; i < N; ++i)
+    if (c->ptr[i + 1] < c->ptr[i]) return set_error(MGX_ERR_INVALID, "ptr must be non-decreasing (site %lld)", i);
+  const long long nnz = c->ptr[N];
+  if (nnz > 0 && (!c->nbr || !c->typ || !c->table)) return set_error(MGX_ERR_INVALID, "nbr, typ and table must not be null");
+  if (c->ntypes < (nnz > 0 ? 1 : 0)) return set_error(MGX_ERR_INVALID, "ntypes must be >= 1");
+  for (long long k = 0; k < nnz; ++k) {
+    if (c->nbr[k] < 0 || c->nbr[k] >= N) return set_error(MGX_ERR_INVALID, "nbr[%lld] = %d outside 0..N-1", k, c->nbr[k]);
+    if (c->typ[k] < 0 || c->typ[k] >= c->ntypes) return set_error(MGX_ERR_INVALID, "typ[%lld] = %d outside 0..ntypes-1", k, c->typ[k]);
+  }
+  std::vector<double> inv(N);
+  for (long long i = 0; i < N; ++i) {
+    if (!(c->mu_site[i] > 0.0)) return set_error(MGX_ERR_INVALID, "mu_site[%lld] must be > 0", i);
+    inv[i] = 1.0 / (c->mu_site[i] * 5.7883818060e-2);
+  }
+  Model* m = new Model();
+  DevLattice& d = m->d;
+  d.ns = 1;
+  d.L0 = 1;
+  d.L1 = 1;
+  d.L2 = (int)N;
+  d.ncell = (int)N;
+  d.N = N;
+  d.pbc0 = d.pbc1 = d.pbc2 = 1;
+  d.width = W;
+  d.B0 = c->B[0];
+  d.B1 = c->B[1];
+  d.B2 = c->B[2];
+  d.layout = 1;
+  m->nbond = 0;
+  m->slot_of_bond = new int[1];
+  const int nt = std::max(c->ntypes, 1);
+  // dev_block: [off (2 ints) | J (nt*W) | A_sub (9) | inv_mu | mu | sign (1 each)]
+  const size_t s_J = 16, n_J = sizeof(double) * (size_t)nt * W;
+  const size_t s_A = s_J + n_J, s_inv = s_A + 9 * sizeof(double), s_mu = s_inv + 8, s_sg = s_mu + 8, total = s_sg + 8;
+  std::vector<char> host(total, 0);
+  if (c->ntypes > 0) std::memcpy(host.data() + s_J, c->table, sizeof(double) * (size_t)c->ntypes * W);
+  const double one = 1.0;
+  std::memcpy(host.data() + s_inv, &one, 8);
+  std::memcpy(host.data() + s_mu, &one, 8);
+  std::memcpy(host.data() + s_sg, &one, 8);
+  const size_t c_ptr = 0, c_nbr = sizeof(long long) * (N + 1), c_typ = c_nbr + sizeof(int) * (size_t)std::max(nnz, 1LL);
+  const size_t c_total = c_typ + sizeof(int) * (size_t)std::max(nnz, 1LL);
+  cudaError_t err = cudaMalloc(&m->dev_block, total);
+  if (err == cudaSuccess) err = cudaMemcpy(m->dev_block, host.data(), total, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMalloc(&m->csr_block, c_total);
+  if (err == cudaSuccess) err = cudaMemcpy((char*)m->csr_block + c_ptr, c->ptr, sizeof(long long) * (N + 1), cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && nnz > 0) err = cudaMemcpy((char*)m->csr_block + c_nbr, c->nbr, sizeof(int) * nnz, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess && nnz > 0) err = cudaMemcpy((char*)m->csr_block + c_typ, c->typ, sizeof(int) * nnz, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMalloc(&m->mu_site, sizeof(double) * N);
+  if (err == cudaSuccess) err = cudaMalloc(&m->inv_mu_site, sizeof(double) * N);
+  if (err == cudaSuccess) err = cudaMemcpy(m->mu_site, c->mu_site, sizeof(double) * N, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(m->inv_mu_site, inv.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) {
+    mgx_model_destroy(reinterpret_cast<mgx_model*>(m));
+    return cuda_error(err, "mgx_model_create_csr");
+  }
+  char* base = (char*)m->dev_block;
+  d.bond_off = (const int*)base;
+  d.bond_geo = nullptr;
+  d.bond_J = (const double*)(base + s_J);
+  d.A_sub = (const double*)(base + s_A);
+  d.inv_mu_sub = (const double*)(base + s_inv);
+  d.mu_sub = (const double*)(base + s_mu);
+  d.sign_sub = (const double*)(base + s_sg);
+  d.mu_site = m->mu_site;
+  d.inv_mu_site = m->inv_mu_site;
+  d.csr_ptr = (const long long*)((char*)m->csr_block + c_ptr);
+  d.csr_nbr = (const int*)((char*)m->csr_block + c_nbr);
+  d.csr_typ = (const int*)((char*)m->csr_block + c_typ);
+  d.has_A = 0;
+  if (c->A_site) {
+    bool any = false;
+    for (long long k = 0; k < 9 * N; ++k) any |= c->A_site[k] != 0.0;
+    if (any) {
+      std::vector<double> v((size_t)9 * N);
+      for (long long i = 0; i < N; ++i)
+        for (int k = 0; k < 9; ++k) v[(size_t)k * N + i] = c->A_site[(size_t)i * 9 + k];
+      err = cudaMalloc(&m->A_site, sizeof(double) * v.size());
+      if (err == cudaSuccess) err = cudaMemcpy(m->A_site, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice);
+      if (err != cudaSuccess) { mgx_model_destroy(reinterpret_cast<mgx_model*>(m)); return cuda_error(err, "A_site"); }
+      d.A_site = m->A_site;
+      d.has_A = 1;
+    }
+  }
+  if (c->sign_site) {
+    err = cudaMalloc(&m->sign_site, sizeof(double) * N);
+    if (err == cudaSuccess) err = cudaMemcpy(m->sign_site, c->sign_site, sizeof(double) * N, cudaMemcpyHostToDevice);
+    if (err != cudaSuccess) { mgx_model_destroy(reinterpret_cast<mgx_model*>(m)); return cuda_error(err, "sign_site"); }
+    d.sign_site = m->sign_site;
+  }
+  if (c->pinned) {
+    bool any = false;
+    for (long long i = 0; i < N; ++i) any |= c->pinned[i] != 0;
+    if (any) {
+      std::vector<uint8_t> v(N);
+      for (long long i = 0; i < N; ++i) v[i] = c->pinned[i] ? 1 : 0;
+      err = cudaMalloc(&m->pinned, N);
+      if (err == cudaSuccess) err = cudaMemcpy(m->pinned, v.data(), N, cudaMemcpyHostToDevice);
+      if (err != cudaSuccess) { mgx_model_destroy(reinterpret_cast<mgx_model*>(m)); return cuda_error(err, "pinned"); }
+      d.pinned = m->pinned;
+    }
+  }
+  *out = reinterpret_cast<mgx_model*>(m);
+  return MGX_OK;
+}
+
 mgx_status mgx_model_destroy(mgx_model* mm) {
   Model* m = reinterpret_cast<Model*>(mm);
   if (!m) return MGX_OK;
@@ -247,6 +362,8 @@ mgx_status mgx_model_destroy(mgx_model* mm) {
   cudaFree(m->mu_site);
   cudaFree(m->pinned);
   cudaFree(m->partials);
+  cudaFree(m->csr_block);
+  cudaFree(m->sign_site);
   delete[] m->slot_of_bond;
   delete m;
   return MGX_OK;

@@ -106,6 +106,8 @@ extern "C" mgx_status mgx_llg_step_noalloc(const mgx_model* mm, const mgx_llg_pa
 
   LLGPlan view;                        // host-side descriptor only; owns nothing
   view.model = m;
+  view.sigma_zero = true;
+  for (int s = 0; s < ns; ++s) view.sigma_zero &= sp.v[2 * ns + s] == 0.0;
   DevLLG& d = view.p;
   d.dt = p->dt;
   d.half_dt = 0.5 * p->dt;

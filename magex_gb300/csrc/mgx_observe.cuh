@@ -60,7 +60,7 @@ __device__ __forceinline__ void observe_site(const DevLattice& L, const double* 
   v[1] = ex;
   v[2] = ey;
   v[3] = ez;
-  const double sg = L.sign_sub[s];
+  const double sg = L.sign_site ? L.sign_site[q] : L.sign_sub[s];
   v[4] = sg * ex;
   v[5] = sg * ey;
   v[6] = sg * ez;

@@ -55,7 +55,7 @@ __device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P
 template <int W, int NOISE, int INTEG>
 __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& P, const double* __restrict__ e,
                                              const double* __restrict__ noise, long long q, uint64_t step,
-                                             double* __restrict__ Hout = nullptr) {
+                                             double* __restrict__ Hout = nullptr, double* __restrict__ rout = nullptr) {
   const long long N = L.N;
   const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
   if (L.pinned && L.pinned[q]) {
@@ -92,6 +92,7 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
   const double y = fma(P.dt, fy, ey);
   const double z = fma(P.dt, fz, ez);
   const double r = rsqrt(x * x + y * y + z * z);
+  if (rout) rout[q] = r;
   P.ep[q] = x * r; P.ep[N + q] = y * r; P.ep[2 * N + q] = z * r;
   P.k1[q] = fx; P.k1[N + q] = fy; P.k1[2 * N + q] = fz;
 }
@@ -101,13 +102,17 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
 template <int W, int NOISE, int INTEG>
 __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& P, double* __restrict__ e,
                                              const double* __restrict__ noise, long long q, uint64_t step,
-                                             double* __restrict__ Hout = nullptr, double* __restrict__ eout = nullptr) {
+                                             double* __restrict__ Hout = nullptr, double* __restrict__ eout = nullptr,
+                                             double* __restrict__ fout = nullptr, double* __restrict__ rout = nullptr) {
   if (L.pinned && L.pinned[q]) {
     if (eout) {
       eout[q] = e[q]; eout[L.N + q] = e[L.N + q]; eout[2 * L.N + q] = e[2 * L.N + q];
     }
     if (Hout) {
       Hout[q] = 0.0; Hout[L.N + q] = 0.0; Hout[2 * L.N + q] = 0.0;
+    }
+    if (fout) {
+      fout[q] = 0.0; fout[L.N + q] = 0.0; fout[2 * L.N + q] = 0.0;
     }
     return;
   }
@@ -125,6 +130,9 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
   const double pre = P.pre_site ? __ldg(P.pre_site + q) : __ldg(P.pre_sub + s);
   double fx, fy, fz;
   llg_rhs(px, py, pz, bx, by, bz, a, pre, P.precession != 0, fx, fy, fz);
+  if (fout) {
+    fout[q] = fx; fout[N + q] = fy; fout[2 * N + q] = fz;
+  }
   const double k1x = P.k1[q], k1y = P.k1[N + q], k1z = P.k1[2 * N + q];
   double x = e[q], y = e[N + q], z = e[2 * N + q];
   if (INTEG == MGX_INTEGRATOR_DEPONDT) {
@@ -136,6 +144,7 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
     z = fma(P.half_dt, k1z + fz, z);
   }
   const double r = rsqrt(x * x + y * y + z * z);
+  if (rout) rout[q] = r;
   double* o = eout ? eout : e;
   o[q] = x * r; o[N + q] = y * r; o[2 * N + q] = z * r;
 }

@@ -12,7 +12,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .lattice import Supercell
+from .lattice import NeighbourList, Supercell
 
 
 def _require_cuda():
@@ -35,12 +35,26 @@ def supercell_from_system(system):
     kernels do not implement (biquadratic, four-spin, dipolar, cubic / higher uniaxial, quadruplets)
     raise NotImplementedError, as ``magex/cuda_backend.py:315-316`` does.
     """
-    if isinstance(system, Supercell):
+    if isinstance(system, (Supercell, NeighbourList)):
         sc = system
     else:
+        if getattr(system, "has_higher", False):
+            raise NotImplementedError("biquadratic / four-spin couplings are not supported by the GB300 kernels")
         sc = Supercell(system.uc, system.L, system.pbc, getattr(system, "B", (0.0, 0.0, 0.0)))
-        if int(system.N) != sc.N:
-            raise NotImplementedError("carved systems (vacancies, shapes) are not supported by the GB300 stencil kernels")
+        Jsp = getattr(system, "Jsp", None)
+        if int(system.N) != sc.N or (Jsp is not None and not _stencil_matches(sc, Jsp)):
+            # carved or edited: the per-site neighbour-list layout
+            sc = NeighbourList.from_matrix(Jsp, np.asarray(system.mu, float), np.asarray(system.A, float),
+                                           np.asarray(system.signs, float), getattr(system, "B", (0.0, 0.0, 0.0)))
+            for name in ("pinned", "pinned_dir", "site_T", "alpha_site"):
+                v = getattr(system, name, None)
+                if v is not None:
+                    setattr(sc, name, np.array(v))
+            sc.terms = list(getattr(system, "terms", []) or [])
+            if sc.terms:
+                raise NotImplementedError("extra energy terms (dipolar, cubic, higher uniaxial, quadruplets) "
+                                          "are not supported by the GB300 kernels")
+            return sc
         A = np.asarray(system.A, float).reshape(sc.N, 3, 3)
         if not np.array_equal(A, np.tile(sc.A_sub, (sc.ncell, 1, 1))):
             sc.A_site = A.copy()
@@ -52,11 +66,6 @@ def supercell_from_system(system):
             if v is not None:
                 setattr(sc, name, np.array(v))
         sc.terms = list(getattr(system, "terms", []) or [])
-        if getattr(system, "has_higher", False):
-            raise NotImplementedError("biquadratic / four-spin couplings are not supported by the GB300 kernels")
-        Jsp = getattr(system, "Jsp", None)
-        if Jsp is not None:
-            _check_stencil_matches(sc, Jsp)
     if sc.terms:
         raise NotImplementedError("extra energy terms (dipolar, cubic, higher uniaxial, quadruplets) "
                                   "are not supported by the GB300 kernels")
@@ -65,8 +74,8 @@ def supercell_from_system(system):
     return sc
 
 
-def _check_stencil_matches(sc, Jsp):
-    """The stencil must reproduce the system's sparse coupling matrix (same nonzeros and values)."""
+def _stencil_matches(sc, Jsp):
+    """True when the stencil reproduces the system's sparse coupling matrix (same non-zeros and values)."""
     import scipy.sparse as sp
     ptr, nbr, typ, table = sc.neighbour_csr()
     N = sc.N
@@ -78,9 +87,7 @@ def _check_stencil_matches(sc, Jsp):
     mine = sp.csr_matrix((blocks.ravel(), (R, Cc)), shape=(3 * N, 3 * N))
     diff = abs(Jsp.tocsr() - mine)
     scale = max(float(abs(Jsp).max()) if Jsp.nnz else 0.0, 1e-300)
-    if diff.nnz and float(diff.max()) > 1e-12 * scale:
-        raise NotImplementedError("the system's coupling matrix is not the translation-invariant stencil of its "
-                                  "unit cell (edited exchange); this layout is not supported by the GB300 kernels")
+    return not (diff.nnz and float(diff.max()) > 1e-12 * scale)
 
 
 class DeviceModel:
@@ -92,6 +99,10 @@ class DeviceModel:
         self.sc = sc
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         self.N = sc.N
+        self._keep = []
+        if isinstance(sc, NeighbourList):
+            self._create_csr(sc)
+            return
         nb = len(sc.bond_src)
         if nb > _lib.MAX_BONDS:
             raise NotImplementedError(f"{nb} couplings per cell exceed the kernel limit of {_lib.MAX_BONDS}")
@@ -136,6 +147,38 @@ class DeviceModel:
             _lib.check(self.lib.mgx_model_create(C.byref(d), C.byref(sites), C.byref(h)), "mgx_model_create")
         self.handle = h
         self._keep = []
+        self._B = np.array(sc.B, float)
+        self._obs = torch.empty(8, dtype=torch.float64, device=self.device)
+        self._tri = None
+        self.field_owner = None
+
+    def _create_csr(self, sc):
+        c = _lib.CSRDesc()
+        c.nsites = sc.N
+        ptr = np.ascontiguousarray(sc.ptr, np.int64)
+        nbr = np.ascontiguousarray(sc.nbr, np.int32)
+        typ = np.ascontiguousarray(sc.typ, np.int32)
+        tab = np.ascontiguousarray(sc.table, np.float64).reshape(-1)
+        mu = np.ascontiguousarray(sc.mu_site, np.float64)
+        sg = np.ascontiguousarray(sc.signs_site, np.float64)
+        A = None if sc.A_site is None else np.ascontiguousarray(sc.A_site, np.float64).reshape(-1)
+        pin = None if sc.pinned is None else np.ascontiguousarray(np.asarray(sc.pinned, bool), np.uint8)
+        keep = [ptr, nbr, typ, tab, mu, sg, A, pin]
+        c.ptr = ptr.ctypes.data_as(C.POINTER(C.c_int64))
+        c.nbr, c.typ = _lib.iptr(nbr), _lib.iptr(typ)
+        c.ntypes = len(sc.table)
+        c.width = sc.width
+        c.table = _lib.dptr(tab)
+        c.A_site = _lib.dptr(A)
+        c.mu_site = _lib.dptr(mu)
+        c.sign_site = _lib.dptr(sg)
+        c.pinned = _lib.u8ptr(pin)
+        c.B[:] = [float(x) for x in sc.B]
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.mgx_model_create_csr(C.byref(c), C.byref(h)), "mgx_model_create_csr")
+        del keep
+        self.handle = h
         self._B = np.array(sc.B, float)
         self._obs = torch.empty(8, dtype=torch.float64, device=self.device)
         self._tri = None

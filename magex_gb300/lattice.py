@@ -246,3 +246,88 @@ class Supercell:
         return (f"GB300 supercell {self.L} pbc {self.pbc}: N = {self.N} spins, {self.ns} sublattices, "
                 f"{len(self.bond_src)} stencil couplings (table width {self.width}), "
                 f"B = {self.B.tolist()} T, mu_B = {MU_B}")
+
+
+class NeighbourList:
+    """Arbitrary spin system as per-site neighbour lists (carved shapes, vacancies, edited exchange).
+
+    Built from a 3N x 3N coupling matrix the way magex builds its kernel tables
+    (``magex/fast.py:587-627``): the 3x3 blocks of each (site, neighbour) pair, neighbours sorted by
+    index, identical blocks stored once in a type table, compressed to width 1 / 4 when exact.  Carries
+    the per-site arrays the LLG path reads; the device layout of its spins is magex's site order.
+    """
+
+    def __init__(self, ptr, nbr, typ, tensors, mu, A=None, signs=None, field=(0.0, 0.0, 0.0)):
+        self.N = int(len(ptr) - 1)
+        self.ns, self.ncell = 1, self.N
+        self.L, self.pbc = (1, 1, self.N), (True, True, True)
+        self.ptr = np.ascontiguousarray(ptr, np.int64)
+        self.nbr = np.ascontiguousarray(nbr, np.int32)
+        self.typ = np.ascontiguousarray(typ, np.int32)
+        self.bond_J = np.asarray(tensors, float).reshape(-1, 3, 3)
+        self.width, self.table = compress_tensors(self.bond_J)
+        self.mu_site = np.ascontiguousarray(mu, float).reshape(self.N)
+        self.mu_sub = np.ones(1)
+        self.A_site = None if A is None else np.ascontiguousarray(A, float).reshape(self.N, 3, 3)
+        self.A_sub = np.zeros((1, 3, 3))
+        self.signs_site = np.ones(self.N) if signs is None else np.asarray(signs, float).reshape(self.N)
+        self.signs_sub = np.ones(1)
+        self.pinned = None
+        self.pinned_dir = None
+        self.site_T = None
+        self.alpha_site = None
+        self.terms = []
+        self.biquadratic = []
+        self.four_spin = 0.0
+        self.set_field(field)
+
+    @classmethod
+    def from_matrix(cls, Jsp, mu, A=None, signs=None, field=(0.0, 0.0, 0.0)):
+        """From a 3N x 3N (scipy) coupling matrix with J_ij in rows 3i..3i+2, columns 3j..3j+2."""
+        J = Jsp.tocoo()
+        N = J.shape[0] // 3
+        i, j = J.row // 3, J.col // 3
+        comp = 3 * (J.row % 3) + J.col % 3
+        key = i.astype(np.int64) * N + j
+        pairs, inv = np.unique(key, return_inverse=True)
+        blocks = np.zeros((len(pairs), 9))
+        np.add.at(blocks, (inv.reshape(-1), comp), J.data)
+        src = pairs // N
+        nbr = (pairs % N).astype(np.int32)
+        ptr = np.zeros(N + 1, np.int64)
+        np.add.at(ptr, src + 1, 1)
+        tensors, typ = np.unique(blocks, axis=0, return_inverse=True) if len(blocks) else (np.zeros((0, 9)), np.zeros(0, int))
+        return cls(np.cumsum(ptr), nbr, np.asarray(typ).reshape(-1), tensors, mu, A, signs, field)
+
+    def set_field(self, B):
+        self.B = np.asarray(B, float).reshape(3)
+
+    @property
+    def mu(self):
+        return self.mu_site
+
+    @property
+    def signs(self):
+        return self.signs_site
+
+    @property
+    def A(self):
+        return self.A_site if self.A_site is not None else np.zeros((self.N, 3, 3))
+
+    @property
+    def has_A(self):
+        return self.A_site is not None and bool(np.max(np.abs(self.A_site)) > 0)
+
+    @property
+    def has_higher(self):
+        return False
+
+    @property
+    def sublattice(self):
+        return np.zeros(self.N, int)
+
+    def neighbour_csr(self):
+        return self.ptr, self.nbr, self.typ, np.ascontiguousarray(self.bond_J.reshape(-1, 9))
+
+    def order_parameter(self, e):
+        return float(np.linalg.norm((self.signs[:, None] * e).sum(0)) / self.N)

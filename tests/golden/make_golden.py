@@ -132,6 +132,40 @@ def main(ref_root):
               temperature_profile=dict(axis="x", T0=5.0, T1=30.0))
     traj("sc_structure", ucs["sc_dmi"], (6, 6, 4), (1, 1, 1), (0, 0, 0.5), 0.1, 1e-3, 10.0, 6, 10, {10},
          structure=st)
+    # arbitrary lattices (per-site neighbour lists): a carved sphere with vacancies, and two materials
+    # with interface exchange scaling; the reference's coupling matrix and per-site arrays are stored
+    def irregular(tag, uc, L, pbc, B, structure, alpha, dt, T, seed, steps):
+        s = RS.SpinSystem(uc, L, pbc, B)
+        apply_structure(s, structure)
+        J = s.Jsp.tocsr()
+        out[f"{tag}/Jsp_indptr"] = J.indptr.astype(np.int64)
+        out[f"{tag}/Jsp_indices"] = J.indices.astype(np.int64)
+        out[f"{tag}/Jsp_data"] = J.data
+        out[f"{tag}/A"] = np.asarray(s.A, float)
+        out[f"{tag}/mu"] = np.asarray(s.mu, float)
+        out[f"{tag}/signs"] = np.asarray(s.signs, float)
+        for name in ("pinned", "site_T", "alpha_site"):
+            v = getattr(s, name, None)
+            if v is not None:
+                out[f"{tag}/{name}"] = np.asarray(v)
+        e = s.init_spins("random", seed=seed)
+        sol = LLGSolver(s, alpha, dt, T, seed)
+        out[f"{tag}/e0"] = e.copy()
+        for _ in range(steps):
+            e = sol.step(e)
+        out[f"{tag}/e{steps}"] = e.copy()
+        out[f"{tag}/energy"] = np.array(s.energy(e))
+        out[f"{tag}/torque"] = np.array(sol.max_torque(e))
+        models["irregular__" + tag] = dict(L=list(L), pbc=[bool(x) for x in pbc], B=list(map(float, B)),
+                                           alpha=alpha, dt=dt, T=T, seed=seed, steps=steps, N=int(s.N))
+
+    irregular("sc_sphere", ucs["sc_dmi"], (9, 9, 9), (0, 0, 0), (0.1, 0.0, 0.4),
+              dict(shape="sphere", size=11.0, vacancies=dict(fraction=0.1, seed=3)), 0.2, 1e-3, 20.0, 4, 20)
+    irregular("sc_interface", ucs["sc_dmi"], (6, 6, 6), (1, 1, 1), (0.0, 0.0, 0.5),
+              dict(layers=[dict(material="A", thickness=3), dict(material="B", thickness=3)],
+                   exchange_scale=[[1.0, 0.5], [0.5, 0.8]],
+                   pinned=[dict(region="bottom", layers=1)]), 0.1, 1e-3, 0.0, 5, 20)
+
     # Larmor precession of one free spin (magex tests/test_spindyn.py:36-45)
     s = RS.SpinSystem(uc_of("free", RM.make_model("sc", J=[0.0])), (1, 1, 1), field=(0, 0, 2.0))
     sol = LLGSolver(s, alpha=0.0, dt=1e-3)

@@ -48,3 +48,19 @@ def apply_structure_subset(sc, st):
         prof = float(tp["T0"]) + (float(tp["T1"]) - float(tp["T0"])) * u
         sc.site_T = prof if sc.site_T is None else np.where(np.isnan(sc.site_T), prof, sc.site_T)
     return sc
+
+
+def golden_irregular(golden, golden_models, tag):
+    """NeighbourList of a golden carved / exchange-edited system, built from the reference's stored
+    3N x 3N coupling matrix and per-site arrays (A, mu, signs, pinned, site T, damping)."""
+    import scipy.sparse as sp
+    from magex_gb300.lattice import NeighbourList
+    meta = golden_models["irregular__" + tag]
+    N = meta["N"]
+    J = sp.csr_matrix((golden[f"{tag}/Jsp_data"], golden[f"{tag}/Jsp_indices"], golden[f"{tag}/Jsp_indptr"]),
+                      shape=(3 * N, 3 * N))
+    nl = NeighbourList.from_matrix(J, golden[f"{tag}/mu"], golden[f"{tag}/A"], golden[f"{tag}/signs"], meta["B"])
+    for name in ("pinned", "site_T", "alpha_site"):
+        if f"{tag}/{name}" in golden.files:
+            setattr(nl, name, np.array(golden[f"{tag}/{name}"]))
+    return nl, meta, J

@@ -16,7 +16,8 @@ J1, D, K, BZ, ALPHA, DT = 1.0, 0.3, 0.05, 2.0, 0.3, 1e-4
 
 
 def _params(theta, S):
-    """(T (nbond,3,3), A (1,3,3), B (3)) torch tensors from theta = (J1, D, K, Bz)."""
+    """(T (ngroups,3,3), A (1,3,3), B (3)) torch tensors from theta = (J1, D, K, Bz); S holds the DMI basis
+    matrix of each coupling group (its canonical coupling)."""
     j1, d, k, bz = theta[0], theta[1], theta[2], theta[3]
     eye = torch.eye(3, dtype=torch.float64, device=theta.device)
     T = j1 * eye[None] + d * S
@@ -32,9 +33,20 @@ def _setup(L, nsteps, seg):
     from magex_gb300.workloads import film_parameter_basis, triangular_film
     sc = triangular_film(L=L, field=(0, 0, BZ))
     adj = AdjointLLG(sc, alpha=ALPHA, dt=DT, seg_steps=seg)
-    S = torch.as_tensor(film_parameter_basis(sc), dtype=torch.float64)
+    S = torch.as_tensor(group_basis(adj, film_parameter_basis(sc)), dtype=torch.float64)
+    assert adj.groups.ngroups == 3                      # 6 nearest neighbours = 3 reverse pairs
     assert np.allclose(adj.T0, (J1 * np.eye(3)[None] + D * S.numpy()), atol=1e-15)
     return sc, adj, S
+
+
+def group_basis(adj, S_bond):
+    """Per-group DMI basis from the per-coupling one (the group tensor is its canonical coupling's)."""
+    G = adj.groups
+    out = np.zeros((G.ngroups, 3, 3))
+    for b in range(len(G.group)):
+        if not G.transposed[b]:
+            out[G.group[b]] = S_bond[b]
+    return out
 
 
 def _loss_and_grads(adj, S, e0, target, theta0, nsteps):
@@ -79,7 +91,7 @@ def test_adjoint_matches_torch_autograd_16x16(cuda):
     theta = torch.tensor(theta0, dtype=torch.float64, requires_grad=True)
     e = torch.as_tensor(e0).clone().requires_grad_(True)
     T, A, B = _params(theta, S)
-    eT = heun_trajectory(sc, idx, T, A, B, e, ALPHA, DT, nsteps)
+    eT = heun_trajectory(sc, idx, groups_bond_tensors(adj.groups, T), A, B, e, ALPHA, DT, nsteps)
     loss = ((eT - target.cpu()) ** 2).sum()
     loss.backward()
     assert abs(L_gpu - float(loss)) <= 1e-10 * abs(float(loss))
@@ -126,7 +138,7 @@ def test_adjoint_thermal_pathwise(cuda):
     from magex_gb300.workloads import film_parameter_basis, triangular_film
     sc = triangular_film(L=24, field=(0, 0, BZ))
     adj = AdjointLLG(sc, alpha=ALPHA, dt=DT, temperature=15.0, seed=5, seg_steps=30)
-    S = torch.as_tensor(film_parameter_basis(sc), dtype=torch.float64)
+    S = torch.as_tensor(group_basis(adj, film_parameter_basis(sc)), dtype=torch.float64)
     e0 = sc.init_spins("random", seed=3)
     target = torch.as_tensor(sc.init_spins("random", seed=4), device=adj.device)
     nsteps = 100
@@ -199,3 +211,51 @@ def groups_bond_tensors(groups, T):
     Tb = T[torch.as_tensor(groups.group, dtype=torch.long)]
     tr = torch.as_tensor(groups.transposed, dtype=torch.bool)[:, None, None]
     return torch.where(tr, Tb.transpose(1, 2), Tb)
+
+
+def test_adjoint_per_bond_groups_equal_pair_groups(cuda):
+    """Per-coupling and reverse-pair parameterisations give the same gradient of the same loss."""
+    from magex_gb300.adjoint import AdjointLLG, CouplingGroups, llg_trajectory
+    from magex_gb300.workloads import film_parameter_basis, triangular_film, uniaxial_sia
+    sc = triangular_film(L=20, field=(0, 0, BZ))
+    S_bond = torch.as_tensor(film_parameter_basis(sc))
+    e0 = torch.as_tensor(sc.init_spins("random", seed=1))
+    target = torch.as_tensor(sc.init_spins("random", seed=2))
+    grads = []
+    for groups in (CouplingGroups.per_bond(sc), CouplingGroups.symmetric_pairs(sc)):
+        adj = AdjointLLG(sc, groups, alpha=ALPHA, dt=DT, seg_steps=25)
+        Sg = torch.zeros((groups.ngroups, 3, 3), dtype=torch.float64)
+        for b in range(len(groups.group)):
+            if not groups.transposed[b]:
+                Sg[groups.group[b]] = S_bond[b]
+        theta = torch.tensor([J1, D], dtype=torch.float64, requires_grad=True)
+        T = theta[0] * torch.eye(3, dtype=torch.float64)[None] + theta[1] * Sg
+        A = torch.as_tensor(uniaxial_sia(K))[None]
+        B = torch.tensor([0.0, 0.0, BZ], dtype=torch.float64)
+        eT = llg_trajectory(adj, e0.to(adj.device), T, A, B, 60)
+        ((eT - target.to(adj.device)) ** 2).sum().backward()
+        grads.append(theta.grad.numpy().copy())
+    assert np.allclose(grads[0], grads[1], rtol=1e-10, atol=1e-12)
+
+
+def test_adjoint_resident_segments_equal_recompute(cuda):
+    """Keeping segments resident (no recomputation) gives the same gradient as recomputing them."""
+    from magex_gb300.adjoint import AdjointLLG, llg_trajectory
+    from magex_gb300.workloads import film_parameter_basis, triangular_film, uniaxial_sia
+    sc = triangular_film(L=24, field=(0, 0, BZ))
+    e0 = torch.as_tensor(sc.init_spins("random", seed=1))
+    target = torch.as_tensor(sc.init_spins("random", seed=2))
+    out = []
+    for cache in (0, 1 << 30, 3 * 8 * 14 * sc.N * 20):     # none, all, a part of the 5 segments
+        adj = AdjointLLG(sc, alpha=ALPHA, dt=DT, seg_steps=20, cache_bytes=cache)
+        S = torch.as_tensor(group_basis(adj, film_parameter_basis(sc)))
+        theta = torch.tensor([J1, D], dtype=torch.float64, requires_grad=True)
+        e = e0.clone().to(adj.device).requires_grad_(True)
+        T = theta[0] * torch.eye(3, dtype=torch.float64)[None] + theta[1] * S
+        A = torch.as_tensor(uniaxial_sia(K))[None]
+        B = torch.tensor([0.0, 0.0, BZ], dtype=torch.float64)
+        eT = llg_trajectory(adj, e, T, A, B, 100)
+        ((eT - target.to(adj.device)) ** 2).sum().backward()
+        out.append((theta.grad.numpy().copy(), e.grad.cpu().numpy()))
+    for g, ge in out[1:]:
+        assert np.array_equal(g, out[0][0]) and np.array_equal(ge, out[0][1])

@@ -169,3 +169,20 @@ def test_invalid_inputs_raise(cuda, golden_models):
     sol = GB300LLG(sc)
     with pytest.raises(ValueError):
         sol.step(np.zeros((3, 3)))
+
+
+@pytest.mark.parametrize("tag", ["sc_sphere", "sc_interface"])
+def test_irregular_lattice_matches_reference(cuda, golden, golden_models, tag):
+    """Neighbour-list (CSR) layout: carved sphere with vacancies (thermal, reference noise stream) and
+    interface exchange scaling with a pinned layer, against the reference's trajectories."""
+    from helpers import golden_irregular
+    from magex_gb300.llg import GB300LLG
+    nl, meta, _ = golden_irregular(golden, golden_models, tag)
+    sol = GB300LLG(nl, meta["alpha"], meta["dt"], meta["T"], meta["seed"], noise="host")
+    e = golden[f"{tag}/e0"].copy()
+    for _ in range(meta["steps"]):
+        e = sol.step(e)
+    assert np.abs(e - golden[f"{tag}/e{meta['steps']}"]).max() <= 1e-12 * meta["steps"]
+    E = float(golden[f"{tag}/energy"])
+    assert abs(sol.energy(e) - E) <= 1e-12 * abs(E)
+    assert abs(sol.max_torque(e) - float(golden[f"{tag}/torque"])) <= 1e-10 * max(1.0, float(golden[f"{tag}/torque"]))
