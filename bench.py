@@ -291,7 +291,6 @@ def run_gb300(args):
     from magex_gb300.workloads import bcc_two_site
     import ctypes as C
 
-    dev = torch.device("cuda", torch.cuda.current_device())
     lib = _lib.load()
     peak64 = C.c_double()
     _lib.check(lib.mgx_measure_fp64_peak(C.byref(peak64)), "fp64 peak")
@@ -344,10 +343,8 @@ def run_gb300(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
 
-    t_max = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
-    if ws > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    total_ms, e2e_s = float(t_max[0]), float(t_max[1])
+    from magex_gb300.replicas import max_over_ranks
+    total_ms, e2e_s = max_over_ranks([total_ms, e2e_s], dist if ws > 1 else None)
     if rank != 0:
         dist.destroy_process_group()
         return
