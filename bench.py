@@ -276,6 +276,36 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
             "grad_J1_D": [float(x) for x in g]}
 
 
+def bench_df32(L, K, warmup):
+    """The same workload with the exchange gather in compensated FP32 pairs (precision="df32"): spins,
+    rhs and integration stay FP64.  Reported beside the FP64 value, never as it."""
+    import torch
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=L, field=FIELD)
+    e0 = sc.init_spins("random", seed=1)
+    sols = {p: GB300LLG(sc, ALPHA, DT, TEMP, seed=1000, precision=p) for p in ("fp64", "df32")}
+    lat = {p: sols[p].model.to_lattice(e0) for p in sols}
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        sols["df32"].run_lattice(lat["df32"], 1)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    sols["df32"].run_lattice(lat["df32"], K)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / K
+    # same Philox stream through the FP64 plan: the deviation after warmup + K steps
+    sols["fp64"].run_lattice(lat["fp64"], warmup + K)
+    torch.cuda.synchronize()
+    dev = float((lat["fp64"] - lat["df32"]).abs().max())
+    return {"precision": "exchange gather in compensated FP32 pairs (~44 bits), everything else FP64",
+            "value": sc.N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": K,
+            "max_abs_deviation_from_fp64_plan": dev, "deviation_after_steps": warmup + K,
+            "hbm_roofline_frac": 72.0 * sc.N / (0.5 * ms * 1e-3) / 1e9 / 6760.6}
+
+
 def run_gb300(args):
     import torch
     ws, rank, local = dist_env()
@@ -384,6 +414,8 @@ def run_gb300(args):
         "gpu_launches": 2 * K,
         "clocks": clocks,
     }
+    if ws == 1:
+        line["df32_gather_variant"] = bench_df32(args.L, min(K, 200), args.warmup)
     if ws == 1 and not args.no_batched:
         line["batched"] = bench_batched()
     if ws == 1 and not args.no_adjoint:
@@ -411,7 +443,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
-    ap.add_argument("--only", choices=["adjoint", "batched"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batched", "df32"], default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=2000)
     ap.add_argument("--adjoint-L", type=int, default=128)
@@ -423,7 +455,12 @@ def main():
         torch.cuda.set_device(0)
         from magex_gb300 import build
         build.build_library()
-        out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps) if args.only == "adjoint" else bench_batched()
+        if args.only == "adjoint":
+            out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps)
+        elif args.only == "df32":
+            out = bench_df32(args.L, args.steps, args.warmup)
+        else:
+            out = bench_batched()
         print(json.dumps(out), flush=True)
         return
     if args.impl == "reference":

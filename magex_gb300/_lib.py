@@ -15,6 +15,7 @@ LIB_PATH = os.path.join(HERE, "libmgx.so")
 MGX_OK, MGX_ERR_INVALID, MGX_ERR_UNSUPPORTED, MGX_ERR_CUDA, MGX_ERR_NOMEM = 0, 1, 2, 3, 4
 HEUN, DEPONDT = 0, 1
 NOISE_NONE, NOISE_HOST, NOISE_PHILOX = 0, 1, 2
+PRECISION_FP64, PRECISION_DF32_GATHER = 0, 1
 MAX_SUBLATTICES = 16
 MAX_BONDS = 256
 NOALLOC_MAX_SITES = 262144
@@ -37,7 +38,7 @@ class SiteDesc(C.Structure):
 
 class LLGParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("alpha", C.c_double), ("alpha_site", _dp), ("precession", C.c_int32),
-                ("integrator", C.c_int32), ("noise", C.c_int32), ("seed", C.c_uint64)]
+                ("integrator", C.c_int32), ("noise", C.c_int32), ("seed", C.c_uint64), ("precision", C.c_int32)]
 
 
 class CSRDesc(C.Structure):

@@ -405,6 +405,7 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   if (ngroups < 1 || ngroups > 4096) return set_error(MGX_ERR_INVALID, "ngroups must be in 1..4096");
   if (R->nbond > 0 && (!rev_group || !rev_transposed)) return set_error(MGX_ERR_INVALID, "group arrays are required");
   if (p->alpha_site) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint supports a uniform damping only");
+  if (p->precision != MGX_PRECISION_FP64) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint uses the FP64 gather");
   if (p->integrator != MGX_INTEGRATOR_HEUN) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint is implemented for heun");
   if (p->noise == MGX_NOISE_HOST) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint recomputes noise: use none or philox");
   if (!(p->dt > 0.0)) return set_error(MGX_ERR_INVALID, "dt must be positive");

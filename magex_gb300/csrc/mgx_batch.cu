@@ -266,6 +266,7 @@ mgx_status mgx_batch_create(const mgx_model* const* models, const mgx_llg_params
     const mgx_llg_params& p = params[k];
     if (!(p.dt > 0.0)) return set_error(MGX_ERR_INVALID, "system %d: dt must be positive", k);
     if (p.alpha_site) return set_error(MGX_ERR_INVALID, "system %d: batched systems take a uniform alpha", k);
+    if (p.precision != MGX_PRECISION_FP64) return set_error(MGX_ERR_INVALID, "batched systems use the FP64 gather");
     if (p.noise != params[0].noise || p.integrator != params[0].integrator)
       return set_error(MGX_ERR_INVALID, "all systems of a batch share the noise mode and the integrator");
     if (p.integrator != MGX_INTEGRATOR_HEUN && p.integrator != MGX_INTEGRATOR_DEPONDT)

@@ -90,10 +90,24 @@ struct DevLLG {
   double* k1;                // [3][N] predictor slope (Heun) or rotation rate (Depondt)
 };
 
+// Tables of the compensated-FP32 gather (MGX_PRECISION_DF32_GATHER): every coupling as 9 (hi, lo)
+// float pairs pre-scaled by 2 / (mu mu_B) of the receiving sublattice, -2 A / (mu mu_B) per
+// sublattice, and the (hi, lo) copies of the spin fields that the gather reads.
+struct DevDF {
+  const float2* J;               // [nbond*9]
+  const double* nA2;             // [ns*9]
+  int hasA, diagA;
+  float2* es;                    // [3][N] split of e
+  float2* eps;                   // [3][N] split of ep
+};
+
 struct LLGPlan {
   const Model* model;
   DevLLG p;
   bool sigma_zero = true;        // every thermal amplitude is 0: the noise-free kernels are used
+  int precision = 0;
+  DevDF df{};
+  void* df_block = nullptr;
   void* sub_block = nullptr;     // alpha_sub | pre_sub | sigma_sub
   double* site_block = nullptr;  // alpha_site | pre_site
   double* sigma_site = nullptr;
@@ -110,6 +124,11 @@ inline int site_block_size(long long N) {
 
 // Enqueue the predictor (stages & 1) and / or the corrector (stages & 2) of one step on st.
 void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
+// Compensated-FP32 gather form (mgx_llg_df.cu): tables built at plan creation, the split copy of e
+// refreshed at the start of every library call, then predictor / corrector as above.
+mgx_status build_df_tables(LLGPlan* pl);
+void enqueue_df_split(const LLGPlan* pl, const double* e, cudaStream_t st);
+void enqueue_df_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
 
 // ------------------------------------------------------------------ small device helpers
 __device__ __forceinline__ void site_coords(const DevLattice& L, long long q, int& s, int& c0, int& c1, int& c2) {

@@ -60,6 +60,10 @@ static void dispatch_noise(const LLGPlan* pl, double* e, const double* noise, ui
 
 void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st,
                       int stages) {
+  if (pl->precision == MGX_PRECISION_DF32_GATHER) {
+    enqueue_df_step(pl, e, noise, step, st, stages);
+    return;
+  }
   switch (pl->model->d.width) {
     case 1: dispatch_noise<1>(pl, e, noise, step, stages, st); break;
     case 4: dispatch_noise<4>(pl, e, noise, step, stages, st); break;
@@ -94,6 +98,8 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
     return set_error(MGX_ERR_INVALID, "integrator %d is not heun (0) or depondt (1)", p->integrator);
   if (p->noise < MGX_NOISE_NONE || p->noise > MGX_NOISE_PHILOX)
     return set_error(MGX_ERR_INVALID, "noise mode %d is not none (0), host (1) or philox (2)", p->noise);
+  if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_DF32_GATHER)
+    return set_error(MGX_ERR_INVALID, "precision %d is not fp64 (0) or df32-gather (1)", p->precision);
   const int ns = m->d.ns;
   const long long N = m->d.N;
   LLGPlan* pl = new LLGPlan();
@@ -143,6 +149,14 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
     d.alpha_site = pl->site_block;
     d.pre_site = pl->site_block + N;
   }
+  if (p->precision == MGX_PRECISION_DF32_GATHER) {
+    pl->precision = MGX_PRECISION_DF32_GATHER;
+    const mgx_status st = build_df_tables(pl);
+    if (st != MGX_OK) {
+      mgx_llg_destroy(reinterpret_cast<mgx_llg*>(pl));
+      return st;
+    }
+  }
   *out = reinterpret_cast<mgx_llg*>(pl);
   return MGX_OK;
 }
@@ -154,6 +168,7 @@ mgx_status mgx_llg_destroy(mgx_llg* pp) {
   cudaFree(pl->site_block);
   cudaFree(pl->sigma_site);
   cudaFree(pl->scratch);
+  cudaFree(pl->df_block);
   delete pl;
   return MGX_OK;
 }
@@ -197,6 +212,7 @@ mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t st
   if (!pl || !e) return set_error(MGX_ERR_INVALID, "mgx_llg_step: null argument");
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step: host-noise plan needs a noise buffer");
+  if (pl->precision == MGX_PRECISION_DF32_GATHER) enqueue_df_split(pl, e, (cudaStream_t)stream);
   enqueue_llg_step(pl, e, noise, step, (cudaStream_t)stream, 3);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
@@ -208,6 +224,7 @@ mgx_status mgx_llg_stage(mgx_llg* pp, int32_t stage, double* e, const double* no
   if (stage != 0 && stage != 1) return set_error(MGX_ERR_INVALID, "stage %d is not 0 (predictor) or 1 (corrector)", stage);
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
     return set_error(MGX_ERR_INVALID, "mgx_llg_stage: host-noise plan needs a noise buffer");
+  if (stage == 0 && pl->precision == MGX_PRECISION_DF32_GATHER) enqueue_df_split(pl, e, (cudaStream_t)stream);
   enqueue_llg_step(pl, e, noise, step, (cudaStream_t)stream, stage == 0 ? 1 : 2);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
@@ -219,6 +236,7 @@ mgx_status mgx_llg_run(mgx_llg* pp, double* e, int64_t nsteps, uint64_t step0, v
   if (nsteps < 0) return set_error(MGX_ERR_INVALID, "nsteps must be >= 0");
   if (pl->p.noise == MGX_NOISE_HOST)
     return set_error(MGX_ERR_INVALID, "mgx_llg_run: host-noise plans step one at a time (mgx_llg_step)");
+  if (pl->precision == MGX_PRECISION_DF32_GATHER && nsteps > 0) enqueue_df_split(pl, e, (cudaStream_t)stream);
   for (int64_t n = 0; n < nsteps; ++n) enqueue_llg_step(pl, e, nullptr, step0 + (uint64_t)n, (cudaStream_t)stream, 3);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;

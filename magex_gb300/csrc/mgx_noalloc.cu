@@ -78,6 +78,8 @@ extern "C" mgx_status mgx_llg_step_noalloc(const mgx_model* mm, const mgx_llg_pa
   if (p->alpha_site)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: per-site damping (alpha_site) needs a plan; "
                                       "pass a uniform alpha");
+  if (p->precision != MGX_PRECISION_FP64)
+    return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: only the FP64 gather (precision 0) is available");
   if (!(p->dt > 0.0)) return set_error(MGX_ERR_INVALID, "dt must be a positive number");
   if (p->integrator != MGX_INTEGRATOR_HEUN && p->integrator != MGX_INTEGRATOR_DEPONDT)
     return set_error(MGX_ERR_INVALID, "integrator %d is not heun (0) or depondt (1)", p->integrator);

@@ -9,6 +9,11 @@ columns as magex ``magex/llg.py:48-283``.  The spins stay on the GPU for the who
 Heun step is two fused sm_103a kernels (libmgx: ``mgx_llg_step`` / ``mgx_llg_run``); observables
 rows are computed on the device by ``mgx_observables``.
 
+Arithmetic (``precision=``): "fp64" (default) runs everything in FP64; "df32" keeps the spins, the
+on-site and Zeeman terms, the right-hand side and the integration in FP64 and evaluates the exchange
+sum in compensated FP32 pairs (~44 significant bits), about 4x faster on GB300, whose FP64 units run
+at 1/61 of the FP32 rate.
+
 Thermal noise (``noise=``):
   "philox"  counter-based Philox4x32-10 keyed by (seed, site, step), generated inside the kernels
             (default; the trajectory differs from any magex backend, as magex's own numba and NumPy
@@ -43,7 +48,7 @@ class GB300LLG:
 
     def __init__(self, system, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
                  thermostat="classical", integrator="heun", stt=None, sot=None, backend="gb300",
-                 noise="philox", device=None):
+                 noise="philox", precision="fp64", device=None):
         if integrator not in INTEGRATORS:
             raise ValueError(f"integrator must be one of {INTEGRATORS}")
         if integrator not in _SUPPORTED:
@@ -57,6 +62,9 @@ class GB300LLG:
             raise ValueError("backend must be 'gb300'")
         if noise not in ("philox", "host"):
             raise ValueError("noise must be 'philox' or 'host'")
+        if precision not in ("fp64", "df32"):
+            raise ValueError("precision must be 'fp64' or 'df32' (exchange gather in compensated FP32 pairs)")
+        self.precision = precision
         self.sys = system
         self.sc = supercell_from_system(system)
         self.model = DeviceModel(self.sc, device)
@@ -94,6 +102,7 @@ class GB300LLG:
         p.integrator = _SUPPORTED[integrator]
         p.noise = _lib.NOISE_HOST if noise == "host" else _lib.NOISE_PHILOX
         p.seed = _philox_key(seed)
+        p.precision = _lib.PRECISION_DF32_GATHER if precision == "df32" else _lib.PRECISION_FP64
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.model.lib.mgx_llg_create(self.model.handle, C.byref(p), C.byref(h)), "mgx_llg_create")

@@ -54,7 +54,7 @@ def test_version_and_errors_without_gpu(lib):
 
 def test_struct_layouts_match_header():
     # sizes of the C structs as laid out by the x86-64 / aarch64 LP64 ABIs
-    assert C.sizeof(_lib.LLGParams) == 48
+    assert C.sizeof(_lib.LLGParams) == 56
     assert C.sizeof(_lib.SiteDesc) == 24
     assert C.sizeof(_lib.LatticeDesc) == 4 + 12 + 12 + 4 + 3 * 8 + 4 + 4 + 4 * 8 + 24
 
