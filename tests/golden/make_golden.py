@@ -177,6 +177,28 @@ def main(ref_root):
     out["larmor/e1000"] = e
     out["larmor/phase"] = np.unwrap(np.array(ph))
 
+    # ---------------------------------------------------------------- thermal equilibrium statistics
+    # Langevin run of an sc ferromagnet below T_c with the reference's noise stream; block means of
+    # E/N and |M| (20 blocks) give the means and their standard errors that a run with any other
+    # noise stream must reproduce within 3 sigma.
+    th = dict(L=8, alpha=0.5, dt=2e-3, T=15.0, Bz=0.2, seed=21, equil=3000, sample=40000, every=20)
+    s = RS.SpinSystem(ucs["sc"], (th["L"],) * 3, (1, 1, 1), (0.0, 0.0, th["Bz"]))
+    sol = LLGSolver(s, alpha=th["alpha"], dt=th["dt"], temperature=th["T"], seed=th["seed"])
+    e = s.init_spins("ferro")
+    for _ in range(th["equil"]):
+        e = sol.step(e)
+    Es, Ms = [], []
+    for k in range(th["sample"]):
+        e = sol.step(e)
+        if k % th["every"] == th["every"] - 1:
+            Es.append(s.energy(e, per_spin=True))
+            Ms.append(np.linalg.norm(e.mean(0)))
+    for key, x in (("E", np.array(Es)), ("M", np.array(Ms))):
+        blocks = x.reshape(20, -1).mean(1)
+        out[f"thermal/{key}_mean"] = np.array(blocks.mean())
+        out[f"thermal/{key}_sem"] = np.array(blocks.std(ddof=1) / np.sqrt(20))
+    out["thermal/params"] = np.array(json.dumps(th))
+
     # ---------------------------------------------------------------- topological charge
     s = RS.SpinSystem(ucs["tri"], (30, 30, 1), (1, 1, 0))
     c = s.positions[:, :2].mean(0)

@@ -64,3 +64,25 @@ def golden_irregular(golden, golden_models, tag):
         if f"{tag}/{name}" in golden.files:
             setattr(nl, name, np.array(golden[f"{tag}/{name}"]))
     return nl, meta, J
+
+
+def thermal_system(golden, golden_models):
+    """The sc ferromagnet of the reference's thermal-equilibrium fixture and its run parameters."""
+    import json
+    th = json.loads(str(golden["thermal/params"]))
+    sc = Supercell(load_results(golden_models["sc"]["model"]), (th["L"],) * 3, (True, True, True),
+                   (0.0, 0.0, th["Bz"]))
+    return sc, th
+
+
+def block_stats(x, nblocks=20):
+    """Mean of a time series and the standard error of the mean from nblocks block averages."""
+    x = np.asarray(x, float)
+    b = x[: len(x) // nblocks * nblocks].reshape(nblocks, -1).mean(1)
+    return float(b.mean()), float(b.std(ddof=1) / np.sqrt(nblocks))
+
+
+def assert_within_3_sigma(golden, key, mean, sem):
+    ref, ref_sem = float(golden[f"thermal/{key}_mean"]), float(golden[f"thermal/{key}_sem"])
+    bound = 3.0 * np.hypot(ref_sem, sem)
+    assert abs(mean - ref) <= bound, (key, mean, ref, bound)

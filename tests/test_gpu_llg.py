@@ -186,3 +186,29 @@ def test_irregular_lattice_matches_reference(cuda, golden, golden_models, tag):
     E = float(golden[f"{tag}/energy"])
     assert abs(sol.energy(e) - E) <= 1e-12 * abs(E)
     assert abs(sol.max_torque(e) - float(golden[f"{tag}/torque"])) <= 1e-10 * max(1.0, float(golden[f"{tag}/torque"]))
+
+
+def test_philox_thermal_equilibrium_within_3_sigma_of_reference(cuda, golden, golden_models):
+    """Equilibrium <E>/N and <|M|> with in-kernel Philox noise agree with the reference's own
+    Langevin run (default_rng stream, same model, T, alpha, dt and sampling) within 3 combined
+    standard errors; two independent Philox seeds are averaged."""
+    from helpers import assert_within_3_sigma, block_stats, thermal_system
+    from magex_gb300.llg import GB300LLG
+    sc, th = thermal_system(golden, golden_models)
+    E, M = [], []
+    for seed in (5, 6):
+        sol = GB300LLG(sc, th["alpha"], th["dt"], th["T"], seed)
+        lat = sol.model.to_lattice(sc.init_spins("ferro"))
+        sol.run_lattice(lat, th["equil"])
+        Es, Ms = [], []
+        for _ in range(th["sample"] // th["every"]):
+            sol.run_lattice(lat, th["every"])
+            o = sol.model.observables(lat).cpu().numpy()
+            Es.append(o[0] / sc.N)
+            Ms.append(np.linalg.norm(o[1:4]) / sc.N)
+        E.append(block_stats(Es))
+        M.append(block_stats(Ms))
+    for key, st in (("E", E), ("M", M)):
+        mean = 0.5 * (st[0][0] + st[1][0])
+        sem = 0.5 * np.hypot(st[0][1], st[1][1])
+        assert_within_3_sigma(golden, key, mean, sem)

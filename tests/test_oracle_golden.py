@@ -101,3 +101,23 @@ def test_oracle_ziggurat_moments():
     assert abs(x.mean()) < 0.006 and abs(x.var() - 1) < 0.006
     assert abs((x ** 4).mean() / x.var() ** 2 - 3) < 0.03
     assert abs((np.abs(x) > 3).mean() / 0.0026998 - 1) < 0.08
+
+
+def test_oracle_thermal_equilibrium_within_3_sigma_of_reference(golden, golden_models):
+    """Equilibrium <E>/N and <|M|> of a Langevin run with the oracle's own (ziggurat) noise stream
+    agree with the reference's run (its default_rng stream) within 3 combined standard errors."""
+    from helpers import assert_within_3_sigma, block_stats, thermal_system
+    sc, th = thermal_system(golden, golden_models)
+    ora = OracleLLG(sc, th["alpha"], th["dt"], th["T"], 7, noise="ziggurat", csr="stencil")
+    e = sc.init_spins("ferro")
+    for _ in range(th["equil"]):
+        ora.step_inplace(e)
+    E, M = [], []
+    for k in range(th["sample"]):
+        ora.step_inplace(e)
+        if k % th["every"] == th["every"] - 1:
+            o = ora.observables(e)
+            E.append(o[0] / sc.N)
+            M.append(np.linalg.norm(o[1:4]) / sc.N)
+    for key, x in (("E", E), ("M", M)):
+        assert_within_3_sigma(golden, key, *block_stats(x))
