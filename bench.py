@@ -276,6 +276,99 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
             "grad_J1_D": [float(x) for x in g]}
 
 
+def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
+    """Large batched + adjoint workload: nsys two-site bcc L^3 systems (524,288 spins each at L = 64),
+    4 shells (8+6+12+24) with one seeded full 3x3 tensor per shell (iso 20/10/-1/1 meV, 1% anisotropic,
+    DMI 5% of |J|), transposed on reverse bonds, SIA K = 0.01 meV, B = (0, 0, 0.5) T, T ~ U[0, 600] K,
+    alpha 0.05, dt 0.1 fs, Philox, FP64.  Times K steps of the batched form against per-system plain
+    plans, then the adjoint of the mean-energy loss w.r.t. the 4 shell tensors on one system at 300 K
+    over adj_steps steps, with the checkpointed segments kept in HBM as far as the free memory allows."""
+    import torch
+    from magex_gb300.adjoint import AdjointLLG, CouplingGroups, energy_per_site, llg_trajectory
+    from magex_gb300.batched import BatchedLLG
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site, uniaxial_sia
+    rng = np.random.default_rng(seed)
+    Ts = [float(t) for t in rng.uniform(0.0, 600.0, nsys)]
+    sc = bcc_two_site(L=L, J=(20.0, 10.0, -1.0, 1.0), dmi_frac=0.05, per="shell", seed=1, field=FIELD)
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ens = BatchedLLG([sc] * nsys, ALPHA, DT, Ts, list(range(1, nsys + 1)))
+    ens.set_spins([sc.init_spins("random", seed=k) for k in range(nsys)])
+    ens.run(2, graph_chunk=2)
+    torch.cuda.synchronize()
+    a.record(stream)
+    ens.run(K, graph_chunk=K)
+    b.record(stream)
+    b.synchronize()
+    t_batch = a.elapsed_time(b) * 1e-3
+    rows = ens.rows()
+    del ens
+    sols = [GB300LLG(sc, ALPHA, DT, Ts[k], 1 + k) for k in range(nsys)]
+    lats = [sol.model.to_lattice(sc.init_spins("random", seed=k)) for k, sol in enumerate(sols)]
+    for sol, lat in zip(sols, lats):
+        sol.run_lattice(lat, 1)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for sol, lat in zip(sols, lats):
+        sol.run_lattice(lat, K)
+    b.record(stream)
+    b.synchronize()
+    t_plain = a.elapsed_time(b) * 1e-3
+    del sols, lats
+    torch.cuda.empty_cache()
+    ntot = nsys * sc.N
+
+    groups = CouplingGroups.per_shell(sc)
+    free, _ = torch.cuda.mem_get_info()
+    cache = int(0.6 * free)
+    adj = AdjointLLG(sc, groups, alpha=ALPHA, dt=DT, temperature=300.0, seed=77, seg_steps=100, cache_bytes=cache)
+    plain = GB300LLG(sc, ALPHA, DT, 300.0, 77)
+    A0 = torch.as_tensor(np.stack([uniaxial_sia(0.01)] * sc.ns))
+    B0 = torch.tensor(FIELD, dtype=torch.float64)
+    e0 = torch.as_tensor(sc.init_spins("random", seed=5), device=adj.device)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+
+    def once(record):
+        T = torch.as_tensor(adj.T0).clone().requires_grad_(True)
+        lat = plain.model.to_lattice(e0)
+        torch.cuda.synchronize()
+        if record:
+            ev[0].record(stream)
+        plain.run_lattice(lat, adj_steps)
+        if record:
+            ev[1].record(stream)
+        eT = llg_trajectory(adj, e0, T, A0, B0, adj_steps)
+        if record:
+            ev[2].record(stream)
+        loss = energy_per_site(sc, groups, eT, T, A0, B0).mean()
+        if record:
+            ev[3].record(stream)
+        loss.backward()
+        if record:
+            ev[4].record(stream)
+        torch.cuda.synchronize()
+        return float(loss.detach()), T.grad
+
+    once(False)
+    loss, g = once(True)
+    t = [ev[0].elapsed_time(ev[k]) for k in range(1, 5)]
+    return {"workload": f"{nsys} two-site bcc {L}^3 systems ({ntot:,} spins), 4 shells 8+6+12+24 with seeded "
+                        "per-shell full 3x3 tensors (iso 20/10/-1/1 meV, 1% anisotropic, DMI 5%), K=0.01 meV, "
+                        "B=(0,0,0.5) T, T~U[0,600] K, alpha 0.05, dt 0.1 fs, Philox, FP64",
+            "batched_value": ntot * K / t_batch, "plain_value": ntot * K / t_plain, "unit": UNIT, "steps": K,
+            "speedup_vs_plain": t_plain / t_batch, "batched_ms_per_step": 1e3 * t_batch / K,
+            "final_mean_E_per_spin": float(np.mean(rows[:, 1])),
+            "adjoint": {"system": f"one {L}^3 system ({sc.N:,} spins) at 300 K", "steps": adj_steps,
+                        "loss": "mean energy per spin after the trajectory (meV)",
+                        "parameters": "4 shell tensors (36 entries), canonical and transposed bonds",
+                        "resident_segments": len(adj._segments(adj_steps)), "cache_bytes": cache,
+                        "forward_plain_ms": t[0], "forward_checkpointed_ms": t[1] - t[0],
+                        "loss_ms": t[2] - t[1], "backward_ms": t[3] - t[2],
+                        "adjoint_over_forward": (t[3] - t[2]) / t[0], "loss_value": loss,
+                        "grad_norm_per_shell": [float(x) for x in g.reshape(4, -1).norm(dim=1)]}}
+
+
 def bench_df32(L, K, warmup):
     """The same workload with the exchange gather in compensated FP32 pairs (precision="df32"): spins,
     rhs and integration stay FP64.  Reported beside the FP64 value, never as it."""
@@ -423,6 +516,8 @@ def run_gb300(args):
         # the same trajectory with every segment kept in HBM (2000 steps x 14 N doubles = 3.7 GB): no recompute
         line["adjoint_resident"] = bench_adjoint(cache_bytes=8 << 30)
         line["adjoint_large"] = bench_adjoint(L=1024, nsteps=200, seg=50)
+    if ws == 1 and not args.no_batched and not args.no_adjoint:
+        line["large_batched_adjoint"] = bench_config5()
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -443,9 +538,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
-    ap.add_argument("--only", choices=["adjoint", "batched", "df32"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "config5"], default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
-    ap.add_argument("--adjoint-steps", type=int, default=2000)
+    ap.add_argument("--adjoint-steps", type=int, default=None)
     ap.add_argument("--adjoint-L", type=int, default=128)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -456,9 +551,11 @@ def main():
         from magex_gb300 import build
         build.build_library()
         if args.only == "adjoint":
-            out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps)
+            out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps or 2000)
         elif args.only == "df32":
             out = bench_df32(args.L, args.steps, args.warmup)
+        elif args.only == "config5":
+            out = bench_config5(K=min(args.steps, 50), adj_steps=args.adjoint_steps or 1000)
         else:
             out = bench_batched()
         print(json.dumps(out), flush=True)

@@ -285,3 +285,50 @@ class _Trajectory(torch.autograd.Function):
 def llg_trajectory(adj, e0, T, A, B, nsteps):
     """Spins after nsteps Heun steps from e0 ((N,3) tensor), differentiable in e0, T, A and B."""
     return _Trajectory.apply(e0, T, A, B, adj, int(nsteps))
+
+
+_BOND_SITES: dict = {}
+
+
+def bond_sites(sc, device):
+    """Per stencil coupling b: (src, dst) magex site indices of every cell where it acts (cached)."""
+    key = (id(sc), str(device))
+    hit = _BOND_SITES.get(key)
+    if hit is not None and hit[0] is sc:
+        return hit[1]
+    L = np.array(sc.L)
+    c = np.stack(np.meshgrid(*[np.arange(n) for n in sc.L], indexing="ij"), -1).reshape(-1, 3)
+    out = []
+    for b in range(len(sc.bond_src)):
+        t = c + sc.bond_R[b][None, :]
+        ok = np.ones(len(c), bool)
+        for a in range(3):
+            if sc.pbc[a]:
+                t[:, a] %= L[a]
+            else:
+                ok &= (t[:, a] >= 0) & (t[:, a] < L[a])
+        cs, ts = c[ok], t[ok]
+        src = ((cs[:, 0] * L[1] + cs[:, 1]) * L[2] + cs[:, 2]) * sc.ns + sc.bond_src[b]
+        dst = ((ts[:, 0] * L[1] + ts[:, 1]) * L[2] + ts[:, 2]) * sc.ns + sc.bond_dst[b]
+        out.append((torch.as_tensor(src, device=device), torch.as_tensor(dst, device=device)))
+    _BOND_SITES.clear()
+    _BOND_SITES[key] = (sc, out)
+    return out
+
+
+def energy_per_site(sc, groups, e, T, A, B):
+    """Per-site energy (meV) of spins e ((N, 3), magex order) with the couplings of the parameter
+    tensors T (ngroups, 3, 3), single-ion tensors A (ns, 3, 3) and field B (3,), differentiable in all
+    four (torch autograd).  Terms as magex/spinmodel.py:475-484: -e.h - mu_B mu e.B + e A e, with
+    h_i = sum_j J_ij e_j; their sum is the total energy, their mean the mean-energy loss."""
+    dev, dt = e.device, e.dtype
+    T = T.to(dev, dt)
+    Tb = T[torch.as_tensor(groups.group, dtype=torch.long, device=dev)]
+    tr = torch.as_tensor(groups.transposed, dtype=torch.bool, device=dev)[:, None, None]
+    Jb = torch.where(tr, Tb.transpose(1, 2), Tb)
+    h = torch.zeros_like(e)
+    for b, (src, dst) in enumerate(bond_sites(sc, dev)):
+        h = h.index_add(0, src, e[dst] @ Jb[b].T)
+    As = A.to(dev, dt)[torch.as_tensor(sc.sublattice, dtype=torch.long, device=dev)]
+    mu = torch.as_tensor(sc.mu, dtype=dt, device=dev)
+    return torch.einsum("ia,iab,ib->i", e, As, e) - (e * h).sum(1) - MU_B * mu * (e @ B.to(dev, dt))
