@@ -369,6 +369,34 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
                         "grad_norm_per_shell": [float(x) for x in g.reshape(4, -1).norm(dim=1)]}}
 
 
+def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1):
+    """Monte Carlo colour sweeps on the 128^3 two-site bcc workload (4,194,304 spins, z = 26, full
+    3x3 tensors), T = 300 K, in-kernel Philox draws: site updates per second (one update = one trial
+    move or one over-relaxation reflection of one spin)."""
+    import torch
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=L, field=FIELD)
+    mc = MetropolisMC(sc, TEMP, seed=1, sigma=0.3, overrelax=overrelax, move=move)
+    lat = mc.model.to_lattice(sc.init_spins("random", seed=1))
+    mc.sweep_lattice(lat, 3)
+    mc.acceptance()
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    mc.sweep_lattice(lat, sweeps)
+    b.record(stream)
+    b.synchronize()
+    t = a.elapsed_time(b) * 1e-3
+    updates = sc.N * (1 + overrelax) * sweeps
+    return {"workload": f"two-site bcc {L}^3 ({sc.N:,} spins), T = 300 K, {move} moves + {overrelax} over-relaxation "
+                        "pass per sweep, Philox, FP64",
+            "value": updates / t, "unit": "site-updates/s", "sweeps": sweeps, "ms_per_sweep": 1e3 * t / sweeps,
+            "colour_classes": mc.ncolors, "acceptance": mc.acceptance(),
+            "gpu_launches_per_sweep": mc.ncolors * (1 + overrelax)}
+
+
 def bench_df32(L, K, warmup):
     """The same workload with the exchange gather in compensated FP32 pairs (precision="df32"): spins,
     rhs and integration stay FP64.  Reported beside the FP64 value, never as it."""
@@ -518,6 +546,8 @@ def run_gb300(args):
         line["adjoint_large"] = bench_adjoint(L=1024, nsteps=200, seg=50)
     if ws == 1 and not args.no_batched and not args.no_adjoint:
         line["large_batched_adjoint"] = bench_config5()
+    if ws == 1 and not args.no_batched:
+        line["monte_carlo"] = bench_mc(L=args.L)
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -538,7 +568,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
-    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "config5"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "config5", "mc"], default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
     ap.add_argument("--adjoint-L", type=int, default=128)
@@ -554,6 +584,8 @@ def main():
             out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps or 2000)
         elif args.only == "df32":
             out = bench_df32(args.L, args.steps, args.warmup)
+        elif args.only == "mc":
+            out = bench_mc(L=args.L, sweeps=min(args.steps, 100))
         elif args.only == "config5":
             out = bench_config5(K=min(args.steps, 50), adj_steps=args.adjoint_steps or 1000)
         else:

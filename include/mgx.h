@@ -274,6 +274,50 @@ mgx_status mgx_topological_charge(const mgx_model* m, const double* e, const int
  * The LLG kernels are bound by this rate on GB300, so it is the denominator of their roofline. */
 mgx_status mgx_measure_fp64_peak(double* flops_per_s);
 
+/* ---------------------------------------------------------------- Monte Carlo colour sweeps
+ * Replace MetropolisMC (magex/montecarlo.py:71-230) with its NumPy moves, the numba colour pass
+ * _mc_group (magex/fast.py:393-490) and CudaMC / _k_mc (magex/cuda_backend.py:220-304,380-418).
+ *
+ * First-fit greedy colouring in magex site order (magex/montecarlo.py:35-48, the graph of every
+ * coupling in both directions): host-only, no GPU needed.  colour: host [N] output. */
+mgx_status mgx_colour_stencil(const mgx_lattice_desc* lat, int32_t* colour, int32_t* ncolours);
+/* The same for an explicit adjacency (host CSR over magex site indices; self-loops are ignored). */
+mgx_status mgx_colour_graph(int64_t nsites, const int64_t* ptr, const int32_t* nbr, int32_t* colour,
+                            int32_t* ncolours);
+
+typedef struct mgx_mc mgx_mc;
+enum { MGX_MC_GAUSSIAN = 0, MGX_MC_UNIFORM = 1, MGX_MC_HEATBATH = 2, MGX_MC_HINZKE = 3 };
+enum { MGX_MC_RNG_PHILOX = 0, MGX_MC_RNG_HOST = 1 };
+typedef struct mgx_mc_params {
+  int32_t move;              /* MGX_MC_* trial move of MetropolisMC(move=...) */
+  int32_t overrelax;         /* over-relaxation passes per sweep (MetropolisMC(overrelax=...)) */
+  int32_t rng;               /* MGX_MC_RNG_PHILOX (key seed) or MGX_MC_RNG_HOST (draws per sweep) */
+  double sigma;              /* Gaussian cone width (adapted by the caller, magex/montecarlo.py:257-261) */
+  uint64_t seed;
+} mgx_mc_params;
+/* group_sites: host, magex site indices of every colour class in update order, concatenated
+ * (group_sizes[g] each; pinned sites left out, as magex/montecarlo.py:93-99). */
+mgx_status mgx_mc_create(const mgx_model* m, const mgx_mc_params* p, const int64_t* group_sites,
+                         const int64_t* group_sizes, int32_t ngroups, mgx_mc** out);
+mgx_status mgx_mc_destroy(mgx_mc* mc);
+/* Inverse temperatures 1 / (k_B T) (1/meV; +inf at T = 0): host [ns] per sublattice, or host [N] per
+ * site in magex order (site temperatures, magex/montecarlo.py:149-154).  Synchronous. */
+mgx_status mgx_mc_set_beta(mgx_mc* mc, const double* beta_sub, const double* beta_site);
+mgx_status mgx_mc_set_sigma(mgx_mc* mc, double sigma);
+/* Doubles of host draws one sweep consumes (MGX_MC_RNG_HOST). */
+mgx_status mgx_mc_host_draws(const mgx_mc* mc, int64_t* ndoubles);
+/* nsweeps sweeps of the lattice-layout spins e (device): one pass of the trial move over every class
+ * in order, then `overrelax` reflection passes over every class (magex/montecarlo.py:181-210).
+ * MGX_MC_RNG_HOST: nsweeps = 1 and host_draws (device) holds, class after class, the draws of the
+ * NumPy sweep in its order: gaussian / uniform: normal (n, 3) then uniform (n); heatbath: uniform (n),
+ * uniform (n), uniform (n); hinzke: integer k in {0,1,2} (n, as doubles), normal (n, 3), normal (n, 3),
+ * uniform (n); classes where some beta is infinite use the gaussian layout; then per over-relaxation
+ * pass and class: uniform (n). */
+mgx_status mgx_mc_sweep(mgx_mc* mc, double* e, int64_t nsweeps, const double* host_draws, void* stream);
+/* Accepted trial moves and tried moves since the last reset (MetropolisMC.acceptance); synchronises
+ * the stream. */
+mgx_status mgx_mc_counts(mgx_mc* mc, uint64_t* accepted, uint64_t* tried, int32_t reset, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

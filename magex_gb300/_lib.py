@@ -19,6 +19,8 @@ PRECISION_FP64, PRECISION_DF32_GATHER = 0, 1
 MAX_SUBLATTICES = 16
 MAX_BONDS = 256
 NOALLOC_MAX_SITES = 262144
+MC_GAUSSIAN, MC_UNIFORM, MC_HEATBATH, MC_HINZKE = 0, 1, 2, 3
+MC_RNG_PHILOX, MC_RNG_HOST = 0, 1
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int32)
@@ -47,6 +49,11 @@ class CSRDesc(C.Structure):
                 ("sign_site", _dp), ("pinned", _u8p), ("B", C.c_double * 3)]
 
 
+class MCParams(C.Structure):
+    _fields_ = [("move", C.c_int32), ("overrelax", C.c_int32), ("rng", C.c_int32), ("sigma", C.c_double),
+                ("seed", C.c_uint64)]
+
+
 #: every exported entry point with (restype, argtypes); the CPU tests check the export list against
 #: include/mgx.h
 SIGNATURES = {
@@ -66,6 +73,17 @@ SIGNATURES = {
     "mgx_llg_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]),
     "mgx_llg_stage": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "mgx_measure_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
+    "mgx_colour_stencil": (C.c_int32, [C.POINTER(LatticeDesc), _ip, _ip]),
+    "mgx_colour_graph": (C.c_int32, [C.c_int64, C.POINTER(C.c_int64), _ip, _ip, _ip]),
+    "mgx_mc_create": (C.c_int32, [C.c_void_p, C.POINTER(MCParams), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                  C.c_int32, C.POINTER(C.c_void_p)]),
+    "mgx_mc_destroy": (C.c_int32, [C.c_void_p]),
+    "mgx_mc_set_beta": (C.c_int32, [C.c_void_p, _dp, _dp]),
+    "mgx_mc_set_sigma": (C.c_int32, [C.c_void_p, C.c_double]),
+    "mgx_mc_host_draws": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "mgx_mc_sweep": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "mgx_mc_counts": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int32,
+                                  C.c_void_p]),
     "mgx_llg_step_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(LLGParams), _dp, C.c_void_p, C.c_void_p, C.c_uint64,
                                          C.c_void_p]),
     "mgx_batch_create": (C.c_int32, [C.POINTER(C.c_void_p), C.POINTER(LLGParams), C.c_int32, C.POINTER(C.c_void_p)]),

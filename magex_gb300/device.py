@@ -90,6 +90,30 @@ def _stencil_matches(sc, Jsp):
     return not (diff.nnz and float(diff.max()) > 1e-12 * scale)
 
 
+def stencil_desc(sc):
+    """mgx_lattice_desc of a Supercell and the host arrays it points into (keep them alive)."""
+    d = _lib.LatticeDesc()
+    d.ns = sc.ns
+    d.L[:] = list(sc.L)
+    d.pbc[:] = [int(p) for p in sc.pbc]
+    d.nbond = len(sc.bond_src)
+    src = np.ascontiguousarray(sc.bond_src, np.int32)
+    dst = np.ascontiguousarray(sc.bond_dst, np.int32)
+    R = np.ascontiguousarray(sc.bond_R, np.int32).reshape(-1)
+    tab = np.ascontiguousarray(sc.table, np.float64).reshape(-1)
+    A = np.ascontiguousarray(sc.A_sub, np.float64).reshape(-1)
+    mu = np.ascontiguousarray(sc.mu_sub, np.float64)
+    sg = np.ascontiguousarray(sc.signs_sub, np.float64)
+    d.bond_src, d.bond_dst, d.bond_R = _lib.iptr(src), _lib.iptr(dst), _lib.iptr(R)
+    d.width = sc.width
+    d.bond_table = _lib.dptr(tab)
+    d.A_sub = _lib.dptr(A)
+    d.mu_sub = _lib.dptr(mu)
+    d.sign_sub = _lib.dptr(sg)
+    d.B[:] = [float(x) for x in sc.B]
+    return d, [src, dst, R, tab, A, mu, sg]
+
+
 class DeviceModel:
     """An ``mgx_model`` on the current CUDA device built from a Supercell."""
 
@@ -108,27 +132,7 @@ class DeviceModel:
             raise NotImplementedError(f"{nb} couplings per cell exceed the kernel limit of {_lib.MAX_BONDS}")
         if sc.ns > _lib.MAX_SUBLATTICES:
             raise NotImplementedError(f"{sc.ns} sublattices exceed the kernel limit of {_lib.MAX_SUBLATTICES}")
-        self._keep = []
-        d = _lib.LatticeDesc()
-        d.ns = sc.ns
-        d.L[:] = list(sc.L)
-        d.pbc[:] = [int(p) for p in sc.pbc]
-        d.nbond = nb
-        src = np.ascontiguousarray(sc.bond_src, np.int32)
-        dst = np.ascontiguousarray(sc.bond_dst, np.int32)
-        R = np.ascontiguousarray(sc.bond_R, np.int32).reshape(-1)
-        tab = np.ascontiguousarray(sc.table, np.float64).reshape(-1)
-        A = np.ascontiguousarray(sc.A_sub, np.float64).reshape(-1)
-        mu = np.ascontiguousarray(sc.mu_sub, np.float64)
-        sg = np.ascontiguousarray(sc.signs_sub, np.float64)
-        self._keep += [src, dst, R, tab, A, mu, sg]
-        d.bond_src, d.bond_dst, d.bond_R = _lib.iptr(src), _lib.iptr(dst), _lib.iptr(R)
-        d.width = sc.width
-        d.bond_table = _lib.dptr(tab)
-        d.A_sub = _lib.dptr(A)
-        d.mu_sub = _lib.dptr(mu)
-        d.sign_sub = _lib.dptr(sg)
-        d.B[:] = [float(x) for x in sc.B]
+        d, self._keep = stencil_desc(sc)
         sites = _lib.SiteDesc()
         if sc.A_site is not None:
             a = np.ascontiguousarray(sc.A_site, np.float64).reshape(-1)

@@ -199,6 +199,61 @@ def main(ref_root):
         out[f"thermal/{key}_sem"] = np.array(blocks.std(ddof=1) / np.sqrt(20))
     out["thermal/params"] = np.array(json.dumps(th))
 
+    # ---------------------------------------------------------------- Monte Carlo (magex/montecarlo.py)
+    from magex import montecarlo as RMC
+
+    def mc_traj(tag, uc, L, pbc, B, T, seed, move, overrelax, sigma, sweeps, init_seed, structure=None):
+        s = RS.SpinSystem(uc, L, pbc, B)
+        if structure:
+            apply_structure(s, structure)
+        mc = RMC.MetropolisMC(s, T, seed, sigma, overrelax, move)
+        assert mc.fast is None, "the golden MC runs use magex's NumPy sweep"
+        e = s.init_spins("random", seed=init_seed)
+        out[f"mc/{tag}/e0"] = e.copy()
+        out[f"mc/{tag}/colour"] = RMC.greedy_coloring(s.N, s.bonds).astype(np.int32)
+        acc = []
+        for k in range(1, sweeps + 1):
+            e = mc.sweep(e)
+            out[f"mc/{tag}/e{k}"] = e.copy()
+            acc.append([mc.accepted, mc.tried])
+        out[f"mc/{tag}/accepted_tried"] = np.array(acc, np.int64)
+        out[f"mc/{tag}/energy"] = np.array(s.energy(e))
+        models["mc__" + tag] = dict(model=None, L=list(L), pbc=[bool(x) for x in pbc], B=list(map(float, B)),
+                                    T=T, seed=seed, move=move, overrelax=overrelax, sigma=sigma, sweeps=sweeps,
+                                    structure=structure, N=int(s.N), ncolors=mc.ncolors)
+
+    mc_traj("gauss_dmi", ucs["sc_dmi"], (6, 6, 6), (1, 1, 1), (0.1, 0.0, 0.4), 10.0, 3, "gaussian", 1, 0.6, 5, 1)
+    mc_traj("uniform_sc", ucs["sc"], (4, 4, 4), (1, 1, 1), (0.0, 0.0, 0.0), 20.0, 4, "uniform", 0, 0.6, 5, 2)
+    mc_traj("heatbath_tri", ucs["tri"], (8, 8, 1), (1, 1, 0), (0.0, 0.0, 1.0), 5.0, 5, "heatbath", 1, 0.6, 5, 3)
+    mc_traj("hinzke_bcc2", ucs["bcc2"], (2, 2, 2), (1, 1, 1), (0.0, 0.0, 0.5), 300.0, 6, "hinzke", 0, 0.4, 5, 4)
+    mc_traj("T0_afm", ucs["sc_afm"], (4, 4, 4), (1, 1, 1), (0.0, 0.0, 0.0), 0.0, 7, "heatbath", 1, 0.3, 5, 5)
+    mc_traj("open_kagome", ucs["kagome"], (4, 3, 1), (0, 0, 0), (0.0, 0.2, 0.1), 8.0, 8, "gaussian", 2, 0.5, 4, 6)
+    mc_traj("structure", ucs["sc_dmi"], (6, 6, 4), (1, 1, 1), (0, 0, 0.5), 10.0, 9, "heatbath", 1, 0.6, 4, 7,
+            structure=st)
+    mc_traj("bcc2_shell4", ucs["bcc2_shell4"], (3, 3, 3), (1, 1, 1), (0.0, 0.0, 0.2), 150.0, 10, "gaussian", 1,
+            0.3, 3, 8)
+    # carved sphere with vacancies (neighbour lists): the structure of the sc_sphere LLG case
+    mc_traj("sphere", ucs["sc_dmi"], (9, 9, 9), (0, 0, 0), (0.1, 0.0, 0.4), 6.0, 11, "gaussian", 1, 0.6, 3, 9,
+            structure=dict(shape="sphere", size=11.0, vacancies=dict(fraction=0.1, seed=3)))
+
+    # one (L, T) point of magex's Monte Carlo run (equilibrium E, C, m, chi, U4 with 10-block errors)
+    cpt = dict(sigma=0.6, overrelax=1, move="gaussian", init="ferro", init_axis=(0, 0, 1), therm_sweeps=1000,
+               meas_sweeps=4000, sample_every=2)
+    row = RMC._point((ucs["sc"], (8, 8, 8), (1, 1, 1), (0.0, 0.0, 0.0), 25.0, cpt, 12))
+    models["mc_point"] = dict(c=cpt, L=[8, 8, 8], T=25.0, seed=12,
+                              row={k: (float(v) if np.isscalar(v) else v) for k, v in row.items()
+                                   if k not in ("spins", "seconds", "mvec")})
+
+    # T_c estimation from rows of two sizes (synthetic rows with a Binder crossing)
+    Ts = np.linspace(20.0, 40.0, 9)
+    rows = []
+    for Lc, slope in ((4, 0.010), (8, 0.022)):
+        for T in Ts:
+            x = np.tanh((31.0 - T) * slope * 10)
+            rows.append(dict(L=[Lc] * 3, T=float(T), chi=float(np.exp(-((T - 30.5 - 4.0 / Lc) / 3.0) ** 2) * Lc),
+                             C=float(1.0 / (1 + (T - 29.0) ** 2)), U4=float(0.55 + 0.1 * x)))
+    models["mc_tc"] = dict(rows=rows, estimate=RMC.estimate_tc(rows))
+
     # ---------------------------------------------------------------- topological charge
     s = RS.SpinSystem(ucs["tri"], (30, 30, 1), (1, 1, 0))
     c = s.positions[:, :2].mean(0)

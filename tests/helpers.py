@@ -86,3 +86,23 @@ def assert_within_3_sigma(golden, key, mean, sem):
     ref, ref_sem = float(golden[f"thermal/{key}_mean"]), float(golden[f"thermal/{key}_sem"])
     bound = 3.0 * np.hypot(ref_sem, sem)
     assert abs(mean - ref) <= bound, (key, mean, ref, bound)
+
+
+UC_OF = {"gauss_dmi": "sc_dmi", "uniform_sc": "sc", "heatbath_tri": "tri", "hinzke_bcc2": "bcc2",
+         "T0_afm": "sc_afm", "open_kagome": "kagome", "structure": "sc_dmi", "bcc2_shell4": "bcc2_shell4"}
+MC_TAGS = list(UC_OF) + ["sphere"]
+
+
+def mc_system(golden, golden_models, tag):
+    """The system of a golden Monte Carlo case (Supercell, or NeighbourList for the carved sphere)."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.spinmodel import load_results
+    meta = golden_models["mc__" + tag]
+    if tag == "sphere":
+        nl, _, _ = golden_irregular(golden, golden_models, "sc_sphere")
+        return nl, meta
+    sc = Supercell(load_results(golden_models[UC_OF[tag]]["model"]), tuple(meta["L"]), tuple(meta["pbc"]),
+                   tuple(meta["B"]))
+    if meta["structure"]:
+        apply_structure_subset(sc, meta["structure"])
+    return sc, meta

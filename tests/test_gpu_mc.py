@@ -1,0 +1,153 @@
+"""Monte Carlo colour sweeps on the GB300 against the reference.
+
+* rng="host": the kernels consume magex's own NumPy draws and reproduce MetropolisMC.sweep
+  (magex/montecarlo.py:181-210) sweep by sweep (spins to 1e-12, accepted / tried counts exactly);
+* rng="philox": the physics checks of the reference's own MC tests (exact single-spin average,
+  Langevin law, moves agree, ordered / paramagnetic limits) and one (L, T) point of magex's run
+  (magex/montecarlo.py:251-307) whose E and m agree within 3 combined standard errors.
+"""
+import numpy as np
+import pytest
+
+from helpers import MC_TAGS, mc_system
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("tag", MC_TAGS)
+def test_host_rng_sweeps_match_reference(cuda, golden, golden_models, tag):
+    from magex_gb300.mc import MetropolisMC
+    sc, meta = mc_system(golden, golden_models, tag)
+    mc = MetropolisMC(sc, meta["T"], meta["seed"], meta["sigma"], meta["overrelax"], meta["move"], rng="host")
+    assert mc.ncolors == meta["ncolors"]
+    e = golden[f"mc/{tag}/e0"].copy()
+    counts = golden[f"mc/{tag}/accepted_tried"]
+    for k in range(1, meta["sweeps"] + 1):
+        out = mc.sweep(e)
+        assert out is e                                      # in place, as magex
+        err = np.abs(e - golden[f"mc/{tag}/e{k}"]).max()
+        assert err <= 1e-12, (tag, k, err)
+        assert mc.counts() == tuple(int(x) for x in counts[k - 1]), (tag, k)
+    E = float(golden[f"mc/{tag}/energy"])
+    assert abs(mc.model.observables(mc.model.to_lattice(e))[0].item() - E) <= 1e-11 * max(1.0, abs(E))
+
+
+def test_point_matches_reference_within_3_sigma(cuda, golden_models):
+    """magex's (L, T) Monte Carlo point (sc 8^3, J = 1 meV, 25 K, Gaussian moves + over-relaxation,
+    1000 + 4000 sweeps): E/N and m from in-kernel Philox draws within 3 combined standard errors."""
+    from magex_gb300.mc import point
+    from magex_gb300.spinmodel import load_results
+    g = golden_models["mc_point"]
+    ref = g["row"]
+    uc = load_results(golden_models["sc"]["model"])
+    c = dict(g["c"])
+    c["init_axis"] = tuple(c["init_axis"])
+    row = point((uc, tuple(g["L"]), (True, True, True), (0.0, 0.0, 0.0), g["T"], c, 99))
+    for key, err in (("E", "dE"), ("m", "dm")):
+        bound = 3.0 * np.hypot(ref[err], row[err])
+        assert abs(row[key] - ref[key]) <= bound, (key, row[key], ref[key], bound)
+    assert abs(row["acceptance"] - ref["acceptance"]) < 0.05
+    assert row["ncolors"] == ref["ncolors"]
+
+
+@pytest.mark.parametrize("move", ["gaussian", "uniform", "heatbath", "hinzke"])
+def test_exact_single_spin_average(cuda, golden_models, move):
+    """Independent spins with SIA and a tilted field: <m_z> equals the quadrature of the Boltzmann
+    weight (the reference's test, tests/test_fast.py:50-71)."""
+    from magex_gb300.constants import K_B, MU_B
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.spinmodel import load_results, make_model
+    sc = Supercell(load_results(make_model("sc", J=[0.0], K=1.0)), (16, 16, 16), (False, False, False), (0.2, 0, 2.0))
+    T = 10.0
+    th = np.linspace(0, np.pi, 601)
+    ph = np.linspace(0, 2 * np.pi, 601)
+    TH, PH = np.meshgrid(th, ph, indexing="ij")
+    E3 = np.stack([np.sin(TH) * np.cos(PH), np.sin(TH) * np.sin(PH), np.cos(TH)], -1)
+    En = np.einsum("...a,ab,...b->...", E3, sc.A_sub[0], E3) - 2 * MU_B * (E3 @ np.array([0.2, 0, 2.0]))
+    w = np.exp(-(En - En.min()) / (K_B * T)) * np.sin(TH)
+    integ = lambda f: np.trapezoid(np.trapezoid(f, ph, axis=1), th)      # noqa: E731
+    mz = integ(w * E3[..., 2]) / integ(w)
+    mc = MetropolisMC(sc, T, 3, 0.6, 1, move)
+    lat = mc.model.to_lattice(sc.init_spins("ferro"))
+    ms = []
+    for n in range(400):
+        mc.sweep_lattice(lat)
+        if n > 50:
+            ms.append(float(lat[2].mean()))
+    assert abs(np.mean(ms) - mz) < 4 * np.std(ms) / np.sqrt(len(ms) / 3) + 1e-3
+
+
+def test_langevin_free_spins(cuda):
+    """Free spins in a field: <m_z> = coth(x) - 1/x (tests/test_spindyn.py:80-93)."""
+    from magex_gb300.constants import K_B, MU_B
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.spinmodel import load_results, make_model
+    sc = Supercell(load_results(make_model("sc", J=[0.0], moment=2.0)), (6, 6, 6), field=(0, 0, 5.0))
+    T = 5.0
+    mc = MetropolisMC(sc, T, seed=3, overrelax=0)
+    lat = mc.model.to_lattice(sc.init_spins("random", seed=1))
+    acc = []
+    for k in range(600):
+        mc.sweep_lattice(lat)
+        if k > 100:
+            acc.append(float(lat[2].mean()))
+    x = 2.0 * MU_B * 5.0 / (K_B * T)
+    assert abs(np.mean(acc) - (1 / np.tanh(x) - 1 / x)) < 0.01
+
+
+def test_moves_agree(cuda):
+    """Gaussian and heat-bath moves sample the same <E> (tests/test_universal.py:155-170)."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.spinmodel import load_results, make_model
+    uc = load_results(make_model("sc", J=[1.0], K=0.3))
+    out = {}
+    for mv in ("gaussian", "heatbath"):
+        sc = Supercell(uc, (6, 6, 6), field=(0, 0, 0.5))
+        mc = MetropolisMC(sc, 20.0, 1, 0.6, 0, mv)
+        lat = mc.model.to_lattice(sc.init_spins("ferro"))
+        Es = []
+        for n in range(1500):
+            mc.sweep_lattice(lat)
+            if n > 300 and n % 5 == 0:
+                Es.append(mc.model.observables(lat)[0].item() / sc.N)
+        out[mv] = np.mean(Es)
+    assert abs(out["gaussian"] - out["heatbath"]) < 0.04
+
+
+def test_ordered_and_paramagnetic_limits(cuda):
+    """Order parameter near 1 at 0.2 T_mf and small at 2 T_mf (tests/test_spindyn.py:66-78)."""
+    from magex_gb300.constants import K_B
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.spinmodel import load_results, make_model
+    sc = Supercell(load_results(make_model("sc", J=[1.0])), (4, 4, 4))
+    Tmf = 2.0 * 6 * 1.0 / (3.0 * K_B)               # mean-field T_c of the sc ferromagnet, E = -sum J e.e
+    for T, lo, hi in ((0.2 * Tmf, 0.8, 1.01), (2.0 * Tmf, 0.0, 0.35)):
+        mc = MetropolisMC(sc, T, seed=1)
+        lat = mc.model.to_lattice(sc.init_spins("reference"))
+        ms = []
+        for k in range(300):
+            mc.sweep_lattice(lat)
+            if k > 100:
+                o = mc.model.observables(lat).cpu().numpy()
+                ms.append(np.linalg.norm(o[4:7]) / sc.N)
+        assert lo < np.mean(ms) < hi
+
+
+def test_philox_sweeps_are_deterministic_and_keep_unit_norm(cuda):
+    import torch
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=8)
+    runs = []
+    for _ in range(2):
+        mc = MetropolisMC(sc, 300.0, seed=5, overrelax=1, move="hinzke")
+        lat = mc.model.to_lattice(sc.init_spins("random", seed=2))
+        mc.sweep_lattice(lat, 5)
+        runs.append(lat.clone())
+        assert 0.0 < mc.acceptance() < 1.0
+    assert torch.equal(runs[0], runs[1])
+    assert float((torch.linalg.vector_norm(runs[0], dim=0) - 1).abs().max()) < 1e-14
