@@ -369,7 +369,7 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
                         "grad_norm_per_shell": [float(x) for x in g.reshape(4, -1).norm(dim=1)]}}
 
 
-def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1):
+def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True):
     """Monte Carlo colour sweeps on the 128^3 two-site bcc workload (4,194,304 spins, z = 26, full
     3x3 tensors), T = 300 K, in-kernel Philox draws: site updates per second (one update = one trial
     move or one over-relaxation reflection of one spin)."""
@@ -389,12 +389,30 @@ def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1):
     b.record(stream)
     b.synchronize()
     t = a.elapsed_time(b) * 1e-3
+    ncol = mc.ncolors
     updates = sc.N * (1 + overrelax) * sweeps
+    acc = mc.acceptance()
+    del mc, lat
+    cpu = None
+    if cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import OracleMC, max_threads
+        ora = OracleMC(sc, TEMP, 1, 0.3, overrelax, move, csr="stencil")
+        e = sc.init_spins("random", seed=1)
+        ora.sweep(e)
+        n, t0 = 0, time.perf_counter()
+        while n < 2 or (time.perf_counter() - t0 < 10.0 and n < 10):
+            ora.sweep(e)
+            n += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": sc.N * (1 + overrelax) * n / el, "unit": "site-updates/s", "cores": max_threads(),
+               "kind": "port", "sample": f"{n} sweeps of the same lattice, {el:.1f} s: C restatement of magex's "
+                                         "NumPy colour sweep (OpenMP over each class) with magex's NumPy draws"}
     return {"workload": f"two-site bcc {L}^3 ({sc.N:,} spins), T = 300 K, {move} moves + {overrelax} over-relaxation "
                         "pass per sweep, Philox, FP64",
             "value": updates / t, "unit": "site-updates/s", "sweeps": sweeps, "ms_per_sweep": 1e3 * t / sweeps,
-            "colour_classes": mc.ncolors, "acceptance": mc.acceptance(),
-            "gpu_launches_per_sweep": mc.ncolors * (1 + overrelax)}
+            "colour_classes": ncol, "acceptance": acc, "gpu_launches_per_sweep": ncol * (1 + overrelax),
+            "cpu_baseline": cpu}
 
 
 def bench_df32(L, K, warmup):
@@ -547,7 +565,7 @@ def run_gb300(args):
     if ws == 1 and not args.no_batched and not args.no_adjoint:
         line["large_batched_adjoint"] = bench_config5()
     if ws == 1 and not args.no_batched:
-        line["monte_carlo"] = bench_mc(L=args.L)
+        line["monte_carlo"] = bench_mc(L=args.L, cpu_baseline=not args.no_cpu_baseline)
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

@@ -13,11 +13,15 @@
  *                       magex/llg.py:250-252,265 (max torque, mean spin).
  *   oracle_gauss3       magex/fast.py:123-200 (xorshift64* streams over 256 fixed chunks and the
  *                       128-layer Marsaglia-Tsang ziggurat), the reference's multithreaded noise.
+ *   oracle_greedy_colour, oracle_mc_group
+ *                       magex/montecarlo.py:35-48,181-227 (colour classes and the NumPy Monte Carlo
+ *                       sweep with its moves), at the end of this file.
  *
  * Neighbour data is magex's per-site block list (magex/fast.py:587-627): ptr (N+1), nbr, typ and a
  * coupling table of width 1 (J), 4 (J, D) or 9 (3x3 row-major), in magex site order.
  * Build: see oracle/Makefile (gcc -O2 -fopenmp, plain C99, no target-specific flags).
  */
+#define _DEFAULT_SOURCE
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -372,4 +376,168 @@ int64_t oracle_stencil_csr(int ns, const int32_t* L, const int32_t* pbc, int nbo
     ptr[site + 1] = n;
   }
   return ptr[N];
+}
+
+/* ================================================================ Monte Carlo colour sweeps
+ * oracle_greedy_colour  magex/montecarlo.py:35-48: first-fit greedy colouring in site order of the
+ *                       graph adj + adj^T (self-loops ignored).
+ * oracle_mc_group       one group update of MetropolisMC.sweep (magex/montecarlo.py:181-210) with
+ *                       its NumPy moves (magex/montecarlo.py:51-68,136-147,212-227), consuming draws
+ *                       that the caller made with magex's generator in magex's order:
+ *                         move 0 gaussian / 1 uniform: normal (n,3), uniform (n)
+ *                         move 2 heat bath:            uniform (n), uniform (n), uniform (n)
+ *                         move 3 hinzke:               k (n), normal (n,3), normal (n,3), uniform (n)
+ *                         move 4 over-relaxation:      uniform (n)
+ *                       Returns the number of accepted moves.  All sites of the group see the spins
+ *                       of before the pass, as in magex's vectorised update. */
+int32_t oracle_greedy_colour(int64_t N, const int64_t* ptr, const int32_t* nbr, int32_t* colour) {
+  int64_t* tptr = (int64_t*)calloc((size_t)N + 1, sizeof(int64_t));
+  int32_t* tnbr = (int32_t*)malloc(sizeof(int32_t) * (size_t)(ptr[N] > 0 ? ptr[N] : 1));
+  int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)(N > 0 ? N : 1));
+  for (int64_t k = 0; k < ptr[N]; ++k) tptr[nbr[k] + 1]++;
+  for (int64_t v = 0; v < N; ++v) tptr[v + 1] += tptr[v];
+  for (int64_t v = 0; v < N; ++v) fill[v] = tptr[v];
+  for (int64_t v = 0; v < N; ++v)
+    for (int64_t k = ptr[v]; k < ptr[v + 1]; ++k) tnbr[fill[nbr[k]]++] = (int32_t)v;
+  int32_t ncol = 0, cap = 64;
+  int64_t* mark = (int64_t*)malloc(sizeof(int64_t) * (size_t)cap);
+  for (int32_t c = 0; c < cap; ++c) mark[c] = -1;
+  for (int64_t v = 0; v < N; ++v) colour[v] = -1;
+  for (int64_t v = 0; v < N; ++v) {
+    for (int pass = 0; pass < 2; ++pass) {
+      const int64_t* p = pass ? tptr : ptr;
+      const int32_t* q = pass ? tnbr : nbr;
+      for (int64_t k = p[v]; k < p[v + 1]; ++k) {
+        const int32_t c = colour[q[k]];
+        if (q[k] == v || c < 0) continue;
+        while (c >= cap) {
+          mark = (int64_t*)realloc(mark, sizeof(int64_t) * (size_t)cap * 2);
+          for (int32_t x = cap; x < 2 * cap; ++x) mark[x] = -1;
+          cap *= 2;
+        }
+        mark[c] = v;
+      }
+    }
+    int32_t c = 0;
+    while (c < cap && mark[c] == v) ++c;
+    colour[v] = c;
+    if (c + 1 > ncol) ncol = c + 1;
+  }
+  free(mark);
+  free(fill);
+  free(tnbr);
+  free(tptr);
+  return ncol;
+}
+
+static void nrm3(double* v) {
+  const double n = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  v[0] /= n;
+  v[1] /= n;
+  v[2] /= n;
+}
+
+static double eAe(const oracle_model* m, int64_t i, const double* v) {
+  const double* A = m->A + 9 * i;
+  return v[0] * (A[0] * v[0] + A[1] * v[1] + A[2] * v[2]) + v[1] * (A[3] * v[0] + A[4] * v[1] + A[5] * v[2]) +
+         v[2] * (A[6] * v[0] + A[7] * v[1] + A[8] * v[2]);
+}
+
+int64_t oracle_mc_group(const oracle_model* m, const int64_t* idx, int64_t n, int move, const double* beta,
+                        double sigma, const double* draws, double* e, int nthreads) {
+  double* en = (double*)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
+  unsigned char* acc = (unsigned char*)malloc((size_t)(n > 0 ? n : 1));
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int64_t t = 0; t < n; ++t) {
+    const int64_t i = idx[t];
+    double h[3];
+    hfield(m, i, e, h);
+    const double* eo = e + 3 * i;
+    double* v = en + 3 * t;
+    const double mu = m->mu[i], bt = beta[i];
+    double extra = 0.0, ua;
+    if (move == 4) {                                    /* reflection about the exchange field */
+      const double hh = h[0] * h[0] + h[1] * h[1] + h[2] * h[2];
+      v[0] = eo[0]; v[1] = eo[1]; v[2] = eo[2];
+      if (hh > 1e-14) {
+        const double p = 2.0 * ((eo[0] * h[0] + eo[1] * h[1] + eo[2] * h[2]) / hh);
+        v[0] = p * h[0] - eo[0];
+        v[1] = p * h[1] - eo[1];
+        v[2] = p * h[2] - eo[2];
+      }
+      nrm3(v);
+      ua = draws[t];
+    } else if (move == 2) {                             /* heat bath of H = 2h + mu_B mu B */
+      const double zf = MU_B * mu;
+      const double H[3] = {2.0 * h[0] + zf * m->B[0], 2.0 * h[1] + zf * m->B[1], 2.0 * h[2] + zf * m->B[2]};
+      const double u1 = draws[t], u2 = draws[n + t];
+      ua = draws[2 * n + t];
+      const double Hn = sqrt(H[0] * H[0] + H[1] * H[1] + H[2] * H[2]);
+      const double x = bt * Hn;
+      const int small = x < 1e-8;
+      double c = small ? 2.0 * u1 - 1.0 : 1.0 + log1p(-u1 * (-expm1(-2.0 * x))) / x;
+      if (c > 1.0) c = 1.0;
+      if (c < -1.0) c = -1.0;
+      const double ph = 2.0 * M_PI * u2;
+      double z[3] = {0.0, 0.0, 1.0};
+      if (!small) {
+        const double d = Hn > 0 ? Hn : 1.0;
+        z[0] = H[0] / d; z[1] = H[1] / d; z[2] = H[2] / d;
+      }
+      const double a[3] = {fabs(z[0]) < 0.9 ? 1.0 : 0.0, fabs(z[0]) < 0.9 ? 0.0 : 1.0, 0.0};
+      double t1[3] = {z[1] * a[2] - z[2] * a[1], z[2] * a[0] - z[0] * a[2], z[0] * a[1] - z[1] * a[0]};
+      nrm3(t1);
+      const double t2[3] = {z[1] * t1[2] - z[2] * t1[1], z[2] * t1[0] - z[0] * t1[2], z[0] * t1[1] - z[1] * t1[0]};
+      const double s = sqrt(1.0 - c * c), cp = cos(ph), sp = sin(ph);
+      for (int k = 0; k < 3; ++k) v[k] = c * z[k] + s * (cp * t1[k] + sp * t2[k]);
+      nrm3(v);
+      extra = (v[0] - eo[0]) * H[0] + (v[1] - eo[1]) * H[1] + (v[2] - eo[2]) * H[2];
+    } else {
+      const double* g = draws + (move == 3 ? n : 0) + 3 * t;
+      if (move == 1) {
+        v[0] = g[0]; v[1] = g[1]; v[2] = g[2];
+      } else {
+        v[0] = eo[0] + sigma * g[0]; v[1] = eo[1] + sigma * g[1]; v[2] = eo[2] + sigma * g[2];
+      }
+      nrm3(v);
+      if (move == 3) {
+        const int k = (int)draws[t];
+        if (k == 1) {
+          const double* f = draws + 4 * n + 3 * t;
+          v[0] = f[0]; v[1] = f[1]; v[2] = f[2];
+          nrm3(v);
+        } else if (k == 2) {
+          v[0] = -eo[0]; v[1] = -eo[1]; v[2] = -eo[2];
+        }
+        ua = draws[7 * n + t];
+      } else {
+        ua = draws[3 * n + t];
+      }
+    }
+    const double d[3] = {v[0] - eo[0], v[1] - eo[1], v[2] - eo[2]};
+    double dE = -2.0 * (d[0] * h[0] + d[1] * h[1] + d[2] * h[2]) -
+                MU_B * mu * (d[0] * m->B[0] + d[1] * m->B[1] + d[2] * m->B[2]);
+    if (m->A) dE += eAe(m, i, v) - eAe(m, i, eo);
+    dE += extra;
+    int ok = dE <= (move == 4 ? 1e-12 : 0.0);
+    if (!ok) {
+      double a = dE * bt;
+      if (a > 700.0) a = 700.0;
+      ok = ua < exp(-a);
+    }
+    acc[t] = (unsigned char)ok;
+  }
+  int64_t nacc = 0;
+  for (int64_t t = 0; t < n; ++t)
+    if (acc[t]) {
+      const int64_t i = idx[t];
+      e[3 * i] = en[3 * t];
+      e[3 * i + 1] = en[3 * t + 1];
+      e[3 * i + 2] = en[3 * t + 2];
+      ++nacc;
+    }
+  free(acc);
+  free(en);
+  return nacc;
 }

@@ -65,6 +65,11 @@ def load():
         ip = C.POINTER(C.c_int32)
         lib.oracle_stencil_csr.argtypes = [C.c_int, ip, ip, C.c_int, ip, ip, ip, ip, C.POINTER(C.c_int64), ip, ip]
         lib.oracle_stencil_csr.restype = C.c_int64
+        lib.oracle_greedy_colour.argtypes = [C.c_int64, C.POINTER(C.c_int64), ip, ip]
+        lib.oracle_greedy_colour.restype = C.c_int32
+        lib.oracle_mc_group.argtypes = [C.POINTER(_Model), C.POINTER(C.c_int64), C.c_int64, C.c_int, _dp, C.c_double,
+                                        _dp, _dp, C.c_int]
+        lib.oracle_mc_group.restype = C.c_int64
         _lib = lib
     return _lib
 
@@ -210,3 +215,75 @@ class OracleLLG:
         o = self.observables(e)
         N = self.sc.N
         return [self.time, o[0] / N, o[1] / N, o[2] / N, o[3] / N, float(np.linalg.norm(o[4:7]) / N), float(o[7])]
+
+
+class OracleMC:
+    """CPU restatement of magex's MetropolisMC NumPy sweep (magex/montecarlo.py:71-230): greedy colour
+    classes, trial moves gaussian / uniform / heatbath / hinzke, over-relaxation passes, with the draws
+    made by ``numpy.random.default_rng(seed)`` in magex's order (so it reproduces magex's trajectory).
+    Built on OracleLLG's model arrays (same neighbour lists)."""
+
+    MOVES = {"gaussian": 0, "uniform": 1, "heatbath": 2, "hinzke": 3}
+
+    def __init__(self, sc, temperature, seed=None, sigma=0.6, overrelax=1, move="gaussian", threads=0,
+                 csr="blocks"):
+        self.llg = OracleLLG(sc, csr=csr, threads=threads)
+        self.lib = self.llg.lib
+        self.sc = sc
+        a = self.llg._arrays
+        col = np.empty(sc.N, np.int32)
+        ip = C.POINTER(C.c_int32)
+        nc = self.lib.oracle_greedy_colour(sc.N, _p(a["ptr"], C.POINTER(C.c_int64)), _p(a["nbr"], ip), _p(col, ip))
+        self.colour = col
+        pinned = None if getattr(sc, "pinned", None) is None else np.asarray(sc.pinned, bool)
+        self.groups = []
+        for c in range(nc):
+            idx = np.flatnonzero(col == c).astype(np.int64)
+            if pinned is not None:
+                idx = idx[~pinned[idx]]
+            if len(idx):
+                self.groups.append(np.ascontiguousarray(idx))
+        self.ncolors = len(self.groups)
+        self.T = float(temperature)
+        self.rng = np.random.default_rng(seed)
+        self.sigma = float(sigma)
+        self.overrelax = int(overrelax)
+        self.move = move
+        self.threads = int(threads)
+        self.accepted = 0
+        self.tried = 0
+
+    def _beta(self):
+        sT = getattr(self.sc, "site_T", None)
+        if sT is not None:
+            T = np.where(np.isnan(sT), self.T, sT)
+            return np.ascontiguousarray(1.0 / (K_B * np.maximum(T, 1e-9)))
+        b = 1.0 / (K_B * self.T) if self.T > 0 else np.inf
+        return np.full(self.sc.N, b)
+
+    def _group(self, e, idx, mv, draws, beta):
+        return int(self.lib.oracle_mc_group(C.byref(self.llg._m), _p(idx, C.POINTER(C.c_int64)), len(idx), mv,
+                                            _p(beta), self.sigma, _p(np.ascontiguousarray(draws, np.float64)),
+                                            _p(e), self.threads))
+
+    def sweep(self, e):
+        """One sweep of e ((N, 3) float64 C-contiguous array), in place."""
+        rng = self.rng
+        beta = self._beta()
+        self.llg._m.B[:] = [float(x) for x in self.sc.B]
+        for idx in self.groups:
+            n = len(idx)
+            if self.move == "heatbath" and np.all(np.isfinite(beta[idx])):
+                mv, parts = 2, [rng.random(n), rng.random(n)]
+            elif self.move == "hinzke":
+                mv, parts = 3, [rng.integers(0, 3, n).astype(np.float64), rng.normal(size=(n, 3)).ravel(),
+                                rng.normal(size=(n, 3)).ravel()]
+            else:
+                mv, parts = (1 if self.move == "uniform" else 0), [rng.normal(size=(n, 3)).ravel()]
+            parts.append(rng.random(n))
+            self.accepted += self._group(e, idx, mv, np.concatenate(parts), beta)
+            self.tried += n
+        for _ in range(self.overrelax):
+            for idx in self.groups:
+                self._group(e, idx, 4, rng.random(len(idx)), beta)
+        return e

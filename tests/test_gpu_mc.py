@@ -151,3 +151,23 @@ def test_philox_sweeps_are_deterministic_and_keep_unit_norm(cuda):
         assert 0.0 < mc.acceptance() < 1.0
     assert torch.equal(runs[0], runs[1])
     assert float((torch.linalg.vector_norm(runs[0], dim=0) - 1).abs().max()) < 1e-14
+
+
+def test_host_rng_sweeps_match_oracle_bcc_16cube(cuda):
+    """Config-2 Hamiltonian (two-site bcc, full 3x3 tensors, z = 26) on 16^3 (8,192 spins) at 300 K:
+    GPU sweeps with magex's NumPy draws equal the oracle's restatement of magex's sweep.  Over-relaxation
+    is deterministic and amplifies rounding differences (about 4x per sweep), hence 1e-11 after 3."""
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.workloads import bcc_two_site
+    from oracle import OracleMC
+    sc = bcc_two_site(L=16)
+    e0 = sc.init_spins("random", seed=4)
+    gpu = MetropolisMC(sc, 300.0, 21, 0.3, 1, "gaussian", rng="host")
+    ora = OracleMC(sc, 300.0, 21, 0.3, 1, "gaussian", csr="stencil")
+    assert gpu.ncolors == ora.ncolors
+    a, b = e0.copy(), e0.copy()
+    for k in range(3):
+        gpu.sweep(a)
+        ora.sweep(b)
+        assert np.abs(a - b).max() <= 1e-11
+        assert gpu.counts() == (ora.accepted, ora.tried)

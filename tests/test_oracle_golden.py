@@ -121,3 +121,20 @@ def test_oracle_thermal_equilibrium_within_3_sigma_of_reference(golden, golden_m
             M.append(np.linalg.norm(o[1:4]) / sc.N)
     for key, x in (("E", E), ("M", M)):
         assert_within_3_sigma(golden, key, *block_stats(x))
+
+
+@pytest.mark.parametrize("tag", ["gauss_dmi", "uniform_sc", "heatbath_tri", "hinzke_bcc2", "T0_afm", "open_kagome",
+                                 "structure", "bcc2_shell4", "sphere"])
+def test_oracle_mc_sweeps_match_reference(golden, golden_models, tag):
+    """The oracle's Monte Carlo sweep (same NumPy draws) reproduces magex's MetropolisMC trajectories."""
+    from helpers import mc_system
+    from oracle import OracleMC
+    sc, meta = mc_system(golden, golden_models, tag)
+    mc = OracleMC(sc, meta["T"], meta["seed"], meta["sigma"], meta["overrelax"], meta["move"])
+    assert np.array_equal(mc.colour, golden[f"mc/{tag}/colour"])
+    e = golden[f"mc/{tag}/e0"].copy()
+    counts = golden[f"mc/{tag}/accepted_tried"]
+    for k in range(1, meta["sweeps"] + 1):
+        mc.sweep(e)
+        assert np.abs(e - golden[f"mc/{tag}/e{k}"]).max() <= 1e-12, (tag, k)
+        assert (mc.accepted, mc.tried) == tuple(int(x) for x in counts[k - 1])
