@@ -415,6 +415,40 @@ def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True):
             "cpu_baseline": cpu}
 
 
+def bench_sqw(L=128, reps=20):
+    """S(q, w) sampling cost on the 128^3 two-site bcc lattice: one device Fourier projection of the
+    spins onto a Gamma-X-M-Gamma-R path of commensurate wave vectors (every point at L resolution)."""
+    import torch
+    from magex_gb300.device import DeviceModel
+    from magex_gb300.spectra import FourierProjector
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=L, field=FIELD)
+    dm = DeviceModel(sc)
+    h = L // 2
+    G, X, M, R = np.zeros(3), np.array([0.5, 0, 0]), np.array([0.5, 0.5, 0]), np.array([0.5, 0.5, 0.5])
+    pts = []
+    for a, b in ((G, X), (X, M), (M, G), (G, R)):
+        for k in range(h):
+            pts.append(a + (b - a) * k / h)
+    q = np.round(np.array(pts) * L) / L
+    proj = FourierProjector(dm, q)
+    lat = dm.to_lattice(sc.init_spins("random", seed=1))
+    out = proj.project(lat)
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        proj.project(lat, out=out)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / reps
+    return {"workload": f"two-site bcc {L}^3 ({sc.N:,} spins), {len(q)} wave vectors on Gamma-X-M-Gamma-R",
+            "ms_per_sample": ms, "hbm_gbs": 24.0 * sc.N / (ms * 1e-3) / 1e9,
+            "note": "one pass over e (24 B per spin) plus O(nq ns L^2) work; magex's dense phase matrix for this "
+                    f"case would hold {16 * sc.N * len(q) / 1e9:.0f} GB"}
+
+
 def bench_df32(L, K, warmup):
     """The same workload with the exchange gather in compensated FP32 pairs (precision="df32"): spins,
     rhs and integration stay FP64.  Reported beside the FP64 value, never as it."""
@@ -566,6 +600,7 @@ def run_gb300(args):
         line["large_batched_adjoint"] = bench_config5()
     if ws == 1 and not args.no_batched:
         line["monte_carlo"] = bench_mc(L=args.L, cpu_baseline=not args.no_cpu_baseline)
+        line["sqw_projection"] = bench_sqw(L=args.L)
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -586,7 +621,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
-    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "config5", "mc"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "config5", "mc", "sqw"], default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
     ap.add_argument("--adjoint-L", type=int, default=128)
@@ -602,6 +637,8 @@ def main():
             out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps or 2000)
         elif args.only == "df32":
             out = bench_df32(args.L, args.steps, args.warmup)
+        elif args.only == "sqw":
+            out = bench_sqw(L=args.L)
         elif args.only == "mc":
             out = bench_mc(L=args.L, sweeps=min(args.steps, 100))
         elif args.only == "config5":

@@ -318,6 +318,18 @@ mgx_status mgx_mc_sweep(mgx_mc* mc, double* e, int64_t nsweeps, const double* ho
  * the stream. */
 mgx_status mgx_mc_counts(mgx_mc* mc, uint64_t* accepted, uint64_t* tried, int32_t reset, void* stream);
 
+/* ---------------------------------------------------------------- S(q, w) sampling
+ * Device-side Fourier projection m_q = N^-1/2 sum_i e_i exp(-i q.r_i) of lattice-layout spins, the
+ * per-sample product ph^T e of magex/spectra.py:53-66 (structure_factor).  qfrac: host [nq*3]
+ * fractional coordinates of q in the reciprocal lattice of the unit cell (any q, commensurate or not);
+ * sub_phase: host [nq*ns*2] exp(-i q.p_s) of the sublattice positions as (re, im).  Stencil models. */
+typedef struct mgx_fourier mgx_fourier;
+mgx_status mgx_fourier_create(const mgx_model* m, int32_t nq, const double* qfrac, const double* sub_phase,
+                              mgx_fourier** out);
+/* mq: device [nq*3*2] output, (re, im) of m_q^x, m_q^y, m_q^z per q. */
+mgx_status mgx_fourier_project(mgx_fourier* f, const double* e, double* mq, void* stream);
+mgx_status mgx_fourier_destroy(mgx_fourier* f);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,6 +73,9 @@ SIGNATURES = {
     "mgx_llg_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]),
     "mgx_llg_stage": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "mgx_measure_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
+    "mgx_fourier_create": (C.c_int32, [C.c_void_p, C.c_int32, _dp, _dp, C.POINTER(C.c_void_p)]),
+    "mgx_fourier_project": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_fourier_destroy": (C.c_int32, [C.c_void_p]),
     "mgx_colour_stencil": (C.c_int32, [C.POINTER(LatticeDesc), _ip, _ip]),
     "mgx_colour_graph": (C.c_int32, [C.c_int64, C.POINTER(C.c_int64), _ip, _ip, _ip]),
     "mgx_mc_create": (C.c_int32, [C.c_void_p, C.POINTER(MCParams), C.POINTER(C.c_int64), C.POINTER(C.c_int64),

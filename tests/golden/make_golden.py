@@ -254,6 +254,28 @@ def main(ref_root):
                              C=float(1.0 / (1 + (T - 29.0) ** 2)), U4=float(0.55 + 0.1 * x)))
     models["mc_tc"] = dict(rows=rows, estimate=RMC.estimate_tc(rows))
 
+    # ---------------------------------------------------------------- S(q, w) (magex/spectra.py:49-84)
+    from magex import spectra as RSP
+
+    def sqw(tag, uc, L, pbc, B, alpha, dt, T, seed, qfrac, nsteps, sample_every, nseg):
+        s = RS.SpinSystem(uc, L, pbc, B)
+        sol = LLGSolver(s, alpha, dt, T, seed)
+        e = s.init_spins("reference")
+        out[f"sqw/{tag}/e0"] = e.copy()
+        E, Sp, Sl, e = RSP.structure_factor(s, sol, e, np.asarray(qfrac, float), nsteps, sample_every, nseg)
+        out[f"sqw/{tag}/E"] = E
+        out[f"sqw/{tag}/S_perp"] = Sp
+        out[f"sqw/{tag}/S_par"] = Sl
+        out[f"sqw/{tag}/e_end"] = e
+        models["sqw__" + tag] = dict(L=list(L), pbc=[bool(x) for x in pbc], B=list(map(float, B)), alpha=alpha, dt=dt,
+                                     T=T, seed=seed, qfrac=np.asarray(qfrac, float).tolist(), nsteps=nsteps,
+                                     sample_every=sample_every, nseg=nseg)
+
+    sqw("tri", ucs["tri"], (8, 8, 1), (1, 1, 0), (0.0, 0.0, 1.0), 0.05, 1e-3, 5.0, 13,
+        [[0, 0, 0], [0.125, 0, 0], [0.25, 0, 0], [0.5, 0, 0], [1 / 3, 1 / 3, 0], [0.3, 0.1, 0]], 400, 5, 2)
+    sqw("bcc2", ucs["bcc2"], (4, 4, 4), (1, 1, 1), (0.0, 0.0, 0.5), 0.1, 1e-4, 50.0, 14,
+        [[0, 0, 0], [0.25, 0, 0], [0.25, 0.25, 0.25], [0.5, 0.5, 0.5], [0, 0, 0.75], [0.2, 0.35, 0.6]], 240, 4, 2)
+
     # ---------------------------------------------------------------- topological charge
     s = RS.SpinSystem(ucs["tri"], (30, 30, 1), (1, 1, 0))
     c = s.positions[:, :2].mean(0)
