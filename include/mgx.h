@@ -330,6 +330,22 @@ mgx_status mgx_fourier_create(const mgx_model* m, int32_t nq, const double* qfra
 mgx_status mgx_fourier_project(mgx_fourier* f, const double* e, double* mq, void* stream);
 mgx_status mgx_fourier_destroy(mgx_fourier* f);
 
+/* ---------------------------------------------------------------- outputs at scale (host only)
+ * The text writers of magex/observables.py:122-161 and magex/llg.py:286-297, formatted in parallel;
+ * the files are byte-for-byte those of magex's Python writers.  All arrays are host arrays in magex
+ * site order: pos [n*3] (Angstrom), spins [n*3], mu [n], sublattice [n] indexing names[nnames]. */
+mgx_status mgx_write_xyz(const char* path, int64_t n, const double* pos, const double* spins, const double* mu,
+                         const int32_t* sublattice, const char* const* names, int32_t nnames, const char* comment,
+                         int32_t append);
+/* scalars [nscalars*n] written as "SCALARS name double 1" blocks after the spin vectors */
+mgx_status mgx_write_vtk(const char* path, int64_t n, const double* pos, const double* spins, const double* scalars,
+                         const char* const* scalar_names, int32_t nscalars);
+mgx_status mgx_write_ovf(const char* path, int64_t n, const double* pos, const double* spins);
+/* numpy.savetxt(path, values (nrows, ncols), delimiter=",", fmt=fmt, header=header, comments="") for
+ * fmt one of "%.6f", "%.8g", "%.6g", "%.8e"; header may be NULL. */
+mgx_status mgx_write_csv(const char* path, int64_t nrows, int32_t ncols, const double* values, const char* fmt,
+                         const char* header);
+
 #ifdef __cplusplus
 }
 #endif

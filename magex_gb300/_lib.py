@@ -73,6 +73,11 @@ SIGNATURES = {
     "mgx_llg_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]),
     "mgx_llg_stage": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "mgx_measure_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
+    "mgx_write_xyz": (C.c_int32, [C.c_char_p, C.c_int64, _dp, _dp, _dp, _ip, C.POINTER(C.c_char_p), C.c_int32,
+                                  C.c_char_p, C.c_int32]),
+    "mgx_write_vtk": (C.c_int32, [C.c_char_p, C.c_int64, _dp, _dp, _dp, C.POINTER(C.c_char_p), C.c_int32]),
+    "mgx_write_ovf": (C.c_int32, [C.c_char_p, C.c_int64, _dp, _dp]),
+    "mgx_write_csv": (C.c_int32, [C.c_char_p, C.c_int64, C.c_int32, _dp, C.c_char_p, C.c_char_p]),
     "mgx_fourier_create": (C.c_int32, [C.c_void_p, C.c_int32, _dp, _dp, C.POINTER(C.c_void_p)]),
     "mgx_fourier_project": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_fourier_destroy": (C.c_int32, [C.c_void_p]),

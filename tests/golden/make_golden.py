@@ -276,6 +276,36 @@ def main(ref_root):
     sqw("bcc2", ucs["bcc2"], (4, 4, 4), (1, 1, 1), (0.0, 0.0, 0.5), 0.1, 1e-4, 50.0, 14,
         [[0, 0, 0], [0.25, 0, 0], [0.25, 0.25, 0.25], [0.5, 0.5, 0.5], [0, 0, 0.75], [0.2, 0.35, 0.6]], 240, 4, 2)
 
+    # ---------------------------------------------------------------- output files (magex/observables.py, llg.py)
+    import hashlib
+    from magex import observables as ROBS
+    from magex.llg import _write_table, save_spins
+
+    def digest(path):
+        with open(path, "rb") as f:
+            data = f.read()
+        return dict(sha256=hashlib.sha256(data).hexdigest(), size=len(data))
+
+    files = {}
+    for tag, uc, L, pbc in (("tri", ucs["tri"], (6, 5, 1), (1, 1, 0)), ("bcc2", ucs["bcc2"], (3, 2, 2), (1, 1, 1))):
+        s = RS.SpinSystem(uc, L, pbc, (0.0, 0.0, 0.5))
+        e = s.init_spins("random", seed=21)
+        e[0] = [1e-9, -2.5e-7, -1.0]                    # tiny and negative components exercise the formats
+        out[f"out/{tag}/e"] = e
+        d = {}
+        for name, fn in (("xyz", lambda q: ROBS.write_xyz(q, s, e, comment="t=1.5 ps")),
+                         ("vtk", lambda q: ROBS.write_vtk(q, s, e, extra=dict(E=np.linspace(-3, 4e-6, s.N)))),
+                         ("ovf", lambda q: ROBS.write_ovf_atomistic(q, s, e)),
+                         ("csv", lambda q: save_spins(q.replace(".csv", ".npz"), s, e))):
+            q = os.path.join(tmp, f"{tag}.{name}")
+            fn(q)
+            d[name] = digest(q)
+        files[tag] = dict(L=list(L), pbc=[bool(x) for x in pbc], files=d)
+    q = os.path.join(tmp, "table.csv")
+    _write_table(q, out["sc16/table"])
+    files["table"] = digest(q)
+    models["outputs"] = files
+
     # ---------------------------------------------------------------- topological charge
     s = RS.SpinSystem(ucs["tri"], (30, 30, 1), (1, 1, 0))
     c = s.positions[:, :2].mean(0)
