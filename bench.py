@@ -449,35 +449,43 @@ def bench_sqw(L=128, reps=20):
                     f"case would hold {16 * sc.N * len(q) / 1e9:.0f} GB"}
 
 
-def bench_df32(L, K, warmup):
-    """The same workload with the exchange gather in compensated FP32 pairs (precision="df32"): spins,
-    rhs and integration stay FP64.  Reported beside the FP64 value, never as it."""
+def bench_reduced(L, K, warmup, precision):
+    """The same workload with a reduced-FP64 step form: precision="df32" (exchange gather on compensated
+    FP32 pairs) or "int48" (exchange gather in exact 48-bit fixed-point integer arithmetic); both keep
+    the spins, the integration and the renormalisation FP64 and evaluate the rest of the field and the
+    right-hand side on FP32 pairs.  Reported beside the FP64 value, never as it."""
     import torch
     from magex_gb300.llg import GB300LLG
     from magex_gb300.workloads import bcc_two_site
     sc = bcc_two_site(L=L, field=FIELD)
     e0 = sc.init_spins("random", seed=1)
-    sols = {p: GB300LLG(sc, ALPHA, DT, TEMP, seed=1000, precision=p) for p in ("fp64", "df32")}
+    sols = {p: GB300LLG(sc, ALPHA, DT, TEMP, seed=1000, precision=p) for p in ("fp64", precision)}
     lat = {p: sols[p].model.to_lattice(e0) for p in sols}
     stream = torch.cuda.current_stream()
     for _ in range(warmup):
-        sols["df32"].run_lattice(lat["df32"], 1)
+        sols[precision].run_lattice(lat[precision], 1)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     a.record(stream)
-    sols["df32"].run_lattice(lat["df32"], K)
+    sols[precision].run_lattice(lat[precision], K)
     b.record(stream)
     b.synchronize()
     ms = a.elapsed_time(b) / K
     # same Philox stream through the FP64 plan: the deviation after warmup + K steps
     sols["fp64"].run_lattice(lat["fp64"], warmup + K)
     torch.cuda.synchronize()
-    dev = float((lat["fp64"] - lat["df32"]).abs().max())
-    return {"precision": "exchange gather in compensated FP32 pairs (~44 bits), everything else FP64",
+    dev = float((lat["fp64"] - lat[precision]).abs().max())
+    what = {"df32": "exchange gather on compensated FP32 pairs (~44 bits)",
+            "int48": "exchange gather as exact integer arithmetic on 48-bit fixed point (INT32 pipe)"}[precision]
+    # algorithmic bytes per spin-step: predictor e, split in; ep, k1, split out; corrector split, k1, e in; e, split out
+    split = 8
+    nbytes = (24 + split + 24 + 24 + 3 * split) + (3 * split + 24 + 24 + 24 + 3 * split) - split
+    return {"precision": what + "; integration and renormalisation FP64, field remainder and right-hand side "
+                                "on FP32 pairs",
             "value": sc.N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": K,
             "max_abs_deviation_from_fp64_plan": dev, "deviation_after_steps": warmup + K,
-            "hbm_roofline_frac": 72.0 * sc.N / (0.5 * ms * 1e-3) / 1e9 / 6760.6}
-
+            "algorithmic_bytes_per_spin_step": nbytes,
+            "hbm_roofline_frac": nbytes * sc.N / (ms * 1e-3) / 1e9 / 6760.6}
 
 def run_gb300(args):
     import torch
@@ -588,7 +596,8 @@ def run_gb300(args):
         "clocks": clocks,
     }
     if ws == 1:
-        line["df32_gather_variant"] = bench_df32(args.L, min(K, 200), args.warmup)
+        line["df32_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "df32")
+        line["int48_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "int48")
     if ws == 1 and not args.no_batched:
         line["batched"] = bench_batched()
     if ws == 1 and not args.no_adjoint:
@@ -621,7 +630,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
-    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "config5", "mc", "sqw"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "config5", "mc", "sqw"], default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
     ap.add_argument("--adjoint-L", type=int, default=128)
@@ -635,8 +644,8 @@ def main():
         build.build_library()
         if args.only == "adjoint":
             out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps or 2000)
-        elif args.only == "df32":
-            out = bench_df32(args.L, args.steps, args.warmup)
+        elif args.only in ("df32", "int48"):
+            out = bench_reduced(args.L, args.steps, args.warmup, args.only)
         elif args.only == "sqw":
             out = bench_sqw(L=args.L)
         elif args.only == "mc":

@@ -48,10 +48,12 @@ enum {
 
 enum { MGX_INTEGRATOR_HEUN = 0, MGX_INTEGRATOR_DEPONDT = 1 };
 enum { MGX_NOISE_NONE = 0, MGX_NOISE_HOST = 1, MGX_NOISE_PHILOX = 2 };
-/* Arithmetic of the exchange gather: FP64 (default), or compensated FP32 pairs (hi + lo, about 44
- * significant bits) with FP64 everywhere else, the GB300-native form: this part runs FP64 at 1/61 of
- * its FP32 rate. */
-enum { MGX_PRECISION_FP64 = 0, MGX_PRECISION_DF32_GATHER = 1 };
+/* Arithmetic of the exchange gather: FP64 (default); compensated FP32 pairs (hi + lo, about 44
+ * significant bits); or exact integer products and sums of 48-bit fixed-point couplings and spins on
+ * the INT32 multiply-add pipe (64 per clock per SM against 2 FP64 FMAs).  The two reduced forms keep
+ * the integration and renormalisation in FP64 and the rest of the field and the right-hand side on
+ * FP32 pairs (Heun).  The GB300-native forms: FP64 runs at 1/61 of the FP32 rate on this part. */
+enum { MGX_PRECISION_FP64 = 0, MGX_PRECISION_DF32_GATHER = 1, MGX_PRECISION_INT48_GATHER = 2 };
 
 typedef struct mgx_model mgx_model;
 typedef struct mgx_llg mgx_llg;
@@ -96,9 +98,9 @@ typedef struct mgx_llg_params {
   int32_t integrator;        /* MGX_INTEGRATOR_HEUN or MGX_INTEGRATOR_DEPONDT */
   int32_t noise;             /* MGX_NOISE_NONE / _HOST (caller supplies N(0,1) draws) / _PHILOX */
   uint64_t seed;             /* Philox key (MGX_NOISE_PHILOX) */
-  int32_t precision;         /* MGX_PRECISION_FP64 or MGX_PRECISION_DF32_GATHER (stencil models with
-                              * per-sublattice moments and single-ion tensors; the couplings are
-                              * snapshotted when the plan is created) */
+  int32_t precision;         /* MGX_PRECISION_FP64, _DF32_GATHER or _INT48_GATHER (the reduced forms:
+                              * stencil models with per-sublattice moments and single-ion tensors; the
+                              * couplings are snapshotted when the plan is created) */
 } mgx_llg_params;
 
 /* ---------------------------------------------------------------- library */

@@ -94,11 +94,31 @@ struct DevLLG {
 // float pairs pre-scaled by 2 / (mu mu_B) of the receiving sublattice, -2 A / (mu mu_B) per
 // sublattice, and the (hi, lo) copies of the spin fields that the gather reads.
 struct DevDF {
-  const float2* J;               // [nbond*9]
+  const float4* J;               // [nbond*5]: the 9 (hi, lo) pairs of a coupling padded to 10 (80 B)
+  const int2* lin;               // [nbond] (linear offset of the neighbour of an interior cell, signed R2)
+  int4 reach[MGX_MAX_SUBLATTICES];  // per receiving sublattice: max |R| along each axis
+  float2 alpha[MGX_MAX_SUBLATTICES], pre[MGX_MAX_SUBLATTICES], sig[MGX_MAX_SUBLATTICES];  // (hi, lo) splits
+  float2 B[3];                   // (hi, lo) split of the external field, refreshed at every launch
+  const float2* nA2f;            // [ns*9] (hi, lo) split of nA2
   const double* nA2;             // [ns*9]
   int hasA, diagA;
   float2* es;                    // [3][N] split of e
   float2* eps;                   // [3][N] split of ep
+};
+
+// Tables of the fixed-point integer gather (MGX_PRECISION_INT48_GATHER): couplings and on-site
+// tensors as 48-bit fixed-point numbers in two balanced int32 halves (v = hi 2^24 + lo, |lo| <= 2^23)
+// at a per-sublattice power-of-two scale, and the fixed-point copies of the spin fields.
+struct DevFX {
+  const int4* J;                 // [nbond*5]: 9 (hi, lo) pairs of a coupling padded to 10 (80 B)
+  const int4* A;                 // [ns*5]: -2 A / (mu mu_B) in the same format, or nullptr
+  const int2* lin;               // [nbond] (linear offset of the neighbour of an interior cell, signed R2)
+  int4 reach[MGX_MAX_SUBLATTICES];
+  float scale[MGX_MAX_SUBLATTICES];   // 2^(sigma_s - 48): value of one unit of the accumulator
+  float2 alpha[MGX_MAX_SUBLATTICES], pre[MGX_MAX_SUBLATTICES], sig[MGX_MAX_SUBLATTICES];
+  float2 B[3];                   // (hi, lo) split of the external field, refreshed at every launch
+  int2* es;                      // [3][N] fixed-point split of e
+  int2* eps;                     // [3][N] fixed-point split of ep
 };
 
 struct LLGPlan {
@@ -108,6 +128,8 @@ struct LLGPlan {
   int precision = 0;
   DevDF df{};
   void* df_block = nullptr;
+  DevFX fx{};
+  void* fx_block = nullptr;
   void* sub_block = nullptr;     // alpha_sub | pre_sub | sigma_sub
   double* site_block = nullptr;  // alpha_site | pre_site
   double* sigma_site = nullptr;
@@ -122,6 +144,12 @@ inline int site_block_size(long long N) {
   return 64;
 }
 
+// (hi, lo) float pair of a double: hi = float(x), lo = float(x - hi)
+inline float2 split_host(double x) {
+  const float hi = (float)x;
+  return make_float2(hi, (float)(x - (double)hi));
+}
+
 // Enqueue the predictor (stages & 1) and / or the corrector (stages & 2) of one step on st.
 void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
 // Compensated-FP32 gather form (mgx_llg_df.cu): tables built at plan creation, the split copy of e
@@ -129,6 +157,10 @@ void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_
 mgx_status build_df_tables(LLGPlan* pl);
 void enqueue_df_split(const LLGPlan* pl, const double* e, cudaStream_t st);
 void enqueue_df_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
+// Fixed-point integer gather form (mgx_llg_fx.cu), organised the same way.
+mgx_status build_fx_tables(LLGPlan* pl);
+void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st);
+void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
 
 // ------------------------------------------------------------------ small device helpers
 __device__ __forceinline__ void site_coords(const DevLattice& L, long long q, int& s, int& c0, int& c1, int& c2) {

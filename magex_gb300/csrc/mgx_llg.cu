@@ -60,6 +60,10 @@ static void dispatch_noise(const LLGPlan* pl, double* e, const double* noise, ui
 
 void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st,
                       int stages) {
+  if (pl->precision == MGX_PRECISION_INT48_GATHER) {
+    enqueue_fx_step(pl, e, noise, step, st, stages);
+    return;
+  }
   if (pl->precision == MGX_PRECISION_DF32_GATHER) {
     enqueue_df_step(pl, e, noise, step, st, stages);
     return;
@@ -98,8 +102,10 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
     return set_error(MGX_ERR_INVALID, "integrator %d is not heun (0) or depondt (1)", p->integrator);
   if (p->noise < MGX_NOISE_NONE || p->noise > MGX_NOISE_PHILOX)
     return set_error(MGX_ERR_INVALID, "noise mode %d is not none (0), host (1) or philox (2)", p->noise);
-  if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_DF32_GATHER)
-    return set_error(MGX_ERR_INVALID, "precision %d is not fp64 (0) or df32-gather (1)", p->precision);
+  if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_DF32_GATHER &&
+      p->precision != MGX_PRECISION_INT48_GATHER)
+    return set_error(MGX_ERR_INVALID, "precision %d is not fp64 (0), df32-gather (1) or int48-gather (2)",
+                     p->precision);
   const int ns = m->d.ns;
   const long long N = m->d.N;
   LLGPlan* pl = new LLGPlan();
@@ -149,9 +155,9 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
     d.alpha_site = pl->site_block;
     d.pre_site = pl->site_block + N;
   }
-  if (p->precision == MGX_PRECISION_DF32_GATHER) {
-    pl->precision = MGX_PRECISION_DF32_GATHER;
-    const mgx_status st = build_df_tables(pl);
+  if (p->precision != MGX_PRECISION_FP64) {
+    pl->precision = p->precision;
+    const mgx_status st = p->precision == MGX_PRECISION_DF32_GATHER ? build_df_tables(pl) : build_fx_tables(pl);
     if (st != MGX_OK) {
       mgx_llg_destroy(reinterpret_cast<mgx_llg*>(pl));
       return st;
@@ -169,6 +175,7 @@ mgx_status mgx_llg_destroy(mgx_llg* pp) {
   cudaFree(pl->sigma_site);
   cudaFree(pl->scratch);
   cudaFree(pl->df_block);
+  cudaFree(pl->fx_block);
   delete pl;
   return MGX_OK;
 }
@@ -186,10 +193,12 @@ mgx_status mgx_llg_set_sigma(mgx_llg* pp, const double* sigma_sub, const double*
       zero &= sigma_sub[s] == 0.0;
     }
     MGX_CUDA_TRY(cudaMemcpy((double*)pl->sub_block + 2 * ns, sigma_sub, sizeof(double) * ns, cudaMemcpyHostToDevice));
+    for (int s = 0; s < ns; ++s) pl->df.sig[s] = pl->fx.sig[s] = split_host(sigma_sub[s]);
   } else {
     std::vector<double> cur(ns);
     MGX_CUDA_TRY(cudaMemcpy(cur.data(), (double*)pl->sub_block + 2 * ns, sizeof(double) * ns, cudaMemcpyDeviceToHost));
     for (double x : cur) zero &= x == 0.0;
+    for (int s = 0; s < ns; ++s) pl->df.sig[s] = pl->fx.sig[s] = split_host(cur[s]);
   }
   if (sigma_site) {
     std::vector<double> v = site_to_lattice(sigma_site, ns, pl->model->d.ncell);
@@ -207,12 +216,19 @@ mgx_status mgx_llg_set_sigma(mgx_llg* pp, const double* sigma_sub, const double*
   return MGX_OK;
 }
 
+// The reduced-arithmetic forms gather from a split copy of the spins: refresh it from e at the start
+// of every library call (the caller may have changed e in between).
+static void enqueue_reduced_split(const LLGPlan* pl, const double* e, cudaStream_t st) {
+  if (pl->precision == MGX_PRECISION_DF32_GATHER) enqueue_df_split(pl, e, st);
+  if (pl->precision == MGX_PRECISION_INT48_GATHER) enqueue_fx_split(pl, e, st);
+}
+
 mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t step, void* stream) {
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl || !e) return set_error(MGX_ERR_INVALID, "mgx_llg_step: null argument");
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step: host-noise plan needs a noise buffer");
-  if (pl->precision == MGX_PRECISION_DF32_GATHER) enqueue_df_split(pl, e, (cudaStream_t)stream);
+  enqueue_reduced_split(pl, e, (cudaStream_t)stream);
   enqueue_llg_step(pl, e, noise, step, (cudaStream_t)stream, 3);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
@@ -224,7 +240,7 @@ mgx_status mgx_llg_stage(mgx_llg* pp, int32_t stage, double* e, const double* no
   if (stage != 0 && stage != 1) return set_error(MGX_ERR_INVALID, "stage %d is not 0 (predictor) or 1 (corrector)", stage);
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
     return set_error(MGX_ERR_INVALID, "mgx_llg_stage: host-noise plan needs a noise buffer");
-  if (stage == 0 && pl->precision == MGX_PRECISION_DF32_GATHER) enqueue_df_split(pl, e, (cudaStream_t)stream);
+  if (stage == 0) enqueue_reduced_split(pl, e, (cudaStream_t)stream);
   enqueue_llg_step(pl, e, noise, step, (cudaStream_t)stream, stage == 0 ? 1 : 2);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
@@ -236,7 +252,7 @@ mgx_status mgx_llg_run(mgx_llg* pp, double* e, int64_t nsteps, uint64_t step0, v
   if (nsteps < 0) return set_error(MGX_ERR_INVALID, "nsteps must be >= 0");
   if (pl->p.noise == MGX_NOISE_HOST)
     return set_error(MGX_ERR_INVALID, "mgx_llg_run: host-noise plans step one at a time (mgx_llg_step)");
-  if (pl->precision == MGX_PRECISION_DF32_GATHER && nsteps > 0) enqueue_df_split(pl, e, (cudaStream_t)stream);
+  if (nsteps > 0) enqueue_reduced_split(pl, e, (cudaStream_t)stream);
   for (int64_t n = 0; n < nsteps; ++n) enqueue_llg_step(pl, e, nullptr, step0 + (uint64_t)n, (cudaStream_t)stream, 3);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;

@@ -1,0 +1,394 @@
+// Heun / Depondt step with the exchange gather as exact integer arithmetic (MGX_PRECISION_INT48_GATHER).
+//
+// On GB300 the INT32 multiply-add pipe runs 64 operations per clock per SM and the FP64 pipe 2, so
+// h = sum_j J_ij e_j (9 z multiply-adds per site and stage) is evaluated in fixed point:
+//   * every spin component is held as v = round(e 2^48) (|v| <= 2^48) in two int32 halves,
+//     v = hi 2^24 + lo with lo in [-2^23, 2^23), written by the stage that produces the spins;
+//   * every coupling entry (pre-scaled by 2 / (mu mu_B) of the receiving sublattice) and the on-site
+//     tensor -2 A / (mu mu_B) likewise, at a power-of-two scale 2^sigma_s >= their largest magnitude;
+//   * J e = [J_hi e_hi 2^48 + (J_hi e_lo + J_lo e_hi) 2^24 + J_lo e_lo] 2^(sigma - 96): the first
+//     two terms are accumulated exactly with 32x32->64-bit multiply-adds (mad.wide.s32) in two int64
+//     accumulators (at most 2^55 and 2^56 for 26 neighbours); the last (|J_lo e_lo| <= 2^46, zero
+//     mean with balanced halves) is dropped.
+// The sum is exact; the only errors are the 2^-49 roundings of the spins and couplings to fixed point,
+// about 1e-11 T in the field of the 26-neighbour bcc workload (FP64's own rounding of the gather is
+// of the same order).  The accumulators are turned into (hi, lo) float pairs, the Zeeman and thermal
+// fields and the right-hand side are evaluated on pairs (mgx_dfp.cuh) and the integration,
+// renormalisation and fixed-point split of the new spins are FP64.  The Depondt form keeps an FP64
+// tail after the integer gather.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <vector>
+
+#include "mgx_dfp.cuh"
+#include "mgx_step.cuh"
+
+namespace mgx {
+
+constexpr double kTwo48 = 281474976710656.0;     // 2^48
+
+// v = hi 2^24 + lo with hi = round(v / 2^24) and lo in [-2^23, 2^23): balanced halves, so that the
+// dropped lo x lo products have zero mean
+__device__ __forceinline__ int2 fx_halves(long long v) {
+  const long long hi = (v + (1LL << 23)) >> 24;
+  return make_int2((int)hi, (int)(v - (hi << 24)));
+}
+
+__device__ __forceinline__ int2 fx_split(double x) { return fx_halves(__double2ll_rn(x * kTwo48)); }
+
+__device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
+  long long d;
+  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  return d;
+}
+
+struct FxAcc {
+  long long hh[3] = {0, 0, 0};   // sum J_hi e_hi        (units 2^(sigma - 48))
+  long long x[3] = {0, 0, 0};    // sum J_hi e_lo + J_lo e_hi (units 2^(sigma - 72))
+};
+
+// acc += M x for a 3x3 fixed-point tensor M (10 (hi, lo) int pairs, 80 B) and a fixed-point spin x
+__device__ __forceinline__ void fx_mat(const int4* __restrict__ T, int2 x0, int2 x1, int2 x2, FxAcc& a) {
+  const int4 t01 = __ldg(T), t23 = __ldg(T + 1), t45 = __ldg(T + 2), t67 = __ldg(T + 3), t89 = __ldg(T + 4);
+  const int2 m[9] = {make_int2(t01.x, t01.y), make_int2(t01.z, t01.w), make_int2(t23.x, t23.y),
+                     make_int2(t23.z, t23.w), make_int2(t45.x, t45.y), make_int2(t45.z, t45.w),
+                     make_int2(t67.x, t67.y), make_int2(t67.z, t67.w), make_int2(t89.x, t89.y)};
+  const int2 xv[3] = {x0, x1, x2};
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int2 j = m[3 * c + d];
+      a.hh[c] = mad_wide(j.x, xv[d].x, a.hh[c]);
+      a.x[c] = mad_wide(j.x, xv[d].y, mad_wide(j.y, xv[d].x, a.x[c]));
+    }
+}
+
+// Exchange (+ on-site) field of lattice index q = (s, c0, c1, c2) from the fixed-point field xs, as
+// (hi, lo) float pairs in tesla.  Interior cells (whole stencil inside the supercell along axes 0
+// and 1) index neighbours as q + a per-coupling constant, corrected for the periodic seam of axis 2.
+__device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
+                                          long long q, int s, int c0, int c1, int c2, dfp h[3]) {
+  FxAcc a;
+  const long long N = L.N;
+  const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
+  const int4 r = F.reach[s];
+  const bool inner01 = c0 >= r.x && c0 < L.L0 - r.x && c1 >= r.y && c1 < L.L1 - r.y;
+  const bool inner2 = L.pbc2 ? r.z < L.L2 : (c2 >= r.z && c2 < L.L2 - r.z);
+  if (inner01 && inner2) {
+    // 32-bit index arithmetic (N < 2^31 for every lattice this path accepts)
+    const int2* __restrict__ x0 = xs;
+    const int2* __restrict__ x1 = xs + N;
+    const int2* __restrict__ x2 = xs + 2 * N;
+    const int qi = (int)q, L2 = L.L2;
+    for (int b = b0; b < b1; ++b) {
+      const int2 li = __ldg(F.lin + b);
+      const int n2 = c2 + li.y;
+      const int j = qi + li.x + (n2 < 0 ? L2 : 0) - (n2 >= L2 ? L2 : 0);
+      fx_mat(F.J + 5 * b, __ldg(x0 + j), __ldg(x1 + j), __ldg(x2 + j), a);
+    }
+  } else {
+    for (int b = b0; b < b1; ++b) {
+      const int4 g = __ldg(L.bond_geo + b);
+      int n0 = c0 + g.y, n1 = c1 + g.z, n2 = c2 + g.w;
+      bool ok = true;
+      if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
+      if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
+      if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
+      if (!ok) continue;
+      const long long j = (long long)g.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
+      fx_mat(F.J + (long long)b * 5, __ldg(xs + j), __ldg(xs + N + j), __ldg(xs + 2 * N + j), a);
+    }
+  }
+  if (F.A) fx_mat(F.A + 5 * s, __ldg(xs + q), __ldg(xs + N + q), __ldg(xs + 2 * N + q), a);
+  const float sc = F.scale[s];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    // value = (hh + x 2^-24) 2^(sigma - 48); fold x in with rounding, then split into two floats
+    const long long v = a.hh[c] + ((a.x[c] + (1LL << 23)) >> 24);
+    const float hi = __ll2float_rn(v);
+    const float lo = __ll2float_rn(v - __float2ll_rn(hi));
+    h[c] = {__fmul_rn(hi, sc), __fmul_rn(lo, sc)};
+  }
+}
+
+// spin of the site as a (hi, lo) float pair from its fixed-point halves (exact)
+__device__ __forceinline__ dfp fx_spin(int2 v) {
+  return {__fmul_rn((float)v.x, 5.9604644775390625e-8f), __fmul_rn((float)v.y, 3.552713678800501e-15f)};
+}
+
+template <int NOISE>
+__device__ __forceinline__ void fx_thermal(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                           const double* __restrict__ noise, long long q, int s, uint64_t step,
+                                           dfp B[3]) {
+  if (NOISE == MGX_NOISE_NONE) return;
+  double g[3];
+  if (NOISE == MGX_NOISE_HOST) {
+    g[0] = __ldg(noise + q);
+    g[1] = __ldg(noise + L.N + q);
+    g[2] = __ldg(noise + 2 * L.N + q);
+  } else {
+    philox_normal3(P.seed, magex_site(L, q, s), step, g[0], g[1], g[2]);   // FP32 draws: exact as floats
+  }
+  if (NOISE == MGX_NOISE_PHILOX && !P.sigma_site) {
+    const dfp sg = dfp_of(F.sig[s]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) B[c] = dfp_add(B[c], dfp_mul(sg, {(float)g[c], 0.f}));
+  } else {
+    const double sig = P.sigma_site ? __ldg(P.sigma_site + q) : __ldg(P.sigma_sub + s);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 b = split_double(sig * g[c]);
+      B[c] = dfp_add(B[c], {b.x, b.y});
+    }
+  }
+}
+
+template <int NOISE>
+__device__ __forceinline__ void fx_rhs(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                       const int2* __restrict__ xs, const double* __restrict__ noise, long long q,
+                                       int s, int c0, int c1, int c2, uint64_t step, double f[3]) {
+  dfp B[3], e[3], fd[3];
+  fx_gather(L, F, xs, q, s, c0, c1, c2, B);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) B[c] = dfp_add(B[c], dfp_of(F.B[c]));
+  fx_thermal<NOISE>(L, P, F, noise, q, s, step, B);
+  const long long N = L.N;
+  e[0] = fx_spin(xs[q]);
+  e[1] = fx_spin(xs[N + q]);
+  e[2] = fx_spin(xs[2 * N + q]);
+  dfp_rhs(e, B, dfp_of(F.alpha[s]), dfp_of(F.pre[s]), P.precession != 0, fd);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) f[c] = dfp_double(fd[c]);
+}
+
+// Depondt tail: FP64 field from the integer gather, as the FP64 kernels
+template <int NOISE>
+__device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                           const int2* __restrict__ xs, const double* __restrict__ noise,
+                                           long long q, int s, int c0, int c1, int c2, uint64_t step, double& bx,
+                                           double& by, double& bz) {
+  dfp h[3];
+  fx_gather(L, F, xs, q, s, c0, c1, c2, h);
+  bx = dfp_double(h[0]) + L.B0;
+  by = dfp_double(h[1]) + L.B1;
+  bz = dfp_double(h[2]) + L.B2;
+  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
+}
+
+__global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, int2* __restrict__ xs, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) xs[i] = fx_split(x[i]);
+}
+
+template <int NOISE, int INTEG>
+__global__ void __launch_bounds__(256) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
+                                                    const double* __restrict__ e, const double* __restrict__ noise,
+                                                    uint64_t step) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= L.N) return;
+  const long long N = L.N;
+  const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
+  if (L.pinned && L.pinned[q]) {
+    P.ep[q] = ex; P.ep[N + q] = ey; P.ep[2 * N + q] = ez;
+    P.k1[q] = 0.0; P.k1[N + q] = 0.0; P.k1[2 * N + q] = 0.0;
+    F.eps[q] = F.es[q]; F.eps[N + q] = F.es[N + q]; F.eps[2 * N + q] = F.es[2 * N + q];
+    return;
+  }
+  int s, c0, c1, c2;
+  site_coords(L, q, s, c0, c1, c2);
+  double f[3], x, y, z;
+  if (INTEG == MGX_INTEGRATOR_HEUN) {
+    fx_rhs<NOISE>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, f);
+    x = fma(P.dt, f[0], ex);
+    y = fma(P.dt, f[1], ey);
+    z = fma(P.dt, f[2], ez);
+    const double r = rsqrt(x * x + y * y + z * z);
+    x *= r; y *= r; z *= r;
+  } else {
+    double bx, by, bz;
+    fx_field64<NOISE>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    double fx, fy, fz;
+    llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
+    f[0] = ey * fz - ez * fy; f[1] = ez * fx - ex * fz; f[2] = ex * fy - ey * fx;
+    x = ex; y = ey; z = ez;
+    rotate(x, y, z, P.dt * f[0], P.dt * f[1], P.dt * f[2]);
+  }
+  P.ep[q] = x; P.ep[N + q] = y; P.ep[2 * N + q] = z;
+  P.k1[q] = f[0]; P.k1[N + q] = f[1]; P.k1[2 * N + q] = f[2];
+  F.eps[q] = fx_split(x); F.eps[N + q] = fx_split(y); F.eps[2 * N + q] = fx_split(z);
+}
+
+template <int NOISE, int INTEG>
+__global__ void __launch_bounds__(256) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
+                                                    double* __restrict__ e, const double* __restrict__ noise,
+                                                    uint64_t step) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= L.N) return;
+  if (L.pinned && L.pinned[q]) return;                 // e and its split stay as they are
+  const long long N = L.N;
+  int s, c0, c1, c2;
+  site_coords(L, q, s, c0, c1, c2);
+  const double k1x = P.k1[q], k1y = P.k1[N + q], k1z = P.k1[2 * N + q];
+  double x = e[q], y = e[N + q], z = e[2 * N + q];
+  if (INTEG == MGX_INTEGRATOR_HEUN) {
+    double f[3];
+    fx_rhs<NOISE>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, f);
+    x = fma(P.half_dt, k1x + f[0], x);
+    y = fma(P.half_dt, k1y + f[1], y);
+    z = fma(P.half_dt, k1z + f[2], z);
+  } else {
+    const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
+    double bx, by, bz;
+    fx_field64<NOISE>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    double fx, fy, fz;
+    llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
+    const double wx = py * fz - pz * fy, wy = pz * fx - px * fz, wz = px * fy - py * fx;
+    rotate(x, y, z, P.half_dt * (k1x + wx), P.half_dt * (k1y + wy), P.half_dt * (k1z + wz));
+  }
+  const double r = rsqrt(x * x + y * y + z * z);
+  x *= r; y *= r; z *= r;
+  e[q] = x; e[N + q] = y; e[2 * N + q] = z;
+  F.es[q] = fx_split(x); F.es[N + q] = fx_split(y); F.es[2 * N + q] = fx_split(z);
+}
+
+template <int NOISE, int INTEG>
+static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
+  const DevLattice& L = pl->model->d;
+  DevFX F = pl->fx;
+  F.B[0] = split_host(L.B0);
+  F.B[1] = split_host(L.B1);
+  F.B[2] = split_host(L.B2);
+  const int tpb = site_block_size(L.N);
+  const unsigned grid = (unsigned)((L.N + tpb - 1) / tpb);
+  if (stages & 1) k_predict_fx<NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
+  if (stages & 2) k_correct_fx<NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
+}
+
+template <int NOISE>
+static void fx_integ(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
+  if (pl->p.integrator == MGX_INTEGRATOR_DEPONDT) launch_fx<NOISE, MGX_INTEGRATOR_DEPONDT>(pl, e, noise, step, stages, st);
+  else launch_fx<NOISE, MGX_INTEGRATOR_HEUN>(pl, e, noise, step, stages, st);
+}
+
+void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages) {
+  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
+  switch (mode) {
+    case MGX_NOISE_HOST: fx_integ<MGX_NOISE_HOST>(pl, e, noise, step, stages, st); break;
+    case MGX_NOISE_PHILOX: fx_integ<MGX_NOISE_PHILOX>(pl, e, noise, step, stages, st); break;
+    default: fx_integ<MGX_NOISE_NONE>(pl, e, noise, step, stages, st); break;
+  }
+}
+
+void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st) {
+  const long long n = 3 * pl->model->d.N;
+  k_fx_split<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(e, pl->fx.es, n);
+}
+
+// balanced (hi, lo) int32 halves of round(v 2^(48 - sigma)), |v| <= 2^sigma
+static int2 fx_host(double v, int sigma) {
+  const long long w = std::llround(std::ldexp(v, 48 - sigma));
+  const long long hi = (w + (1LL << 23)) >> 24;
+  return make_int2((int)hi, (int)(w - (hi << 24)));
+}
+
+mgx_status build_fx_tables(LLGPlan* pl) {
+  const Model* m = pl->model;
+  const DevLattice& d = m->d;
+  if (d.layout != 0) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather needs a lattice stencil model");
+  if (d.N >= (1LL << 31)) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather indexes at most 2^31 - 1 sites");
+  if (d.A_site || d.mu_site) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather needs per-sublattice A and mu");
+  if (pl->p.alpha_site || pl->p.sigma_site) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather needs uniform damping");
+  const int ns = d.ns, nb = m->nbond, W = d.width;
+  const long long N = d.N;
+  std::vector<int> off(ns + 1);
+  std::vector<double> J((size_t)std::max(nb, 1) * W), A(9 * ns), inv(ns);
+  std::vector<int4> geo((size_t)std::max(nb, 1));
+  MGX_CUDA_TRY(cudaMemcpy(off.data(), d.bond_off, sizeof(int) * (ns + 1), cudaMemcpyDeviceToHost));
+  if (nb > 0) {
+    MGX_CUDA_TRY(cudaMemcpy(J.data(), d.bond_J, sizeof(double) * nb * W, cudaMemcpyDeviceToHost));
+    MGX_CUDA_TRY(cudaMemcpy(geo.data(), d.bond_geo, sizeof(int4) * nb, cudaMemcpyDeviceToHost));
+  }
+  MGX_CUDA_TRY(cudaMemcpy(A.data(), d.A_sub, sizeof(double) * 9 * ns, cudaMemcpyDeviceToHost));
+  MGX_CUDA_TRY(cudaMemcpy(inv.data(), d.inv_mu_sub, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+  // scaled 3x3 tensors: couplings 2 J / (mu mu_B), on-site -2 A / (mu mu_B) of the receiving sublattice
+  std::vector<double> M((size_t)std::max(nb, 1) * 9, 0.0), nA(9 * ns);
+  for (int s = 0; s < ns; ++s)
+    for (int b = off[s]; b < off[s + 1]; ++b) {
+      const double* t = J.data() + (size_t)b * W;
+      double T[9];
+      if (W == 1) {
+        for (int k = 0; k < 9; ++k) T[k] = (k % 4 == 0) ? t[0] : 0.0;
+      } else if (W == 4) {   // J I + antisymmetric part with (J^A e) = e x D
+        T[0] = t[0]; T[1] = t[3]; T[2] = -t[2];
+        T[3] = -t[3]; T[4] = t[0]; T[5] = t[1];
+        T[6] = t[2]; T[7] = -t[1]; T[8] = t[0];
+      } else {
+        for (int k = 0; k < 9; ++k) T[k] = t[k];
+      }
+      for (int k = 0; k < 9; ++k) M[(size_t)b * 9 + k] = 2.0 * inv[s] * T[k];
+    }
+  bool hasA = false;
+  for (int s = 0; s < ns; ++s)
+    for (int k = 0; k < 9; ++k) {
+      nA[9 * s + k] = -2.0 * inv[s] * A[9 * s + k];
+      hasA |= A[9 * s + k] != 0.0;
+    }
+  // per-sublattice scale 2^sigma >= every magnitude it multiplies (so every half fits 25 bits)
+  std::vector<int> sigma(ns, 0);
+  for (int s = 0; s < ns; ++s) {
+    double mx = 0.0;
+    for (int b = off[s]; b < off[s + 1]; ++b)
+      for (int k = 0; k < 9; ++k) mx = std::max(mx, std::fabs(M[(size_t)b * 9 + k]));
+    for (int k = 0; k < 9; ++k) mx = std::max(mx, std::fabs(nA[9 * s + k]));
+    int e = 0;
+    if (mx > 0.0) std::frexp(mx, &e);            // mx < 2^e
+    sigma[s] = e;
+    pl->fx.scale[s] = std::ldexp(1.0f, e - 48);
+  }
+  std::vector<int2> Jq((size_t)std::max(nb, 1) * 10, make_int2(0, 0)), Aq((size_t)ns * 10, make_int2(0, 0));
+  for (int s = 0; s < ns; ++s) {
+    for (int b = off[s]; b < off[s + 1]; ++b)
+      for (int k = 0; k < 9; ++k) Jq[(size_t)b * 10 + k] = fx_host(M[(size_t)b * 9 + k], sigma[s]);
+    for (int k = 0; k < 9; ++k) Aq[(size_t)s * 10 + k] = fx_host(nA[9 * s + k], sigma[s]);
+  }
+  // interior fast path: signed offsets, linear neighbour offset and reach per receiving sublattice
+  std::vector<int2> lin((size_t)std::max(nb, 1), make_int2(0, 0));
+  const int Ls[3] = {d.L0, d.L1, d.L2}, pbc[3] = {d.pbc0, d.pbc1, d.pbc2};
+  for (int s = 0; s < MGX_MAX_SUBLATTICES; ++s) pl->fx.reach[s] = make_int4(0, 0, 0, 0);
+  for (int s = 0; s < ns; ++s)
+    for (int b = off[s]; b < off[s + 1]; ++b) {
+      int R[3] = {geo[b].y, geo[b].z, geo[b].w};
+      for (int a = 0; a < 3; ++a)
+        if (pbc[a] && R[a] > Ls[a] / 2) R[a] -= Ls[a];
+      lin[b] = make_int2((geo[b].x - s) * d.ncell + (R[0] * d.L1 + R[1]) * d.L2 + R[2], R[2]);
+      int4& r = pl->fx.reach[s];
+      r.x = std::max(r.x, std::abs(R[0]));
+      r.y = std::max(r.y, std::abs(R[1]));
+      r.z = std::max(r.z, std::abs(R[2]));
+    }
+  std::vector<double> ap(2 * ns);
+  MGX_CUDA_TRY(cudaMemcpy(ap.data(), pl->p.alpha_sub, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+  MGX_CUDA_TRY(cudaMemcpy(ap.data() + ns, pl->p.pre_sub, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+  for (int s = 0; s < ns; ++s) {
+    pl->fx.alpha[s] = split_host(ap[s]);
+    pl->fx.pre[s] = split_host(ap[ns + s]);
+  }
+  const size_t nJ = sizeof(int2) * Jq.size(), nA2 = sizeof(int2) * Aq.size(), nL = sizeof(int2) * lin.size();
+  const size_t o_A = (nJ + 15) / 16 * 16, o_L = (o_A + nA2 + 15) / 16 * 16, o_es = (o_L + nL + 15) / 16 * 16;
+  const size_t n_split = sizeof(int2) * 3 * (size_t)N;
+  MGX_CUDA_TRY(cudaMalloc(&pl->fx_block, o_es + 2 * n_split));
+  char* base = (char*)pl->fx_block;
+  MGX_CUDA_TRY(cudaMemcpy(base, Jq.data(), nJ, cudaMemcpyHostToDevice));
+  MGX_CUDA_TRY(cudaMemcpy(base + o_A, Aq.data(), nA2, cudaMemcpyHostToDevice));
+  MGX_CUDA_TRY(cudaMemcpy(base + o_L, lin.data(), nL, cudaMemcpyHostToDevice));
+  pl->fx.J = (const int4*)base;
+  pl->fx.A = hasA ? (const int4*)(base + o_A) : nullptr;
+  pl->fx.lin = (const int2*)(base + o_L);
+  pl->fx.es = (int2*)(base + o_es);
+  pl->fx.eps = (int2*)(base + o_es + n_split);
+  return MGX_OK;
+}
+
+}  // namespace mgx

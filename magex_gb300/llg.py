@@ -9,10 +9,12 @@ columns as magex ``magex/llg.py:48-283``.  The spins stay on the GPU for the who
 Heun step is two fused sm_103a kernels (libmgx: ``mgx_llg_step`` / ``mgx_llg_run``); observables
 rows are computed on the device by ``mgx_observables``.
 
-Arithmetic (``precision=``): "fp64" (default) runs everything in FP64; "df32" keeps the spins, the
-on-site and Zeeman terms, the right-hand side and the integration in FP64 and evaluates the exchange
-sum in compensated FP32 pairs (~44 significant bits), about 4x faster on GB300, whose FP64 units run
-at 1/61 of the FP32 rate.
+Arithmetic (``precision=``): "fp64" (default) runs everything in FP64.  GB300's FP64 units run at
+1/61 of its FP32 rate, so two reduced forms keep the spins, the integration and the renormalisation
+in FP64 and move the rest off the FP64 pipe (Heun: field and right-hand side on compensated FP32
+pairs): "df32" evaluates the exchange sum on compensated FP32 pairs (~44 significant bits), "int48"
+as exact integer products and sums of 48-bit fixed-point couplings and spins on the INT32 pipe.
+Both stay within the per-step parity tolerance against magex (tests/test_gpu_df.py).
 
 Thermal noise (``noise=``):
   "philox"  counter-based Philox4x32-10 keyed by (seed, site, step), generated inside the kernels
@@ -62,8 +64,9 @@ class GB300LLG:
             raise ValueError("backend must be 'gb300'")
         if noise not in ("philox", "host"):
             raise ValueError("noise must be 'philox' or 'host'")
-        if precision not in ("fp64", "df32"):
-            raise ValueError("precision must be 'fp64' or 'df32' (exchange gather in compensated FP32 pairs)")
+        if precision not in ("fp64", "df32", "int48"):
+            raise ValueError("precision must be 'fp64', 'df32' (exchange gather in compensated FP32 pairs) or "
+                             "'int48' (exchange gather in exact 48-bit fixed-point integer arithmetic)")
         self.precision = precision
         self.sys = system
         self.sc = supercell_from_system(system)
@@ -102,7 +105,8 @@ class GB300LLG:
         p.integrator = _SUPPORTED[integrator]
         p.noise = _lib.NOISE_HOST if noise == "host" else _lib.NOISE_PHILOX
         p.seed = _philox_key(seed)
-        p.precision = _lib.PRECISION_DF32_GATHER if precision == "df32" else _lib.PRECISION_FP64
+        p.precision = {"fp64": _lib.PRECISION_FP64, "df32": _lib.PRECISION_DF32_GATHER,
+                       "int48": _lib.PRECISION_INT48_GATHER}[precision]
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.model.lib.mgx_llg_create(self.model.handle, C.byref(p), C.byref(h)), "mgx_llg_create")

@@ -1,8 +1,10 @@
-"""Compensated-FP32 exchange gather (precision="df32"): same parity tolerances as the FP64 kernels.
+"""Reduced-FP64 step forms: same parity tolerances as the FP64 kernels.
 
-The spins, on-site and Zeeman terms, right-hand side and integration stay FP64; only the exchange sum
-is evaluated in FP32 (hi, lo) pairs with error-free TwoProduct / TwoSum steps.  The tests hold it to
-the FP64 kernels' bars against the reference's trajectories: 1e-12 per step, 1e-9 after 1000 steps.
+precision="df32": the exchange sum on FP32 (hi, lo) pairs with error-free TwoProduct / TwoSum steps;
+precision="int48": the exchange (and on-site) sum as exact integer arithmetic on 48-bit fixed-point
+couplings and spins.  Both keep the spins, the integration and the renormalisation in FP64 and (Heun)
+evaluate the rest of the field and the right-hand side on FP32 pairs.  The tests hold them to the FP64
+kernels' bars against the reference's trajectories: 1e-12 per step, 1e-9 after 1000 steps.
 """
 import numpy as np
 import pytest
@@ -16,12 +18,16 @@ STENCIL_TRAJ = ["sc16", "sc6_thermal", "bcc2_thermal", "bcc2_T0", "bcc2_shell4",
                 "tri_depondt_thermal", "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb"]
 
 
+PRECISIONS = ["df32", "int48"]
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
 @pytest.mark.parametrize("tag", STENCIL_TRAJ)
-def test_df32_trajectory_matches_reference(cuda, golden, golden_models, tag):
+def test_reduced_trajectory_matches_reference(cuda, golden, golden_models, tag, precision):
     from magex_gb300.llg import GB300LLG
     sc, meta = golden_supercell(golden_models, tag)
     sol = GB300LLG(sc, meta["alpha"], meta["dt"], meta["T"], meta["seed"], integrator=meta["integrator"],
-                   noise="host", precision="df32")
+                   noise="host", precision=precision)
     e = golden[f"{tag}/e0"].copy()
     for n in range(1, meta["steps"] + 1):
         e = sol.step(e)
@@ -30,26 +36,28 @@ def test_df32_trajectory_matches_reference(cuda, golden, golden_models, tag):
             assert err <= min(1e-9, 1e-12 * n + 1e-13), (tag, n, err)
 
 
-def test_df32_sc16_1000_steps(cuda, golden, golden_models):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_reduced_sc16_1000_steps(cuda, golden, golden_models, precision):
     from magex_gb300.llg import GB300LLG
     sc, meta = golden_supercell(golden_models, "sc16")
-    sol = GB300LLG(sc, meta["alpha"], meta["dt"], 0.0, meta["seed"], precision="df32")
+    sol = GB300LLG(sc, meta["alpha"], meta["dt"], 0.0, meta["seed"], precision=precision)
     lat = sol.model.to_lattice(golden["sc16/e0"])
     sol.run_lattice(lat, 1000)
     e = sol.model.from_lattice(lat).cpu().numpy()
     assert np.abs(e - golden["sc16/e1000"]).max() <= 1e-9
 
 
-def test_df32_full_size_bcc_against_fp64(cuda):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_reduced_full_size_bcc_against_fp64(cuda, precision):
     """Config-2 lattice (4,194,304 spins, 26 neighbours, full tensors), T = 300 K, same Philox stream:
-    20 steps of the df32 plan stay within 1e-12 per step of the FP64 plan."""
+    20 steps of the reduced plan stay within 1e-12 per step of the FP64 plan."""
     from magex_gb300.llg import GB300LLG
     from magex_gb300.workloads import bcc_two_site
     sc = bcc_two_site(L=128)
     e0 = sc.init_spins("random", seed=5)
     out = []
-    for precision in ("fp64", "df32"):
-        sol = GB300LLG(sc, 0.05, 1e-4, 300.0, 77, precision=precision)
+    for prec in ("fp64", precision):
+        sol = GB300LLG(sc, 0.05, 1e-4, 300.0, 77, precision=prec)
         lat = sol.model.to_lattice(e0)
         sol.run_lattice(lat, 20)
         out.append(lat)
@@ -58,9 +66,28 @@ def test_df32_full_size_bcc_against_fp64(cuda):
     assert float((torch.linalg.vector_norm(out[1], dim=0) - 1).abs().max()) < 1e-14
 
 
-def test_df32_refuses_unsupported_layouts(cuda, golden, golden_models):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_reduced_refuses_unsupported_layouts(cuda, golden, golden_models, precision):
     from helpers import golden_irregular
     from magex_gb300.llg import GB300LLG
     nl, meta, _ = golden_irregular(golden, golden_models, "sc_sphere")
     with pytest.raises(NotImplementedError):
-        GB300LLG(nl, 0.1, 1e-3, precision="df32")
+        GB300LLG(nl, 0.1, 1e-3, precision=precision)
+
+
+def test_int48_field_is_closer_to_fp64_than_df32(cuda):
+    """bcc 32^3, random spins: the integer gather's effective field differs from FP64 by about the
+    2^-48 fixed-point rounding (absolute), the compensated-FP32 one by ~2^-44 relative."""
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=32)
+    e0 = sc.init_spins("random", seed=8)
+    out = {}
+    for prec in ("fp64", "df32", "int48"):
+        sol = GB300LLG(sc, 0.05, 1e-4, 0.0, 1, precision=prec)
+        lat = sol.model.to_lattice(e0)
+        sol.run_lattice(lat, 1)
+        out[prec] = lat
+    d_df = float((out["df32"] - out["fp64"]).abs().max())
+    d_fx = float((out["int48"] - out["fp64"]).abs().max())
+    assert d_fx <= 2e-15 and d_df <= 2e-14, (d_fx, d_df)
