@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, 
 }
 
 template <int NOISE, int INTEG>
-__global__ void __launch_bounds__(256) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
+__global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                     const double* __restrict__ e, const double* __restrict__ noise,
                                                     uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) k_predict_fx(const DevLattice L, const De
 }
 
 template <int NOISE, int INTEG>
-__global__ void __launch_bounds__(256) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
+__global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                     double* __restrict__ e, const double* __restrict__ noise,
                                                     uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
