@@ -140,6 +140,17 @@ int64_t mgx_model_nsites(const mgx_model* m);
  * parameters (magex rebuilds FastModel after editing couplings, magex/fast.py:631). */
 mgx_status mgx_model_set_couplings(mgx_model* m, const double* bond_table);
 mgx_status mgx_model_set_onsite(mgx_model* m, const double* A_sub);
+/* Slab decomposition of one supercell along axis 0 (the halo-exchange path of magex/mpi_spin.py:
+ * 150-180): this model is a slab of the whole lattice.  In-kernel Philox counters use local cell +
+ * cell_offset as the cell index of the whole lattice (so the noise equals the unsplit run's), and
+ * mgx_observables sums only cells with own_begin <= c0 < own_end (the halo layers are owned by the
+ * neighbouring slabs).  Lattice (stencil) models only. */
+mgx_status mgx_model_set_partition(mgx_model* m, int64_t cell_offset, int32_t own_begin, int32_t own_end);
+/* Copy the c0 layers [c0_begin, c0_end) of a (3, N) lattice-layout field x (device) into a packed buffer
+ * buf (3 * ns * (c0_end - c0_begin) * L1 * L2 doubles, component-major then sublattice; device or
+ * pinned host) when to_buffer != 0, or back from it into x: the halo messages of a slab decomposition. */
+mgx_status mgx_lattice_layers(const mgx_model* m, double* x, int32_t c0_begin, int32_t c0_end, double* buf,
+                              int32_t to_buffer, void* stream);
 
 /* (N,3) magex-order device array <-> lattice-layout device array (3*N doubles each). */
 mgx_status mgx_pack_spins(const mgx_model* m, const double* aos, double* lat, void* stream);
@@ -150,6 +161,9 @@ mgx_status mgx_unpack_spins(const mgx_model* m, const double* lat, double* aos, 
  * Allocates the predictor scratch (6*N doubles) on the current device. */
 mgx_status mgx_llg_create(const mgx_model* m, const mgx_llg_params* p, mgx_llg** out);
 mgx_status mgx_llg_destroy(mgx_llg* plan);
+/* Device pointer of the plan's predicted spins ep ((3, N) lattice layout), written by stage 0 and read
+ * by stage 1: a slab decomposition exchanges its halo layers between the two stages. */
+mgx_status mgx_llg_predicted(mgx_llg* plan, double** ep);
 /* Thermal-field amplitude sigma_i = sqrt(2 alpha_i k_B T_i / (gamma mu_i mu_B dt)) (magex/llg.py:111):
  * per sublattice (host [ns]) or per site (host [N] magex order, overrides).  Zero means no noise. */
 mgx_status mgx_llg_set_sigma(mgx_llg* plan, const double* sigma_sub, const double* sigma_site);

@@ -64,6 +64,10 @@ SIGNATURES = {
     "mgx_model_create_csr": (C.c_int32, [C.POINTER(CSRDesc), C.POINTER(C.c_void_p)]),
     "mgx_model_set_field": (C.c_int32, [C.c_void_p, _dp]),
     "mgx_model_nsites": (C.c_int64, [C.c_void_p]),
+    "mgx_model_set_partition": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int32, C.c_int32]),
+    "mgx_lattice_layers": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
+                                       C.c_void_p]),
+    "mgx_llg_predicted": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "mgx_pack_spins": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_unpack_spins": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_llg_create": (C.c_int32, [C.c_void_p, C.POINTER(LLGParams), C.POINTER(C.c_void_p)]),

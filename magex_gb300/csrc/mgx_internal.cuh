@@ -55,6 +55,10 @@ struct DevLattice {
   const int* csr_nbr;            // [nnz]
   const int* csr_typ;            // [nnz]
   const double* sign_site;       // [N] order-parameter signs, or nullptr
+  // slab of a larger supercell (mgx_model_set_partition): Philox counters use cell + cell_offset as
+  // the cell of the whole lattice; observables sum only cells with own0_begin <= c0 < own0_end
+  long long cell_offset;
+  int own0_begin, own0_end;
 };
 
 struct Model {

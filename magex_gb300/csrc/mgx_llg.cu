@@ -167,6 +167,13 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
   return MGX_OK;
 }
 
+mgx_status mgx_llg_predicted(mgx_llg* pp, double** ep) {
+  LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
+  if (!pl || !ep) return set_error(MGX_ERR_INVALID, "mgx_llg_predicted: null argument");
+  *ep = pl->p.ep;
+  return MGX_OK;
+}
+
 mgx_status mgx_llg_destroy(mgx_llg* pp) {
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl) return MGX_OK;

@@ -153,6 +153,9 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
   DevLattice& d = m->d;
   d.ns = ns;
   d.L0 = lat->L[0];
+  d.cell_offset = 0;
+  d.own0_begin = 0;
+  d.own0_end = lat->L[0];
   d.L1 = lat->L[1];
   d.L2 = lat->L[2];
   d.ncell = (int)ncell_ll;
@@ -265,6 +268,9 @@ mgx_status mgx_model_create_csr(const mgx_csr_desc* c, mgx_model** out) {
   DevLattice& d = m->d;
   d.ns = 1;
   d.L0 = 1;
+  d.cell_offset = 0;
+  d.own0_begin = 0;
+  d.own0_end = 1;
   d.L1 = 1;
   d.L2 = (int)N;
   d.ncell = (int)N;
@@ -405,6 +411,40 @@ mgx_status mgx_model_set_field(mgx_model* mm, const double B[3]) {
   m->d.B0 = B[0];
   m->d.B1 = B[1];
   m->d.B2 = B[2];
+  return MGX_OK;
+}
+
+mgx_status mgx_model_set_partition(mgx_model* mm, int64_t cell_offset, int32_t own_begin, int32_t own_end) {
+  Model* m = reinterpret_cast<Model*>(mm);
+  if (!m) return set_error(MGX_ERR_INVALID, "mgx_model_set_partition: null model");
+  if (m->d.layout != 0) return set_error(MGX_ERR_UNSUPPORTED, "mgx_model_set_partition: lattice (stencil) models only");
+  if (own_begin < 0 || own_end > m->d.L0 || own_begin > own_end)
+    return set_error(MGX_ERR_INVALID, "mgx_model_set_partition: owned range [%d, %d) outside [0, %d)", own_begin,
+                     own_end, m->d.L0);
+  m->d.cell_offset = cell_offset;
+  m->d.own0_begin = own_begin;
+  m->d.own0_end = own_end;
+  return MGX_OK;
+}
+
+mgx_status mgx_lattice_layers(const mgx_model* mm, double* x, int32_t c0_begin, int32_t c0_end, double* buf,
+                              int32_t to_buffer, void* stream) {
+  const Model* m = reinterpret_cast<const Model*>(mm);
+  if (!m || !x || !buf) return set_error(MGX_ERR_INVALID, "mgx_lattice_layers: null argument");
+  if (m->d.layout != 0) return set_error(MGX_ERR_UNSUPPORTED, "mgx_lattice_layers: lattice (stencil) models only");
+  if (c0_begin < 0 || c0_end > m->d.L0 || c0_begin > c0_end)
+    return set_error(MGX_ERR_INVALID, "mgx_lattice_layers: layers [%d, %d) outside [0, %d)", c0_begin, c0_end, m->d.L0);
+  if (c0_begin == c0_end) return MGX_OK;
+  // the layers of every (component, sublattice) block are one contiguous run: one strided 2D copy
+  const size_t layer = (size_t)m->d.L1 * m->d.L2;
+  const size_t width = sizeof(double) * layer * (size_t)(c0_end - c0_begin);
+  const size_t pitch = sizeof(double) * (size_t)m->d.ncell;
+  const size_t rows = 3 * (size_t)m->d.ns;
+  double* field = x + layer * (size_t)c0_begin;
+  if (to_buffer)
+    MGX_CUDA_TRY(cudaMemcpy2DAsync(buf, width, field, pitch, width, rows, cudaMemcpyDefault, (cudaStream_t)stream));
+  else
+    MGX_CUDA_TRY(cudaMemcpy2DAsync(field, pitch, buf, width, width, rows, cudaMemcpyDefault, (cudaStream_t)stream));
   return MGX_OK;
 }
 

@@ -34,9 +34,10 @@ template <int W>
 __device__ __forceinline__ void observe_site(const DevLattice& L, const double* __restrict__ e, long long q,
                                              double* v) {
   const long long N = L.N;
-  const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
   int s, c0, c1, c2;
   site_coords(L, q, s, c0, c1, c2);
+  if (c0 < L.own0_begin || c0 >= L.own0_end) return;      // halo layer of a slab: owned elsewhere
+  const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
   double hx, hy, hz;
   exchange_field<W>(L, e, s, c0, c1, c2, hx, hy, hz);
   double Ae[3] = {0.0, 0.0, 0.0};

@@ -11,7 +11,7 @@ namespace mgx {
 
 // magex site number of lattice index q (layout-independent Philox counter)
 __device__ __forceinline__ uint64_t magex_site(const DevLattice& L, long long q, int s) {
-  return (uint64_t)(q - (long long)s * L.ncell) * (uint64_t)L.ns + (uint64_t)s;
+  return (uint64_t)(q - (long long)s * L.ncell + L.cell_offset) * (uint64_t)L.ns + (uint64_t)s;
 }
 
 // Rodrigues rotation of (x,y,z) by the rotation vector w (angle |w|), magex/fast.py:271-282

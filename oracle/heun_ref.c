@@ -6,7 +6,7 @@
  *
  * What it restates (operation order of the reference's fused CPU kernels):
  *   oracle_step         magex/fast.py:336-390  (_fused1 predictor, _fused2 corrector; Heun and
- *                       Depondt), with the field of magex/fast.py:87-120,309-317 and the right-hand
+ *   oracle_stage        Depondt; oracle_stage runs one of the two), with the field of magex/fast.py:87-120,309-317 and the right-hand
  *                       side of magex/fast.py:225-236; the thermal field b is an input (already
  *                       scaled by sigma), as in magex's extras path magex/llg.py:200-208.
  *   oracle_observables  magex/spinmodel.py:475-484 (energy), :517-519 (order parameter),
@@ -142,12 +142,14 @@ int oracle_max_threads(void) {
 #endif
 }
 
-/* One Heun (depondt = 0) or Depondt (depondt = 1) step in place on e (N*3, magex order).
- * alpha: N damping values; b: N*3 thermal field (T) or NULL; ep, k1: N*3 scratch. */
-void oracle_step(const oracle_model* m, const double* alpha, double dt, int prec, int depondt, const double* b,
-                 double* e, double* ep, double* k1, int nthreads) {
+/* One stage of a Heun (depondt = 0) or Depondt (depondt = 1) step (magex order, N*3 arrays):
+ * stage 0 (predictor) reads e and writes ep and k1; stage 1 (corrector) reads ep and k1 and updates e
+ * in place.  alpha: N damping values; b: N*3 thermal field (T) or NULL. */
+void oracle_stage(const oracle_model* m, const double* alpha, double dt, int prec, int depondt, const double* b,
+                  double* e, double* ep, double* k1, int stage, int nthreads) {
   const int64_t N = m->N;
   set_threads(nthreads);
+  if (stage != 0) goto corrector;
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < N; ++i) {
     if (m->pinned && m->pinned[i]) {
@@ -187,6 +189,8 @@ void oracle_step(const oracle_model* m, const double* alpha, double dt, int prec
       ep[3 * i + 2] = z * q;
     }
   }
+  return;
+corrector:
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < N; ++i) {
     if (m->pinned && m->pinned[i]) continue;
@@ -216,6 +220,13 @@ void oracle_step(const oracle_model* m, const double* alpha, double dt, int prec
     e[3 * i + 1] = y * q;
     e[3 * i + 2] = z * q;
   }
+}
+
+/* One full step in place on e: both stages. */
+void oracle_step(const oracle_model* m, const double* alpha, double dt, int prec, int depondt, const double* b,
+                 double* e, double* ep, double* k1, int nthreads) {
+  oracle_stage(m, alpha, dt, prec, depondt, b, e, ep, k1, 0, nthreads);
+  oracle_stage(m, alpha, dt, prec, depondt, b, e, ep, k1, 1, nthreads);
 }
 
 /* out[8] = E, sum e (3), sum s e (3), max |e x B_eff| (pinned sites have zero field). */

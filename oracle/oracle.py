@@ -57,6 +57,9 @@ def load():
         lib = C.CDLL(LIB)
         lib.oracle_step.argtypes = [C.POINTER(_Model), _dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
         lib.oracle_step.restype = None
+        lib.oracle_stage.argtypes = [C.POINTER(_Model), _dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int,
+                                     C.c_int]
+        lib.oracle_stage.restype = None
         lib.oracle_observables.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, C.c_int]
         lib.oracle_observables.restype = None
         lib.oracle_gauss3.argtypes = [_dp, C.POINTER(C.c_uint64), C.c_int, _dp, C.POINTER(C.c_uint8), C.c_int64, C.c_int]
@@ -202,6 +205,18 @@ class OracleLLG:
                              _p(b), _p(e), _p(self._ep), _p(self._k1), self.threads)
         self.time += self.dt
         return e
+
+    def stage(self, e, b, stage):
+        """Predictor (stage 0: e -> self.ep, self.k1) or corrector (stage 1: e updated in place from
+        self.ep, self.k1) with the given thermal field b ((N, 3) or None)."""
+        self._m.B[:] = [float(x) for x in self.sc.B]
+        self.lib.oracle_stage(C.byref(self._m), _p(self._alpha_arr), self.dt, int(self.precession), int(self.depondt),
+                              _p(b), _p(e), _p(self._ep), _p(self._k1), int(stage), self.threads)
+        return e
+
+    @property
+    def ep(self):
+        return self._ep
 
     def observables(self, e):
         e = np.ascontiguousarray(e, np.float64)
