@@ -270,7 +270,8 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
     t_bwd = ev[2].elapsed_time(ev[3])
     return {"workload": f"triangular {L}x{L} film, J1=1 meV, D/J=0.3, K=0.05 meV, B_z=2 T, T=0, alpha 0.3, "
                         f"dt 0.1 fs, {nsteps} Heun steps, checkpoint every {seg}, loss sum|e(T)-target|^2, FP64",
-            "resident_segments": len(adj._segments(nsteps)) if cache_bytes else 0,
+            "cache_bytes": cache_bytes,
+            "resident_segments": min(len(adj._segments(nsteps)), adj._cache_budget() // (8 * adj.storage_doubles)),
             "forward_plain_ms": t_plain, "forward_checkpointed_ms": t_fwd, "backward_ms": t_bwd,
             "adjoint_over_forward": t_bwd / t_plain, "gradient_total_over_forward": (t_fwd + t_bwd) / t_plain,
             "grad_J1_D": [float(x) for x in g]}
@@ -602,8 +603,9 @@ def run_gb300(args):
         line["batched"] = bench_batched()
     if ws == 1 and not args.no_adjoint:
         line["adjoint"] = bench_adjoint()
-        # the same trajectory with every segment kept in HBM (2000 steps x 14 N doubles = 3.7 GB): no recompute
-        line["adjoint_resident"] = bench_adjoint(cache_bytes=8 << 30)
+        # the same trajectory with the default checkpoint policy: segments resident in up to half the
+        # free HBM (2000 steps x 14 N doubles = 3.7 GB here), so nothing is recomputed
+        line["adjoint_resident"] = bench_adjoint(cache_bytes="auto")
         line["adjoint_large"] = bench_adjoint(L=1024, nsteps=200, seg=50)
     if ws == 1 and not args.no_batched and not args.no_adjoint:
         line["large_batched_adjoint"] = bench_config5()

@@ -13,9 +13,10 @@ chain rule.  ``A`` holds the per-sublattice single-ion tensors and ``B`` the ext
 The forward pass runs the trajectory in segments of ``seg_steps`` steps and keeps the spins at
 segment starts (checkpoints).  The backward pass recomputes each segment from its checkpoint,
 storing per step e, ep, both total fields and the two normalisation factors, then runs the adjoint
-kernels (libmgx ``mgx_adjoint_*``) back through the segment.  With ``cache_bytes`` > 0 the last
-segments that fit keep their states from the forward pass and are not recomputed (checkpointing
-sized to the memory one grants it).  Thermal (Philox) noise is regenerated bit-identically
+kernels (libmgx ``mgx_adjoint_*``) back through the segment.  The last segments that fit in
+``cache_bytes`` keep their states from the forward pass and are not recomputed: checkpointing sized
+to the memory one grants it ("auto", the default: half of the free device memory; 0: recompute every
+segment).  Thermal (Philox) noise is regenerated bit-identically
 from (seed, site, step), so the gradient is the pathwise derivative of the same noisy trajectory.
 magex itself has no gradients; parity of this module is pinned against central finite differences
 and against torch autograd of a dense FP64 restatement (tests/test_gpu_adjoint.py).
@@ -130,7 +131,7 @@ class AdjointLLG:
     """Forward / adjoint engine of Heun trajectories on one supercell (uniform alpha per run)."""
 
     def __init__(self, sc, groups=None, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
-                 seg_steps=100, cache_bytes=0, device=None):
+                 seg_steps=100, cache_bytes="auto", device=None):
         if sc.alpha_site is not None or sc.site_T is not None or sc.A_site is not None:
             raise NotImplementedError("the adjoint supports uniform damping, temperature and per-sublattice A")
         if sc.terms or sc.has_higher:
@@ -165,7 +166,18 @@ class AdjointLLG:
         ns, G = sc.ns, self.groups.ngroups
         self._grads = torch.empty(9 * G + 9 * ns + 3, dtype=torch.float64, device=self.device)
         self.storage_doubles = int(self.lib.mgx_adjoint_storage_doubles(h))
-        self.cache_bytes = int(cache_bytes)
+        if cache_bytes != "auto" and int(cache_bytes) < 0:
+            raise ValueError("cache_bytes must be 'auto' or >= 0")
+        self.cache_bytes = cache_bytes if cache_bytes == "auto" else int(cache_bytes)
+
+    def _cache_budget(self):
+        """Bytes of resident segment states: the given cache_bytes, or with "auto" half of the device
+        memory free when the forward pass starts (GB300's HBM holds thousands of states of a 10^5-10^6
+        spin lattice, so most trajectories run without any recomputation)."""
+        if self.cache_bytes == "auto":
+            free, _ = torch.cuda.mem_get_info(self.device)
+            return int(0.5 * free)
+        return self.cache_bytes
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -209,7 +221,7 @@ class AdjointLLG:
         cache_bytes allows, the last segments also keep their full states (a resident segment costs
         mgx_adjoint_storage_doubles doubles), so the backward pass does not recompute them."""
         segs = self._segments(int(nsteps))
-        ncache = min(len(segs), self.cache_bytes // (8 * self.storage_doubles))
+        ncache = min(len(segs), self._cache_budget() // (8 * self.storage_doubles))
         cache = [torch.empty(self.storage_doubles, dtype=torch.float64, device=self.device) for _ in range(ncache)]
         first_cached = len(segs) - ncache
         ckpts = []
