@@ -477,12 +477,15 @@ def bench_reduced(L, K, warmup, precision):
     torch.cuda.synchronize()
     dev = float((lat["fp64"] - lat[precision]).abs().max())
     what = {"df32": "exchange gather on compensated FP32 pairs (~44 bits)",
-            "int48": "exchange gather as exact integer arithmetic on 48-bit fixed point (INT32 pipe)"}[precision]
+            "int48": "exchange gather as exact integer arithmetic on 48-bit fixed point (INT32 pipe)",
+            "fp64_fixed": "exchange and on-site sums exact on 56-bit fixed point (INT32 pipe); every "
+                          "floating-point operation FP64"}[precision]
     # algorithmic bytes per spin-step: predictor e, split in; ep, k1, split out; corrector split, k1, e in; e, split out
     split = 8
     nbytes = (24 + split + 24 + 24 + 3 * split) + (3 * split + 24 + 24 + 24 + 3 * split) - split
-    return {"precision": what + "; integration and renormalisation FP64, field remainder and right-hand side "
-                                "on FP32 pairs",
+    tail = ("" if precision == "fp64_fixed" else
+            "; integration and renormalisation FP64, field remainder and right-hand side on FP32 pairs")
+    return {"precision": what + tail,
             "value": sc.N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": K,
             "max_abs_deviation_from_fp64_plan": dev, "deviation_after_steps": warmup + K,
             "algorithmic_bytes_per_spin_step": nbytes,
@@ -599,6 +602,7 @@ def run_gb300(args):
     if ws == 1:
         line["df32_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "df32")
         line["int48_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "int48")
+        line["fp64_fixed_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "fp64_fixed")
     if ws == 1 and not args.no_batched:
         line["batched"] = bench_batched()
     if ws == 1 and not args.no_adjoint:
@@ -632,7 +636,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
-    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "config5", "mc", "sqw"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "fp64_fixed", "config5", "mc", "sqw"],
+                    default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
     ap.add_argument("--adjoint-L", type=int, default=128)
@@ -646,7 +651,7 @@ def main():
         build.build_library()
         if args.only == "adjoint":
             out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps or 2000)
-        elif args.only in ("df32", "int48"):
+        elif args.only in ("df32", "int48", "fp64_fixed"):
             out = bench_reduced(args.L, args.steps, args.warmup, args.only)
         elif args.only == "sqw":
             out = bench_sqw(L=args.L)

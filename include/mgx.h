@@ -49,11 +49,15 @@ enum {
 enum { MGX_INTEGRATOR_HEUN = 0, MGX_INTEGRATOR_DEPONDT = 1 };
 enum { MGX_NOISE_NONE = 0, MGX_NOISE_HOST = 1, MGX_NOISE_PHILOX = 2 };
 /* Arithmetic of the exchange gather: FP64 (default); compensated FP32 pairs (hi + lo, about 44
- * significant bits); or exact integer products and sums of 48-bit fixed-point couplings and spins on
- * the INT32 multiply-add pipe (64 per clock per SM against 2 FP64 FMAs).  The two reduced forms keep
- * the integration and renormalisation in FP64 and the rest of the field and the right-hand side on
- * FP32 pairs (Heun).  The GB300-native forms: FP64 runs at 1/61 of the FP32 rate on this part. */
-enum { MGX_PRECISION_FP64 = 0, MGX_PRECISION_DF32_GATHER = 1, MGX_PRECISION_INT48_GATHER = 2 };
+ * significant bits); or exact integer products and sums of fixed-point couplings and spins on the
+ * INT32 multiply-add pipe (wide multiply-adds at ~28 per clock per SM against 2 FP64 FMAs).  The
+ * 48-bit integer and the FP32-pair forms keep the integration and renormalisation in FP64 and the rest
+ * of the field and the right-hand side on FP32 pairs (Heun).  MGX_PRECISION_FP64_FIXED_GATHER keeps
+ * every floating-point operation FP64 and evaluates the exchange and on-site sums exactly on 56-bit
+ * fixed-point values: the inputs are quantised 2^-57 below their scale and the sum is rounded once,
+ * so its error stays below that of an FP64 FMA chain.  GB300 runs FP64 at 1/61 of its FP32 rate. */
+enum { MGX_PRECISION_FP64 = 0, MGX_PRECISION_DF32_GATHER = 1, MGX_PRECISION_INT48_GATHER = 2,
+       MGX_PRECISION_FP64_FIXED_GATHER = 3 };
 
 typedef struct mgx_model mgx_model;
 typedef struct mgx_llg mgx_llg;
@@ -98,7 +102,7 @@ typedef struct mgx_llg_params {
   int32_t integrator;        /* MGX_INTEGRATOR_HEUN or MGX_INTEGRATOR_DEPONDT */
   int32_t noise;             /* MGX_NOISE_NONE / _HOST (caller supplies N(0,1) draws) / _PHILOX */
   uint64_t seed;             /* Philox key (MGX_NOISE_PHILOX) */
-  int32_t precision;         /* MGX_PRECISION_FP64, _DF32_GATHER or _INT48_GATHER (the reduced forms:
+  int32_t precision;         /* MGX_PRECISION_FP64, _DF32_GATHER, _INT48_GATHER or _FP64_FIXED_GATHER (not FP64:
                               * stencil models with per-sublattice moments and single-ion tensors; the
                               * couplings are snapshotted when the plan is created) */
 } mgx_llg_params;

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(HERE, "libmgx.so")
 MGX_OK, MGX_ERR_INVALID, MGX_ERR_UNSUPPORTED, MGX_ERR_CUDA, MGX_ERR_NOMEM = 0, 1, 2, 3, 4
 HEUN, DEPONDT = 0, 1
 NOISE_NONE, NOISE_HOST, NOISE_PHILOX = 0, 1, 2
-PRECISION_FP64, PRECISION_DF32_GATHER, PRECISION_INT48_GATHER = 0, 1, 2
+PRECISION_FP64, PRECISION_DF32_GATHER, PRECISION_INT48_GATHER, PRECISION_FP64_FIXED_GATHER = 0, 1, 2, 3
 MAX_SUBLATTICES = 16
 MAX_BONDS = 256
 NOALLOC_MAX_SITES = 262144

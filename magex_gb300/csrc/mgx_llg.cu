@@ -60,7 +60,7 @@ static void dispatch_noise(const LLGPlan* pl, double* e, const double* noise, ui
 
 void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st,
                       int stages) {
-  if (pl->precision == MGX_PRECISION_INT48_GATHER) {
+  if (pl->precision == MGX_PRECISION_INT48_GATHER || pl->precision == MGX_PRECISION_FP64_FIXED_GATHER) {
     enqueue_fx_step(pl, e, noise, step, st, stages);
     return;
   }
@@ -102,10 +102,9 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
     return set_error(MGX_ERR_INVALID, "integrator %d is not heun (0) or depondt (1)", p->integrator);
   if (p->noise < MGX_NOISE_NONE || p->noise > MGX_NOISE_PHILOX)
     return set_error(MGX_ERR_INVALID, "noise mode %d is not none (0), host (1) or philox (2)", p->noise);
-  if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_DF32_GATHER &&
-      p->precision != MGX_PRECISION_INT48_GATHER)
-    return set_error(MGX_ERR_INVALID, "precision %d is not fp64 (0), df32-gather (1) or int48-gather (2)",
-                     p->precision);
+  if (p->precision < MGX_PRECISION_FP64 || p->precision > MGX_PRECISION_FP64_FIXED_GATHER)
+    return set_error(MGX_ERR_INVALID, "precision %d is not fp64 (0), df32-gather (1), int48-gather (2) or "
+                     "fp64-fixed-gather (3)", p->precision);
   const int ns = m->d.ns;
   const long long N = m->d.N;
   LLGPlan* pl = new LLGPlan();
@@ -227,7 +226,8 @@ mgx_status mgx_llg_set_sigma(mgx_llg* pp, const double* sigma_sub, const double*
 // of every library call (the caller may have changed e in between).
 static void enqueue_reduced_split(const LLGPlan* pl, const double* e, cudaStream_t st) {
   if (pl->precision == MGX_PRECISION_DF32_GATHER) enqueue_df_split(pl, e, st);
-  if (pl->precision == MGX_PRECISION_INT48_GATHER) enqueue_fx_split(pl, e, st);
+  if (pl->precision == MGX_PRECISION_INT48_GATHER || pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
+    enqueue_fx_split(pl, e, st);
 }
 
 mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t step, void* stream) {

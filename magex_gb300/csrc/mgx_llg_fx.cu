@@ -26,16 +26,20 @@
 
 namespace mgx {
 
-constexpr double kTwo48 = 281474976710656.0;     // 2^48
-
-// v = hi 2^24 + lo with hi = round(v / 2^24) and lo in [-2^23, 2^23): balanced halves, so that the
-// dropped lo x lo products have zero mean
+// Two fixed-point formats: LIMB = 24 (MGX_PRECISION_INT48_GATHER, 48-bit values, FP32-pair tail) and
+// LIMB = 28 (MGX_PRECISION_FP64_FIXED_GATHER, 56-bit values, FP64 tail).  A value is v = round(x 2^(2 LIMB))
+// held as v = hi 2^LIMB + lo with hi = round(v / 2^LIMB) and lo in [-2^(LIMB-1), 2^(LIMB-1)): balanced
+// halves, so that the dropped lo x lo products have zero mean.
+template <int LIMB>
 __device__ __forceinline__ int2 fx_halves(long long v) {
-  const long long hi = (v + (1LL << 23)) >> 24;
-  return make_int2((int)hi, (int)(v - (hi << 24)));
+  const long long hi = (v + (1LL << (LIMB - 1))) >> LIMB;
+  return make_int2((int)hi, (int)(v - (hi << LIMB)));
 }
 
-__device__ __forceinline__ int2 fx_split(double x) { return fx_halves(__double2ll_rn(x * kTwo48)); }
+template <int LIMB>
+__device__ __forceinline__ int2 fx_split(double x) {
+  return fx_halves<LIMB>(__double2ll_rn(x * (double)(1LL << (2 * LIMB))));
+}
 
 __device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
   long long d;
@@ -68,9 +72,8 @@ __device__ __forceinline__ void fx_mat(const int4* __restrict__ T, int2 x0, int2
 // Exchange (+ on-site) field of lattice index q = (s, c0, c1, c2) from the fixed-point field xs, as
 // (hi, lo) float pairs in tesla.  Interior cells (whole stencil inside the supercell along axes 0
 // and 1) index neighbours as q + a per-coupling constant, corrected for the periodic seam of axis 2.
-__device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
-                                          long long q, int s, int c0, int c1, int c2, dfp h[3]) {
-  FxAcc a;
+__device__ __forceinline__ void fx_accumulate(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
+                                              long long q, int s, int c0, int c1, int c2, FxAcc& a) {
   const long long N = L.N;
   const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
   const int4 r = F.reach[s];
@@ -102,6 +105,13 @@ __device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, c
     }
   }
   if (F.A) fx_mat(F.A + 5 * s, __ldg(xs + q), __ldg(xs + N + q), __ldg(xs + 2 * N + q), a);
+}
+
+// 48-bit form: field as (hi, lo) float pairs in tesla
+__device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
+                                          long long q, int s, int c0, int c1, int c2, dfp h[3]) {
+  FxAcc a;
+  fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
   const float sc = F.scale[s];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -111,6 +121,16 @@ __device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, c
     const float lo = __ll2float_rn(v - __float2ll_rn(hi));
     h[c] = {__fmul_rn(hi, sc), __fmul_rn(lo, sc)};
   }
+}
+
+// 56-bit form: field in FP64, (hh + x 2^-28) 2^(sigma - 56) with one final rounding
+__device__ __forceinline__ void fx_gather64(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
+                                            long long q, int s, int c0, int c1, int c2, double h[3]) {
+  FxAcc a;
+  fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
+  const double sc = (double)F.scale[s];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) h[c] = fma((double)a.x[c], 3.7252902984619141e-9, (double)a.hh[c]) * sc;
 }
 
 // spin of the site as a (hi, lo) float pair from its fixed-point halves (exact)
@@ -163,29 +183,40 @@ __device__ __forceinline__ void fx_rhs(const DevLattice& L, const DevLLG& P, con
   for (int c = 0; c < 3; ++c) f[c] = dfp_double(fd[c]);
 }
 
-// Depondt tail: FP64 field from the integer gather, as the FP64 kernels
-template <int NOISE>
+// FP64 field of the site from the integer gather (+ Zeeman and thermal): the 56-bit form's field, and
+// the field of the Depondt integrator for both forms
+template <int NOISE, int PREC>
 __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                            const int2* __restrict__ xs, const double* __restrict__ noise,
                                            long long q, int s, int c0, int c1, int c2, uint64_t step, double& bx,
                                            double& by, double& bz) {
-  dfp h[3];
-  fx_gather(L, F, xs, q, s, c0, c1, c2, h);
-  bx = dfp_double(h[0]) + L.B0;
-  by = dfp_double(h[1]) + L.B1;
-  bz = dfp_double(h[2]) + L.B2;
+  double h[3];
+  if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
+    fx_gather64(L, F, xs, q, s, c0, c1, c2, h);
+  } else {
+    dfp hp[3];
+    fx_gather(L, F, xs, q, s, c0, c1, c2, hp);
+    h[0] = dfp_double(hp[0]);
+    h[1] = dfp_double(hp[1]);
+    h[2] = dfp_double(hp[2]);
+  }
+  bx = h[0] + L.B0;
+  by = h[1] + L.B1;
+  bz = h[2] + L.B2;
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
 }
 
+template <int PREC>
 __global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, int2* __restrict__ xs, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) xs[i] = fx_split(x[i]);
+  if (i < n) xs[i] = fx_split<PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24>(x[i]);
 }
 
-template <int NOISE, int INTEG>
+template <int NOISE, int INTEG, int PREC>
 __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
-                                                    const double* __restrict__ e, const double* __restrict__ noise,
-                                                    uint64_t step) {
+                                                       const double* __restrict__ e, const double* __restrict__ noise,
+                                                       uint64_t step) {
+  constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
   const long long N = L.N;
@@ -200,7 +231,14 @@ __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const
   site_coords(L, q, s, c0, c1, c2);
   double f[3], x, y, z;
   if (INTEG == MGX_INTEGRATOR_HEUN) {
-    fx_rhs<NOISE>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, f);
+    if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
+      double bx, by, bz;
+      fx_field64<NOISE, PREC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
+      llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
+              f[2]);
+    } else {
+      fx_rhs<NOISE>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, f);
+    }
     x = fma(P.dt, f[0], ex);
     y = fma(P.dt, f[1], ey);
     z = fma(P.dt, f[2], ez);
@@ -208,7 +246,7 @@ __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const
     x *= r; y *= r; z *= r;
   } else {
     double bx, by, bz;
-    fx_field64<NOISE>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    fx_field64<NOISE, PREC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
     double fx, fy, fz;
     llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     f[0] = ey * fz - ez * fy; f[1] = ez * fx - ex * fz; f[2] = ex * fy - ey * fx;
@@ -217,13 +255,14 @@ __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const
   }
   P.ep[q] = x; P.ep[N + q] = y; P.ep[2 * N + q] = z;
   P.k1[q] = f[0]; P.k1[N + q] = f[1]; P.k1[2 * N + q] = f[2];
-  F.eps[q] = fx_split(x); F.eps[N + q] = fx_split(y); F.eps[2 * N + q] = fx_split(z);
+  F.eps[q] = fx_split<LIMB>(x); F.eps[N + q] = fx_split<LIMB>(y); F.eps[2 * N + q] = fx_split<LIMB>(z);
 }
 
-template <int NOISE, int INTEG>
+template <int NOISE, int INTEG, int PREC>
 __global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
-                                                    double* __restrict__ e, const double* __restrict__ noise,
-                                                    uint64_t step) {
+                                                       double* __restrict__ e, const double* __restrict__ noise,
+                                                       uint64_t step) {
+  constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
   if (L.pinned && L.pinned[q]) return;                 // e and its split stay as they are
@@ -234,14 +273,22 @@ __global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const
   double x = e[q], y = e[N + q], z = e[2 * N + q];
   if (INTEG == MGX_INTEGRATOR_HEUN) {
     double f[3];
-    fx_rhs<NOISE>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, f);
+    if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
+      const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
+      double bx, by, bz;
+      fx_field64<NOISE, PREC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
+      llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
+              f[2]);
+    } else {
+      fx_rhs<NOISE>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, f);
+    }
     x = fma(P.half_dt, k1x + f[0], x);
     y = fma(P.half_dt, k1y + f[1], y);
     z = fma(P.half_dt, k1z + f[2], z);
   } else {
     const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
     double bx, by, bz;
-    fx_field64<NOISE>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    fx_field64<NOISE, PREC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
     double fx, fy, fz;
     llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     const double wx = py * fz - pz * fy, wy = pz * fx - px * fz, wz = px * fy - py * fx;
@@ -250,10 +297,10 @@ __global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const
   const double r = rsqrt(x * x + y * y + z * z);
   x *= r; y *= r; z *= r;
   e[q] = x; e[N + q] = y; e[2 * N + q] = z;
-  F.es[q] = fx_split(x); F.es[N + q] = fx_split(y); F.es[2 * N + q] = fx_split(z);
+  F.es[q] = fx_split<LIMB>(x); F.es[N + q] = fx_split<LIMB>(y); F.es[2 * N + q] = fx_split<LIMB>(z);
 }
 
-template <int NOISE, int INTEG>
+template <int NOISE, int INTEG, int PREC>
 static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
   const DevLattice& L = pl->model->d;
   DevFX F = pl->fx;
@@ -262,35 +309,49 @@ static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_
   F.B[2] = split_host(L.B2);
   const int tpb = site_block_size(L.N);
   const unsigned grid = (unsigned)((L.N + tpb - 1) / tpb);
-  if (stages & 1) k_predict_fx<NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
-  if (stages & 2) k_correct_fx<NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
+  if (stages & 1) k_predict_fx<NOISE, INTEG, PREC><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
+  if (stages & 2) k_correct_fx<NOISE, INTEG, PREC><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
 }
 
-template <int NOISE>
+template <int NOISE, int PREC>
 static void fx_integ(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
-  if (pl->p.integrator == MGX_INTEGRATOR_DEPONDT) launch_fx<NOISE, MGX_INTEGRATOR_DEPONDT>(pl, e, noise, step, stages, st);
-  else launch_fx<NOISE, MGX_INTEGRATOR_HEUN>(pl, e, noise, step, stages, st);
+  if (pl->p.integrator == MGX_INTEGRATOR_DEPONDT)
+    launch_fx<NOISE, MGX_INTEGRATOR_DEPONDT, PREC>(pl, e, noise, step, stages, st);
+  else
+    launch_fx<NOISE, MGX_INTEGRATOR_HEUN, PREC>(pl, e, noise, step, stages, st);
+}
+
+template <int PREC>
+static void fx_noise(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
+  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
+  switch (mode) {
+    case MGX_NOISE_HOST: fx_integ<MGX_NOISE_HOST, PREC>(pl, e, noise, step, stages, st); break;
+    case MGX_NOISE_PHILOX: fx_integ<MGX_NOISE_PHILOX, PREC>(pl, e, noise, step, stages, st); break;
+    default: fx_integ<MGX_NOISE_NONE, PREC>(pl, e, noise, step, stages, st); break;
+  }
 }
 
 void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages) {
-  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
-  switch (mode) {
-    case MGX_NOISE_HOST: fx_integ<MGX_NOISE_HOST>(pl, e, noise, step, stages, st); break;
-    case MGX_NOISE_PHILOX: fx_integ<MGX_NOISE_PHILOX>(pl, e, noise, step, stages, st); break;
-    default: fx_integ<MGX_NOISE_NONE>(pl, e, noise, step, stages, st); break;
-  }
+  if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
+    fx_noise<MGX_PRECISION_FP64_FIXED_GATHER>(pl, e, noise, step, stages, st);
+  else
+    fx_noise<MGX_PRECISION_INT48_GATHER>(pl, e, noise, step, stages, st);
 }
 
 void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st) {
   const long long n = 3 * pl->model->d.N;
-  k_fx_split<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(e, pl->fx.es, n);
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
+    k_fx_split<MGX_PRECISION_FP64_FIXED_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, n);
+  else
+    k_fx_split<MGX_PRECISION_INT48_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, n);
 }
 
-// balanced (hi, lo) int32 halves of round(v 2^(48 - sigma)), |v| <= 2^sigma
-static int2 fx_host(double v, int sigma) {
-  const long long w = std::llround(std::ldexp(v, 48 - sigma));
-  const long long hi = (w + (1LL << 23)) >> 24;
-  return make_int2((int)hi, (int)(w - (hi << 24)));
+// balanced (hi, lo) int32 halves of round(v 2^(2 limb - sigma)), |v| <= 2^sigma
+static int2 fx_host(double v, int sigma, int limb) {
+  const long long w = std::llround(std::ldexp(v, 2 * limb - sigma));
+  const long long hi = (w + (1LL << (limb - 1))) >> limb;
+  return make_int2((int)hi, (int)(w - (hi << limb)));
 }
 
 mgx_status build_fx_tables(LLGPlan* pl) {
@@ -335,23 +396,34 @@ mgx_status build_fx_tables(LLGPlan* pl) {
       nA[9 * s + k] = -2.0 * inv[s] * A[9 * s + k];
       hasA |= A[9 * s + k] != 0.0;
     }
-  // per-sublattice scale 2^sigma >= every magnitude it multiplies (so every half fits 25 bits)
+  // per-sublattice scale 2^sigma.  48-bit form: 2^sigma >= every magnitude (every half fits 25 bits;
+  // every product is below 2^48, so the accumulators hold 2^14 terms per component).  56-bit form:
+  // 2^sigma >= the sum of all magnitudes of the sublattice, so that |sum J_hi e_hi| <= 2^56 sum |J|
+  // / 2^sigma <= 2^62 whatever the number of couplings: no int64 accumulator can overflow.
+  const int limb = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   std::vector<int> sigma(ns, 0);
   for (int s = 0; s < ns; ++s) {
-    double mx = 0.0;
+    double mx = 0.0, sum = 0.0;
     for (int b = off[s]; b < off[s + 1]; ++b)
-      for (int k = 0; k < 9; ++k) mx = std::max(mx, std::fabs(M[(size_t)b * 9 + k]));
-    for (int k = 0; k < 9; ++k) mx = std::max(mx, std::fabs(nA[9 * s + k]));
+      for (int k = 0; k < 9; ++k) {
+        mx = std::max(mx, std::fabs(M[(size_t)b * 9 + k]));
+        sum += std::fabs(M[(size_t)b * 9 + k]);
+      }
+    for (int k = 0; k < 9; ++k) {
+      mx = std::max(mx, std::fabs(nA[9 * s + k]));
+      sum += std::fabs(nA[9 * s + k]);
+    }
+    const double bound = limb == 28 ? sum : mx;
     int e = 0;
-    if (mx > 0.0) std::frexp(mx, &e);            // mx < 2^e
+    if (bound > 0.0) std::frexp(bound, &e);      // bound < 2^e
     sigma[s] = e;
-    pl->fx.scale[s] = std::ldexp(1.0f, e - 48);
+    pl->fx.scale[s] = std::ldexp(1.0f, e - 2 * limb);
   }
   std::vector<int2> Jq((size_t)std::max(nb, 1) * 10, make_int2(0, 0)), Aq((size_t)ns * 10, make_int2(0, 0));
   for (int s = 0; s < ns; ++s) {
     for (int b = off[s]; b < off[s + 1]; ++b)
-      for (int k = 0; k < 9; ++k) Jq[(size_t)b * 10 + k] = fx_host(M[(size_t)b * 9 + k], sigma[s]);
-    for (int k = 0; k < 9; ++k) Aq[(size_t)s * 10 + k] = fx_host(nA[9 * s + k], sigma[s]);
+      for (int k = 0; k < 9; ++k) Jq[(size_t)b * 10 + k] = fx_host(M[(size_t)b * 9 + k], sigma[s], limb);
+    for (int k = 0; k < 9; ++k) Aq[(size_t)s * 10 + k] = fx_host(nA[9 * s + k], sigma[s], limb);
   }
   // interior fast path: signed offsets, linear neighbour offset and reach per receiving sublattice
   std::vector<int2> lin((size_t)std::max(nb, 1), make_int2(0, 0));

@@ -14,7 +14,10 @@ Arithmetic (``precision=``): "fp64" (default) runs everything in FP64.  GB300's 
 in FP64 and move the rest off the FP64 pipe (Heun: field and right-hand side on compensated FP32
 pairs): "df32" evaluates the exchange sum on compensated FP32 pairs (~44 significant bits), "int48"
 as exact integer products and sums of 48-bit fixed-point couplings and spins on the INT32 pipe.
-Both stay within the per-step parity tolerance against magex (tests/test_gpu_df.py).
+Both stay within the per-step parity tolerance against magex (tests/test_gpu_df.py).  "fp64_fixed"
+keeps every floating-point operation FP64 and evaluates the exchange and on-site sums exactly on
+56-bit fixed-point spins and couplings (INT32 pipe): its only extra error, the 2^-57 quantisation of
+the inputs, is below the rounding of an FP64 multiply-add chain.
 
 Thermal noise (``noise=``):
   "philox"  counter-based Philox4x32-10 keyed by (seed, site, step), generated inside the kernels
@@ -45,6 +48,11 @@ def _philox_key(seed):
     return int(ss.generate_state(1, dtype=np.uint64)[0])
 
 
+
+#: arithmetic forms of the step (precision=...), see the module docstring
+PRECISIONS = {"fp64": _lib.PRECISION_FP64, "df32": _lib.PRECISION_DF32_GATHER, "int48": _lib.PRECISION_INT48_GATHER,
+              "fp64_fixed": _lib.PRECISION_FP64_FIXED_GATHER}
+
 class GB300LLG:
     """Stochastic Heun / Depondt LLG on one GB300, with the API of magex ``LLGSolver``."""
 
@@ -64,9 +72,8 @@ class GB300LLG:
             raise ValueError("backend must be 'gb300'")
         if noise not in ("philox", "host"):
             raise ValueError("noise must be 'philox' or 'host'")
-        if precision not in ("fp64", "df32", "int48"):
-            raise ValueError("precision must be 'fp64', 'df32' (exchange gather in compensated FP32 pairs) or "
-                             "'int48' (exchange gather in exact 48-bit fixed-point integer arithmetic)")
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
         self.precision = precision
         self.sys = system
         self.sc = supercell_from_system(system)
@@ -105,8 +112,7 @@ class GB300LLG:
         p.integrator = _SUPPORTED[integrator]
         p.noise = _lib.NOISE_HOST if noise == "host" else _lib.NOISE_PHILOX
         p.seed = _philox_key(seed)
-        p.precision = {"fp64": _lib.PRECISION_FP64, "df32": _lib.PRECISION_DF32_GATHER,
-                       "int48": _lib.PRECISION_INT48_GATHER}[precision]
+        p.precision = PRECISIONS[precision]
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             _lib.check(self.model.lib.mgx_llg_create(self.model.handle, C.byref(p), C.byref(h)), "mgx_llg_create")

@@ -18,7 +18,7 @@ STENCIL_TRAJ = ["sc16", "sc6_thermal", "bcc2_thermal", "bcc2_T0", "bcc2_shell4",
                 "tri_depondt_thermal", "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb"]
 
 
-PRECISIONS = ["df32", "int48"]
+PRECISIONS = ["df32", "int48", "fp64_fixed"]
 
 
 @pytest.mark.parametrize("precision", PRECISIONS)
@@ -75,19 +75,21 @@ def test_reduced_refuses_unsupported_layouts(cuda, golden, golden_models, precis
         GB300LLG(nl, 0.1, 1e-3, precision=precision)
 
 
-def test_int48_field_is_closer_to_fp64_than_df32(cuda):
-    """bcc 32^3, random spins: the integer gather's effective field differs from FP64 by about the
-    2^-48 fixed-point rounding (absolute), the compensated-FP32 one by ~2^-44 relative."""
+def test_fixed_point_forms_against_fp64_one_step(cuda):
+    """bcc 32^3, random spins, one T = 0 step: the 56-bit fixed-point gather with an FP64 tail agrees
+    with the FP64 plan at FP64 rounding level, the 48-bit one within its 2^-48 quantisation, the
+    compensated-FP32 one within ~2^-44 of the field."""
     from magex_gb300.llg import GB300LLG
     from magex_gb300.workloads import bcc_two_site
     sc = bcc_two_site(L=32)
     e0 = sc.init_spins("random", seed=8)
     out = {}
-    for prec in ("fp64", "df32", "int48"):
+    for prec in ("fp64", "df32", "int48", "fp64_fixed"):
         sol = GB300LLG(sc, 0.05, 1e-4, 0.0, 1, precision=prec)
         lat = sol.model.to_lattice(e0)
         sol.run_lattice(lat, 1)
         out[prec] = lat
     d_df = float((out["df32"] - out["fp64"]).abs().max())
     d_fx = float((out["int48"] - out["fp64"]).abs().max())
-    assert d_fx <= 2e-15 and d_df <= 2e-14, (d_fx, d_df)
+    d_64 = float((out["fp64_fixed"] - out["fp64"]).abs().max())
+    assert d_64 <= 1e-15 and d_fx <= 2e-15 and d_df <= 2e-14, (d_64, d_fx, d_df)
