@@ -118,7 +118,7 @@ struct DevFX {
   const int4* A;                 // [ns*5]: -2 A / (mu mu_B) in the same format, or nullptr
   const int2* lin;               // [nbond] (linear offset of the neighbour of an interior cell, signed R2)
   int4 reach[MGX_MAX_SUBLATTICES];
-  float scale[MGX_MAX_SUBLATTICES];   // 2^(sigma_s - 48): value of one unit of the accumulator
+  double scale[MGX_MAX_SUBLATTICES];  // 2^(sigma_s - 2 limb): value of one unit of the accumulator
   float2 alpha[MGX_MAX_SUBLATTICES], pre[MGX_MAX_SUBLATTICES], sig[MGX_MAX_SUBLATTICES];
   float2 B[3];                   // (hi, lo) split of the external field, refreshed at every launch
   int2* es;                      // [3][N] fixed-point split of e

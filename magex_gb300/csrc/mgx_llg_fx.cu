@@ -112,7 +112,7 @@ __device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, c
                                           long long q, int s, int c0, int c1, int c2, dfp h[3]) {
   FxAcc a;
   fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
-  const float sc = F.scale[s];
+  const float sc = (float)F.scale[s];            // >= 2^-100 (checked when the tables are built)
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     // value = (hh + x 2^-24) 2^(sigma - 48); fold x in with rounding, then split into two floats
@@ -128,7 +128,7 @@ __device__ __forceinline__ void fx_gather64(const DevLattice& L, const DevFX& F,
                                             long long q, int s, int c0, int c1, int c2, double h[3]) {
   FxAcc a;
   fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
-  const double sc = (double)F.scale[s];
+  const double sc = F.scale[s];
 #pragma unroll
   for (int c = 0; c < 3; ++c) h[c] = fma((double)a.x[c], 3.7252902984619141e-9, (double)a.hh[c]) * sc;
 }
@@ -416,8 +416,11 @@ mgx_status build_fx_tables(LLGPlan* pl) {
     const double bound = limb == 28 ? sum : mx;
     int e = 0;
     if (bound > 0.0) std::frexp(bound, &e);      // bound < 2^e
+    if (e < -50 || e > 900)
+      return set_error(MGX_ERR_UNSUPPORTED, "couplings of sublattice %d (scale 2^%d T) are outside the range of "
+                       "the fixed-point gather", s, e);
     sigma[s] = e;
-    pl->fx.scale[s] = std::ldexp(1.0f, e - 2 * limb);
+    pl->fx.scale[s] = std::ldexp(1.0, e - 2 * limb);
   }
   std::vector<int2> Jq((size_t)std::max(nb, 1) * 10, make_int2(0, 0)), Aq((size_t)ns * 10, make_int2(0, 0));
   for (int s = 0; s < ns; ++s) {
