@@ -370,7 +370,7 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
                         "grad_norm_per_shell": [float(x) for x in g.reshape(4, -1).norm(dim=1)]}}
 
 
-def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True):
+def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True, precision="fp64"):
     """Monte Carlo colour sweeps on the 128^3 two-site bcc workload (4,194,304 spins, z = 26, full
     3x3 tensors), T = 300 K, in-kernel Philox draws: site updates per second (one update = one trial
     move or one over-relaxation reflection of one spin)."""
@@ -378,7 +378,7 @@ def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True):
     from magex_gb300.mc import MetropolisMC
     from magex_gb300.workloads import bcc_two_site
     sc = bcc_two_site(L=L, field=FIELD)
-    mc = MetropolisMC(sc, TEMP, seed=1, sigma=0.3, overrelax=overrelax, move=move)
+    mc = MetropolisMC(sc, TEMP, seed=1, sigma=0.3, overrelax=overrelax, move=move, precision=precision)
     lat = mc.model.to_lattice(sc.init_spins("random", seed=1))
     mc.sweep_lattice(lat, 3)
     mc.acceptance()
@@ -410,7 +410,8 @@ def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True):
                "kind": "port", "sample": f"{n} sweeps of the same lattice, {el:.1f} s: C restatement of magex's "
                                          "NumPy colour sweep (OpenMP over each class) with magex's NumPy draws"}
     return {"workload": f"two-site bcc {L}^3 ({sc.N:,} spins), T = 300 K, {move} moves + {overrelax} over-relaxation "
-                        "pass per sweep, Philox, FP64",
+                        "pass per sweep, Philox, FP64" + (" with the exact fixed-point exchange sum"
+                                                          if precision == "fp64_fixed" else ""),
             "value": updates / t, "unit": "site-updates/s", "sweeps": sweeps, "ms_per_sweep": 1e3 * t / sweeps,
             "colour_classes": ncol, "acceptance": acc, "gpu_launches_per_sweep": ncol * (1 + overrelax),
             "cpu_baseline": cpu}
@@ -615,6 +616,7 @@ def run_gb300(args):
         line["large_batched_adjoint"] = bench_config5()
     if ws == 1 and not args.no_batched:
         line["monte_carlo"] = bench_mc(L=args.L, cpu_baseline=not args.no_cpu_baseline)
+        line["monte_carlo_fp64_fixed"] = bench_mc(L=args.L, cpu_baseline=False, precision="fp64_fixed")
         line["sqw_projection"] = bench_sqw(L=args.L)
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
@@ -656,7 +658,8 @@ def main():
         elif args.only == "sqw":
             out = bench_sqw(L=args.L)
         elif args.only == "mc":
-            out = bench_mc(L=args.L, sweeps=min(args.steps, 100))
+            out = [bench_mc(L=args.L, sweeps=min(args.steps, 100), cpu_baseline=False, precision=p)
+                   for p in ("fp64", "fp64_fixed")]
         elif args.only == "config5":
             out = bench_config5(K=min(args.steps, 50), adj_steps=args.adjoint_steps or 1000)
         else:

@@ -314,6 +314,9 @@ typedef struct mgx_mc_params {
   int32_t rng;               /* MGX_MC_RNG_PHILOX (key seed) or MGX_MC_RNG_HOST (draws per sweep) */
   double sigma;              /* Gaussian cone width (adapted by the caller, magex/montecarlo.py:257-261) */
   uint64_t seed;
+  int32_t precision;         /* MGX_PRECISION_FP64, or MGX_PRECISION_FP64_FIXED_GATHER: the exchange field
+                              * of every trial move as an exact 56-bit fixed-point sum (stencil models
+                              * with per-sublattice A and mu) */
 } mgx_mc_params;
 /* group_sites: host, magex site indices of every colour class in update order, concatenated
  * (group_sizes[g] each; pinned sites left out, as magex/montecarlo.py:93-99). */

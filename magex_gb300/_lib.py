@@ -51,7 +51,7 @@ class CSRDesc(C.Structure):
 
 class MCParams(C.Structure):
     _fields_ = [("move", C.c_int32), ("overrelax", C.c_int32), ("rng", C.c_int32), ("sigma", C.c_double),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("precision", C.c_int32)]
 
 
 #: every exported entry point with (restype, argtypes); the CPU tests check the export list against

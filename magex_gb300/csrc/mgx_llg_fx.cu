@@ -22,90 +22,10 @@
 #include <vector>
 
 #include "mgx_dfp.cuh"
+#include "mgx_fx.cuh"
 #include "mgx_step.cuh"
 
 namespace mgx {
-
-// Two fixed-point formats: LIMB = 24 (MGX_PRECISION_INT48_GATHER, 48-bit values, FP32-pair tail) and
-// LIMB = 28 (MGX_PRECISION_FP64_FIXED_GATHER, 56-bit values, FP64 tail).  A value is v = round(x 2^(2 LIMB))
-// held as v = hi 2^LIMB + lo with hi = round(v / 2^LIMB) and lo in [-2^(LIMB-1), 2^(LIMB-1)): balanced
-// halves, so that the dropped lo x lo products have zero mean.
-template <int LIMB>
-__device__ __forceinline__ int2 fx_halves(long long v) {
-  const long long hi = (v + (1LL << (LIMB - 1))) >> LIMB;
-  return make_int2((int)hi, (int)(v - (hi << LIMB)));
-}
-
-template <int LIMB>
-__device__ __forceinline__ int2 fx_split(double x) {
-  return fx_halves<LIMB>(__double2ll_rn(x * (double)(1LL << (2 * LIMB))));
-}
-
-__device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
-  long long d;
-  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
-  return d;
-}
-
-struct FxAcc {
-  long long hh[3] = {0, 0, 0};   // sum J_hi e_hi        (units 2^(sigma - 48))
-  long long x[3] = {0, 0, 0};    // sum J_hi e_lo + J_lo e_hi (units 2^(sigma - 72))
-};
-
-// acc += M x for a 3x3 fixed-point tensor M (10 (hi, lo) int pairs, 80 B) and a fixed-point spin x
-__device__ __forceinline__ void fx_mat(const int4* __restrict__ T, int2 x0, int2 x1, int2 x2, FxAcc& a) {
-  const int4 t01 = __ldg(T), t23 = __ldg(T + 1), t45 = __ldg(T + 2), t67 = __ldg(T + 3), t89 = __ldg(T + 4);
-  const int2 m[9] = {make_int2(t01.x, t01.y), make_int2(t01.z, t01.w), make_int2(t23.x, t23.y),
-                     make_int2(t23.z, t23.w), make_int2(t45.x, t45.y), make_int2(t45.z, t45.w),
-                     make_int2(t67.x, t67.y), make_int2(t67.z, t67.w), make_int2(t89.x, t89.y)};
-  const int2 xv[3] = {x0, x1, x2};
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const int2 j = m[3 * c + d];
-      a.hh[c] = mad_wide(j.x, xv[d].x, a.hh[c]);
-      a.x[c] = mad_wide(j.x, xv[d].y, mad_wide(j.y, xv[d].x, a.x[c]));
-    }
-}
-
-// Exchange (+ on-site) field of lattice index q = (s, c0, c1, c2) from the fixed-point field xs, as
-// (hi, lo) float pairs in tesla.  Interior cells (whole stencil inside the supercell along axes 0
-// and 1) index neighbours as q + a per-coupling constant, corrected for the periodic seam of axis 2.
-__device__ __forceinline__ void fx_accumulate(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
-                                              long long q, int s, int c0, int c1, int c2, FxAcc& a) {
-  const long long N = L.N;
-  const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
-  const int4 r = F.reach[s];
-  const bool inner01 = c0 >= r.x && c0 < L.L0 - r.x && c1 >= r.y && c1 < L.L1 - r.y;
-  const bool inner2 = L.pbc2 ? r.z < L.L2 : (c2 >= r.z && c2 < L.L2 - r.z);
-  if (inner01 && inner2) {
-    // 32-bit index arithmetic (N < 2^31 for every lattice this path accepts)
-    const int2* __restrict__ x0 = xs;
-    const int2* __restrict__ x1 = xs + N;
-    const int2* __restrict__ x2 = xs + 2 * N;
-    const int qi = (int)q, L2 = L.L2;
-    for (int b = b0; b < b1; ++b) {
-      const int2 li = __ldg(F.lin + b);
-      const int n2 = c2 + li.y;
-      const int j = qi + li.x + (n2 < 0 ? L2 : 0) - (n2 >= L2 ? L2 : 0);
-      fx_mat(F.J + 5 * b, __ldg(x0 + j), __ldg(x1 + j), __ldg(x2 + j), a);
-    }
-  } else {
-    for (int b = b0; b < b1; ++b) {
-      const int4 g = __ldg(L.bond_geo + b);
-      int n0 = c0 + g.y, n1 = c1 + g.z, n2 = c2 + g.w;
-      bool ok = true;
-      if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
-      if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
-      if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
-      if (!ok) continue;
-      const long long j = (long long)g.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
-      fx_mat(F.J + (long long)b * 5, __ldg(xs + j), __ldg(xs + N + j), __ldg(xs + 2 * N + j), a);
-    }
-  }
-  if (F.A) fx_mat(F.A + 5 * s, __ldg(xs + q), __ldg(xs + N + q), __ldg(xs + 2 * N + q), a);
-}
 
 // 48-bit form: field as (hi, lo) float pairs in tesla
 __device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
@@ -354,13 +274,11 @@ static int2 fx_host(double v, int sigma, int limb) {
   return make_int2((int)hi, (int)(w - (hi << limb)));
 }
 
-mgx_status build_fx_tables(LLGPlan* pl) {
-  const Model* m = pl->model;
+mgx_status fx_build(const Model* m, int limb, bool field_scaled, int ncopies, DevFX* fx, void** block) {
   const DevLattice& d = m->d;
   if (d.layout != 0) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather needs a lattice stencil model");
   if (d.N >= (1LL << 31)) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather indexes at most 2^31 - 1 sites");
   if (d.A_site || d.mu_site) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather needs per-sublattice A and mu");
-  if (pl->p.alpha_site || pl->p.sigma_site) return set_error(MGX_ERR_UNSUPPORTED, "the integer gather needs uniform damping");
   const int ns = d.ns, nb = m->nbond, W = d.width;
   const long long N = d.N;
   std::vector<int> off(ns + 1);
@@ -373,8 +291,8 @@ mgx_status build_fx_tables(LLGPlan* pl) {
   }
   MGX_CUDA_TRY(cudaMemcpy(A.data(), d.A_sub, sizeof(double) * 9 * ns, cudaMemcpyDeviceToHost));
   MGX_CUDA_TRY(cudaMemcpy(inv.data(), d.inv_mu_sub, sizeof(double) * ns, cudaMemcpyDeviceToHost));
-  // scaled 3x3 tensors: couplings 2 J / (mu mu_B), on-site -2 A / (mu mu_B) of the receiving sublattice
-  std::vector<double> M((size_t)std::max(nb, 1) * 9, 0.0), nA(9 * ns);
+  // 3x3 tensors of the receiving sublattice
+  std::vector<double> M((size_t)std::max(nb, 1) * 9, 0.0), nA(9 * ns, 0.0);
   for (int s = 0; s < ns; ++s)
     for (int b = off[s]; b < off[s + 1]; ++b) {
       const double* t = J.data() + (size_t)b * W;
@@ -388,20 +306,22 @@ mgx_status build_fx_tables(LLGPlan* pl) {
       } else {
         for (int k = 0; k < 9; ++k) T[k] = t[k];
       }
-      for (int k = 0; k < 9; ++k) M[(size_t)b * 9 + k] = 2.0 * inv[s] * T[k];
+      const double f = field_scaled ? 2.0 * inv[s] : 1.0;
+      for (int k = 0; k < 9; ++k) M[(size_t)b * 9 + k] = f * T[k];
     }
   bool hasA = false;
-  for (int s = 0; s < ns; ++s)
-    for (int k = 0; k < 9; ++k) {
-      nA[9 * s + k] = -2.0 * inv[s] * A[9 * s + k];
-      hasA |= A[9 * s + k] != 0.0;
-    }
+  if (field_scaled)
+    for (int s = 0; s < ns; ++s)
+      for (int k = 0; k < 9; ++k) {
+        nA[9 * s + k] = -2.0 * inv[s] * A[9 * s + k];
+        hasA |= A[9 * s + k] != 0.0;
+      }
   // per-sublattice scale 2^sigma.  48-bit form: 2^sigma >= every magnitude (every half fits 25 bits;
   // every product is below 2^48, so the accumulators hold 2^14 terms per component).  56-bit form:
   // 2^sigma >= the sum of all magnitudes of the sublattice, so that |sum J_hi e_hi| <= 2^56 sum |J|
   // / 2^sigma <= 2^62 whatever the number of couplings: no int64 accumulator can overflow.
-  const int limb = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   std::vector<int> sigma(ns, 0);
+  for (int s = 0; s < MGX_MAX_SUBLATTICES; ++s) fx->scale[s] = 0.0;
   for (int s = 0; s < ns; ++s) {
     double mx = 0.0, sum = 0.0;
     for (int b = off[s]; b < off[s + 1]; ++b)
@@ -417,10 +337,10 @@ mgx_status build_fx_tables(LLGPlan* pl) {
     int e = 0;
     if (bound > 0.0) std::frexp(bound, &e);      // bound < 2^e
     if (e < -50 || e > 900)
-      return set_error(MGX_ERR_UNSUPPORTED, "couplings of sublattice %d (scale 2^%d T) are outside the range of "
-                       "the fixed-point gather", s, e);
+      return set_error(MGX_ERR_UNSUPPORTED, "couplings of sublattice %d (scale 2^%d) are outside the range of the "
+                       "fixed-point gather", s, e);
     sigma[s] = e;
-    pl->fx.scale[s] = std::ldexp(1.0, e - 2 * limb);
+    fx->scale[s] = std::ldexp(1.0, e - 2 * limb);
   }
   std::vector<int2> Jq((size_t)std::max(nb, 1) * 10, make_int2(0, 0)), Aq((size_t)ns * 10, make_int2(0, 0));
   for (int s = 0; s < ns; ++s) {
@@ -431,18 +351,41 @@ mgx_status build_fx_tables(LLGPlan* pl) {
   // interior fast path: signed offsets, linear neighbour offset and reach per receiving sublattice
   std::vector<int2> lin((size_t)std::max(nb, 1), make_int2(0, 0));
   const int Ls[3] = {d.L0, d.L1, d.L2}, pbc[3] = {d.pbc0, d.pbc1, d.pbc2};
-  for (int s = 0; s < MGX_MAX_SUBLATTICES; ++s) pl->fx.reach[s] = make_int4(0, 0, 0, 0);
+  for (int s = 0; s < MGX_MAX_SUBLATTICES; ++s) fx->reach[s] = make_int4(0, 0, 0, 0);
   for (int s = 0; s < ns; ++s)
     for (int b = off[s]; b < off[s + 1]; ++b) {
       int R[3] = {geo[b].y, geo[b].z, geo[b].w};
       for (int a = 0; a < 3; ++a)
         if (pbc[a] && R[a] > Ls[a] / 2) R[a] -= Ls[a];
       lin[b] = make_int2((geo[b].x - s) * d.ncell + (R[0] * d.L1 + R[1]) * d.L2 + R[2], R[2]);
-      int4& r = pl->fx.reach[s];
+      int4& r = fx->reach[s];
       r.x = std::max(r.x, std::abs(R[0]));
       r.y = std::max(r.y, std::abs(R[1]));
       r.z = std::max(r.z, std::abs(R[2]));
     }
+  const size_t nJ = sizeof(int2) * Jq.size(), nA2 = sizeof(int2) * Aq.size(), nL = sizeof(int2) * lin.size();
+  const size_t o_A = (nJ + 15) / 16 * 16, o_L = (o_A + nA2 + 15) / 16 * 16, o_es = (o_L + nL + 15) / 16 * 16;
+  const size_t n_split = sizeof(int2) * 3 * (size_t)N;
+  MGX_CUDA_TRY(cudaMalloc(block, o_es + (size_t)ncopies * n_split));
+  char* base = (char*)*block;
+  MGX_CUDA_TRY(cudaMemcpy(base, Jq.data(), nJ, cudaMemcpyHostToDevice));
+  MGX_CUDA_TRY(cudaMemcpy(base + o_A, Aq.data(), nA2, cudaMemcpyHostToDevice));
+  MGX_CUDA_TRY(cudaMemcpy(base + o_L, lin.data(), nL, cudaMemcpyHostToDevice));
+  fx->J = (const int4*)base;
+  fx->A = hasA ? (const int4*)(base + o_A) : nullptr;
+  fx->lin = (const int2*)(base + o_L);
+  fx->es = (int2*)(base + o_es);
+  fx->eps = ncopies > 1 ? (int2*)(base + o_es + n_split) : nullptr;
+  return MGX_OK;
+}
+
+mgx_status build_fx_tables(LLGPlan* pl) {
+  if (pl->p.alpha_site || pl->p.sigma_site)
+    return set_error(MGX_ERR_UNSUPPORTED, "the integer gather needs uniform damping");
+  const int limb = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
+  const mgx_status st = fx_build(pl->model, limb, true, 2, &pl->fx, &pl->fx_block);
+  if (st != MGX_OK) return st;
+  const int ns = pl->model->d.ns;
   std::vector<double> ap(2 * ns);
   MGX_CUDA_TRY(cudaMemcpy(ap.data(), pl->p.alpha_sub, sizeof(double) * ns, cudaMemcpyDeviceToHost));
   MGX_CUDA_TRY(cudaMemcpy(ap.data() + ns, pl->p.pre_sub, sizeof(double) * ns, cudaMemcpyDeviceToHost));
@@ -450,20 +393,15 @@ mgx_status build_fx_tables(LLGPlan* pl) {
     pl->fx.alpha[s] = split_host(ap[s]);
     pl->fx.pre[s] = split_host(ap[ns + s]);
   }
-  const size_t nJ = sizeof(int2) * Jq.size(), nA2 = sizeof(int2) * Aq.size(), nL = sizeof(int2) * lin.size();
-  const size_t o_A = (nJ + 15) / 16 * 16, o_L = (o_A + nA2 + 15) / 16 * 16, o_es = (o_L + nL + 15) / 16 * 16;
-  const size_t n_split = sizeof(int2) * 3 * (size_t)N;
-  MGX_CUDA_TRY(cudaMalloc(&pl->fx_block, o_es + 2 * n_split));
-  char* base = (char*)pl->fx_block;
-  MGX_CUDA_TRY(cudaMemcpy(base, Jq.data(), nJ, cudaMemcpyHostToDevice));
-  MGX_CUDA_TRY(cudaMemcpy(base + o_A, Aq.data(), nA2, cudaMemcpyHostToDevice));
-  MGX_CUDA_TRY(cudaMemcpy(base + o_L, lin.data(), nL, cudaMemcpyHostToDevice));
-  pl->fx.J = (const int4*)base;
-  pl->fx.A = hasA ? (const int4*)(base + o_A) : nullptr;
-  pl->fx.lin = (const int2*)(base + o_L);
-  pl->fx.es = (int2*)(base + o_es);
-  pl->fx.eps = (int2*)(base + o_es + n_split);
   return MGX_OK;
+}
+
+void enqueue_fx_split_n(const double* x, int2* xs, long long n, int limb, cudaStream_t st) {
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (limb == 28)
+    k_fx_split<MGX_PRECISION_FP64_FIXED_GATHER><<<grid, 256, 0, st>>>(x, xs, n);
+  else
+    k_fx_split<MGX_PRECISION_INT48_GATHER><<<grid, 256, 0, st>>>(x, xs, n);
 }
 
 }  // namespace mgx

@@ -18,7 +18,7 @@
 #include <cmath>
 #include <vector>
 
-#include "mgx_internal.cuh"
+#include "mgx_fx.cuh"
 
 namespace mgx {
 
@@ -41,6 +41,9 @@ struct McPlan {
   unsigned long long* acc = nullptr;       // device accepted-move counter
   unsigned long long tried = 0;
   std::vector<long long> sites_host;
+  bool fixed = false;                      // exchange field from the exact 56-bit fixed-point gather
+  DevFX fx{};
+  void* fx_block = nullptr;
 };
 
 // ------------------------------------------------------------------ random numbers
@@ -95,13 +98,13 @@ enum { MC_GAUSSIAN = 0, MC_UNIFORM = 1, MC_HEATBATH = 2, MC_HINZKE = 3, MC_OVERR
 
 // One pass over the n sites of a colour class.  hr: host-supplied draws of this pass (RNG_HOST), laid
 // out as documented at mgx_mc_sweep; otherwise Philox with counter (site, sweep, pass).
-template <int W, int MOVE, bool HOSTRNG>
+template <int W, int MOVE, bool HOSTRNG, bool FIXED>
 __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __restrict__ e,
                                                  const long long* __restrict__ sites, long long n,
                                                  const double* __restrict__ beta_sub,
                                                  const double* __restrict__ beta_site, double sigma,
                                                  const double* __restrict__ hr, uint64_t seed, uint64_t sweep,
-                                                 int pass, unsigned long long* acc) {
+                                                 int pass, unsigned long long* acc, const DevFX F) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   bool ok = false;
   if (t < n) {
@@ -111,7 +114,17 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
     site_coords(L, q, s, c0, c1, c2);
     const long long m = (L.layout == 1) ? q : (long long)(q - (long long)s * L.ncell) * L.ns + s;
     double hx, hy, hz;
-    exchange_field<W>(L, e, s, c0, c1, c2, hx, hy, hz);
+    if (FIXED) {
+      // exact 56-bit fixed-point sum h = sum_j J_ij e_j, rounded once to FP64
+      FxAcc a;
+      fx_accumulate(L, F, F.es, q, s, c0, c1, c2, a);
+      const double sc = F.scale[s];
+      hx = fma((double)a.x[0], 3.7252902984619141e-9, (double)a.hh[0]) * sc;
+      hy = fma((double)a.x[1], 3.7252902984619141e-9, (double)a.hh[1]) * sc;
+      hz = fma((double)a.x[2], 3.7252902984619141e-9, (double)a.hh[2]) * sc;
+    } else {
+      exchange_field<W>(L, e, s, c0, c1, c2, hx, hy, hz);
+    }
     const double ox = e[q], oy = e[N + q], oz = e[2 * N + q];
     const double mu = L.mu_site ? __ldg(L.mu_site + q) : __ldg(L.mu_sub + s);
     const double bt = beta_site ? __ldg(beta_site + q) : __ldg(beta_sub + s);
@@ -230,6 +243,11 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
       e[q] = nx;
       e[N + q] = ny;
       e[2 * N + q] = nz;
+      if (FIXED) {
+        F.es[q] = fx_split<28>(nx);
+        F.es[N + q] = fx_split<28>(ny);
+        F.es[2 * N + q] = fx_split<28>(nz);
+      }
     }
   }
   const int cnt = __syncthreads_count(ok);
@@ -243,12 +261,21 @@ static void launch_pass(const McPlan* mc, double* e, int g, const double* hr, in
   if (n == 0) return;
   const unsigned grid = (unsigned)((n + 127) / 128);
   const long long* sites = mc->sites + mc->goff[g];
-  if (hr)
-    k_mc_pass<W, MOVE, true><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
-                                                   mc->seed, mc->sweep, pass, mc->acc);
-  else
-    k_mc_pass<W, MOVE, false><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, nullptr,
-                                                    mc->seed, mc->sweep, pass, mc->acc);
+  if (mc->fixed) {
+    if (hr)
+      k_mc_pass<W, MOVE, true, true><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
+                                                           mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+    else
+      k_mc_pass<W, MOVE, false, true><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
+                                                            nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+  } else {
+    if (hr)
+      k_mc_pass<W, MOVE, true, false><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
+                                                            mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+    else
+      k_mc_pass<W, MOVE, false, false><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
+                                                             nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+  }
 }
 
 template <int W>
@@ -378,6 +405,7 @@ extern "C" mgx_status mgx_colour_graph(int64_t N, const int64_t* ptr, const int3
 
 static void mc_free(McPlan* mc) {
   if (!mc) return;
+  cudaFree(mc->fx_block);
   cudaFree(mc->sites);
   cudaFree(mc->beta);
   cudaFree(mc->beta_site);
@@ -396,6 +424,9 @@ extern "C" mgx_status mgx_mc_create(const mgx_model* mm, const mgx_mc_params* p,
   if (p->overrelax < 0) return set_error(MGX_ERR_INVALID, "mgx_mc_create: overrelax must be >= 0");
   if (p->rng != MGX_MC_RNG_PHILOX && p->rng != MGX_MC_RNG_HOST)
     return set_error(MGX_ERR_INVALID, "mgx_mc_create: rng %d is not philox (0) or host (1)", p->rng);
+  if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_FP64_FIXED_GATHER)
+    return set_error(MGX_ERR_INVALID, "mgx_mc_create: precision %d is not fp64 (0) or fp64-fixed-gather (3)",
+                     p->precision);
   const DevLattice& d = m->d;
   const long long N = d.N;
   McPlan* mc = new McPlan();
@@ -439,6 +470,14 @@ extern "C" mgx_status mgx_mc_create(const mgx_model* mm, const mgx_mc_params* p,
   if (err != cudaSuccess) {
     mc_free(mc);
     return cuda_error(err, "mgx_mc_create");
+  }
+  if (p->precision == MGX_PRECISION_FP64_FIXED_GATHER) {
+    const mgx_status st = fx_build(m, 28, false, 1, &mc->fx, &mc->fx_block);
+    if (st != MGX_OK) {
+      mc_free(mc);
+      return st;
+    }
+    mc->fixed = true;
   }
   *out = reinterpret_cast<mgx_mc*>(mc);
   return MGX_OK;
@@ -504,6 +543,7 @@ extern "C" mgx_status mgx_mc_sweep(mgx_mc* h, double* e, int64_t nsweeps, const 
   if (mc->rng == MGX_MC_RNG_HOST && (nsweeps > 1 || (nsweeps == 1 && !host_draws)))
     return set_error(MGX_ERR_INVALID, "mgx_mc_sweep: host draws cover one sweep per call");
   cudaStream_t st = (cudaStream_t)stream;
+  if (mc->fixed && nsweeps > 0) enqueue_fx_split_n(e, mc->fx.es, 3 * mc->model->d.N, 28, st);
   for (int64_t k = 0; k < nsweeps; ++k) {
     const double* hr = mc->rng == MGX_MC_RNG_HOST ? host_draws : nullptr;
     long long off = 0;

@@ -66,15 +66,20 @@ class MetropolisMC:
 
     Same arguments as magex; ``backend`` and ``dipolar_exact`` are accepted for signature
     compatibility (dipolar and other long-range terms raise NotImplementedError).  ``rng`` selects
-    in-kernel Philox draws or magex's own NumPy stream.  ``T`` and ``sigma`` may be reassigned between
+    in-kernel Philox draws or magex's own NumPy stream; ``precision="fp64_fixed"`` evaluates the
+    exchange field of the trial moves as an exact 56-bit fixed-point sum on the integer pipes (stencil
+    models with per-sublattice A and mu; every floating-point operation stays FP64).  ``T`` and ``sigma`` may be reassigned between
     sweeps (annealing, magex/montecarlo.py:257-261)."""
 
     def __init__(self, system, temperature, seed=None, sigma=0.6, overrelax=1, move="gaussian",
-                 backend="gb300", dipolar_exact="auto", rng="philox", device=None):
+                 backend="gb300", dipolar_exact="auto", rng="philox", precision="fp64", device=None):
         if move not in MOVES:
             raise ValueError(f"unknown move '{move}' (gaussian, uniform, heatbath, hinzke)")
         if rng not in ("philox", "host"):
             raise ValueError("rng must be 'philox' or 'host'")
+        if precision not in ("fp64", "fp64_fixed"):
+            raise ValueError("precision must be 'fp64' or 'fp64_fixed' (exchange field as an exact 56-bit "
+                             "fixed-point sum, every floating-point operation FP64)")
         self.sys = system
         self.sc = supercell_from_system(system)
         self.move = move
@@ -103,6 +108,7 @@ class MetropolisMC:
         p.rng = _lib.MC_RNG_HOST if rng == "host" else _lib.MC_RNG_PHILOX
         p.sigma = float(sigma)
         p.seed = int(np.random.SeedSequence(seed).generate_state(1, np.uint64)[0])
+        p.precision = _lib.PRECISION_FP64_FIXED_GATHER if precision == "fp64_fixed" else _lib.PRECISION_FP64
         h = C.c_void_p()
         lib = _lib.load()
         with torch.cuda.device(self.device):
