@@ -168,6 +168,10 @@ mgx_status mgx_llg_destroy(mgx_llg* plan);
 /* Device pointer of the plan's predicted spins ep ((3, N) lattice layout), written by stage 0 and read
  * by stage 1: a slab decomposition exchanges its halo layers between the two stages. */
 mgx_status mgx_llg_predicted(mgx_llg* plan, double** ep);
+/* The reduced and fixed-point forms gather the corrector's neighbours from a split copy of ep ((3, N)
+ * elements of 8 bytes: float pairs or int32 halves), written by stage 0; a slab decomposition
+ * exchanges its halo layers too.  NULL for the FP64 form. */
+mgx_status mgx_llg_predicted_split(mgx_llg* plan, void** eps);
 /* Thermal-field amplitude sigma_i = sqrt(2 alpha_i k_B T_i / (gamma mu_i mu_B dt)) (magex/llg.py:111):
  * per sublattice (host [ns]) or per site (host [N] magex order, overrides).  Zero means no noise. */
 mgx_status mgx_llg_set_sigma(mgx_llg* plan, const double* sigma_sub, const double* sigma_site);

@@ -68,6 +68,7 @@ SIGNATURES = {
     "mgx_lattice_layers": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
                                        C.c_void_p]),
     "mgx_llg_predicted": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "mgx_llg_predicted_split": (C.c_int32, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "mgx_pack_spins": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_unpack_spins": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_llg_create": (C.c_int32, [C.c_void_p, C.POINTER(LLGParams), C.POINTER(C.c_void_p)]),

@@ -173,6 +173,15 @@ mgx_status mgx_llg_predicted(mgx_llg* pp, double** ep) {
   return MGX_OK;
 }
 
+mgx_status mgx_llg_predicted_split(mgx_llg* pp, void** eps) {
+  LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
+  if (!pl || !eps) return set_error(MGX_ERR_INVALID, "mgx_llg_predicted_split: null argument");
+  *eps = nullptr;
+  if (pl->precision == MGX_PRECISION_DF32_GATHER) *eps = pl->df.eps;
+  if (pl->precision == MGX_PRECISION_INT48_GATHER || pl->precision == MGX_PRECISION_FP64_FIXED_GATHER) *eps = pl->fx.eps;
+  return MGX_OK;
+}
+
 mgx_status mgx_llg_destroy(mgx_llg* pp) {
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl) return MGX_OK;

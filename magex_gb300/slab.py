@@ -83,20 +83,20 @@ class SlabGeometry:
 
 
 class SlabLLG:
-    """One slab of a slab-decomposed GB300 LLG run (FP64, Philox noise).
+    """One slab of a slab-decomposed GB300 LLG run (Philox noise; any precision form).
 
     Built from the unit-cell model and the whole lattice's size, boundaries and field; the solver is a
     GB300LLG on the local supercell (owned layers + halos) whose noise and observables are those of
     the whole lattice."""
 
     def __init__(self, uc, L, pbc, field, alpha, dt, temperature, seed, rank, world, precession=True,
-                 integrator="heun", device=None):
+                 integrator="heun", precision="fp64", device=None):
         from .llg import GB300LLG
         whole = Supercell(uc, L, pbc, field)
         self.geo = SlabGeometry(L, pbc, halo_depth(whole), world, rank)
         self.sc = Supercell(uc, self.geo.L_local, self.geo.pbc_local, field)
         self.solver = GB300LLG(self.sc, alpha, dt, temperature, seed, precession=precession, integrator=integrator,
-                               device=device)
+                               precision=precision, device=device)
         self.model = self.solver.model
         self.lib = _lib.load()
         _lib.check(self.lib.mgx_model_set_partition(self.model.handle, self.geo.cell_offset, *self.geo.own),
@@ -104,6 +104,9 @@ class SlabLLG:
         ptr = C.c_void_p()
         _lib.check(self.lib.mgx_llg_predicted(self.solver.handle, C.byref(ptr)), "mgx_llg_predicted")
         self._ep = ptr
+        eps = C.c_void_p()
+        _lib.check(self.lib.mgx_llg_predicted_split(self.solver.handle, C.byref(eps)), "mgx_llg_predicted_split")
+        self._eps = eps if eps.value else None      # split copy of ep the reduced / fixed-point forms gather from
         self._layer = 3 * self.sc.ns * self.sc.L[1] * self.sc.L[2]
         self._sites = self.geo.global_sites(self.sc.ns)
 
@@ -117,7 +120,13 @@ class SlabLLG:
         return self.model.from_lattice(lat).cpu().numpy()[self.geo.owned_rows(self.sc.ns)]
 
     def _ptr(self, which, lat):
+        if which == "eps":
+            return self._eps
         return self._ep if which == "ep" else C.c_void_p(lat.data_ptr())
+
+    def _fields(self, which):
+        """Arrays exchanged for a halo message: ep travels with its split copy (8-byte elements too)."""
+        return ("ep", "eps") if which == "ep" and self._eps is not None else (which,)
 
     def _layers(self, which, lat, c0a, c0b, buf, to_buffer, stream=None):
         _lib.check(self.lib.mgx_lattice_layers(self.model.handle, self._ptr(which, lat), c0a, c0b,
@@ -125,24 +134,32 @@ class SlabLLG:
                    "mgx_lattice_layers")
 
     def pack(self, which, lat):
-        """Boundary layers to send: the first h owned layers to the left neighbour, the last h to the right."""
+        """Boundary layers to send: the first h owned layers to the left neighbour, the last h to the right
+        (one message per side, the exchanged arrays one after the other)."""
         g, out = self.geo, {}
         a, b = g.own
-        if g.left_rank is not None:
-            out["left"] = torch.empty(self._layer * g.h, dtype=torch.float64, device=lat.device)
-            self._layers(which, lat, a, a + g.h, out["left"], True)
-        if g.right_rank is not None:
-            out["right"] = torch.empty(self._layer * g.h, dtype=torch.float64, device=lat.device)
-            self._layers(which, lat, b - g.h, b, out["right"], True)
+        fields = self._fields(which)
+        n = self._layer * g.h
+        for side, lo in (("left", a), ("right", b - g.h)):
+            if (g.left_rank if side == "left" else g.right_rank) is None:
+                continue
+            buf = torch.empty(n * len(fields), dtype=torch.float64, device=lat.device)
+            for k, f in enumerate(fields):
+                self._layers(f, lat, lo, lo + g.h, buf[k * n:(k + 1) * n], True)
+            out[side] = buf
         return out
 
     def unpack(self, which, lat, recv):
         """Received halo layers into layers [0, hl) and [own_end, own_end + hr)."""
         g = self.geo
-        if "left" in recv:
-            self._layers(which, lat, 0, g.hl, recv["left"].to(lat.device), False)
-        if "right" in recv:
-            self._layers(which, lat, g.own[1], g.own[1] + g.hr, recv["right"].to(lat.device), False)
+        fields = self._fields(which)
+        for side, lo, depth in (("left", 0, g.hl), ("right", g.own[1], g.hr)):
+            if side not in recv:
+                continue
+            buf = recv[side].to(lat.device)
+            n = self._layer * depth
+            for k, f in enumerate(fields):
+                self._layers(f, lat, lo, lo + depth, buf[k * n:(k + 1) * n], False)
 
     # ------------------------------------------------------------------ stages and observables
     def stage(self, lat, k):

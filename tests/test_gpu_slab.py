@@ -8,13 +8,14 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fixed", "df32"])
 @pytest.mark.parametrize("name,L,pbc,B,world", [
     ("bcc2", (12, 6, 5), (1, 1, 1), (0.0, 0.0, 0.5), 2),
     ("bcc2", (12, 6, 5), (1, 1, 1), (0.0, 0.0, 0.5), 4),
     ("sc_open", (9, 4, 4), (0, 0, 0), (0.2, 0.0, 2.0), 3),
     ("tri_two_shell", (10, 8, 1), (1, 1, 0), (0.0, 0.0, 1.0), 2),
 ])
-def test_slabs_equal_unsplit_run(cuda, golden_models, name, L, pbc, B, world):
+def test_slabs_equal_unsplit_run(cuda, golden_models, name, L, pbc, B, world, precision):
     from magex_gb300.lattice import Supercell
     from magex_gb300.llg import GB300LLG
     from magex_gb300.slab import LoopbackTransport, SlabLLG, SlabRun
@@ -23,13 +24,13 @@ def test_slabs_equal_unsplit_run(cuda, golden_models, name, L, pbc, B, world):
     alpha, dt, T, seed, steps = 0.1, 1e-4, 150.0, 17, 12
     sc = Supercell(uc, L, pbc, B)
     e0 = sc.init_spins("random", seed=3)
-    full = GB300LLG(sc, alpha, dt, T, seed)
+    full = GB300LLG(sc, alpha, dt, T, seed, precision=precision)
     lat = full.model.to_lattice(e0)
     full.run_lattice(lat, steps)
     ref = full.model.from_lattice(lat).cpu().numpy()
     ref_obs = full.model.observables(lat).cpu().numpy()
 
-    slabs = [SlabLLG(uc, L, pbc, B, alpha, dt, T, seed, r, world) for r in range(world)]
+    slabs = [SlabLLG(uc, L, pbc, B, alpha, dt, T, seed, r, world, precision=precision) for r in range(world)]
     run = SlabRun(slabs, LoopbackTransport())
     lats = [sl.scatter(e0) for sl in slabs]
     run.run(lats, steps)
