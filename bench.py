@@ -164,7 +164,7 @@ def read_ncu_traffic():
     return out
 
 
-def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None):
+def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None, precision="fp64"):
     """Uneven-film ensemble: 256 triangular films L in {32, 48, ..., 256}, J1 = 1 meV, interfacial DMI
     D/J = 0.3, K = 0.05 meV, B_z ~ U[0, 3] T, T ~ U[0, 20] K, alpha 0.1, dt 0.1 fs, Philox, seeded.
     Times the batched form (one persistent launch per stage, graph replays, autotuned launch shape)
@@ -178,7 +178,7 @@ def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None):
     Ts = [s["T"] for s in spec]
     seeds = list(range(1, nsys + 1))
     e0 = [sc.init_spins("random", seed=k) for k, sc in enumerate(films)]
-    ens = BatchedLLG(films, 0.1, 1e-4, Ts, seeds)
+    ens = BatchedLLG(films, 0.1, 1e-4, Ts, seeds, precision=precision)
     ens.set_spins(e0)
     ens.set_triangles([triangle_list(sc) for sc in films])
     best, timings = ens.autotune(steps=3)
@@ -194,7 +194,7 @@ def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None):
     t_batch = a.elapsed_time(b) * 1e-3
     rows = ens.rows()
     Q = ens.topological_charge()
-    sols = [GB300LLG(sc, 0.1, 1e-4, Ts[k], seeds[k]) for k, sc in enumerate(films)]
+    sols = [GB300LLG(sc, 0.1, 1e-4, Ts[k], seeds[k], precision=precision) for k, sc in enumerate(films)]
     lats = [sol.model.to_lattice(e0[k]) for k, sol in enumerate(sols)]
     for sol, lat in zip(sols, lats):
         sol.run_lattice(lat, 2)
@@ -209,7 +209,8 @@ def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None):
     v_plain = ntot * K_plain / t_plain
     return {"workload": f"{nsys} triangular films, L in {{32,48,...,256}} (uneven, {ntot:,} spins in total), "
                         "J1=1 meV, interfacial DMI D/J=0.3, K=0.05 meV, B_z~U[0,3] T, T~U[0,20] K, alpha 0.1, "
-                        "dt 0.1 fs, Philox, FP64",
+                        "dt 0.1 fs, Philox, FP64" + (" with the exact fixed-point exchange sum (batched and plain)"
+                                                     if precision == "fp64_fixed" else ""),
             "value": v_batch, "unit": UNIT, "steps": K_batch, "plain_value": v_plain, "plain_steps": K_plain,
             "speedup_vs_plain": v_batch / v_plain, "launch": {"threads": best[0], "ctas_per_sm": best[1]},
             "autotune_ms_per_step": {f"{t}x{c}": round(v, 4) for (t, c), v in timings.items()},
@@ -277,7 +278,7 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
             "grad_J1_D": [float(x) for x in g]}
 
 
-def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
+def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0, precision="fp64"):
     """Large batched + adjoint workload: nsys two-site bcc L^3 systems (524,288 spins each at L = 64),
     4 shells (8+6+12+24) with one seeded full 3x3 tensor per shell (iso 20/10/-1/1 meV, 1% anisotropic,
     DMI 5% of |J|), transposed on reverse bonds, SIA K = 0.01 meV, B = (0, 0, 0.5) T, T ~ U[0, 600] K,
@@ -294,7 +295,7 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
     sc = bcc_two_site(L=L, J=(20.0, 10.0, -1.0, 1.0), dmi_frac=0.05, per="shell", seed=1, field=FIELD)
     stream = torch.cuda.current_stream()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ens = BatchedLLG([sc] * nsys, ALPHA, DT, Ts, list(range(1, nsys + 1)))
+    ens = BatchedLLG([sc] * nsys, ALPHA, DT, Ts, list(range(1, nsys + 1)), precision=precision)
     ens.set_spins([sc.init_spins("random", seed=k) for k in range(nsys)])
     ens.run(2, graph_chunk=2)
     torch.cuda.synchronize()
@@ -305,7 +306,7 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
     t_batch = a.elapsed_time(b) * 1e-3
     rows = ens.rows()
     del ens
-    sols = [GB300LLG(sc, ALPHA, DT, Ts[k], 1 + k) for k in range(nsys)]
+    sols = [GB300LLG(sc, ALPHA, DT, Ts[k], 1 + k, precision=precision) for k in range(nsys)]
     lats = [sol.model.to_lattice(sc.init_spins("random", seed=k)) for k, sol in enumerate(sols)]
     for sol, lat in zip(sols, lats):
         sol.run_lattice(lat, 1)
@@ -319,6 +320,15 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
     del sols, lats
     torch.cuda.empty_cache()
     ntot = nsys * sc.N
+    head = {"workload": f"{nsys} two-site bcc {L}^3 systems ({ntot:,} spins), 4 shells 8+6+12+24 with seeded "
+                        "per-shell full 3x3 tensors (iso 20/10/-1/1 meV, 1% anisotropic, DMI 5%), K=0.01 meV, "
+                        "B=(0,0,0.5) T, T~U[0,600] K, alpha 0.05, dt 0.1 fs, Philox, FP64" +
+                        (" with the exact fixed-point exchange sum" if precision == "fp64_fixed" else ""),
+            "batched_value": ntot * K / t_batch, "plain_value": ntot * K / t_plain, "unit": UNIT, "steps": K,
+            "speedup_vs_plain": t_plain / t_batch, "batched_ms_per_step": 1e3 * t_batch / K,
+            "final_mean_E_per_spin": float(np.mean(rows[:, 1]))}
+    if adj_steps <= 0:
+        return head
 
     groups = CouplingGroups.per_shell(sc)
     free, _ = torch.cuda.mem_get_info()
@@ -354,12 +364,7 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0):
     once(False)
     loss, g = once(True)
     t = [ev[0].elapsed_time(ev[k]) for k in range(1, 5)]
-    return {"workload": f"{nsys} two-site bcc {L}^3 systems ({ntot:,} spins), 4 shells 8+6+12+24 with seeded "
-                        "per-shell full 3x3 tensors (iso 20/10/-1/1 meV, 1% anisotropic, DMI 5%), K=0.01 meV, "
-                        "B=(0,0,0.5) T, T~U[0,600] K, alpha 0.05, dt 0.1 fs, Philox, FP64",
-            "batched_value": ntot * K / t_batch, "plain_value": ntot * K / t_plain, "unit": UNIT, "steps": K,
-            "speedup_vs_plain": t_plain / t_batch, "batched_ms_per_step": 1e3 * t_batch / K,
-            "final_mean_E_per_spin": float(np.mean(rows[:, 1])),
+    return {**head,
             "adjoint": {"system": f"one {L}^3 system ({sc.N:,} spins) at 300 K", "steps": adj_steps,
                         "loss": "mean energy per spin after the trajectory (meV)",
                         "parameters": "4 shell tensors (36 entries), canonical and transposed bonds",
@@ -606,6 +611,7 @@ def run_gb300(args):
         line["fp64_fixed_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "fp64_fixed")
     if ws == 1 and not args.no_batched:
         line["batched"] = bench_batched()
+        line["batched_fp64_fixed"] = bench_batched(precision="fp64_fixed")
     if ws == 1 and not args.no_adjoint:
         line["adjoint"] = bench_adjoint()
         # the same trajectory with the default checkpoint policy: segments resident in up to half the
@@ -614,6 +620,7 @@ def run_gb300(args):
         line["adjoint_large"] = bench_adjoint(L=1024, nsteps=200, seg=50)
     if ws == 1 and not args.no_batched and not args.no_adjoint:
         line["large_batched_adjoint"] = bench_config5()
+        line["large_batched_fp64_fixed"] = bench_config5(precision="fp64_fixed", adj_steps=0)
     if ws == 1 and not args.no_batched:
         line["monte_carlo"] = bench_mc(L=args.L, cpu_baseline=not args.no_cpu_baseline)
         line["monte_carlo_fp64_fixed"] = bench_mc(L=args.L, cpu_baseline=False, precision="fp64_fixed")
@@ -661,9 +668,10 @@ def main():
             out = [bench_mc(L=args.L, sweeps=min(args.steps, 100), cpu_baseline=False, precision=p)
                    for p in ("fp64", "fp64_fixed")]
         elif args.only == "config5":
-            out = bench_config5(K=min(args.steps, 50), adj_steps=args.adjoint_steps or 1000)
+            out = [bench_config5(K=min(args.steps, 50), adj_steps=args.adjoint_steps or 1000),
+                   bench_config5(K=min(args.steps, 50), adj_steps=0, precision="fp64_fixed")]
         else:
-            out = bench_batched()
+            out = [bench_batched(), bench_batched(precision="fp64_fixed")]
         print(json.dumps(out), flush=True)
         return
     if args.impl == "reference":

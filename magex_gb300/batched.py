@@ -40,11 +40,14 @@ class BatchedLLG:
     """An ensemble of independent Heun / Depondt LLG systems stepped by shared launches."""
 
     def __init__(self, systems, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
-                 integrator="heun", noise="philox", device=None):
+                 integrator="heun", noise="philox", precision="fp64", device=None):
         if integrator not in _SUPPORTED:
             raise NotImplementedError(f"integrator '{integrator}' is not implemented by the GB300 kernels")
         if noise not in ("philox", "host"):
             raise ValueError("noise must be 'philox' or 'host'")
+        if precision not in ("fp64", "fp64_fixed"):
+            raise ValueError("batched systems use precision 'fp64' or 'fp64_fixed'")
+        self.precision = precision
         self.systems = [supercell_from_system(s) for s in systems]
         n = len(self.systems)
         if n == 0:
@@ -73,6 +76,7 @@ class BatchedLLG:
             p.integrator = _SUPPORTED[integrator]
             p.noise = _lib.NOISE_HOST if noise == "host" else _lib.NOISE_PHILOX
             p.seed = _philox_key(seeds[k])
+            p.precision = _lib.PRECISION_FP64_FIXED_GATHER if precision == "fp64_fixed" else _lib.PRECISION_FP64
         handles = (C.c_void_p * n)(*[m.handle.value for m in self.models])
         h = C.c_void_p()
         with torch.cuda.device(self.device):

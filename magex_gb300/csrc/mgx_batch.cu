@@ -15,8 +15,8 @@
 #include <numeric>
 #include <vector>
 
+#include "mgx_fx_step.cuh"
 #include "mgx_observe.cuh"
-#include "mgx_step.cuh"
 
 namespace mgx {
 
@@ -24,6 +24,7 @@ struct BatchSys {
   DevLattice L;
   DevLLG P;
   long long off3;   // offset of the system's spin block in doubles (3 * site offset)
+  DevFX F;          // fixed-point gather tables and split arrays (MGX_PRECISION_FP64_FIXED_GATHER)
 };
 
 struct StepArg {
@@ -68,11 +69,15 @@ struct Batch {
   int graph_chunk = 0;
   const double* graph_e = nullptr;
   int graph_threads = 0, graph_grid = 0;
+  // exact fixed-point exchange sums (every system of the batch, or none)
+  bool fixed = false;
+  std::vector<void*> fx_blocks;
+  int2* fx_split = nullptr;           // es | eps of all systems (2 * 3 * ntot)
 };
 
 constexpr int BATCH_MAX_THREADS = 512;
 
-template <int STAGE, int NOISE, int INTEG>
+template <int STAGE, int NOISE, int INTEG, bool FIXED>
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch_stage(const BatchSys* __restrict__ sys,
                                                                    const int2* __restrict__ tiles, int ntiles,
                                                                    double* __restrict__ e,
@@ -85,6 +90,11 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch_stage(const BatchSy
     if (q >= S.L.N) continue;
     double* es = e + S.off3;
     const double* ns = noise ? noise + S.off3 : nullptr;
+    if (FIXED) {
+      if (STAGE == 0) fx_predict_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER>(S.L, S.P, S.F, es, ns, q, st);
+      else fx_correct_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER>(S.L, S.P, S.F, es, ns, q, st);
+      continue;
+    }
     const int W = S.L.width;
     if (STAGE == 0) {
       if (W == 1) predict_site<1, NOISE, INTEG>(S.L, S.P, es, ns, q, st);
@@ -217,8 +227,13 @@ static int grid_size(const Batch* b) {
 template <int NOISE, int INTEG>
 static void enqueue_batch(const Batch* b, double* e, const double* noise, StepArg step, cudaStream_t st) {
   const int grid = grid_size(b);
-  k_batch_stage<0, NOISE, INTEG><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
-  k_batch_stage<1, NOISE, INTEG><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
+  if (b->fixed) {
+    k_batch_stage<0, NOISE, INTEG, true><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
+    k_batch_stage<1, NOISE, INTEG, true><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
+  } else {
+    k_batch_stage<0, NOISE, INTEG, false><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
+    k_batch_stage<1, NOISE, INTEG, false><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
+  }
 }
 
 static void enqueue_batch_step(const Batch* b, double* e, const double* noise, StepArg step, cudaStream_t st) {
@@ -266,7 +281,10 @@ mgx_status mgx_batch_create(const mgx_model* const* models, const mgx_llg_params
     const mgx_llg_params& p = params[k];
     if (!(p.dt > 0.0)) return set_error(MGX_ERR_INVALID, "system %d: dt must be positive", k);
     if (p.alpha_site) return set_error(MGX_ERR_INVALID, "system %d: batched systems take a uniform alpha", k);
-    if (p.precision != MGX_PRECISION_FP64) return set_error(MGX_ERR_INVALID, "batched systems use the FP64 gather");
+    if (p.precision != params[0].precision)
+      return set_error(MGX_ERR_INVALID, "all systems of a batch share the precision form");
+    if (p.precision != MGX_PRECISION_FP64 && p.precision != MGX_PRECISION_FP64_FIXED_GATHER)
+      return set_error(MGX_ERR_UNSUPPORTED, "batched systems use the FP64 (0) or FP64 fixed-point-gather (3) form");
     if (p.noise != params[0].noise || p.integrator != params[0].integrator)
       return set_error(MGX_ERR_INVALID, "all systems of a batch share the noise mode and the integrator");
     if (p.integrator != MGX_INTEGRATOR_HEUN && p.integrator != MGX_INTEGRATOR_DEPONDT)
@@ -329,6 +347,26 @@ mgx_status mgx_batch_create(const mgx_model* const* models, const mgx_llg_params
     mgx_batch_destroy(reinterpret_cast<mgx_batch*>(b));
     return cuda_error(err, "mgx_batch_create params");
   }
+  if (params[0].precision == MGX_PRECISION_FP64_FIXED_GATHER) {
+    b->fixed = true;
+    err = cudaMalloc(&b->fx_split, sizeof(int2) * 6 * (size_t)b->ntot);
+    if (err != cudaSuccess) {
+      mgx_batch_destroy(reinterpret_cast<mgx_batch*>(b));
+      return cuda_error(err, "mgx_batch_create fixed-point split");
+    }
+    for (int k = 0; k < nsys; ++k) {
+      BatchSys& S = b->host_sys[k];
+      void* blk = nullptr;
+      const mgx_status fst = fx_build(b->models[k], 28, true, 0, &S.F, &blk);
+      if (blk) b->fx_blocks.push_back(blk);
+      if (fst != MGX_OK) {
+        mgx_batch_destroy(reinterpret_cast<mgx_batch*>(b));
+        return fst;
+      }
+      S.F.es = b->fx_split + 3 * b->offset[k];
+      S.F.eps = b->fx_split + 3 * b->ntot + 3 * b->offset[k];
+    }
+  }
   mgx_status st = upload_sys(b);
   if (st == MGX_OK) st = build_tiles(b);
   if (st != MGX_OK) {
@@ -357,6 +395,8 @@ mgx_status mgx_batch_destroy(mgx_batch* bb) {
   cudaFree(b->d_tri_tile_begin);
   cudaFree(b->d_tri_off);
   cudaFree(b->tri_partials);
+  for (void* p : b->fx_blocks) cudaFree(p);
+  cudaFree(b->fx_split);
   delete b;
   return MGX_OK;
 }
@@ -411,6 +451,7 @@ mgx_status mgx_batch_step(mgx_batch* bb, double* e, const double* noise, uint64_
   Batch* b = reinterpret_cast<Batch*>(bb);
   if (!b || !e) return set_error(MGX_ERR_INVALID, "mgx_batch_step: null argument");
   if (b->noise == MGX_NOISE_HOST && !noise) return set_error(MGX_ERR_INVALID, "host-noise batch needs a noise buffer");
+  if (b->fixed) enqueue_fx_split_n(e, b->fx_split, 3 * b->ntot, 28, (cudaStream_t)stream);
   enqueue_batch_step(b, e, noise, StepArg{nullptr, step}, (cudaStream_t)stream);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
@@ -422,6 +463,7 @@ mgx_status mgx_batch_run(mgx_batch* bb, double* e, int64_t nsteps, uint64_t step
   if (nsteps < 0) return set_error(MGX_ERR_INVALID, "nsteps must be >= 0");
   if (b->noise == MGX_NOISE_HOST) return set_error(MGX_ERR_INVALID, "host-noise batches step one at a time");
   cudaStream_t st = (cudaStream_t)stream;
+  if (b->fixed && nsteps > 0) enqueue_fx_split_n(e, b->fx_split, 3 * b->ntot, 28, st);
   int64_t done = 0;
   if (graph_chunk > 0 && nsteps >= graph_chunk) {
     if (!b->graph || b->graph_chunk != graph_chunk || b->graph_e != e || b->graph_threads != b->threads ||

@@ -1,0 +1,197 @@
+// Per-site bodies of the fixed-point-gather step forms (MGX_PRECISION_INT48_GATHER and
+// MGX_PRECISION_FP64_FIXED_GATHER), shared by the single-lattice kernels (mgx_llg_fx.cu) and the
+// batched ensemble (mgx_batch.cu).  See mgx_llg_fx.cu for the arithmetic.
+#pragma once
+
+#include "mgx_dfp.cuh"
+#include "mgx_fx.cuh"
+#include "mgx_step.cuh"
+
+namespace mgx {
+
+// 48-bit form: field as (hi, lo) float pairs in tesla
+__device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
+                                          long long q, int s, int c0, int c1, int c2, dfp h[3]) {
+  FxAcc a;
+  fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
+  const float sc = (float)F.scale[s];            // >= 2^-100 (checked when the tables are built)
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    // value = (hh + x 2^-24) 2^(sigma - 48); fold x in with rounding, then split into two floats
+    const long long v = a.hh[c] + ((a.x[c] + (1LL << 23)) >> 24);
+    const float hi = __ll2float_rn(v);
+    const float lo = __ll2float_rn(v - __float2ll_rn(hi));
+    h[c] = {__fmul_rn(hi, sc), __fmul_rn(lo, sc)};
+  }
+}
+
+// 56-bit form: field in FP64, (hh + x 2^-28) 2^(sigma - 56) with one final rounding
+__device__ __forceinline__ void fx_gather64(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
+                                            long long q, int s, int c0, int c1, int c2, double h[3]) {
+  FxAcc a;
+  fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
+  const double sc = F.scale[s];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) h[c] = fma((double)a.x[c], 3.7252902984619141e-9, (double)a.hh[c]) * sc;
+}
+
+// spin of the site as a (hi, lo) float pair from its fixed-point halves (exact)
+__device__ __forceinline__ dfp fx_spin(int2 v) {
+  return {__fmul_rn((float)v.x, 5.9604644775390625e-8f), __fmul_rn((float)v.y, 3.552713678800501e-15f)};
+}
+
+template <int NOISE>
+__device__ __forceinline__ void fx_thermal(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                           const double* __restrict__ noise, long long q, int s, uint64_t step,
+                                           dfp B[3]) {
+  if (NOISE == MGX_NOISE_NONE) return;
+  double g[3];
+  if (NOISE == MGX_NOISE_HOST) {
+    g[0] = __ldg(noise + q);
+    g[1] = __ldg(noise + L.N + q);
+    g[2] = __ldg(noise + 2 * L.N + q);
+  } else {
+    philox_normal3(P.seed, magex_site(L, q, s), step, g[0], g[1], g[2]);   // FP32 draws: exact as floats
+  }
+  if (NOISE == MGX_NOISE_PHILOX && !P.sigma_site) {
+    const dfp sg = dfp_of(F.sig[s]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) B[c] = dfp_add(B[c], dfp_mul(sg, {(float)g[c], 0.f}));
+  } else {
+    const double sig = P.sigma_site ? __ldg(P.sigma_site + q) : __ldg(P.sigma_sub + s);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float2 b = split_double(sig * g[c]);
+      B[c] = dfp_add(B[c], {b.x, b.y});
+    }
+  }
+}
+
+template <int NOISE>
+__device__ __forceinline__ void fx_rhs(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                       const int2* __restrict__ xs, const double* __restrict__ noise, long long q,
+                                       int s, int c0, int c1, int c2, uint64_t step, double f[3]) {
+  dfp B[3], e[3], fd[3];
+  fx_gather(L, F, xs, q, s, c0, c1, c2, B);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) B[c] = dfp_add(B[c], dfp_of(F.B[c]));
+  fx_thermal<NOISE>(L, P, F, noise, q, s, step, B);
+  const long long N = L.N;
+  e[0] = fx_spin(xs[q]);
+  e[1] = fx_spin(xs[N + q]);
+  e[2] = fx_spin(xs[2 * N + q]);
+  dfp_rhs(e, B, dfp_of(F.alpha[s]), dfp_of(F.pre[s]), P.precession != 0, fd);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) f[c] = dfp_double(fd[c]);
+}
+
+// FP64 field of the site from the integer gather (+ Zeeman and thermal): the 56-bit form's field, and
+// the field of the Depondt integrator for both forms
+template <int NOISE, int PREC>
+__device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                           const int2* __restrict__ xs, const double* __restrict__ noise,
+                                           long long q, int s, int c0, int c1, int c2, uint64_t step, double& bx,
+                                           double& by, double& bz) {
+  double h[3];
+  if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
+    fx_gather64(L, F, xs, q, s, c0, c1, c2, h);
+  } else {
+    dfp hp[3];
+    fx_gather(L, F, xs, q, s, c0, c1, c2, hp);
+    h[0] = dfp_double(hp[0]);
+    h[1] = dfp_double(hp[1]);
+    h[2] = dfp_double(hp[2]);
+  }
+  bx = h[0] + L.B0;
+  by = h[1] + L.B1;
+  bz = h[2] + L.B2;
+  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
+}
+
+// Predictor of site q (0 <= q < L.N) of the fixed-point forms: writes P.ep, P.k1 and the split F.eps at q.
+template <int NOISE, int INTEG, int PREC>
+__device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                                const double* __restrict__ e, const double* __restrict__ noise,
+                                                long long q, uint64_t step) {
+  constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
+  const long long N = L.N;
+  const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
+  if (L.pinned && L.pinned[q]) {
+    P.ep[q] = ex; P.ep[N + q] = ey; P.ep[2 * N + q] = ez;
+    P.k1[q] = 0.0; P.k1[N + q] = 0.0; P.k1[2 * N + q] = 0.0;
+    F.eps[q] = F.es[q]; F.eps[N + q] = F.es[N + q]; F.eps[2 * N + q] = F.es[2 * N + q];
+    return;
+  }
+  int s, c0, c1, c2;
+  site_coords(L, q, s, c0, c1, c2);
+  double f[3], x, y, z;
+  if (INTEG == MGX_INTEGRATOR_HEUN) {
+    if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
+      double bx, by, bz;
+      fx_field64<NOISE, PREC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
+      llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
+              f[2]);
+    } else {
+      fx_rhs<NOISE>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, f);
+    }
+    x = fma(P.dt, f[0], ex);
+    y = fma(P.dt, f[1], ey);
+    z = fma(P.dt, f[2], ez);
+    const double r = rsqrt(x * x + y * y + z * z);
+    x *= r; y *= r; z *= r;
+  } else {
+    double bx, by, bz;
+    fx_field64<NOISE, PREC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    double fx, fy, fz;
+    llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
+    f[0] = ey * fz - ez * fy; f[1] = ez * fx - ex * fz; f[2] = ex * fy - ey * fx;
+    x = ex; y = ey; z = ez;
+    rotate(x, y, z, P.dt * f[0], P.dt * f[1], P.dt * f[2]);
+  }
+  P.ep[q] = x; P.ep[N + q] = y; P.ep[2 * N + q] = z;
+  P.k1[q] = f[0]; P.k1[N + q] = f[1]; P.k1[2 * N + q] = f[2];
+  F.eps[q] = fx_split<LIMB>(x); F.eps[N + q] = fx_split<LIMB>(y); F.eps[2 * N + q] = fx_split<LIMB>(z);
+}
+
+// Corrector of site q: reads the neighbours' F.eps, P.k1 and e at q, writes e and its split F.es at q.
+template <int NOISE, int INTEG, int PREC>
+__device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
+                                                double* __restrict__ e, const double* __restrict__ noise, long long q,
+                                                uint64_t step) {
+  constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
+  if (L.pinned && L.pinned[q]) return;                 // e and its split stay as they are
+  const long long N = L.N;
+  int s, c0, c1, c2;
+  site_coords(L, q, s, c0, c1, c2);
+  const double k1x = P.k1[q], k1y = P.k1[N + q], k1z = P.k1[2 * N + q];
+  double x = e[q], y = e[N + q], z = e[2 * N + q];
+  if (INTEG == MGX_INTEGRATOR_HEUN) {
+    double f[3];
+    if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
+      const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
+      double bx, by, bz;
+      fx_field64<NOISE, PREC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
+      llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
+              f[2]);
+    } else {
+      fx_rhs<NOISE>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, f);
+    }
+    x = fma(P.half_dt, k1x + f[0], x);
+    y = fma(P.half_dt, k1y + f[1], y);
+    z = fma(P.half_dt, k1z + f[2], z);
+  } else {
+    const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
+    double bx, by, bz;
+    fx_field64<NOISE, PREC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    double fx, fy, fz;
+    llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
+    const double wx = py * fz - pz * fy, wy = pz * fx - px * fz, wz = px * fy - py * fx;
+    rotate(x, y, z, P.half_dt * (k1x + wx), P.half_dt * (k1y + wy), P.half_dt * (k1z + wz));
+  }
+  const double r = rsqrt(x * x + y * y + z * z);
+  x *= r; y *= r; z *= r;
+  e[q] = x; e[N + q] = y; e[2 * N + q] = z;
+  F.es[q] = fx_split<LIMB>(x); F.es[N + q] = fx_split<LIMB>(y); F.es[2 * N + q] = fx_split<LIMB>(z);
+}
+
+}  // namespace mgx
