@@ -456,6 +456,45 @@ def bench_sqw(L=128, reps=20):
                     f"case would hold {16 * sc.N * len(q) / 1e9:.0f} GB"}
 
 
+def bench_config1(steps=1000, cpu=True):
+    """Plain FP64 workload of the reference's CPU-runnable case: simple-cubic 16^3 (4,096 spins), 6
+    neighbours, J = 1 meV, mu = 2 mu_B, alpha 0.1, B = 0, T = 0, dt 0.1 fs, 1000 Heun steps from
+    random spins.  Small enough that launches dominate: run_lattice replays CUDA graphs of 32 steps."""
+    import torch
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results, make_model
+    sc = Supercell(load_results(make_model("sc", a=3.0, J=[1.0], moment=2.0)), (16, 16, 16))
+    e0 = sc.init_spins("random", seed=1)
+    out = {"workload": "sc 16^3 (4,096 spins), J = 1 meV, alpha 0.1, T = 0, dt 0.1 fs, 1000 Heun steps, FP64",
+           "unit": UNIT, "steps": steps}
+    for prec in ("fp64", "fp64_fixed"):
+        sol = GB300LLG(sc, 0.1, 1e-4, 0.0, 1, precision=prec)
+        lat = sol.model.to_lattice(e0)
+        sol.run_lattice(lat, 64)
+        stream = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        sol.run_lattice(lat, steps)
+        b.record(stream)
+        b.synchronize()
+        ms = a.elapsed_time(b)
+        out[prec] = {"value": sc.N * steps / (ms * 1e-3), "ms_total": ms, "us_per_step": 1e3 * ms / steps}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        from oracle import OracleLLG, max_threads
+        ora = OracleLLG(sc, 0.1, 1e-4, 0.0, 1, csr="stencil")
+        e = e0.copy()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ora.step_inplace(e)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sc.N * steps / el, "unit": UNIT, "cores": max_threads(), "kind": "port",
+                               "sample": f"the full {steps} steps, {el:.2f} s"}
+    return out
+
+
 def bench_reduced(L, K, warmup, precision):
     """The same workload with a reduced-FP64 step form: precision="df32" (exchange gather on compensated
     FP32 pairs) or "int48" (exchange gather in exact 48-bit fixed-point integer arithmetic); both keep
@@ -606,6 +645,7 @@ def run_gb300(args):
         "clocks": clocks,
     }
     if ws == 1:
+        line["config1_sc16"] = bench_config1(cpu=not args.no_cpu_baseline)
         line["df32_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "df32")
         line["int48_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "int48")
         line["fp64_fixed_gather_variant"] = bench_reduced(args.L, min(K, 200), args.warmup, "fp64_fixed")
@@ -645,7 +685,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
-    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "fp64_fixed", "config5", "mc", "sqw"],
+    ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "fp64_fixed", "config1", "config5", "mc",
+                                       "sqw"],
                     default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
@@ -662,6 +703,8 @@ def main():
             out = bench_adjoint(L=args.adjoint_L, nsteps=args.adjoint_steps or 2000)
         elif args.only in ("df32", "int48", "fp64_fixed"):
             out = bench_reduced(args.L, args.steps, args.warmup, args.only)
+        elif args.only == "config1":
+            out = bench_config1()
         elif args.only == "sqw":
             out = bench_sqw(L=args.L)
         elif args.only == "mc":

@@ -92,6 +92,8 @@ struct DevLLG {
   const double* sigma_site;  // [N] or nullptr
   double* ep;                // [3][N] predicted spins
   double* k1;                // [3][N] predictor slope (Heun) or rotation rate (Depondt)
+  // CUDA-graph replays: the Philox step index is *step_base + the launch's step argument
+  const unsigned long long* step_base = nullptr;
 };
 
 // Tables of the compensated-FP32 gather (MGX_PRECISION_DF32_GATHER): every coupling as 9 (hi, lo)
@@ -138,6 +140,14 @@ struct LLGPlan {
   double* site_block = nullptr;  // alpha_site | pre_site
   double* sigma_site = nullptr;
   double* scratch = nullptr;     // ep | k1
+  // captured step loop of mgx_llg_run (small lattices, where launches dominate)
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  unsigned long long* d_step = nullptr;
+  int graph_chunk = 0, graph_mode = -1;
+  const double* graph_e = nullptr;
+  double graph_B[3] = {0.0, 0.0, 0.0};
+  long long graph_offset = 0;
 };
 
 // Threads per block of the one-site-per-thread kernels: 256, or fewer for small lattices so that the

@@ -16,14 +16,14 @@ template <int W, int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_predict(const DevLattice L, const DevLLG P, const double* __restrict__ e,
                                                  const double* __restrict__ noise, uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) predict_site<W, NOISE, INTEG>(L, P, e, noise, q, step);
+  if (q < L.N) predict_site<W, NOISE, INTEG>(L, P, e, noise, q, P.step_base ? *P.step_base + step : step);
 }
 
 template <int W, int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_correct(const DevLattice L, const DevLLG P, double* __restrict__ e,
                                                  const double* __restrict__ noise, uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) correct_site<W, NOISE, INTEG>(L, P, e, noise, q, step);
+  if (q < L.N) correct_site<W, NOISE, INTEG>(L, P, e, noise, q, P.step_base ? *P.step_base + step : step);
 }
 
 // stages: bit 0 = predictor, bit 1 = corrector
@@ -85,6 +85,54 @@ static std::vector<T> site_to_lattice(const T* src, int ns, int ncell) {
     out[(long long)s * ncell + cell] = src[site];
   }
   return out;
+}
+
+// Small lattices are launch-bound: mgx_llg_run replays a CUDA graph of kGraphChunk steps whose kernels
+// read the Philox step index from a device counter (advanced by a one-thread kernel at the end of the
+// chunk), so every replay draws fresh noise and the trajectory equals the directly launched one.
+constexpr long long kGraphMaxSites = 1LL << 21;
+constexpr int kGraphChunk = 32;
+
+__global__ void k_llg_step_set(unsigned long long* c, unsigned long long v) { *c = v; }
+__global__ void k_llg_step_advance(unsigned long long* c, unsigned long long n) { *c += n; }
+
+static void drop_llg_graph(LLGPlan* pl) {
+  if (pl->graph) cudaGraphExecDestroy(pl->graph);
+  pl->graph = nullptr;
+  pl->graph_e = nullptr;
+  pl->graph_mode = -1;
+}
+
+static mgx_status llg_graph(LLGPlan* pl, double* e) {
+  const DevLattice& L = pl->model->d;
+  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
+  if (pl->graph && pl->graph_e == e && pl->graph_mode == mode && pl->graph_B[0] == L.B0 && pl->graph_B[1] == L.B1 &&
+      pl->graph_B[2] == L.B2 && pl->graph_offset == L.cell_offset)
+    return MGX_OK;
+  drop_llg_graph(pl);
+  if (!pl->d_step) MGX_CUDA_TRY(cudaMalloc(&pl->d_step, sizeof(unsigned long long)));
+  if (!pl->cap_stream) MGX_CUDA_TRY(cudaStreamCreateWithFlags(&pl->cap_stream, cudaStreamNonBlocking));
+  MGX_CUDA_TRY(cudaStreamBeginCapture(pl->cap_stream, cudaStreamCaptureModeThreadLocal));
+  pl->p.step_base = pl->d_step;
+  for (int k = 0; k < kGraphChunk; ++k) enqueue_llg_step(pl, e, nullptr, (uint64_t)k, pl->cap_stream, 3);
+  pl->p.step_base = nullptr;
+  k_llg_step_advance<<<1, 1, 0, pl->cap_stream>>>(pl->d_step, (unsigned long long)kGraphChunk);
+  cudaGraph_t g = nullptr;
+  cudaError_t err = cudaStreamEndCapture(pl->cap_stream, &g);
+  if (err != cudaSuccess) return cuda_error(err, "mgx_llg_run capture");
+  err = cudaGraphInstantiate(&pl->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (err != cudaSuccess) {
+    pl->graph = nullptr;
+    return cuda_error(err, "mgx_llg_run instantiate");
+  }
+  pl->graph_e = e;
+  pl->graph_mode = mode;
+  pl->graph_B[0] = L.B0;
+  pl->graph_B[1] = L.B1;
+  pl->graph_B[2] = L.B2;
+  pl->graph_offset = L.cell_offset;
+  return MGX_OK;
 }
 
 }  // namespace mgx
@@ -191,6 +239,9 @@ mgx_status mgx_llg_destroy(mgx_llg* pp) {
   cudaFree(pl->scratch);
   cudaFree(pl->df_block);
   cudaFree(pl->fx_block);
+  drop_llg_graph(pl);
+  if (pl->cap_stream) cudaStreamDestroy(pl->cap_stream);
+  cudaFree(pl->d_step);
   delete pl;
   return MGX_OK;
 }
@@ -268,8 +319,16 @@ mgx_status mgx_llg_run(mgx_llg* pp, double* e, int64_t nsteps, uint64_t step0, v
   if (nsteps < 0) return set_error(MGX_ERR_INVALID, "nsteps must be >= 0");
   if (pl->p.noise == MGX_NOISE_HOST)
     return set_error(MGX_ERR_INVALID, "mgx_llg_run: host-noise plans step one at a time (mgx_llg_step)");
-  if (nsteps > 0) enqueue_reduced_split(pl, e, (cudaStream_t)stream);
-  for (int64_t n = 0; n < nsteps; ++n) enqueue_llg_step(pl, e, nullptr, step0 + (uint64_t)n, (cudaStream_t)stream, 3);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nsteps > 0) enqueue_reduced_split(pl, e, st);
+  int64_t done = 0;
+  if (pl->model->d.N <= kGraphMaxSites && nsteps >= 2 * kGraphChunk) {
+    const mgx_status gs = llg_graph(pl, e);
+    if (gs != MGX_OK) return gs;
+    k_llg_step_set<<<1, 1, 0, st>>>(pl->d_step, (unsigned long long)step0);
+    for (; done + kGraphChunk <= nsteps; done += kGraphChunk) MGX_CUDA_TRY(cudaGraphLaunch(pl->graph, st));
+  }
+  for (; done < nsteps; ++done) enqueue_llg_step(pl, e, nullptr, step0 + (uint64_t)done, st, 3);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }

@@ -185,9 +185,10 @@ __global__ void __launch_bounds__(256) k_split(const double* __restrict__ x, flo
 template <int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_predict_df(const DevLattice L, const DevLLG P, const DevDF F,
                                                     const double* __restrict__ e, const double* __restrict__ noise,
-                                                    uint64_t step) {
+                                                    uint64_t step_arg) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
+  const uint64_t step = P.step_base ? *P.step_base + step_arg : step_arg;
   const long long N = L.N;
   const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
   if (L.pinned && L.pinned[q]) {
@@ -233,9 +234,10 @@ __global__ void __launch_bounds__(256) k_predict_df(const DevLattice L, const De
 template <int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_correct_df(const DevLattice L, const DevLLG P, const DevDF F,
                                                     double* __restrict__ e, const double* __restrict__ noise,
-                                                    uint64_t step) {
+                                                    uint64_t step_arg) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
+  const uint64_t step = P.step_base ? *P.step_base + step_arg : step_arg;
   if (L.pinned && L.pinned[q]) return;                 // e and its split stay as they are
   const long long N = L.N;
   int s, c0, c1, c2;

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const
                                                        const double* __restrict__ e, const double* __restrict__ noise,
                                                        uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) fx_predict_site<NOISE, INTEG, PREC>(L, P, F, e, noise, q, step);
+  if (q < L.N) fx_predict_site<NOISE, INTEG, PREC>(L, P, F, e, noise, q, P.step_base ? *P.step_base + step : step);
 }
 
 template <int NOISE, int INTEG, int PREC>
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const
                                                        double* __restrict__ e, const double* __restrict__ noise,
                                                        uint64_t step) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) fx_correct_site<NOISE, INTEG, PREC>(L, P, F, e, noise, q, step);
+  if (q < L.N) fx_correct_site<NOISE, INTEG, PREC>(L, P, F, e, noise, q, P.step_base ? *P.step_base + step : step);
 }
 
 template <int NOISE, int INTEG, int PREC>
