@@ -640,7 +640,8 @@ def run_gb300(args):
                           "peak_source": "measured live (mgx_measure_fp64_peak, DFMA loop)"},
         "kernels_ms": {"k_predict": pm, "k_correct": cm},
         "e2e": {"value": N * K * ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 24 * N,
-                "api": "GB300LLG.step(pinned host (N,3) float64) -> pinned host (N,3)"},
+                "api": "GB300LLG.step(pinned host (N,3) float64) -> pinned host (N,3): one mgx_llg_step_host call, "
+                       "copies in axis-0 slabs overlapping the stages"},
         "gpu_launches": 2 * K,
         "clocks": clocks,
     }

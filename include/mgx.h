@@ -189,6 +189,16 @@ mgx_status mgx_llg_run(mgx_llg* plan, double* e, int64_t nsteps, uint64_t step0,
  * corrector (reads ep, k1 and e, writes e).  For callers that exchange halos between the stages,
  * as magex's slab decomposition does (magex/mpi_spin.py:160-174: _fused1, halo(ep), _fused2, halo(e)). */
 mgx_status mgx_llg_stage(mgx_llg* plan, int32_t stage, double* e, const double* noise, uint64_t step, void* stream);
+/* One step of mgx_llg_step on host buffers: e_in and e_out are (N, 3) float64 spins in magex site
+ * order (the arrays magex's LLGSolver.step takes and returns, magex/llg.py:216-227; e_out may equal
+ * e_in).  Replaces the copy in, step and copy out that a Python caller would make, with the copies
+ * overlapping the stages when both buffers are page-locked (pinned) and the plan is an FP64
+ * stencil plan of at least 2^20 sites: the copies then run in axis-0 slabs on a copy stream of the
+ * plan, and the slabs' stages alternate between `stream` and a second stream of the plan.  Work
+ * enqueued on `stream` after this call, and a synchronisation of `stream`, follow all of it.  noise as for mgx_llg_step (device, lattice layout).  The plan keeps two device copies of
+ * the spins for this (6 N doubles) from the first call on. */
+mgx_status mgx_llg_step_host(mgx_llg* plan, const double* e_in, double* e_out, const double* noise, uint64_t step,
+                             void* stream);
 
 /* ---------------------------------------------------------------- batched ensemble
  * Many independent systems (replicas, temperature / field scans, different lattices, uneven sizes)

@@ -77,6 +77,7 @@ SIGNATURES = {
     "mgx_llg_step": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "mgx_llg_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]),
     "mgx_llg_stage": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "mgx_llg_step_host": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "mgx_measure_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
     "mgx_write_xyz": (C.c_int32, [C.c_char_p, C.c_int64, _dp, _dp, _dp, _ip, C.POINTER(C.c_char_p), C.c_int32,
                                   C.c_char_p, C.c_int32]),

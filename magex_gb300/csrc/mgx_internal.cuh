@@ -75,6 +75,7 @@ struct Model {
   int* slot_of_bond = nullptr;   // host [nbond]: position of input coupling b in the device table
   void* csr_block = nullptr;     // ptr | nbr | typ (neighbour-list layout)
   double* sign_site = nullptr;
+  int reach0 = -1;               // largest |R_0| of a coupling in layers (stencil layout), -1 for the list layout
 };
 
 // ------------------------------------------------------------------ LLG plan (mgx_llg.cu)
@@ -127,6 +128,9 @@ struct DevFX {
   int2* eps;                     // [3][N] fixed-point split of ep
 };
 
+// Axis-0 slabs a host-buffer step is split into (copies of one overlap the stages of another).
+#define MGX_HOST_CHUNKS 16
+
 struct LLGPlan {
   const Model* model;
   DevLLG p;
@@ -148,6 +152,12 @@ struct LLGPlan {
   const double* graph_e = nullptr;
   double graph_B[3] = {0.0, 0.0, 0.0};
   long long graph_offset = 0;
+  // step on host buffers (mgx_llg_step_host): device copies of the spins, the copy stream and a
+  // second compute stream (consecutive slabs run on alternate streams so each fills the other's tail)
+  cudaStream_t copy_stream = nullptr, aux_stream = nullptr;
+  double* host_lat = nullptr;    // [3][N] lattice layout
+  double* host_aos = nullptr;    // [N][3] magex order (staging of the copies)
+  cudaEvent_t host_ev[2 * MGX_HOST_CHUNKS + 4] = {};  // in[c] | out[c] | start | done | joined aux | joined main
 };
 
 // Threads per block of the one-site-per-thread kernels: 256, or fewer for small lattices so that the
@@ -164,6 +174,9 @@ inline float2 split_host(double x) {
   return make_float2(hi, (float)(x - (double)hi));
 }
 
+// magex-order (N, 3) rows [begin, begin + count) to / from the lattice layout, on st (mgx_model.cu).
+void enqueue_pack(const Model* m, const double* aos, double* lat, long long begin, long long count, cudaStream_t st);
+void enqueue_unpack(const Model* m, const double* lat, double* aos, long long begin, long long count, cudaStream_t st);
 // Enqueue the predictor (stages & 1) and / or the corrector (stages & 2) of one step on st.
 void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
 // Compensated-FP32 gather form (mgx_llg_df.cu): tables built at plan creation, the split copy of e

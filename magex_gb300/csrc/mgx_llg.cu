@@ -5,6 +5,7 @@
 // The predictor gathers the exchange field from e, adds on-site, Zeeman and thermal fields, stores
 // k1 and the normalised predicted spin ep; the corrector gathers from ep and writes e in place
 // (it reads only its own e, so the in-place update is race-free).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -12,49 +13,74 @@
 
 namespace mgx {
 
+// Sites begin + i (i < count) of sublattice blockIdx.y: the whole lattice is one row of N sites
+// (gridDim.y = 1, begin = 0), a range of cells one row of `count` cells per sublattice.
 template <int W, int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_predict(const DevLattice L, const DevLLG P, const double* __restrict__ e,
-                                                 const double* __restrict__ noise, uint64_t step) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) predict_site<W, NOISE, INTEG>(L, P, e, noise, q, P.step_base ? *P.step_base + step : step);
+                                                 const double* __restrict__ noise, uint64_t step, long long begin,
+                                                 long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count)
+    predict_site<W, NOISE, INTEG>(L, P, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+                                  P.step_base ? *P.step_base + step : step);
 }
 
 template <int W, int NOISE, int INTEG>
 __global__ void __launch_bounds__(256) k_correct(const DevLattice L, const DevLLG P, double* __restrict__ e,
-                                                 const double* __restrict__ noise, uint64_t step) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) correct_site<W, NOISE, INTEG>(L, P, e, noise, q, P.step_base ? *P.step_base + step : step);
+                                                 const double* __restrict__ noise, uint64_t step, long long begin,
+                                                 long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count)
+    correct_site<W, NOISE, INTEG>(L, P, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+                                  P.step_base ? *P.step_base + step : step);
 }
+
+// Cells [cb, cb + cn) of every sublattice (cn = ncell: the whole lattice in one row).
+struct CellRange {
+  long long cb, cn;
+};
 
 // stages: bit 0 = predictor, bit 1 = corrector
 template <int W, int NOISE, int INTEG>
 static void launch_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages,
-                        cudaStream_t st) {
+                        cudaStream_t st, CellRange r) {
   const DevLattice& L = pl->model->d;
-  const int tpb = site_block_size(L.N);
-  const unsigned grid = (unsigned)((L.N + tpb - 1) / tpb);
-  if (stages & 1) k_predict<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step);
-  if (stages & 2) k_correct<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step);
+  const bool whole = r.cb == 0 && r.cn == L.ncell;
+  const long long count = whole ? L.N : r.cn;
+  const int tpb = site_block_size(whole ? L.N : r.cn * L.ns);
+  const dim3 grid((unsigned)((count + tpb - 1) / tpb), whole ? 1u : (unsigned)L.ns);
+  if (stages & 1) k_predict<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
+  if (stages & 2) k_correct<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
 }
 
 template <int W, int NOISE>
 static void dispatch_integ(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages,
-                           cudaStream_t st) {
+                           cudaStream_t st, CellRange r) {
   if (pl->p.integrator == MGX_INTEGRATOR_DEPONDT)
-    launch_step<W, NOISE, MGX_INTEGRATOR_DEPONDT>(pl, e, noise, step, stages, st);
+    launch_step<W, NOISE, MGX_INTEGRATOR_DEPONDT>(pl, e, noise, step, stages, st, r);
   else
-    launch_step<W, NOISE, MGX_INTEGRATOR_HEUN>(pl, e, noise, step, stages, st);
+    launch_step<W, NOISE, MGX_INTEGRATOR_HEUN>(pl, e, noise, step, stages, st, r);
 }
 
 template <int W>
 static void dispatch_noise(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages,
-                           cudaStream_t st) {
+                           cudaStream_t st, CellRange r) {
   // sigma = 0 everywhere: the thermal field is exactly zero, skip generating it
   const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
   switch (mode) {
-    case MGX_NOISE_HOST: dispatch_integ<W, MGX_NOISE_HOST>(pl, e, noise, step, stages, st); break;
-    case MGX_NOISE_PHILOX: dispatch_integ<W, MGX_NOISE_PHILOX>(pl, e, noise, step, stages, st); break;
-    default: dispatch_integ<W, MGX_NOISE_NONE>(pl, e, noise, step, stages, st); break;
+    case MGX_NOISE_HOST: dispatch_integ<W, MGX_NOISE_HOST>(pl, e, noise, step, stages, st, r); break;
+    case MGX_NOISE_PHILOX: dispatch_integ<W, MGX_NOISE_PHILOX>(pl, e, noise, step, stages, st, r); break;
+    default: dispatch_integ<W, MGX_NOISE_NONE>(pl, e, noise, step, stages, st, r); break;
+  }
+}
+
+// FP64 stages on the cells [r.cb, r.cb + r.cn) of every sublattice
+static void enqueue_fp64_range(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st,
+                               int stages, CellRange r) {
+  switch (pl->model->d.width) {
+    case 1: dispatch_noise<1>(pl, e, noise, step, stages, st, r); break;
+    case 4: dispatch_noise<4>(pl, e, noise, step, stages, st, r); break;
+    default: dispatch_noise<9>(pl, e, noise, step, stages, st, r); break;
   }
 }
 
@@ -68,11 +94,7 @@ void enqueue_llg_step(const LLGPlan* pl, double* e, const double* noise, uint64_
     enqueue_df_step(pl, e, noise, step, st, stages);
     return;
   }
-  switch (pl->model->d.width) {
-    case 1: dispatch_noise<1>(pl, e, noise, step, stages, st); break;
-    case 4: dispatch_noise<4>(pl, e, noise, step, stages, st); break;
-    default: dispatch_noise<9>(pl, e, noise, step, stages, st); break;
-  }
+  enqueue_fp64_range(pl, e, noise, step, st, stages, CellRange{0, pl->model->d.ncell});
 }
 
 template <typename T>
@@ -133,6 +155,28 @@ static mgx_status llg_graph(LLGPlan* pl, double* e) {
   pl->graph_B[2] = L.B2;
   pl->graph_offset = L.cell_offset;
   return MGX_OK;
+}
+
+static bool pinned_host(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+static void drop_host_buffers(LLGPlan* pl) {
+  cudaFree(pl->host_lat);
+  cudaFree(pl->host_aos);
+  pl->host_lat = pl->host_aos = nullptr;
+  for (cudaEvent_t& ev : pl->host_ev) {
+    if (ev) cudaEventDestroy(ev);
+    ev = nullptr;
+  }
+  if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
+  if (pl->aux_stream) cudaStreamDestroy(pl->aux_stream);
+  pl->copy_stream = pl->aux_stream = nullptr;
 }
 
 }  // namespace mgx
@@ -242,6 +286,7 @@ mgx_status mgx_llg_destroy(mgx_llg* pp) {
   drop_llg_graph(pl);
   if (pl->cap_stream) cudaStreamDestroy(pl->cap_stream);
   cudaFree(pl->d_step);
+  drop_host_buffers(pl);
   delete pl;
   return MGX_OK;
 }
@@ -297,6 +342,104 @@ mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t st
     return set_error(MGX_ERR_INVALID, "mgx_llg_step: host-noise plan needs a noise buffer");
   enqueue_reduced_split(pl, e, (cudaStream_t)stream);
   enqueue_llg_step(pl, e, noise, step, (cudaStream_t)stream, 3);
+  MGX_CUDA_TRY(cudaGetLastError());
+  return MGX_OK;
+}
+
+// Copies of host buffers inside one step.  The input goes to the device in axis-0 slabs on the plan's
+// copy stream (each packed into the lattice layout as it lands); the predictor of a slab starts once
+// the slabs it gathers from (its own and its neighbours', every slab at least as thick as the
+// couplings' reach) are in; the corrector runs slab by slab and each finished slab goes back to the
+// host while the next ones are computed.  Consecutive slabs alternate between the caller's stream and
+// a second compute stream, so the blocks of one slab fill the tail of the previous one.  The
+// predictor and corrector kernels, and so the result, are those of mgx_llg_step: only the launch grid
+// is split.
+mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, const double* noise, uint64_t step,
+                             void* stream) {
+  LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
+  if (!pl || !e_in || !e_out) return set_error(MGX_ERR_INVALID, "mgx_llg_step_host: null argument");
+  if (pl->p.noise == MGX_NOISE_HOST && !noise)
+    return set_error(MGX_ERR_INVALID, "mgx_llg_step_host: host-noise plan needs a noise buffer");
+  const Model* m = pl->model;
+  const DevLattice& L = m->d;
+  const long long N = L.N;
+  cudaStream_t ms = (cudaStream_t)stream;
+  if (!pl->copy_stream) {
+    // all or nothing: a failed allocation leaves the plan without host buffers
+    cudaError_t err = cudaMalloc(&pl->host_lat, sizeof(double) * 3 * N);
+    if (err == cudaSuccess) err = cudaMalloc(&pl->host_aos, sizeof(double) * 3 * N);
+    for (cudaEvent_t& ev : pl->host_ev)
+      if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->aux_stream, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
+    if (err != cudaSuccess) {
+      drop_host_buffers(pl);
+      return cuda_error(err, "mgx_llg_step_host buffers");
+    }
+  }
+  cudaStream_t cs = pl->copy_stream;
+  cudaEvent_t* ev_in = pl->host_ev;
+  cudaEvent_t* ev_out = pl->host_ev + MGX_HOST_CHUNKS;
+  cudaEvent_t ev_start = pl->host_ev[2 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[2 * MGX_HOST_CHUNKS + 1];
+  cudaEvent_t ev_join_aux = pl->host_ev[2 * MGX_HOST_CHUNKS + 2], ev_join_main = pl->host_ev[2 * MGX_HOST_CHUNKS + 3];
+  // slabs: FP64 stencil plans of at least 2^20 sites with both buffers page-locked; otherwise one piece
+  int nc = 1;
+  if (pl->precision == MGX_PRECISION_FP64 && L.layout == 0 && m->reach0 >= 0 && N >= (1LL << 20) &&
+      pinned_host(e_in) && pinned_host(e_out)) {
+    nc = std::min(MGX_HOST_CHUNKS, L.L0 / std::max(m->reach0, 1));
+    if (nc < 3) nc = 1;
+  }
+  const long long layer = (long long)L.L1 * L.L2;
+  auto cell0 = [&](int c) { return (long long)L.L0 * c / nc * layer; };    // first cell of slab c
+  MGX_CUDA_TRY(cudaEventRecord(ev_start, ms));
+  MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_start, 0));
+  for (int c = 0; c < nc; ++c) {
+    const long long sb = (nc == 1 ? 0 : cell0(c) * L.ns), se = (nc == 1 ? N : cell0(c + 1) * L.ns);
+    MGX_CUDA_TRY(cudaMemcpyAsync(pl->host_aos + 3 * sb, e_in + 3 * sb, sizeof(double) * 3 * (se - sb),
+                                 cudaMemcpyDefault, cs));
+    enqueue_pack(m, pl->host_aos, pl->host_lat, sb, se - sb, cs);
+    MGX_CUDA_TRY(cudaEventRecord(ev_in[c], cs));
+  }
+  double* lat = pl->host_lat;
+  if (nc == 1) {
+    MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_in[0], 0));
+    enqueue_reduced_split(pl, lat, ms);
+    enqueue_llg_step(pl, lat, noise, step, ms, 3);
+    enqueue_unpack(m, lat, pl->host_aos, 0, N, ms);
+    MGX_CUDA_TRY(cudaEventRecord(ev_out[0], ms));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_out[0], 0));
+    MGX_CUDA_TRY(cudaMemcpyAsync(e_out, pl->host_aos, sizeof(double) * 3 * N, cudaMemcpyDefault, cs));
+  } else {
+    cudaStream_t run[2] = {ms, pl->aux_stream};
+    MGX_CUDA_TRY(cudaStreamWaitEvent(run[1], ev_start, 0));
+    // predictors: slab c gathers from slabs c-1 .. c+1 (cyclically when axis 0 is periodic); the
+    // copies land in slab order, so waiting for the last slab needed is enough
+    const bool ring = L.pbc0 != 0;
+    for (int k = 0; k < nc; ++k) {
+      const int c = ring ? (k + 1) % nc : k;
+      cudaStream_t st = run[k & 1];
+      MGX_CUDA_TRY(cudaStreamWaitEvent(st, ev_in[c == 0 && ring ? nc - 1 : std::min(c + 1, nc - 1)], 0));
+      enqueue_fp64_range(pl, lat, noise, step, st, 1, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
+    }
+    // every corrector gathers the predicted spins of its neighbours: both streams pass all predictors
+    MGX_CUDA_TRY(cudaEventRecord(ev_join_aux, run[1]));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_join_aux, 0));
+    MGX_CUDA_TRY(cudaEventRecord(ev_join_main, ms));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(run[1], ev_join_main, 0));
+    for (int c = 0; c < nc; ++c) {
+      cudaStream_t st = run[c & 1];
+      enqueue_fp64_range(pl, lat, noise, step, st, 2, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
+      const long long sb = cell0(c) * L.ns, se = cell0(c + 1) * L.ns;
+      enqueue_unpack(m, lat, pl->host_aos, sb, se - sb, st);
+      MGX_CUDA_TRY(cudaEventRecord(ev_out[c], st));
+      MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_out[c], 0));
+      MGX_CUDA_TRY(cudaMemcpyAsync(e_out + 3 * sb, pl->host_aos + 3 * sb, sizeof(double) * 3 * (se - sb),
+                                   cudaMemcpyDefault, cs));
+    }
+  }
+  // the copy stream waited for every slab of both compute streams: `stream` continues after all of it
+  MGX_CUDA_TRY(cudaEventRecord(ev_done, cs));
+  MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_done, 0));
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }

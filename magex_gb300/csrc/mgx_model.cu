@@ -1,6 +1,7 @@
 // Model creation (stencil tables, per-site overrides), spin layout conversion and error state.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -25,10 +26,12 @@ mgx_status cuda_error(cudaError_t err, const char* where) {
   return set_error(code, "CUDA error %s (%s) in %s", cudaGetErrorName(err), cudaGetErrorString(err), where);
 }
 
-// magex site order (cell*ns + s) -> lattice index (s*ncell + cell)
-__global__ void k_pack(const double* __restrict__ aos, double* __restrict__ lat, int ns, int ncell, long long N) {
-  const long long site = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (site >= N) return;
+// magex site order (cell*ns + s) -> lattice index (s*ncell + cell): magex-order (N, 3) rows [begin, begin + count) <-> lattice layout (3, N)
+__global__ void k_pack(const double* __restrict__ aos, double* __restrict__ lat, int ns, int ncell, long long N,
+                       long long begin, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const long long site = begin + i;
   const long long cell = site / ns;
   const int s = (int)(site - cell * ns);
   const long long q = (long long)s * ncell + cell;
@@ -37,15 +40,27 @@ __global__ void k_pack(const double* __restrict__ aos, double* __restrict__ lat,
   lat[2 * N + q] = aos[3 * site + 2];
 }
 
-__global__ void k_unpack(const double* __restrict__ lat, double* __restrict__ aos, int ns, int ncell, long long N) {
-  const long long site = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (site >= N) return;
+__global__ void k_unpack(const double* __restrict__ lat, double* __restrict__ aos, int ns, int ncell, long long N,
+                         long long begin, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const long long site = begin + i;
   const long long cell = site / ns;
   const int s = (int)(site - cell * ns);
   const long long q = (long long)s * ncell + cell;
   aos[3 * site] = lat[q];
   aos[3 * site + 1] = lat[N + q];
   aos[3 * site + 2] = lat[2 * N + q];
+}
+
+void enqueue_pack(const Model* m, const double* aos, double* lat, long long begin, long long count, cudaStream_t st) {
+  if (count <= 0) return;
+  k_pack<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(aos, lat, m->d.ns, m->d.ncell, m->d.N, begin, count);
+}
+
+void enqueue_unpack(const Model* m, const double* lat, double* aos, long long begin, long long count, cudaStream_t st) {
+  if (count <= 0) return;
+  k_unpack<<<(unsigned)((count + 255) / 256), 256, 0, st>>>(lat, aos, m->d.ns, m->d.ncell, m->d.N, begin, count);
 }
 
 template <typename T>
@@ -108,6 +123,7 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
   std::vector<int> slot_of(std::max(nb, 1), 0);
   std::vector<int4> geo(std::max(nb, 1));
   std::vector<double> J((size_t)std::max(nb, 1) * W, 0.0);
+  int reach0 = 0;
   for (int b = 0; b < nb; ++b) {
     const int i = lat->bond_src[b];
     const int slot = fill[i]++;
@@ -130,6 +146,8 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
       return set_error(MGX_ERR_INVALID,
                        "bond %d couples a site to its own periodic image; fold it into A_sub first", b);
     geo[slot] = make_int4(lat->bond_dst[b], d[0], d[1], d[2]);
+    const int R0 = lat->bond_R[3 * b];
+    reach0 = std::max(reach0, lat->pbc[0] ? std::min(d[0], lat->L[0] - d[0]) : (d[0] == lat->L[0] ? 0 : std::abs(R0)));
     for (int k = 0; k < W; ++k) J[(size_t)slot * W + k] = lat->bond_table[(size_t)b * W + k];
   }
 
@@ -168,6 +186,7 @@ mgx_status mgx_model_create(const mgx_lattice_desc* lat, const mgx_site_desc* si
   d.B1 = lat->B[1];
   d.B2 = lat->B[2];
   m->nbond = nb;
+  m->reach0 = reach0;
 
   // one device block for all small tables: [off | geo | J | A | inv_mu | mu | sign]
   const size_t s_off = 0, n_off = sizeof(int) * (ns + 1);
@@ -457,9 +476,7 @@ mgx_status mgx_pack_spins(const mgx_model* mm, const double* aos, double* lat, v
   const Model* m = reinterpret_cast<const Model*>(mm);
   if (!m || !aos || !lat) return set_error(MGX_ERR_INVALID, "mgx_pack_spins: null argument");
   if (aos == lat) return set_error(MGX_ERR_INVALID, "mgx_pack_spins: in-place conversion is not supported");
-  const long long N = m->d.N;
-  const int tpb = 256;
-  k_pack<<<(unsigned)((N + tpb - 1) / tpb), tpb, 0, (cudaStream_t)stream>>>(aos, lat, m->d.ns, m->d.ncell, N);
+  enqueue_pack(m, aos, lat, 0, m->d.N, (cudaStream_t)stream);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }
@@ -468,9 +485,7 @@ mgx_status mgx_unpack_spins(const mgx_model* mm, const double* lat, double* aos,
   const Model* m = reinterpret_cast<const Model*>(mm);
   if (!m || !aos || !lat) return set_error(MGX_ERR_INVALID, "mgx_unpack_spins: null argument");
   if (aos == lat) return set_error(MGX_ERR_INVALID, "mgx_unpack_spins: in-place conversion is not supported");
-  const long long N = m->d.N;
-  const int tpb = 256;
-  k_unpack<<<(unsigned)((N + tpb - 1) / tpb), tpb, 0, (cudaStream_t)stream>>>(lat, aos, m->d.ns, m->d.ncell, N);
+  enqueue_unpack(m, lat, aos, 0, m->d.N, (cudaStream_t)stream);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }

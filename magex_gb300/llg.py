@@ -168,26 +168,50 @@ class GB300LLG:
         if self.field_func is not None or self.extra_field is not None:
             raise NotImplementedError("field_func / extra_field callables are not supported by the GB300 kernels")
 
-    def step_lattice(self, lat, stream=None):
-        """One step on device spins in the lattice layout ((3, N) float64, in place)."""
+    def _prepare_step(self, stream):
+        """Field and thermal amplitudes up to date; the device noise pointer of this step (host-noise
+        mode: this step's N(0,1) draws from the NumPy stream, packed to the lattice layout)."""
         self._check_supported_callables()
         self.model.sync_field()
         self._update_sigma()
-        noise_ptr = None
-        if self.noise == "host" and self._noisy:
+        if self.noise != "host":
+            return None
+        if self._noisy:
             g = self.rng.normal(size=(self.sc.N, 3))
             self._noise_lat = self.model.to_lattice(g, out=self._noise_lat, stream=stream)
-            noise_ptr = C.c_void_p(self._noise_lat.data_ptr())
-        elif self.noise == "host":
+        elif self._noise_lat is None:
             # T = 0: magex draws nothing (magex/llg.py:107-108); a zero field is added
-            if self._noise_lat is None:
-                self._noise_lat = torch.zeros((3, self.sc.N), dtype=torch.float64, device=self.device)
-            noise_ptr = C.c_void_p(self._noise_lat.data_ptr())
+            self._noise_lat = torch.zeros((3, self.sc.N), dtype=torch.float64, device=self.device)
+        return C.c_void_p(self._noise_lat.data_ptr())
+
+    def _advance(self, nsteps=1):
+        self._step_index += int(nsteps)
+        self.time += self.dt * int(nsteps)
+
+    def step_lattice(self, lat, stream=None):
+        """One step on device spins in the lattice layout ((3, N) float64, in place)."""
+        noise_ptr = self._prepare_step(stream)
         _lib.check(self.model.lib.mgx_llg_step(self.handle, C.c_void_p(lat.data_ptr()), noise_ptr,
                                                C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_step")
-        self._step_index += 1
-        self.time += self.dt
+        self._advance()
         return lat
+
+    def step_host(self, e, out):
+        """One step from host (N, 3) float64 spins `e` (CPU tensor, magex site order) into `out` (may be
+        `e`): one library call (``mgx_llg_step_host``) whose copies overlap the stages when both
+        tensors are pinned.  Returns `out` once it holds the result."""
+        N = self.sc.N
+        for name, t in (("e", e), ("out", out)):
+            if t.is_cuda or t.dtype != torch.float64 or tuple(t.shape) != (N, 3) or not t.is_contiguous():
+                raise ValueError(f"{name} must be a contiguous ({N}, 3) float64 CPU tensor")
+        stream = torch.cuda.current_stream(self.device)
+        noise_ptr = self._prepare_step(stream)
+        _lib.check(self.model.lib.mgx_llg_step_host(self.handle, C.c_void_p(e.data_ptr()), C.c_void_p(out.data_ptr()),
+                                                    noise_ptr, C.c_uint64(self._step_index), stream_ptr(stream)),
+                   "mgx_llg_step_host")
+        stream.synchronize()
+        self._advance()
+        return out
 
     def run_lattice(self, lat, nsteps, stream=None):
         """nsteps steps on device lattice-layout spins; Philox noise only (one library call)."""
@@ -200,8 +224,7 @@ class GB300LLG:
         self._update_sigma()
         _lib.check(self.model.lib.mgx_llg_run(self.handle, C.c_void_p(lat.data_ptr()), C.c_int64(int(nsteps)),
                                               C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_run")
-        self._step_index += int(nsteps)
-        self.time += self.dt * int(nsteps)
+        self._advance(nsteps)
         return lat
 
     def stage_lattice(self, lat, stage, stream=None):
@@ -216,8 +239,7 @@ class GB300LLG:
         _lib.check(self.model.lib.mgx_llg_stage(self.handle, C.c_int32(stage), C.c_void_p(lat.data_ptr()), None,
                                                 C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_stage")
         if stage == 1:
-            self._step_index += 1
-            self.time += self.dt
+            self._advance()
         return lat
 
     # ------------------------------------------------------------------ magex API
@@ -225,23 +247,29 @@ class GB300LLG:
         """One integration step; returns new spins (magex/llg.py:216).
 
         A numpy array in gives a new numpy array out (the input is not modified); an (N, 3) CUDA
-        tensor gives a CUDA tensor; an (N, 3) CPU tensor (pinned for asynchronous copies) gives a
-        CPU tensor, written into ``out`` when given."""
-        on_device = isinstance(e, torch.Tensor) and e.is_cuda
-        lat = self.model.to_lattice(e, out=self._lat)
-        self._lat = lat
-        self.step_lattice(lat)
-        dev = self.model.from_lattice(lat, out=getattr(self, "_aos", None))
-        self._aos = dev
-        if on_device:
+        tensor gives a CUDA tensor; an (N, 3) CPU tensor (pinned: the copies overlap the step) gives
+        a CPU tensor, written into ``out`` when given.  Host arrays go through one library call
+        (``step_host``)."""
+        N = self.sc.N
+        if isinstance(e, torch.Tensor) and e.is_cuda:
+            lat = self.model.to_lattice(e, out=self._lat)
+            self._lat = lat
+            self.step_lattice(lat)
+            dev = self.model.from_lattice(lat, out=getattr(self, "_aos", None))
+            self._aos = dev
             return dev.clone() if out is None else out.copy_(dev)
         if isinstance(e, torch.Tensor):
+            src = e if (e.dtype == torch.float64 and e.is_contiguous()) else e.to(torch.float64).contiguous()
+            if src.shape != (N, 3):
+                raise ValueError(f"spins have shape {tuple(src.shape)}, expected {(N, 3)}")
             if out is None:
-                out = torch.empty((self.sc.N, 3), dtype=torch.float64, pin_memory=e.is_pinned())
-            out.copy_(dev, non_blocking=out.is_pinned())
-            torch.cuda.current_stream(self.device).synchronize()
-            return out
-        return dev.cpu().numpy()
+                out = torch.empty((N, 3), dtype=torch.float64, pin_memory=e.is_pinned())
+            return self.step_host(src, out)
+        a = np.ascontiguousarray(e, dtype=np.float64)
+        src = torch.from_numpy(a if a.flags.writeable else a.copy())
+        if src.shape != (N, 3):
+            raise ValueError(f"spins have shape {tuple(src.shape)}, expected {(N, 3)}")
+        return self.step_host(src, torch.empty((N, 3), dtype=torch.float64)).numpy()
 
     def _row(self, lat):
         obs = self.model.observables(lat).cpu().numpy()

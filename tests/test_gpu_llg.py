@@ -236,3 +236,40 @@ def test_graph_replayed_run_equals_direct_launches(cuda, precision):
     for _ in range(64):
         b.run_lattice(lb, 1)
     assert torch.equal(la, lb)
+
+
+@pytest.mark.parametrize("shells,pbc0,noise,precision", [
+    ((20.0, 10.0, -1.0), True, "philox", "fp64"),
+    ((20.0, 10.0, -1.0, 1.0), True, "philox", "fp64"),      # 4th shell: couplings reach 2 layers
+    ((20.0, 10.0, -1.0), False, "philox", "fp64"),          # open along the slab axis
+    ((20.0, 10.0, -1.0), True, "host", "fp64"),
+    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed"),     # one piece (reduced split refreshed)
+])
+def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precision):
+    """mgx_llg_step_host (pinned host buffers; copies in axis-0 slabs overlapping the stages for FP64
+    plans of >= 2^20 sites) gives the same bits as the step on device spins: also in place, and for
+    pageable numpy input (one piece)."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    from magex_gb300.workloads import bcc_two_site_model
+    sc = Supercell(load_results(bcc_two_site_model(J=shells)), (96, 76, 76), (pbc0, True, True), (0.0, 0.0, 0.5))
+    assert sc.N >= 1 << 20
+    a = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision)
+    b = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision)
+    e0 = sc.init_spins("random", seed=3)
+    h = torch.from_numpy(e0.copy()).pin_memory()
+    out = torch.empty_like(h).pin_memory()
+    lat = b.model.to_lattice(e0)
+    for _ in range(3):
+        a.step_host(h, out)
+        h, out = out, h
+        b.step_lattice(lat)
+    assert torch.equal(h, b.model.from_lattice(lat).cpu())
+    a.step_host(h, h)
+    b.step_lattice(lat)
+    assert torch.equal(h, b.model.from_lattice(lat).cpu())
+    r = a.step(h.numpy().copy())
+    b.step_lattice(lat)
+    assert isinstance(r, np.ndarray) and np.array_equal(r, b.model.from_lattice(lat).cpu().numpy())
+    assert a.time == pytest.approx(b.time) and a._step_index == b._step_index == 5
