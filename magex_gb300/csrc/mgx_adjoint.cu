@@ -115,6 +115,39 @@ __device__ __forceinline__ void store3(double* x, long long N, long long q, doub
   x[2 * N + q] = c;
 }
 
+// Per-site gradient accumulators are K cells N apart: all K loads are issued before any store (the
+// compiler cannot prove that cells N apart do not alias, so a cell-by-cell read-modify-write would
+// wait a full memory round trip per cell).
+template <int K>
+__device__ __forceinline__ void load_cells(const double* p, long long N, double* v) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = p[(long long)k * N];
+}
+template <int K>
+__device__ __forceinline__ void store_cells(double* p, long long N, const double* v) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) p[(long long)k * N] = v[k];
+}
+
+// PA -= g (x) v (single-ion gradient of one stage) and PB += Hbar (field gradient)
+__device__ __forceinline__ void accumulate_onsite(const AdjDev& A, long long N, long long q, bool hasA, double gx,
+                                                  double gy, double gz, double vx, double vy, double vz, double Hbx,
+                                                  double Hby, double Hbz) {
+  double pa[9], pb[3];
+  if (hasA) load_cells<9>(A.PA + q, N, pa);
+  load_cells<3>(A.PB + q, N, pb);
+  if (hasA) {
+    const double gv[3] = {gx, gy, gz}, v[3] = {vx, vy, vz};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) pa[k] -= gv[k / 3] * v[k % 3];
+    store_cells<9>(A.PA + q, N, pa);
+  }
+  pb[0] += Hbx;
+  pb[1] += Hby;
+  pb[2] += Hbz;
+  store_cells<3>(A.PB + q, N, pb);
+}
+
 // Transposed gather sum_rev J^T g_nbr at site q of the reverse stencil, with the parameter-gradient
 // outer products added to PG once per group run: a forward coupling with tensor T_g contributes
 // g_nbr (x) v, one with T_g^T contributes v (x) g_nbr (v = own p or e), so each run keeps the sums of
@@ -134,13 +167,13 @@ __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __
     if (cur_g < 0) return;
     double* P = A.PG + (long long)cur_g * 9 * N + q;
     const double gs[3] = {sx, sy, sz}, gt[3] = {tx, ty, tz};
+    double acc[9];
+    load_cells<9>(P, N, acc);
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        double* cell = P + (long long)(3 * a + b) * N;
-        *cell = fma(vv[a], gt[b], fma(gs[a], vv[b], *cell));
-      }
+      for (int b = 0; b < 3; ++b) acc[3 * a + b] = fma(vv[a], gt[b], fma(gs[a], vv[b], acc[3 * a + b]));
+    store_cells<9>(P, N, acc);
   };
   for (int b = b0; b < b1; ++b) {
     const int2 gr = __ldg(A.group + b);
@@ -226,13 +259,8 @@ __device__ __forceinline__ void adj_local_site(const AdjDev& A, long long q, con
     pbx -= a[0] * gx + a[3] * gy + a[6] * gz;     // -A^T g
     pby -= a[1] * gx + a[4] * gy + a[7] * gz;
     pbz -= a[2] * gx + a[5] * gy + a[8] * gz;
-    const double gv[3] = {gx, gy, gz}, pv[3] = {px, py, pz};
-#pragma unroll
-    for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * pv[k % 3];
   }
-  A.PB[q] += Hbx;
-  A.PB[N + q] += Hby;
-  A.PB[2 * N + q] += Hbz;
+  accumulate_onsite(A, N, q, L.has_A != 0, gx, gy, gz, px, py, pz, Hbx, Hby, Hbz);
   store3(eacc, N, q, ybx, yby, ybz);
   store3(pbar, N, q, pbx, pby, pbz);
   store3(f1bar, N, q, fbx, fby, fbz);
@@ -309,13 +337,8 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
     ax -= a[0] * gx + a[3] * gy + a[6] * gz;
     ay -= a[1] * gx + a[4] * gy + a[7] * gz;
     az -= a[2] * gx + a[5] * gy + a[8] * gz;
-    const double gv[3] = {gx, gy, gz}, ev[3] = {ex, ey, ez};
-#pragma unroll
-    for (int k = 0; k < 9; ++k) A.PA[(long long)k * N + q] -= gv[k / 3] * ev[k % 3];
   }
-  A.PB[q] += Hbx;
-  A.PB[N + q] += Hby;
-  A.PB[2 * N + q] += Hbz;
+  accumulate_onsite(A, N, q, L.has_A != 0, gx, gy, gz, ex, ey, ez, Hbx, Hby, Hbz);
   store3(eacc, N, q, ax, ay, az);
   store3(g1, N, q, gx, gy, gz);
 }
