@@ -271,6 +271,48 @@ class GB300LLG:
             raise ValueError(f"spins have shape {tuple(src.shape)}, expected {(N, 3)}")
         return self.step_host(src, torch.empty((N, 3), dtype=torch.float64)).numpy()
 
+    # ------------------------------------------------------------------ checkpoint / resume
+    def checkpoint(self, e, path):
+        """Write spins and the solver's clock to an .npz: magex's spin-file keys (spins, positions,
+        mu, sublattice, cell, supercell; magex/llg.py:292-296, so the file also serves as an
+        ``init_spins("file")`` input) plus the time, the step counter that keys the Philox noise, the
+        seed, the temperature and the state of the host noise generator.  magex itself saves only the
+        spins (its time and generator state are lost); ``resume`` continues the run exactly."""
+        import json
+        if isinstance(e, torch.Tensor):
+            e = e.detach().cpu().numpy()
+        e = np.ascontiguousarray(e, np.float64).reshape(self.sc.N, 3)
+        sc = self.sc
+        geo = {"mu": sc.mu, "sublattice": sc.sublattice, "supercell": np.array(sc.L)}
+        if hasattr(sc, "uc"):                       # lattice supercells; neighbour lists have no geometry
+            geo.update(positions=sc.positions, cell=sc.uc.cell)
+        np.savez_compressed(path, spins=e, **geo, time=self.time, step=self._step_index,
+                            seed=-1 if self.seed is None else int(self.seed), temperature=self.T, dt=self.dt,
+                            noise=self.noise, rng_state=json.dumps(self.rng.bit_generator.state))
+        return path
+
+    def resume(self, path):
+        """Spins of a checkpoint written by ``checkpoint``; restores the time, the step counter, the
+        temperature and the host generator, so that the continued trajectory equals the
+        uninterrupted one bit for bit.  The solver must have the checkpoint's seed, time step and
+        noise mode (the Philox key is fixed when the solver is created)."""
+        import json
+        with np.load(path) as z:
+            seed = int(z["seed"])
+            mine = -1 if self.seed is None else int(self.seed)
+            if seed != mine or str(z["noise"]) != self.noise or float(z["dt"]) != self.dt:
+                raise ValueError(f"checkpoint {path} was written by a solver with seed {seed}, noise "
+                                 f"'{z['noise']}', dt {float(z['dt'])}; this one has seed {mine}, noise "
+                                 f"'{self.noise}', dt {self.dt}")
+            if z["spins"].shape != (self.sc.N, 3):
+                raise ValueError(f"checkpoint spins have shape {z['spins'].shape}, expected {(self.sc.N, 3)}")
+            e = np.array(z["spins"], np.float64)
+            self.time = float(z["time"])
+            self._step_index = int(z["step"])
+            self.T = float(z["temperature"])
+            self.rng.bit_generator.state = json.loads(str(z["rng_state"]))
+        return e
+
     def _row(self, lat):
         obs = self.model.observables(lat).cpu().numpy()
         N = self.sc.N

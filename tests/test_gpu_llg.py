@@ -273,3 +273,33 @@ def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precisio
     b.step_lattice(lat)
     assert isinstance(r, np.ndarray) and np.array_equal(r, b.model.from_lattice(lat).cpu().numpy())
     assert a.time == pytest.approx(b.time) and a._step_index == b._step_index == 5
+
+
+@pytest.mark.parametrize("noise", ["philox", "host"])
+def test_checkpoint_resume_continues_the_trajectory(cuda, tmp_path, noise):
+    """A run stopped after 12 steps, written with checkpoint() and continued by a fresh solver after
+    resume() equals 30 uninterrupted steps bit for bit (noise counter, clock and host generator
+    restored); a solver with another seed refuses the checkpoint."""
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=6)
+    e0 = sc.init_spins("random", seed=4)
+    ref = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=11, noise=noise)
+    e = e0
+    for _ in range(30):
+        e = ref.step(e)
+    first = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=11, noise=noise)
+    a = e0
+    for _ in range(12):
+        a = first.step(a)
+    path = first.checkpoint(a, str(tmp_path / "ck.npz"))
+    second = GB300LLG(sc, 0.05, 1e-4, 0.0, seed=11, noise=noise)     # T comes from the checkpoint
+    b = second.resume(path)
+    assert second.T == 300.0 and second.time == pytest.approx(12e-4)
+    for _ in range(18):
+        b = second.step(b)
+    assert np.array_equal(b, e)
+    assert second.time == pytest.approx(ref.time)
+    assert np.abs(sc.init_spins("file", path=path) - a).max() < 1e-15   # also a magex spin file
+    with pytest.raises(ValueError):
+        GB300LLG(sc, 0.05, 1e-4, 300.0, seed=12, noise=noise).resume(path)
