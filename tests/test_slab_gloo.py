@@ -137,3 +137,54 @@ def test_slab_decomposition_matches_unsplit_oracle(golden_models, name, world):
     for r in res:
         np.testing.assert_array_equal(r[3][:7], np.arange(7) * tot)
         assert r[3][7] == 7 * world
+
+
+def _silent_peer_worker(rank, world, port, spec_uc, q, done):
+    """Rank 1 joins the group but never sends its halo; rank 0 must get an error, not wait forever."""
+    import datetime
+    import time
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (root, os.path.join(root, "oracle"), os.path.join(root, "tests")):
+        sys.path.insert(0, p)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=3))
+    if rank == 1:
+        done.wait(120)          # stay connected until rank 0 has given up, then leave
+        return
+    from magex_gb300.slab import DistTransport
+    uc, (key, L, pbc, B, alpha, dt, T, steps) = spec_uc
+    sl = OracleSlab(uc, L, pbc, B, alpha, dt, rank, world)
+    e = np.zeros((sl.sc.N, 3))
+    e[:, 2] = 1.0
+    t0 = time.time()
+    try:
+        DistTransport().exchange([sl], [sl.pack("e", e)])
+        q.put(("returned", time.time() - t0, ""))
+    except Exception as err:                      # the process group's timeout ends the receive
+        q.put(("error", time.time() - t0, type(err).__name__))
+    finally:
+        done.set()
+
+
+def test_missing_halo_message_raises_instead_of_hanging(golden_models):
+    """Failure detection on the host: a neighbour that never sends its halo layers makes the
+    exchange raise once the process group's timeout (3 s here) expires; magex's MPI exchange would
+    block forever in Waitall (magex/mpi_spin.py:102)."""
+    from magex_gb300.spinmodel import load_results
+    spec = CASES["bcc_periodic"]
+    uc = load_results(golden_models[spec[0]]["model"])
+    ctx = mp.get_context("spawn")
+    q, done = ctx.Queue(), ctx.Event()
+    port = _free_port()
+    procs = [ctx.Process(target=_silent_peer_worker, args=(r, 2, port, (uc, spec), q, done)) for r in range(2)]
+    for p in procs:
+        p.start()
+    status, elapsed, what = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+        if p.is_alive():
+            p.kill()
+    assert status == "error", (status, elapsed, what)
+    assert elapsed < 60
