@@ -550,6 +550,7 @@ mgx_status mgx_adjoint_set_storage(mgx_adjoint* aa, double* storage) {
 
 mgx_status mgx_adjoint_forward(mgx_adjoint* aa, const double* e0, int32_t nsteps, uint64_t step0, double* e_out,
                                void* stream) {
+  NvtxRange nvtx_range("mgx_adjoint_forward");
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
   if (!a || !e0) return set_error(MGX_ERR_INVALID, "mgx_adjoint_forward: null argument");
   if (nsteps < 1 || nsteps > a->seg_cap)
@@ -582,6 +583,7 @@ mgx_status mgx_adjoint_forward(mgx_adjoint* aa, const double* e0, int32_t nsteps
 }
 
 mgx_status mgx_adjoint_backward(mgx_adjoint* aa, double* ebar, int32_t nsteps, void* stream) {
+  NvtxRange nvtx_range("mgx_adjoint_backward");
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
   if (!a || !ebar) return set_error(MGX_ERR_INVALID, "mgx_adjoint_backward: null argument");
   if (nsteps < 1 || nsteps > a->seg_cap)

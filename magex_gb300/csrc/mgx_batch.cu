@@ -448,6 +448,7 @@ mgx_status mgx_batch_set_launch(mgx_batch* bb, int32_t threads, int32_t ctas_per
 }
 
 mgx_status mgx_batch_step(mgx_batch* bb, double* e, const double* noise, uint64_t step, void* stream) {
+  NvtxRange nvtx_range("mgx_batch_step");
   Batch* b = reinterpret_cast<Batch*>(bb);
   if (!b || !e) return set_error(MGX_ERR_INVALID, "mgx_batch_step: null argument");
   if (b->noise == MGX_NOISE_HOST && !noise) return set_error(MGX_ERR_INVALID, "host-noise batch needs a noise buffer");
@@ -458,6 +459,7 @@ mgx_status mgx_batch_step(mgx_batch* bb, double* e, const double* noise, uint64_
 }
 
 mgx_status mgx_batch_run(mgx_batch* bb, double* e, int64_t nsteps, uint64_t step0, int32_t graph_chunk, void* stream) {
+  NvtxRange nvtx_range("mgx_batch_run");
   Batch* b = reinterpret_cast<Batch*>(bb);
   if (!b || !e) return set_error(MGX_ERR_INVALID, "mgx_batch_run: null argument");
   if (nsteps < 0) return set_error(MGX_ERR_INVALID, "nsteps must be >= 0");

@@ -204,6 +204,7 @@ extern "C" mgx_status mgx_fourier_create(const mgx_model* mm, int32_t nq, const 
 }
 
 extern "C" mgx_status mgx_fourier_project(mgx_fourier* h, const double* e, double* mq, void* stream) {
+  NvtxRange nvtx_range("mgx_fourier_project");
   FourierPlan* f = reinterpret_cast<FourierPlan*>(h);
   if (!f || !e || !mq) return set_error(MGX_ERR_INVALID, "mgx_fourier_project: null argument");
   const DevLattice& d = f->model->d;

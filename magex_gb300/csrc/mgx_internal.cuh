@@ -7,6 +7,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <cstdarg>
@@ -188,6 +189,14 @@ void enqueue_df_step(const LLGPlan* pl, double* e, const double* noise, uint64_t
 mgx_status build_fx_tables(LLGPlan* pl);
 void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st);
 void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
+
+// Host-side NVTX range over one library call (named in profiler timelines; a no-op without a tool).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ------------------------------------------------------------------ small device helpers
 __device__ __forceinline__ void site_coords(const DevLattice& L, long long q, int& s, int& c0, int& c1, int& c2) {

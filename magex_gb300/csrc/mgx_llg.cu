@@ -336,6 +336,7 @@ static void enqueue_reduced_split(const LLGPlan* pl, const double* e, cudaStream
 }
 
 mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t step, void* stream) {
+  NvtxRange nvtx_range("mgx_llg_step");
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl || !e) return set_error(MGX_ERR_INVALID, "mgx_llg_step: null argument");
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
@@ -356,6 +357,7 @@ mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t st
 // is split.
 mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, const double* noise, uint64_t step,
                              void* stream) {
+  NvtxRange nvtx_range("mgx_llg_step_host");
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl || !e_in || !e_out) return set_error(MGX_ERR_INVALID, "mgx_llg_step_host: null argument");
   if (pl->p.noise == MGX_NOISE_HOST && !noise)
@@ -457,6 +459,7 @@ mgx_status mgx_llg_stage(mgx_llg* pp, int32_t stage, double* e, const double* no
 }
 
 mgx_status mgx_llg_run(mgx_llg* pp, double* e, int64_t nsteps, uint64_t step0, void* stream) {
+  NvtxRange nvtx_range("mgx_llg_run");
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl || !e) return set_error(MGX_ERR_INVALID, "mgx_llg_run: null argument");
   if (nsteps < 0) return set_error(MGX_ERR_INVALID, "nsteps must be >= 0");

@@ -538,6 +538,7 @@ extern "C" mgx_status mgx_mc_host_draws(const mgx_mc* h, int64_t* ndoubles) {
 }
 
 extern "C" mgx_status mgx_mc_sweep(mgx_mc* h, double* e, int64_t nsweeps, const double* host_draws, void* stream) {
+  NvtxRange nvtx_range("mgx_mc_sweep");
   McPlan* mc = reinterpret_cast<McPlan*>(h);
   if (!mc || !e || nsweeps < 0) return set_error(MGX_ERR_INVALID, "mgx_mc_sweep: bad argument");
   if (mc->rng == MGX_MC_RNG_HOST && (nsweeps > 1 || (nsweeps == 1 && !host_draws)))
