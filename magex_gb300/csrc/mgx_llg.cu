@@ -324,6 +324,8 @@ mgx_status mgx_llg_set_sigma(mgx_llg* pp, const double* sigma_sub, const double*
     pl->p.sigma_site = nullptr;
   }
   pl->sigma_zero = zero;
+  // the captured step loop holds the amplitudes' splits and the per-site pointer by value
+  drop_llg_graph(pl);
   return MGX_OK;
 }
 

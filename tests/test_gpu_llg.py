@@ -236,6 +236,12 @@ def test_graph_replayed_run_equals_direct_launches(cuda, precision):
     for _ in range(64):
         b.run_lattice(lb, 1)
     assert torch.equal(la, lb)
+    for sol in (a, b):                             # new thermal amplitudes: the graph is re-captured
+        sol.T = 40.0
+    a.run_lattice(la, 64)
+    for _ in range(64):
+        b.run_lattice(lb, 1)
+    assert torch.equal(la, lb)
 
 
 @pytest.mark.parametrize("shells,pbc0,noise,precision", [
