@@ -292,6 +292,9 @@ mgx_status mgx_llg_step_noalloc(const mgx_model* m, const mgx_llg_params* p, con
  *   [7] max_i |e_i x B_eff,i| (T)                             (magex/llg.py:250-252)
  * The sums are deterministic (fixed-shape tree reduction). */
 mgx_status mgx_observables(const mgx_model* m, const double* e, double* out, void* stream);
+/* The same for nlat lattices stored one after the other (lattice k at e + 3 N k, e.g. the chains of a
+ * Monte Carlo ensemble): out [nlat*8]; lattice k's values equal mgx_observables of lattice k. */
+mgx_status mgx_observables_n(const mgx_model* m, const double* e, int32_t nlat, double* out, void* stream);
 /* Effective field B_eff (T) of spins e into B (device, lattice layout) (magex/spinmodel.py:471-473). */
 mgx_status mgx_effective_field(const mgx_model* m, const double* e, double* B, void* stream);
 
@@ -354,6 +357,24 @@ mgx_status mgx_mc_sweep(mgx_mc* mc, double* e, int64_t nsweeps, const double* ho
 /* Accepted trial moves and tried moves since the last reset (MetropolisMC.acceptance); synchronises
  * the stream. */
 mgx_status mgx_mc_counts(mgx_mc* mc, uint64_t* accepted, uint64_t* tried, int32_t reset, void* stream);
+
+/* Ensemble of independent chains on the plan's lattice, swept together: magex runs its (L, T) points
+ * as separate processes (magex/montecarlo.py:390-401, _point :248-291); here every pass of a sweep is
+ * one launch over the class's sites of all chains.  Chain k's spins are the lattice-layout block at
+ * e + 3 N k; it has its own Philox key seeds[k], inverse temperature beta[k] (1/meV, finite, > 0)
+ * and cone width sigma[k] (host arrays of nchains).  Each chain's trajectory equals that of a
+ * one-chain plan with its key, beta and sigma.  Philox FP64 plans without site temperatures;
+ * nchains = 1 with all arrays NULL returns to the plan's own single chain.  Resets the counts. */
+mgx_status mgx_mc_set_chains(mgx_mc* mc, int32_t nchains, const uint64_t* seeds, const double* beta,
+                             const double* sigma);
+/* Per-chain accepted moves since the last reset (host [nchains]) and the tried moves (the same for
+ * every chain); the cone widths (host [nchains]) when sigma is not NULL.  Synchronises the stream. */
+mgx_status mgx_mc_chain_counts(mgx_mc* mc, uint64_t* accepted, uint64_t* tried, double* sigma, int32_t reset,
+                               void* stream);
+/* Cone-width adaptation of every chain from its acceptance a since the last reset, on the device:
+ * sigma <- clip(sigma * 0.5 / max(1 - a, 0.05), 0.02, 4) (magex/montecarlo.py:257-261); resets the
+ * counts. */
+mgx_status mgx_mc_adapt_sigma(mgx_mc* mc, void* stream);
 
 /* ---------------------------------------------------------------- S(q, w) sampling
  * Device-side Fourier projection m_q = N^-1/2 sum_i e_i exp(-i q.r_i) of lattice-layout spins, the

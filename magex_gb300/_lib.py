@@ -98,6 +98,10 @@ SIGNATURES = {
     "mgx_mc_sweep": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "mgx_mc_counts": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), C.c_int32,
                                   C.c_void_p]),
+    "mgx_mc_set_chains": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_mc_chain_counts": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64), C.c_void_p, C.c_int32,
+                                         C.c_void_p]),
+    "mgx_mc_adapt_sigma": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mgx_llg_step_noalloc": (C.c_int32, [C.c_void_p, C.POINTER(LLGParams), _dp, C.c_void_p, C.c_void_p, C.c_uint64,
                                          C.c_void_p]),
     "mgx_batch_create": (C.c_int32, [C.POINTER(C.c_void_p), C.POINTER(LLGParams), C.c_int32, C.POINTER(C.c_void_p)]),
@@ -126,6 +130,7 @@ SIGNATURES = {
     "mgx_adjoint_zero_grads": (C.c_int32, [C.c_void_p, C.c_void_p]),
     "mgx_adjoint_grads": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "mgx_observables_n": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "mgx_effective_field": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                            C.c_void_p, C.c_void_p]),

@@ -24,6 +24,15 @@ namespace mgx {
 
 constexpr double kMuB = 5.7883818060e-2;     // meV / T (magex/spinmodel.py:28)
 
+// Chains of an ensemble (mgx_mc_set_chains): per-chain Philox key, inverse temperature, cone width and
+// accept counter; seed == nullptr for the plan's single chain.
+struct McChains {
+  const uint64_t* seed;
+  const double* beta;
+  const double* sigma;
+  unsigned long long* acc;
+};
+
 struct McPlan {
   const Model* model = nullptr;
   int move = 0;
@@ -44,6 +53,10 @@ struct McPlan {
   bool fixed = false;                      // exchange field from the exact 56-bit fixed-point gather
   DevFX fx{};
   void* fx_block = nullptr;
+  // ensemble (mgx_mc_set_chains): nchains > 1 or chain_block set
+  int nchains = 1;
+  void* chain_block = nullptr;             // device: seed | beta | sigma | acc, nchains each
+  McChains chains{};
 };
 
 // ------------------------------------------------------------------ random numbers
@@ -96,16 +109,27 @@ __device__ __forceinline__ double onsite(const DevLattice& L, long long q, int s
 
 enum { MC_GAUSSIAN = 0, MC_UNIFORM = 1, MC_HEATBATH = 2, MC_HINZKE = 3, MC_OVERRELAX = 4 };
 
-// One pass over the n sites of a colour class.  hr: host-supplied draws of this pass (RNG_HOST), laid
-// out as documented at mgx_mc_sweep; otherwise Philox with counter (site, sweep, pass).
+// One pass over the n sites of a colour class (of chain blockIdx.y of an ensemble).  hr: host-supplied
+// draws of this pass (RNG_HOST), laid out as documented at mgx_mc_sweep; otherwise Philox with counter
+// (site, sweep, pass).
 template <int W, int MOVE, bool HOSTRNG, bool FIXED>
 __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __restrict__ e,
                                                  const long long* __restrict__ sites, long long n,
                                                  const double* __restrict__ beta_sub,
                                                  const double* __restrict__ beta_site, double sigma,
                                                  const double* __restrict__ hr, uint64_t seed, uint64_t sweep,
-                                                 int pass, unsigned long long* acc, const DevFX F) {
+                                                 int pass, unsigned long long* acc, const DevFX F,
+                                                 const McChains chains) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double chain_beta = 0.0;
+  if (chains.seed) {
+    const int k = blockIdx.y;
+    e += (long long)k * 3 * L.N;
+    seed = chains.seed[k];
+    sigma = chains.sigma[k];
+    chain_beta = chains.beta[k];
+    acc = chains.acc + k;
+  }
   bool ok = false;
   if (t < n) {
     const long long N = L.N;
@@ -127,7 +151,7 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
     }
     const double ox = e[q], oy = e[N + q], oz = e[2 * N + q];
     const double mu = L.mu_site ? __ldg(L.mu_site + q) : __ldg(L.mu_sub + s);
-    const double bt = beta_site ? __ldg(beta_site + q) : __ldg(beta_sub + s);
+    const double bt = chains.seed ? chain_beta : (beta_site ? __ldg(beta_site + q) : __ldg(beta_sub + s));
     double nx, ny, nz, ua;
     double extra = 0.0;                       // heat bath: (en - eo).H is added back (nonlinear part only)
     if (MOVE == MC_OVERRELAX) {
@@ -259,22 +283,24 @@ static void launch_pass(const McPlan* mc, double* e, int g, const double* hr, in
   const DevLattice& L = mc->model->d;
   const long long n = mc->gsize[g];
   if (n == 0) return;
-  const unsigned grid = (unsigned)((n + 127) / 128);
+  const dim3 grid((unsigned)((n + 127) / 128), (unsigned)mc->nchains);
   const long long* sites = mc->sites + mc->goff[g];
   if (mc->fixed) {
     if (hr)
       k_mc_pass<W, MOVE, true, true><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
-                                                           mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+                                                           mc->seed, mc->sweep, pass, mc->acc, mc->fx, mc->chains);
     else
       k_mc_pass<W, MOVE, false, true><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
-                                                            nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+                                                            nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
+                                                            mc->chains);
   } else {
     if (hr)
       k_mc_pass<W, MOVE, true, false><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
-                                                            mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+                                                            mc->seed, mc->sweep, pass, mc->acc, mc->fx, mc->chains);
     else
       k_mc_pass<W, MOVE, false, false><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
-                                                             nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx);
+                                                             nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
+                                                             mc->chains);
   }
 }
 
@@ -410,6 +436,7 @@ static void mc_free(McPlan* mc) {
   cudaFree(mc->beta);
   cudaFree(mc->beta_site);
   cudaFree(mc->acc);
+  cudaFree(mc->chain_block);
   delete mc;
 }
 
@@ -578,5 +605,92 @@ extern "C" mgx_status mgx_mc_counts(mgx_mc* h, uint64_t* accepted, uint64_t* tri
     MGX_CUDA_TRY(cudaMemsetAsync(mc->acc, 0, sizeof(unsigned long long), st));
     mc->tried = 0;
   }
+  return MGX_OK;
+}
+
+// sigma <- clip(sigma * 0.5 / max(1 - a, 0.05), 0.02, 4) with a = accepted / tried, counts reset: the
+// arithmetic of magex's adaptation (magex/montecarlo.py:257-261), operation for operation
+__global__ void k_mc_adapt(double* __restrict__ sigma, unsigned long long* __restrict__ acc, int n,
+                           unsigned long long tried) {
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double a = (double)acc[k] / (double)(tried > 0 ? tried : 1ull);
+    const double x = sigma[k] * 0.5 / fmax(1.0 - a, 0.05);
+    sigma[k] = fmin(fmax(x, 0.02), 4.0);
+    acc[k] = 0;
+  }
+}
+
+extern "C" mgx_status mgx_mc_set_chains(mgx_mc* h, int32_t nchains, const uint64_t* seeds, const double* beta,
+                                        const double* sigma) {
+  McPlan* mc = reinterpret_cast<McPlan*>(h);
+  if (!mc) return set_error(MGX_ERR_INVALID, "mgx_mc_set_chains: null plan");
+  if (nchains < 1 || nchains > 65535) return set_error(MGX_ERR_INVALID, "nchains = %d outside 1..65535", nchains);
+  if (nchains == 1 && !seeds && !beta && !sigma) {
+    cudaFree(mc->chain_block);
+    mc->chain_block = nullptr;
+    mc->chains = McChains{};
+    mc->nchains = 1;
+    mc->tried = 0;
+    return MGX_OK;
+  }
+  if (!seeds || !beta || !sigma) return set_error(MGX_ERR_INVALID, "mgx_mc_set_chains: null array");
+  if (mc->rng != MGX_MC_RNG_PHILOX || mc->fixed || mc->beta_site)
+    return set_error(MGX_ERR_UNSUPPORTED, "chains need a Philox FP64 plan without site temperatures");
+  for (int k = 0; k < nchains; ++k) {
+    if (!(beta[k] > 0.0) || !std::isfinite(beta[k]))
+      return set_error(MGX_ERR_INVALID, "beta of chain %d must be finite and > 0", k);
+    if (!(sigma[k] > 0.0) || !std::isfinite(sigma[k]))
+      return set_error(MGX_ERR_INVALID, "sigma of chain %d must be finite and > 0", k);
+  }
+  const size_t n = (size_t)nchains;
+  void* block = nullptr;
+  cudaError_t err = cudaMalloc(&block, 32 * n);
+  char* b = (char*)block;
+  if (err == cudaSuccess) err = cudaMemcpy(b, seeds, 8 * n, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(b + 8 * n, beta, 8 * n, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemcpy(b + 16 * n, sigma, 8 * n, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) err = cudaMemset(b + 24 * n, 0, 8 * n);
+  if (err != cudaSuccess) {
+    cudaFree(block);
+    return cuda_error(err, "mgx_mc_set_chains");
+  }
+  cudaFree(mc->chain_block);
+  mc->chain_block = block;
+  mc->chains = McChains{(const uint64_t*)b, (const double*)(b + 8 * n), (const double*)(b + 16 * n),
+                        (unsigned long long*)(b + 24 * n)};
+  mc->nchains = nchains;
+  mc->tried = 0;
+  mc->hb_ok.assign((size_t)mc->ngroups, 1);          // every beta finite
+  return MGX_OK;
+}
+
+extern "C" mgx_status mgx_mc_chain_counts(mgx_mc* h, uint64_t* accepted, uint64_t* tried, double* sigma,
+                                          int32_t reset, void* stream) {
+  McPlan* mc = reinterpret_cast<McPlan*>(h);
+  if (!mc || !accepted || !tried) return set_error(MGX_ERR_INVALID, "mgx_mc_chain_counts: bad argument");
+  if (!mc->chain_block) return set_error(MGX_ERR_INVALID, "mgx_mc_chain_counts: no chains set");
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t n = (size_t)mc->nchains;
+  std::vector<unsigned long long> a(n);
+  MGX_CUDA_TRY(cudaMemcpyAsync(a.data(), mc->chains.acc, 8 * n, cudaMemcpyDeviceToHost, st));
+  if (sigma) MGX_CUDA_TRY(cudaMemcpyAsync(sigma, mc->chains.sigma, 8 * n, cudaMemcpyDeviceToHost, st));
+  MGX_CUDA_TRY(cudaStreamSynchronize(st));
+  for (size_t k = 0; k < n; ++k) accepted[k] = a[k];
+  *tried = mc->tried;
+  if (reset) {
+    MGX_CUDA_TRY(cudaMemsetAsync(mc->chains.acc, 0, 8 * n, st));
+    mc->tried = 0;
+  }
+  return MGX_OK;
+}
+
+extern "C" mgx_status mgx_mc_adapt_sigma(mgx_mc* h, void* stream) {
+  McPlan* mc = reinterpret_cast<McPlan*>(h);
+  if (!mc) return set_error(MGX_ERR_INVALID, "mgx_mc_adapt_sigma: null plan");
+  if (!mc->chain_block) return set_error(MGX_ERR_INVALID, "mgx_mc_adapt_sigma: no chains set");
+  k_mc_adapt<<<1, 256, 0, (cudaStream_t)stream>>>(const_cast<double*>(mc->chains.sigma), mc->chains.acc, mc->nchains,
+                                                  (unsigned long long)mc->tried);
+  MGX_CUDA_TRY(cudaGetLastError());
+  mc->tried = 0;
   return MGX_OK;
 }

@@ -11,9 +11,13 @@ constexpr int OBS_TPB = 256;
 
 
 // Per site: E_i = e.A.e - e.h - mu_B mu e.B (magex/spinmodel.py:475-484), e, s e, |e x B_eff|.
+// blockIdx.y selects one of several lattices stored one after the other (3 N doubles each); every
+// lattice gets its own partials and the same reduction shape as a single one.
 template <int W>
 __global__ void __launch_bounds__(OBS_TPB) k_observe(const DevLattice L, const double* __restrict__ e,
                                                      double* __restrict__ partial) {
+  e += (long long)blockIdx.y * 3 * L.N;
+  partial += (long long)blockIdx.y * gridDim.x * OBS_NV;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double v[OBS_NV] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (q < L.N) observe_site<W>(L, e, q, v);
@@ -34,6 +38,8 @@ __global__ void __launch_bounds__(OBS_TPB) k_observe(const DevLattice L, const d
 }
 
 __global__ void __launch_bounds__(OBS_TPB) k_finish(const double* __restrict__ partial, int nblk, double* out) {
+  partial += (long long)blockIdx.x * nblk * OBS_NV;
+  out += (long long)blockIdx.x * OBS_NV;
   double v[OBS_NV] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int b = threadIdx.x; b < nblk; b += OBS_TPB)
     for (int k = 0; k < OBS_NV; ++k) {
@@ -115,23 +121,29 @@ using namespace mgx;
 
 extern "C" {
 
-mgx_status mgx_observables(const mgx_model* mm, const double* e, double* out, void* stream) {
+mgx_status mgx_observables_n(const mgx_model* mm, const double* e, int32_t nlat, double* out, void* stream) {
   Model* m = const_cast<Model*>(reinterpret_cast<const Model*>(mm));
   if (!m || !e || !out) return set_error(MGX_ERR_INVALID, "mgx_observables: null argument");
+  if (nlat < 1 || nlat > 65535) return set_error(MGX_ERR_INVALID, "mgx_observables_n: nlat = %d outside 1..65535", nlat);
   const long long nblk_ll = (m->d.N + OBS_TPB - 1) / OBS_TPB;
-  if (nblk_ll > 0x7fffffffLL) return set_error(MGX_ERR_INVALID, "lattice too large for mgx_observables");
+  if (nblk_ll * nlat > 0x7fffffffLL) return set_error(MGX_ERR_INVALID, "lattice too large for mgx_observables");
   const int nblk = (int)nblk_ll;
-  mgx_status st = ensure_partials(m, nblk);
+  mgx_status st = ensure_partials(m, nblk * nlat);
   if (st != MGX_OK) return st;
   cudaStream_t s = (cudaStream_t)stream;
+  const dim3 grid(nblk, nlat);
   switch (m->d.width) {
-    case 1: k_observe<1><<<nblk, OBS_TPB, 0, s>>>(m->d, e, m->partials); break;
-    case 4: k_observe<4><<<nblk, OBS_TPB, 0, s>>>(m->d, e, m->partials); break;
-    default: k_observe<9><<<nblk, OBS_TPB, 0, s>>>(m->d, e, m->partials); break;
+    case 1: k_observe<1><<<grid, OBS_TPB, 0, s>>>(m->d, e, m->partials); break;
+    case 4: k_observe<4><<<grid, OBS_TPB, 0, s>>>(m->d, e, m->partials); break;
+    default: k_observe<9><<<grid, OBS_TPB, 0, s>>>(m->d, e, m->partials); break;
   }
-  k_finish<<<1, OBS_TPB, 0, s>>>(m->partials, nblk, out);
+  k_finish<<<nlat, OBS_TPB, 0, s>>>(m->partials, nblk, out);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
+}
+
+mgx_status mgx_observables(const mgx_model* mm, const double* e, double* out, void* stream) {
+  return mgx_observables_n(mm, e, 1, out, stream);
 }
 
 mgx_status mgx_effective_field(const mgx_model* mm, const double* e, double* B, void* stream) {

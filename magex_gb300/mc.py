@@ -302,6 +302,12 @@ def point(args, rng="philox"):
             mvec.append(v)
             ms.append(np.linalg.norm(v))
     acc = mc.acceptance()
+    spins = mc.model.from_lattice(lat).cpu().numpy() if c.get("keep_spins") else None
+    return _row_of(L, N, T, Es, ms, mvec, acc, mc.sigma, mc.ncolors, time.time() - t0, spins)
+
+
+def _row_of(L, N, T, Es, ms, mvec, acc, sigma, ncolors, seconds, spins):
+    """Row dictionary of one (L, T) point from its samples (magex/montecarlo.py:274-291)."""
     E, m = np.array(Es), np.array(ms)
     kT = K_B * T
     full = _blocks_obs(E, m, N, kT)
@@ -312,11 +318,103 @@ def point(args, rng="philox"):
         err = bl.std(0, ddof=1) / np.sqrt(nb)
     else:
         err = np.zeros(5)
-    spins = mc.model.from_lattice(lat).cpu().numpy() if c.get("keep_spins") else None
     return dict(L=list(L), N=N, T=T, E=full[0], C=full[1], m=full[2], chi=full[3], U4=full[4],
                 dE=err[0], dC=err[1], dm=err[2], dchi=err[3], dU4=err[4], acceptance=acc,
-                sigma=mc.sigma, ncolors=mc.ncolors, mvec=np.mean(mvec, 0).tolist(),
-                seconds=time.time() - t0, spins=spins)
+                sigma=sigma, ncolors=ncolors, mvec=np.mean(mvec, 0).tolist(), seconds=seconds, spins=spins)
+
+
+def _ensemble_key(job):
+    uc, L, pbc, B, T, c, seed = job
+    return (id(uc), tuple(int(x) for x in L), tuple(bool(x) for x in pbc),
+            tuple(float(x) for x in np.asarray(B, float).ravel()), id(c))
+
+
+def points(jobs, max_chains=4096):
+    """Many (L, T) points at once: the rows of ``[point(job) for job in jobs]``, bit for bit.
+
+    magex runs its points as separate processes (magex/montecarlo.py:390-401).  On one GPU the points
+    that share a lattice (the same uc, L, pbc, B and run configuration c; temperatures and seeds
+    differ) run as one ensemble (``mgx_mc_set_chains``): every pass of a sweep is one launch over the
+    class's sites of all chains, the cone widths adapt on the device every 50 thermalisation sweeps,
+    and the samples of E and the order vector are reduced into a device buffer, read once at the end.
+    Each chain's trajectory is that of its own ``point``.  Points with T = 0 or structure edits run one
+    by one.  ``seconds`` of an ensemble's rows is its wall time divided by its number of chains."""
+    from .lattice import Supercell
+    jobs = list(jobs)
+    rows = [None] * len(jobs)
+    groups = {}
+    for i, job in enumerate(jobs):
+        c, T = job[5], float(job[4])
+        if c.get("structure") or not T > 0:
+            rows[i] = point(job)
+            continue
+        groups.setdefault(_ensemble_key(job), []).append(i)
+    for idxs in groups.values():
+        for k0 in range(0, len(idxs), max_chains):
+            part = idxs[k0:k0 + max_chains]
+            for i, row in zip(part, _ensemble([jobs[i] for i in part], Supercell)):
+                rows[i] = row
+    return rows
+
+
+def _ensemble(jobs, Supercell):
+    uc, L, pbc, B, _, c, _ = jobs[0]
+    n = len(jobs)
+    Ts = [float(j[4]) for j in jobs]
+    seeds = [j[6] for j in jobs]
+    system = Supercell(uc, L, pbc, B)
+    N = system.N
+    mc = MetropolisMC(system, Ts[0], seeds[0], c["sigma"], c["overrelax"], c.get("move", "gaussian"))
+    lib, h = mc.lib, mc.handle
+    keys = np.array([np.random.SeedSequence(s).generate_state(1, np.uint64)[0] for s in seeds], np.uint64)
+    beta = np.array([1.0 / (K_B * T) for T in Ts], np.float64)
+    sig0 = np.full(n, float(c["sigma"]), np.float64)
+    _lib.check(lib.mgx_mc_set_chains(h, n, keys.ctypes.data_as(C.c_void_p), _lib.dptr(beta), _lib.dptr(sig0)),
+               "mgx_mc_set_chains")
+    lat = torch.stack([mc.model.to_lattice(system.init_spins(c["init"], c["init_axis"], s)) for s in seeds])
+    mc.model.sync_field()
+    st = stream_ptr()
+    ptr = C.c_void_p(lat.data_ptr())
+
+    def sweep(k):
+        if k > 0:
+            _lib.check(lib.mgx_mc_sweep(h, ptr, int(k), None, st), "mgx_mc_sweep")
+
+    def counts(reset):
+        acc = np.zeros(n, np.uint64)
+        tried = C.c_uint64()
+        sig = np.zeros(n, np.float64)
+        _lib.check(lib.mgx_mc_chain_counts(h, acc.ctypes.data_as(C.c_void_p), C.byref(tried), _lib.dptr(sig),
+                                           int(reset), st), "mgx_mc_chain_counts")
+        return acc, int(tried.value), sig
+
+    t0 = time.time()
+    therm = int(c["therm_sweeps"])
+    for _ in range(therm // 50):                 # sigma adapts after sweeps 50, 100, ... (as point())
+        sweep(50)
+        _lib.check(lib.mgx_mc_adapt_sigma(h, st), "mgx_mc_adapt_sigma")
+    sweep(therm % 50)
+    counts(True)
+    meas, every = int(c["meas_sweeps"]), int(c["sample_every"])
+    nsamp = (meas + every - 1) // every if meas > 0 else 0
+    obs = torch.empty((max(nsamp, 1), n, 8), dtype=torch.float64, device=lat.device)
+    done = 0
+    for j in range(nsamp):                       # samples after sweeps 1, 1 + every, 1 + 2 every, ...
+        sweep(j * every + 1 - done)
+        done = j * every + 1
+        _lib.check(lib.mgx_observables_n(mc.model.handle, ptr, n, C.c_void_p(obs[j].data_ptr()), st),
+                   "mgx_observables_n")
+    sweep(meas - done)
+    acc, tried, sig = counts(True)
+    o = obs[:nsamp].cpu().numpy()
+    seconds = (time.time() - t0) / n
+    rows = []
+    for k in range(n):
+        v = o[:, k, 4:7] / N
+        spins = mc.model.from_lattice(lat[k]).cpu().numpy() if c.get("keep_spins") else None
+        rows.append(_row_of(L, N, jobs[k][4], list(o[:, k, 0]), [np.linalg.norm(x) for x in v], list(v),
+                            int(acc[k]) / max(tried, 1), float(sig[k]), mc.ncolors, seconds, spins))
+    return rows
 
 
 def _peak(T, y):

@@ -177,3 +177,34 @@ def test_host_rng_sweeps_match_oracle_bcc_16cube(cuda):
         ora.sweep(b)
         assert np.abs(a - b).max() <= 1e-11
         assert gpu.counts() == (ora.accepted, ora.tried)
+
+
+ROW_KEYS = ("L", "N", "T", "E", "C", "m", "chi", "U4", "dE", "dC", "dm", "dchi", "dU4", "acceptance", "sigma",
+            "ncolors", "mvec")
+
+
+@pytest.mark.parametrize("move,overrelax", [("gaussian", 1), ("heatbath", 0), ("hinzke", 1)])
+def test_points_ensemble_equals_single_points(cuda, golden_models, move, overrelax):
+    """points() runs the chains that share a lattice as one ensemble (one launch per class and pass for
+    all chains, cone widths adapted on the device, samples reduced on the device): every row equals
+    the row of its own point() bit for bit (sc 6^3 and two-site bcc 4^3 at several temperatures and
+    seeds, one T = 0 job that runs alone)."""
+    from magex_gb300.mc import point, points
+    from magex_gb300.spinmodel import load_results
+    from magex_gb300.workloads import bcc_two_site_model
+    sc_uc = load_results(golden_models["sc"]["model"])
+    bcc_uc = load_results(bcc_two_site_model())
+    c = dict(sigma=0.6, overrelax=overrelax, move=move, init="random", init_axis=(0.0, 0.0, 1.0),
+             therm_sweeps=120, meas_sweeps=163, sample_every=5)
+    jobs = [(sc_uc, (6, 6, 6), (True, True, True), (0.0, 0.0, 0.2), T, c, seed)
+            for T, seed in ((5.0, 1), (15.0, 2), (25.0, 3), (40.0, 4), (25.0, 5))]
+    jobs += [(bcc_uc, (4, 4, 4), (True, True, True), (0.0, 0.0, 0.5), T, c, seed)
+             for T, seed in ((300.0, 7), (900.0, 8))]
+    if move == "gaussian":
+        jobs.append((sc_uc, (6, 6, 6), (True, True, True), (0.0, 0.0, 0.2), 0.0, c, 9))
+    rows = points(jobs)
+    for job, row in zip(jobs, rows):
+        ref = point(job)
+        for key in ROW_KEYS:       # NaN == NaN: C and chi of the T = 0 job divide by k_B T
+            assert np.array_equal(np.asarray(row[key]), np.asarray(ref[key]), equal_nan=True), \
+                (key, job[4], job[6], row[key], ref[key])
