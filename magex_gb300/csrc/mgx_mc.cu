@@ -71,20 +71,36 @@ struct McRandom {
                                     ((uint32_t)(sweep >> 32) << 12) | ((uint32_t)pass << 4) | (uint32_t)slot),
                          make_uint2((uint32_t)(seed ^ 0x4d43u), (uint32_t)(seed >> 32)));
   }
-  // three N(0, 1) draws by Box-Muller from the two blocks of slots (slot, slot + 1)
+  // three N(0, 1) draws by Box-Muller from the block of slot, in FP32 as the LLG thermal field: the
+  // proposal's precision does not enter the acceptance test, and FP64 log / sincos would be about half
+  // of a trial move's FP64 instructions (slot + 1 stays reserved)
   __device__ static void normal3(uint64_t seed, uint64_t site, uint64_t sweep, int pass, int slot, double& g0,
                                  double& g1, double& g2) {
-    const uint4 a = block(seed, site, sweep, pass, slot);
-    const uint4 b = block(seed, site, sweep, pass, slot + 1);
-    const double m1 = sqrt(-2.0 * log(1.0 - u53(a.x, a.y)));      // 1 - u in (0, 1]
-    const double m2 = sqrt(-2.0 * log(1.0 - u53(b.x, b.y)));
-    double s1, c1;
-    sincospi(2.0 * u53(a.z, a.w), &s1, &c1);
-    g0 = m1 * c1;
-    g1 = m1 * s1;
-    g2 = m2 * cospi(2.0 * u53(b.z, b.w));
+    const uint4 r = block(seed, site, sweep, pass, slot);
+    const float tw = 2.3283064365386963e-10f;                 // 2^-32
+    const float u1 = fmaf((float)r.x, tw, 0.5f * tw);          // (0, 1]
+    const float u3 = fmaf((float)r.z, tw, 0.5f * tw);
+    const float m1 = sqrtf(-2.0f * logf(u1));
+    const float m3 = sqrtf(-2.0f * logf(u3));
+    float s1, c1;
+    sincospif(2.0f * ((float)r.y * tw), &s1, &c1);
+    g0 = (double)(m1 * c1);
+    g1 = (double)(m1 * s1);
+    g2 = (double)(m3 * cospif(2.0f * ((float)r.w * tw)));
   }
 };
+
+// u < exp(x) for -700 <= x <= 0 with u a multiple of 2^-53 (Philox u53 or NumPy's random()): the
+// decision of the FP64 comparison, taken in FP32 unless exp(x) is within 1e-5 of u (the FP32
+// exponential of the rounded argument is within 3e-6 of exp(x) for x >= -40).  Below -40, exp(x)
+// < 2^-53 <= every nonzero u.
+__device__ __forceinline__ bool below_exp(double u, double x) {
+  if (x < -40.0) return u == 0.0;
+  const double ef = (double)expf((float)x);
+  if (u < ef * (1.0 - 1e-5)) return true;
+  if (u >= ef * (1.0 + 1e-5)) return false;
+  return u < exp(x);
+}
 
 __device__ __forceinline__ void normalise3(double& x, double& y, double& z) {
   const double n = sqrt(x * x + y * y + z * z);       // magex normalize: e / |e| (magex/spinmodel.py:553)
@@ -261,7 +277,7 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
     ok = dE <= thr;
     if (!ok) {
       const double a = dE * bt;
-      ok = ua < exp(-(a < 700.0 ? a : 700.0));
+      ok = below_exp(ua, -(a < 700.0 ? a : 700.0));
     }
     if (ok) {
       e[q] = nx;
@@ -283,22 +299,24 @@ static void launch_pass(const McPlan* mc, double* e, int g, const double* hr, in
   const DevLattice& L = mc->model->d;
   const long long n = mc->gsize[g];
   if (n == 0) return;
-  const dim3 grid((unsigned)((n + 127) / 128), (unsigned)mc->nchains);
+  // small classes in small blocks, so that they still spread over the SMs
+  const int tpb = n > 152LL * 128 ? 128 : (n > 152LL * 64 ? 64 : 32);
+  const dim3 grid((unsigned)((n + tpb - 1) / tpb), (unsigned)mc->nchains);
   const long long* sites = mc->sites + mc->goff[g];
   if (mc->fixed) {
     if (hr)
-      k_mc_pass<W, MOVE, true, true><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
+      k_mc_pass<W, MOVE, true, true><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
                                                            mc->seed, mc->sweep, pass, mc->acc, mc->fx, mc->chains);
     else
-      k_mc_pass<W, MOVE, false, true><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
+      k_mc_pass<W, MOVE, false, true><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
                                                             nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
                                                             mc->chains);
   } else {
     if (hr)
-      k_mc_pass<W, MOVE, true, false><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
+      k_mc_pass<W, MOVE, true, false><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
                                                             mc->seed, mc->sweep, pass, mc->acc, mc->fx, mc->chains);
     else
-      k_mc_pass<W, MOVE, false, false><<<grid, 128, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
+      k_mc_pass<W, MOVE, false, false><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
                                                              nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
                                                              mc->chains);
   }

@@ -40,20 +40,28 @@ def test_host_rng_sweeps_match_reference(cuda, golden, golden_models, tag, preci
 
 def test_point_matches_reference_within_3_sigma(cuda, golden_models):
     """magex's (L, T) Monte Carlo point (sc 8^3, J = 1 meV, 25 K, Gaussian moves + over-relaxation,
-    1000 + 4000 sweeps): E/N and m from in-kernel Philox draws within 3 combined standard errors."""
-    from magex_gb300.mc import point
+    1000 + 4000 sweeps) against the reference's run: the mean of 8 independent runs with in-kernel
+    Philox draws (one points() ensemble; its standard error from the spread over the runs) agrees in
+    E/N and m within 3 combined standard errors; each run's own 10-block error matches that spread."""
+    from magex_gb300.mc import point, points
     from magex_gb300.spinmodel import load_results
     g = golden_models["mc_point"]
     ref = g["row"]
     uc = load_results(golden_models["sc"]["model"])
     c = dict(g["c"])
     c["init_axis"] = tuple(c["init_axis"])
-    row = point((uc, tuple(g["L"]), (True, True, True), (0.0, 0.0, 0.0), g["T"], c, 99))
+    jobs = [(uc, tuple(g["L"]), (True, True, True), (0.0, 0.0, 0.0), g["T"], c, seed) for seed in range(91, 99)]
+    rows = points(jobs)
     for key, err in (("E", "dE"), ("m", "dm")):
-        bound = 3.0 * np.hypot(ref[err], row[err])
-        assert abs(row[key] - ref[key]) <= bound, (key, row[key], ref[key], bound)
-    assert abs(row["acceptance"] - ref["acceptance"]) < 0.05
-    assert row["ncolors"] == ref["ncolors"]
+        x = np.array([r[key] for r in rows])
+        sem = x.std(ddof=1) / np.sqrt(len(x))
+        bound = 3.0 * np.hypot(ref[err], sem)
+        assert abs(x.mean() - ref[key]) <= bound, (key, x.mean(), ref[key], bound)
+        assert 0.3 < np.mean([r[err] for r in rows]) / x.std(ddof=1) < 3.0      # block errors are honest
+    assert all(abs(r["acceptance"] - ref["acceptance"]) < 0.05 for r in rows)
+    assert all(r["ncolors"] == ref["ncolors"] for r in rows)
+    single = point(jobs[0])
+    assert single["E"] == rows[0]["E"] and single["m"] == rows[0]["m"]
 
 
 @pytest.mark.parametrize("move", ["gaussian", "uniform", "heatbath", "hinzke"])
