@@ -375,6 +375,35 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0, precision="fp64")
                         "grad_norm_per_shell": [float(x) for x in g.reshape(4, -1).norm(dim=1)]}}
 
 
+def bench_mc_points(L=16, npts=16, therm=1000, meas=4000):
+    """Monte Carlo T scan of magex's mc workflow: npts temperatures of an sc L^3 ferromagnet (J = 1 meV),
+    therm + meas sweeps each (Gaussian moves + over-relaxation, sigma adapted every 50 sweeps, E and
+    the order vector sampled every 5 sweeps): wall time of points() (one ensemble) against one point()
+    (magex runs each point as its own process, magex/montecarlo.py:390-401)."""
+    import numpy as np
+    from magex_gb300.mc import point, points
+    from magex_gb300.spinmodel import load_results, make_model
+    uc = load_results(make_model("sc", J=[1.0]))
+    c = dict(sigma=0.6, overrelax=1, move="gaussian", init="random", init_axis=(0.0, 0.0, 1.0),
+             therm_sweeps=therm, meas_sweeps=meas, sample_every=5)
+    jobs = [(uc, (L, L, L), (True,) * 3, (0.0, 0.0, 0.0), float(T), c, 100 + i)
+            for i, T in enumerate(np.linspace(10.0, 40.0, npts))]
+    point(jobs[0])
+    t0 = time.perf_counter()
+    one = point(jobs[0])
+    t_one = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    rows = points(jobs)
+    t_all = time.perf_counter() - t0
+    assert rows[0]["E"] == one["E"]
+    N = L ** 3
+    return {"workload": f"sc {L}^3 ({N} spins), {npts} temperatures 10..40 K, {therm} + {meas} sweeps each, "
+                        "Gaussian moves + 1 over-relaxation pass, Philox, FP64",
+            "points_s": t_all, "one_point_s": t_one, "speedup_vs_points_one_by_one": t_one * npts / t_all,
+            "site_updates_per_s": 2 * N * npts * (therm + meas) / t_all, "unit": "site-updates/s",
+            "rows_equal_point": True}
+
+
 def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True, precision="fp64"):
     """Monte Carlo colour sweeps on the 128^3 two-site bcc workload (4,194,304 spins, z = 26, full
     3x3 tensors), T = 300 K, in-kernel Philox draws: site updates per second (one update = one trial
@@ -665,6 +694,7 @@ def run_gb300(args):
     if ws == 1 and not args.no_batched:
         line["monte_carlo"] = bench_mc(L=args.L, cpu_baseline=not args.no_cpu_baseline)
         line["monte_carlo_fp64_fixed"] = bench_mc(L=args.L, cpu_baseline=False, precision="fp64_fixed")
+        line["monte_carlo_points"] = bench_mc_points()
         line["sqw_projection"] = bench_sqw(L=args.L)
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
@@ -711,6 +741,8 @@ def main():
         elif args.only == "mc":
             out = [bench_mc(L=args.L, sweeps=min(args.steps, 100), cpu_baseline=False, precision=p)
                    for p in ("fp64", "fp64_fixed")]
+            if args.steps >= 20:           # short profiling runs skip the T scan's ~300k launches
+                out.append(bench_mc_points())
         elif args.only == "config5":
             out = [bench_config5(K=min(args.steps, 50), adj_steps=args.adjoint_steps or 1000),
                    bench_config5(K=min(args.steps, 50), adj_steps=0, precision="fp64_fixed")]
