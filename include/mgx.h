@@ -175,6 +175,11 @@ mgx_status mgx_llg_predicted_split(mgx_llg* plan, void** eps);
 /* Thermal-field amplitude sigma_i = sqrt(2 alpha_i k_B T_i / (gamma mu_i mu_B dt)) (magex/llg.py:111):
  * per sublattice (host [ns]) or per site (host [N] magex order, overrides).  Zero means no noise. */
 mgx_status mgx_llg_set_sigma(mgx_llg* plan, const double* sigma_sub, const double* sigma_site);
+/* Per-site field (T) added to the effective field of both stages from now on: device [3*N], lattice
+ * layout, read at every launch (the caller rewrites it between stages for a field that depends on the
+ * spins, as magex evaluates extra_field(e) at e and at the predicted spins, magex/llg.py:124-137);
+ * NULL removes it.  FP64 plans (MGX_ERR_UNSUPPORTED otherwise). */
+mgx_status mgx_llg_set_extra_field(mgx_llg* plan, const double* B_add);
 
 /* One stochastic Heun step in place on e (device, lattice layout):
  *   b = sigma * xi;  k1 = f(e, B(e) + b);  ep = |e + dt k1|^-1 (e + dt k1);

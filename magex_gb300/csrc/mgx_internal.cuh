@@ -96,6 +96,9 @@ struct DevLLG {
   double* k1;                // [3][N] predictor slope (Heun) or rotation rate (Depondt)
   // CUDA-graph replays: the Philox step index is *step_base + the launch's step argument
   const unsigned long long* step_base = nullptr;
+  // caller-supplied per-site field added to the effective field of both stages ([3][N], lattice
+  // layout; mgx_llg_set_extra_field), or nullptr
+  const double* B_add = nullptr;
 };
 
 // Tables of the compensated-FP32 gather (MGX_PRECISION_DF32_GATHER): every coupling as 9 (hi, lo)

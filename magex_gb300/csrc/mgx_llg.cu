@@ -258,6 +258,16 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
   return MGX_OK;
 }
 
+mgx_status mgx_llg_set_extra_field(mgx_llg* pp, const double* B_add) {
+  LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
+  if (!pl) return set_error(MGX_ERR_INVALID, "mgx_llg_set_extra_field: null plan");
+  if (B_add && pl->precision != MGX_PRECISION_FP64)
+    return set_error(MGX_ERR_UNSUPPORTED, "a per-site extra field needs an FP64 plan");
+  if (B_add != pl->p.B_add) drop_llg_graph(pl);      // captured launches hold the pointer by value
+  pl->p.B_add = B_add;
+  return MGX_OK;
+}
+
 mgx_status mgx_llg_predicted(mgx_llg* pp, double** ep) {
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl || !ep) return set_error(MGX_ERR_INVALID, "mgx_llg_predicted: null argument");

@@ -32,6 +32,15 @@ __device__ __forceinline__ void rotate(double& x, double& y, double& z, double w
   z = nz;
 }
 
+// B += the caller's per-site field of this stage (magex's extra_field, magex/llg.py:131-132)
+__device__ __forceinline__ void add_extra(const DevLLG& P, long long N, long long q, double& bx, double& by,
+                                          double& bz) {
+  if (!P.B_add) return;
+  bx += __ldg(P.B_add + q);
+  by += __ldg(P.B_add + N + q);
+  bz += __ldg(P.B_add + 2 * N + q);
+}
+
 template <int NOISE>
 __device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P, const double* __restrict__ noise,
                                             long long q, int s, uint64_t step, double& bx, double& by, double& bz) {
@@ -70,6 +79,7 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
   site_coords(L, q, s, c0, c1, c2);
   double bx, by, bz;
   effective_field<W>(L, e, q, s, c0, c1, c2, ex, ey, ez, bx, by, bz);
+  add_extra(P, N, q, bx, by, bz);
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
   if (Hout) {
     Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
@@ -122,6 +132,7 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
   const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
   double bx, by, bz;
   effective_field<W>(L, P.ep, q, s, c0, c1, c2, px, py, pz, bx, by, bz);
+  add_extra(P, N, q, bx, by, bz);
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
   if (Hout) {
     Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;

@@ -208,6 +208,14 @@ class DeviceModel:
             _lib.check(self.lib.mgx_model_set_field(self.handle, arr), "mgx_model_set_field")
             self._B = B.copy()
 
+    def push_field(self, B):
+        """Set the device model's external field to B (T) now; sync_field restores the owner's field
+        when that differs."""
+        B = np.asarray(B, float).reshape(3)
+        arr = (C.c_double * 3)(*[float(x) for x in B])
+        _lib.check(self.lib.mgx_model_set_field(self.handle, arr), "mgx_model_set_field")
+        self._B = B.copy()
+
     # ------------------------------------------------------------------ layout
     def to_lattice(self, e, out=None, stream=None):
         """(N, 3) spins (numpy or torch, any device) -> (3, N) float64 lattice-layout tensor."""

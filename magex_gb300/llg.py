@@ -164,14 +164,54 @@ class GB300LLG:
             _lib.check(lib.mgx_llg_set_sigma(self.handle, _lib.dptr(sig), None), "mgx_llg_set_sigma")
 
     # ------------------------------------------------------------------ stepping on device
+    def _has_callables(self):
+        return self.field_func is not None or self.extra_field is not None
+
     def _check_supported_callables(self):
-        if self.field_func is not None or self.extra_field is not None:
-            raise NotImplementedError("field_func / extra_field callables are not supported by the GB300 kernels")
+        if self._has_callables():
+            raise NotImplementedError("field_func / extra_field: step with step_lattice / run_lattice / step / run")
+
+    def _uniform_field(self, t):
+        f = np.asarray(self.field_func(t), float)
+        if f.size != 3:
+            raise NotImplementedError("field_func must return one uniform (3,) field for the GB300 kernels "
+                                      "(use extra_field for a per-site field)")
+        return f.reshape(3)
+
+    def _step_callables(self, lat, noise_ptr, stream):
+        """One step with magex's field hooks (magex/llg.py:124-137,216-227): the predictor sees
+        field_func(t) and extra_field(e), the corrector field_func(t + dt) and extra_field(ep).  The
+        uniform part goes into the model's external field, the per-site part into the plan's extra field
+        (mgx_llg_set_extra_field); the kernels are the plain predictor and corrector."""
+        lib, N = self.model.lib, self.sc.N
+        B0 = np.asarray(self.model._B, float).copy()
+        ep = C.c_void_p()
+        _lib.check(lib.mgx_llg_predicted(self.handle, C.byref(ep)), "mgx_llg_predicted")
+        try:
+            for stage, t in ((0, self.time), (1, self.time + self.dt)):
+                if self.field_func is not None:
+                    self.model.push_field(B0 + self._uniform_field(t))
+                if self.extra_field is not None:
+                    src = lat.data_ptr() if stage == 0 else ep.value
+                    aos = torch.empty((N, 3), dtype=torch.float64, device=self.device)
+                    _lib.check(lib.mgx_unpack_spins(self.model.handle, C.c_void_p(src), C.c_void_p(aos.data_ptr()),
+                                                    stream_ptr(stream)), "mgx_unpack_spins")
+                    xf = np.asarray(self.extra_field(aos.cpu().numpy()), float).reshape(N, 3)
+                    self._xf_lat = self.model.to_lattice(xf, out=getattr(self, "_xf_lat", None), stream=stream)
+                    _lib.check(lib.mgx_llg_set_extra_field(self.handle, C.c_void_p(self._xf_lat.data_ptr())),
+                               "mgx_llg_set_extra_field")
+                _lib.check(lib.mgx_llg_stage(self.handle, C.c_int32(stage), C.c_void_p(lat.data_ptr()), noise_ptr,
+                                             C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_stage")
+        finally:
+            if self.field_func is not None:
+                self.model.push_field(B0)
+            if self.extra_field is not None:
+                _lib.check(lib.mgx_llg_set_extra_field(self.handle, None), "mgx_llg_set_extra_field")
+        self._advance()
 
     def _prepare_step(self, stream):
         """Field and thermal amplitudes up to date; the device noise pointer of this step (host-noise
         mode: this step's N(0,1) draws from the NumPy stream, packed to the lattice layout)."""
-        self._check_supported_callables()
         self.model.sync_field()
         self._update_sigma()
         if self.noise != "host":
@@ -191,6 +231,9 @@ class GB300LLG:
     def step_lattice(self, lat, stream=None):
         """One step on device spins in the lattice layout ((3, N) float64, in place)."""
         noise_ptr = self._prepare_step(stream)
+        if self._has_callables():
+            self._step_callables(lat, noise_ptr, stream)
+            return lat
         _lib.check(self.model.lib.mgx_llg_step(self.handle, C.c_void_p(lat.data_ptr()), noise_ptr,
                                                C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_step")
         self._advance()
@@ -204,6 +247,12 @@ class GB300LLG:
         for name, t in (("e", e), ("out", out)):
             if t.is_cuda or t.dtype != torch.float64 or tuple(t.shape) != (N, 3) or not t.is_contiguous():
                 raise ValueError(f"{name} must be a contiguous ({N}, 3) float64 CPU tensor")
+        if self._has_callables():            # the hooks run between the stages: no overlapped copies
+            lat = self.model.to_lattice(e, out=self._lat)
+            self._lat = lat
+            self.step_lattice(lat)
+            out.copy_(self.model.from_lattice(lat))
+            return out
         stream = torch.cuda.current_stream(self.device)
         noise_ptr = self._prepare_step(stream)
         _lib.check(self.model.lib.mgx_llg_step_host(self.handle, C.c_void_p(e.data_ptr()), C.c_void_p(out.data_ptr()),
@@ -215,11 +264,10 @@ class GB300LLG:
 
     def run_lattice(self, lat, nsteps, stream=None):
         """nsteps steps on device lattice-layout spins; Philox noise only (one library call)."""
-        if self.noise == "host":
+        if self.noise == "host" or self._has_callables():
             for _ in range(int(nsteps)):
                 self.step_lattice(lat, stream)
             return lat
-        self._check_supported_callables()
         self.model.sync_field()
         self._update_sigma()
         _lib.check(self.model.lib.mgx_llg_run(self.handle, C.c_void_p(lat.data_ptr()), C.c_int64(int(nsteps)),
@@ -251,13 +299,16 @@ class GB300LLG:
         a CPU tensor, written into ``out`` when given.  Host arrays go through one library call
         (``step_host``)."""
         N = self.sc.N
-        if isinstance(e, torch.Tensor) and e.is_cuda:
+        if self._has_callables() or (isinstance(e, torch.Tensor) and e.is_cuda):
+            on_device = isinstance(e, torch.Tensor) and e.is_cuda
             lat = self.model.to_lattice(e, out=self._lat)
             self._lat = lat
             self.step_lattice(lat)
             dev = self.model.from_lattice(lat, out=getattr(self, "_aos", None))
             self._aos = dev
-            return dev.clone() if out is None else out.copy_(dev)
+            if on_device or isinstance(e, torch.Tensor):
+                return dev.clone().to(e.device) if out is None else out.copy_(dev)
+            return dev.cpu().numpy()
         if isinstance(e, torch.Tensor):
             src = e if (e.dtype == torch.float64 and e.is_contiguous()) else e.to(torch.float64).contiguous()
             if src.shape != (N, 3):
@@ -320,7 +371,8 @@ class GB300LLG:
                 float(np.linalg.norm(obs[4:7]) / N), float(obs[7])]
 
     def max_torque(self, e):
-        """max_i |e_i x B_eff,i| (T) (magex/llg.py:250-252)."""
+        """max_i |e_i x B_eff,i| (T) of the system's effective field, without field_func / extra_field
+        (magex/llg.py:250-252)."""
         return float(self.model.observables(self.model.to_lattice(e))[7].item())
 
     def effective_field(self, e):

@@ -166,6 +166,32 @@ def main(ref_root):
                    exchange_scale=[[1.0, 0.5], [0.5, 0.8]],
                    pinned=[dict(region="bottom", layers=1)]), 0.1, 1e-3, 0.0, 5, 20)
 
+    # time-dependent uniform field (field_func) and state-dependent per-site field (extra_field) on the
+    # solver, magex/llg.py:124-137; the callables are rebuilt from these parameters by the tests
+    sys.path.insert(0, os.path.dirname(HERE))
+    from helpers import callable_fields
+    cparams = dict(pulse=[0.05, 0.0, 0.0], t0=4.5 * 2e-3, amp=0.1, w=50.0, k=[0.0, 0.0, 1.0], c=0.2)
+    ff, xf = callable_fields(cparams)
+    models["callables"] = dict(params=cparams, cases={})
+    for tag, model, L, pbc, B, alpha, dt, steps, keep, use_ff, use_xf, integ in (
+            ("pulse", "sc_dmi", (5, 5, 2), (1, 1, 1), (0.0, 0.0, 0.3), 0.02, 2e-3, 30, {4, 5, 30}, True, False, "heun"),
+            ("extra", "sc_dmi", (4, 4, 4), (1, 1, 1), (0.1, 0.0, 0.4), 0.1, 1e-3, 20, {1, 20}, False, True, "heun"),
+            ("both", "tri", (6, 6, 1), (1, 1, 0), (0.0, 0.0, 1.0), 0.05, 1e-3, 15, {1, 15}, True, True, "depondt")):
+        s = RS.SpinSystem(ucs[model], L, pbc, B)
+        sol = LLGSolver(s, alpha, dt, 0.0, 3, integrator=integ)
+        sol.field_func = ff if use_ff else None
+        sol.extra_field = xf if use_xf else None
+        e = s.init_spins("random", seed=4)
+        out[f"callables/{tag}/e0"] = e.copy()
+        for n in range(1, steps + 1):
+            e = sol.step(e)
+            if n in keep:
+                out[f"callables/{tag}/e{n}"] = e.copy()
+        out[f"callables/{tag}/torque"] = np.array(sol.max_torque(e))
+        models["callables"]["cases"][tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], B=list(B),
+                                                  alpha=alpha, dt=dt, steps=steps, keep=sorted(keep),
+                                                  field_func=use_ff, extra_field=use_xf, integrator=integ)
+
     # Larmor precession of one free spin (magex tests/test_spindyn.py:36-45)
     s = RS.SpinSystem(uc_of("free", RM.make_model("sc", J=[0.0])), (1, 1, 1), field=(0, 0, 2.0))
     sol = LLGSolver(s, alpha=0.0, dt=1e-3)

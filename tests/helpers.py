@@ -106,3 +106,20 @@ def mc_system(golden, golden_models, tag):
     if meta["structure"]:
         apply_structure_subset(sc, meta["structure"])
     return sc, meta
+
+
+def callable_fields(p):
+    """field_func(t) and extra_field(e) of the callables fixtures, from their stored parameters: a
+    uniform field with a pulse that ends at t0 (the FMR kick of magex/programs.py:131) plus a rotating
+    component, and a state-dependent per-site field (the extra_field hook of magex/sld.py:171)."""
+    pulse, t0, amp, w = np.asarray(p["pulse"], float), float(p["t0"]), float(p["amp"]), float(p["w"])
+    k, c = np.asarray(p["k"], float), float(p["c"])
+
+    def field_func(t):
+        f = np.array([0.0, amp * np.sin(w * t), 0.0])
+        return f + pulse if t < t0 else f
+
+    def extra_field(e):
+        return c * np.cross(e, k) + 0.5 * c * e[:, [1, 2, 0]]
+
+    return field_func, extra_field

@@ -342,3 +342,39 @@ def test_site_relabelling_gives_the_same_spins(cuda, golden, golden_models, tag)
         eb = b.step(eb)
     assert np.array_equal(eb, ea[perm])
     assert b.energy(eb) == pytest.approx(a.energy(ea), rel=1e-13, abs=1e-12)
+
+
+@pytest.mark.parametrize("tag", ["pulse", "extra", "both"])
+def test_field_hooks_match_reference(cuda, golden, golden_models, tag):
+    """magex's field hooks on the solver (magex/llg.py:124-137), as magex's FMR program and spin-lattice
+    coupling use them (magex/programs.py:131, magex/sld.py:171): a uniform field_func(t) whose pulse
+    ends between a predictor (t) and its corrector (t + dt), plus a rotating part, and a per-site
+    extra_field(e) evaluated at e and at the predicted spins; Heun and Depondt.  Trajectories and the
+    max torque (field of LLGSolver.field) against the reference's; run() equals the step loop."""
+    from helpers import callable_fields
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    cal = golden_models["callables"]
+    case = cal["cases"][tag]
+    ff, xf = callable_fields(cal["params"])
+    sc = Supercell(load_results(golden_models[case["model"]]["model"]), case["L"], case["pbc"], case["B"])
+
+    def solver():
+        sol = GB300LLG(sc, case["alpha"], case["dt"], 0.0, 3, integrator=case["integrator"])
+        sol.field_func = ff if case["field_func"] else None
+        sol.extra_field = xf if case["extra_field"] else None
+        return sol
+
+    sol = solver()
+    e = golden[f"callables/{tag}/e0"].copy()
+    for n in range(1, case["steps"] + 1):
+        e = sol.step(e)
+        if n in case["keep"]:
+            err = np.abs(e - golden[f"callables/{tag}/e{n}"]).max()
+            assert err <= 1e-12 * n, (tag, n, err)
+    tq = float(golden[f"callables/{tag}/torque"])
+    assert abs(sol.max_torque(e) - tq) <= 1e-10 * max(1.0, tq)
+    e_run, table, _ = solver().run(golden[f"callables/{tag}/e0"].copy(), case["steps"], output_every=case["steps"])
+    assert np.array_equal(e_run, e)
+    assert table[-1, 6] == pytest.approx(tq, rel=1e-10, abs=1e-10)
