@@ -180,6 +180,10 @@ mgx_status mgx_llg_set_sigma(mgx_llg* plan, const double* sigma_sub, const doubl
  * spins, as magex evaluates extra_field(e) at e and at the predicted spins, magex/llg.py:124-137);
  * NULL removes it.  FP64 plans (MGX_ERR_UNSUPPORTED otherwise). */
 mgx_status mgx_llg_set_extra_field(mgx_llg* plan, const double* B_add);
+/* Spin-orbit torque as effective fields B_DL e x p + B_FL p at each stage's spins, p normalised here
+ * (LLGSolver(sot={p, B_DL, B_FL}), magex/llg.py:84-86,126-128); B_DL = B_FL = 0 removes it.  FP64
+ * plans (MGX_ERR_UNSUPPORTED otherwise). */
+mgx_status mgx_llg_set_sot(mgx_llg* plan, const double p[3], double B_DL, double B_FL);
 
 /* One stochastic Heun step in place on e (device, lattice layout):
  *   b = sigma * xi;  k1 = f(e, B(e) + b);  ep = |e + dt k1|^-1 (e + dt k1);

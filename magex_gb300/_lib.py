@@ -75,6 +75,7 @@ SIGNATURES = {
     "mgx_llg_destroy": (C.c_int32, [C.c_void_p]),
     "mgx_llg_set_sigma": (C.c_int32, [C.c_void_p, _dp, _dp]),
     "mgx_llg_set_extra_field": (C.c_int32, [C.c_void_p, C.c_void_p]),
+    "mgx_llg_set_sot": (C.c_int32, [C.c_void_p, _dp, C.c_double, C.c_double]),
     "mgx_llg_step": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "mgx_llg_run": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int64, C.c_uint64, C.c_void_p]),
     "mgx_llg_stage": (C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),

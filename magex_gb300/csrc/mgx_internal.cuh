@@ -99,6 +99,9 @@ struct DevLLG {
   // caller-supplied per-site field added to the effective field of both stages ([3][N], lattice
   // layout; mgx_llg_set_extra_field), or nullptr
   const double* B_add = nullptr;
+  // spin-orbit torque as effective fields B_DL e x p + B_FL p (mgx_llg_set_sot); sot = 0: none
+  int sot = 0;
+  double sot_p0 = 0.0, sot_p1 = 0.0, sot_p2 = 0.0, sot_dl = 0.0, sot_fl = 0.0;
 };
 
 // Tables of the compensated-FP32 gather (MGX_PRECISION_DF32_GATHER): every coupling as 9 (hi, lo)

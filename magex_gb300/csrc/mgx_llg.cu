@@ -268,6 +268,26 @@ mgx_status mgx_llg_set_extra_field(mgx_llg* pp, const double* B_add) {
   return MGX_OK;
 }
 
+mgx_status mgx_llg_set_sot(mgx_llg* pp, const double p[3], double B_DL, double B_FL) {
+  LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
+  if (!pl || !p) return set_error(MGX_ERR_INVALID, "mgx_llg_set_sot: null argument");
+  const double n = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+  const bool on = B_DL != 0.0 || B_FL != 0.0;
+  if (on && !(n > 0.0 && std::isfinite(n) && std::isfinite(B_DL) && std::isfinite(B_FL)))
+    return set_error(MGX_ERR_INVALID, "mgx_llg_set_sot: p must be a finite non-zero vector, B_DL and B_FL finite");
+  if (on && pl->precision != MGX_PRECISION_FP64)
+    return set_error(MGX_ERR_UNSUPPORTED, "spin-orbit torque needs an FP64 plan");
+  drop_llg_graph(pl);                                 // captured launches hold the parameters by value
+  DevLLG& d = pl->p;
+  d.sot = on ? 1 : 0;
+  d.sot_p0 = on ? p[0] / n : 0.0;
+  d.sot_p1 = on ? p[1] / n : 0.0;
+  d.sot_p2 = on ? p[2] / n : 0.0;
+  d.sot_dl = B_DL;
+  d.sot_fl = B_FL;
+  return MGX_OK;
+}
+
 mgx_status mgx_llg_predicted(mgx_llg* pp, double** ep) {
   LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
   if (!pl || !ep) return set_error(MGX_ERR_INVALID, "mgx_llg_predicted: null argument");

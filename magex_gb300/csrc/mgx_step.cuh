@@ -41,6 +41,16 @@ __device__ __forceinline__ void add_extra(const DevLLG& P, long long N, long lon
   bz += __ldg(P.B_add + 2 * N + q);
 }
 
+// B += B_DL e x p + B_FL p at the stage's spin e (spin-orbit torque as effective fields,
+// magex/llg.py:126-128,158-160)
+__device__ __forceinline__ void add_sot(const DevLLG& P, double x, double y, double z, double& bx, double& by,
+                                        double& bz) {
+  if (!P.sot) return;
+  bx += fma(P.sot_dl, y * P.sot_p2 - z * P.sot_p1, P.sot_fl * P.sot_p0);
+  by += fma(P.sot_dl, z * P.sot_p0 - x * P.sot_p2, P.sot_fl * P.sot_p1);
+  bz += fma(P.sot_dl, x * P.sot_p1 - y * P.sot_p0, P.sot_fl * P.sot_p2);
+}
+
 template <int NOISE>
 __device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P, const double* __restrict__ noise,
                                             long long q, int s, uint64_t step, double& bx, double& by, double& bz) {
@@ -79,6 +89,7 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
   site_coords(L, q, s, c0, c1, c2);
   double bx, by, bz;
   effective_field<W>(L, e, q, s, c0, c1, c2, ex, ey, ez, bx, by, bz);
+  add_sot(P, ex, ey, ez, bx, by, bz);
   add_extra(P, N, q, bx, by, bz);
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
   if (Hout) {
@@ -132,6 +143,7 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
   const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
   double bx, by, bz;
   effective_field<W>(L, P.ep, q, s, c0, c1, c2, px, py, pz, bx, by, bz);
+  add_sot(P, px, py, pz, bx, by, bz);
   add_extra(P, N, q, bx, by, bz);
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
   if (Hout) {

@@ -66,8 +66,10 @@ class GB300LLG:
                                       "(heun and depondt are)")
         if thermostat != "classical":
             raise NotImplementedError("the quantum thermostat is not implemented by the GB300 kernels")
-        if stt or sot:
-            raise NotImplementedError("spin-transfer / spin-orbit torques are not implemented by the GB300 kernels")
+        if stt:
+            raise NotImplementedError("spin-transfer torque (spin-current gradients) is not implemented by the GB300 kernels")
+        if sot and precision != "fp64":
+            raise NotImplementedError("spin-orbit torque needs precision='fp64'")
         if backend not in ("gb300", "auto"):
             raise ValueError("backend must be 'gb300'")
         if noise not in ("philox", "host"):
@@ -118,6 +120,13 @@ class GB300LLG:
             _lib.check(self.model.lib.mgx_llg_create(self.model.handle, C.byref(p), C.byref(h)), "mgx_llg_create")
         del al
         self.handle = h
+        self.sot = None
+        if sot:
+            # magex/llg.py:84-86: p normalised, damping-like and field-like amplitudes in tesla
+            pv = np.asarray(sot.get("p", [0, 1, 0]), float)
+            self.sot = (pv / np.linalg.norm(pv), float(sot.get("B_DL", 0.0)), float(sot.get("B_FL", 0.0)))
+            _lib.check(self.model.lib.mgx_llg_set_sot(self.handle, _lib.dptr(np.ascontiguousarray(pv)), self.sot[1],
+                                                      self.sot[2]), "mgx_llg_set_sot")
         self._sigma_key = None
         self._noisy = False
         self._noise_lat = None
@@ -171,42 +180,44 @@ class GB300LLG:
         if self._has_callables():
             raise NotImplementedError("field_func / extra_field: step with step_lattice / run_lattice / step / run")
 
-    def _uniform_field(self, t):
-        f = np.asarray(self.field_func(t), float)
-        if f.size != 3:
-            raise NotImplementedError("field_func must return one uniform (3,) field for the GB300 kernels "
-                                      "(use extra_field for a per-site field)")
-        return f.reshape(3)
-
     def _step_callables(self, lat, noise_ptr, stream):
         """One step with magex's field hooks (magex/llg.py:124-137,216-227): the predictor sees
-        field_func(t) and extra_field(e), the corrector field_func(t + dt) and extra_field(ep).  The
-        uniform part goes into the model's external field, the per-site part into the plan's extra field
-        (mgx_llg_set_extra_field); the kernels are the plain predictor and corrector."""
+        field_func(t) and extra_field(e), the corrector field_func(t + dt) and extra_field(ep).  A
+        uniform (3,) field_func goes into the model's external field; (N, 3) fields are summed on the
+        host into the plan's per-site field (mgx_llg_set_extra_field).  The kernels are the plain
+        predictor and corrector."""
         lib, N = self.model.lib, self.sc.N
         B0 = np.asarray(self.model._B, float).copy()
         ep = C.c_void_p()
         _lib.check(lib.mgx_llg_predicted(self.handle, C.byref(ep)), "mgx_llg_predicted")
         try:
             for stage, t in ((0, self.time), (1, self.time + self.dt)):
+                uni, site = None, None
                 if self.field_func is not None:
-                    self.model.push_field(B0 + self._uniform_field(t))
+                    f = np.asarray(self.field_func(t), float)
+                    if f.size == 3:
+                        uni = f.reshape(3)
+                    else:
+                        site = f.reshape(N, 3).copy()
                 if self.extra_field is not None:
                     src = lat.data_ptr() if stage == 0 else ep.value
                     aos = torch.empty((N, 3), dtype=torch.float64, device=self.device)
                     _lib.check(lib.mgx_unpack_spins(self.model.handle, C.c_void_p(src), C.c_void_p(aos.data_ptr()),
                                                     stream_ptr(stream)), "mgx_unpack_spins")
                     xf = np.asarray(self.extra_field(aos.cpu().numpy()), float).reshape(N, 3)
-                    self._xf_lat = self.model.to_lattice(xf, out=getattr(self, "_xf_lat", None), stream=stream)
-                    _lib.check(lib.mgx_llg_set_extra_field(self.handle, C.c_void_p(self._xf_lat.data_ptr())),
-                               "mgx_llg_set_extra_field")
+                    site = xf if site is None else site + xf
+                self.model.push_field(B0 + uni if uni is not None else B0)
+                if site is not None:
+                    self._xf_lat = self.model.to_lattice(site, out=getattr(self, "_xf_lat", None), stream=stream)
+                    ptr = C.c_void_p(self._xf_lat.data_ptr())
+                else:
+                    ptr = None
+                _lib.check(lib.mgx_llg_set_extra_field(self.handle, ptr), "mgx_llg_set_extra_field")
                 _lib.check(lib.mgx_llg_stage(self.handle, C.c_int32(stage), C.c_void_p(lat.data_ptr()), noise_ptr,
                                              C.c_uint64(self._step_index), stream_ptr(stream)), "mgx_llg_stage")
         finally:
-            if self.field_func is not None:
-                self.model.push_field(B0)
-            if self.extra_field is not None:
-                _lib.check(lib.mgx_llg_set_extra_field(self.handle, None), "mgx_llg_set_extra_field")
+            self.model.push_field(B0)
+            _lib.check(lib.mgx_llg_set_extra_field(self.handle, None), "mgx_llg_set_extra_field")
         self._advance()
 
     def _prepare_step(self, stream):

@@ -169,17 +169,23 @@ def main(ref_root):
     # time-dependent uniform field (field_func) and state-dependent per-site field (extra_field) on the
     # solver, magex/llg.py:124-137; the callables are rebuilt from these parameters by the tests
     sys.path.insert(0, os.path.dirname(HERE))
-    from helpers import callable_fields
+    from helpers import callable_fields, site_field_func
     cparams = dict(pulse=[0.05, 0.0, 0.0], t0=4.5 * 2e-3, amp=0.1, w=50.0, k=[0.0, 0.0, 1.0], c=0.2)
+    sot = dict(p=[0.3, 1.0, 0.2], B_DL=0.4, B_FL=0.15)
     ff, xf = callable_fields(cparams)
-    models["callables"] = dict(params=cparams, cases={})
-    for tag, model, L, pbc, B, alpha, dt, steps, keep, use_ff, use_xf, integ in (
-            ("pulse", "sc_dmi", (5, 5, 2), (1, 1, 1), (0.0, 0.0, 0.3), 0.02, 2e-3, 30, {4, 5, 30}, True, False, "heun"),
-            ("extra", "sc_dmi", (4, 4, 4), (1, 1, 1), (0.1, 0.0, 0.4), 0.1, 1e-3, 20, {1, 20}, False, True, "heun"),
-            ("both", "tri", (6, 6, 1), (1, 1, 0), (0.0, 0.0, 1.0), 0.05, 1e-3, 15, {1, 15}, True, True, "depondt")):
+    models["callables"] = dict(params=cparams, sot=sot, cases={})
+    # use_ff: 0 none, 1 uniform field_func, 2 per-site field_func
+    for tag, model, L, pbc, B, alpha, dt, steps, keep, use_ff, use_xf, use_sot, integ in (
+            ("pulse", "sc_dmi", (5, 5, 2), (1, 1, 1), (0.0, 0.0, 0.3), 0.02, 2e-3, 30, {4, 5, 30}, 1, False, False,
+             "heun"),
+            ("extra", "sc_dmi", (4, 4, 4), (1, 1, 1), (0.1, 0.0, 0.4), 0.1, 1e-3, 20, {1, 20}, 0, True, False, "heun"),
+            ("both", "tri", (6, 6, 1), (1, 1, 0), (0.0, 0.0, 1.0), 0.05, 1e-3, 15, {1, 15}, 1, True, False, "depondt"),
+            ("sot", "sc_dmi", (4, 4, 4), (1, 1, 1), (0.0, 0.0, 0.2), 0.05, 1e-3, 20, {1, 20}, 0, False, True, "heun"),
+            ("sot_site", "tri", (6, 6, 1), (1, 1, 0), (0.0, 0.0, 1.0), 0.05, 1e-3, 15, {1, 15}, 2, False, True,
+             "depondt")):
         s = RS.SpinSystem(ucs[model], L, pbc, B)
-        sol = LLGSolver(s, alpha, dt, 0.0, 3, integrator=integ)
-        sol.field_func = ff if use_ff else None
+        sol = LLGSolver(s, alpha, dt, 0.0, 3, integrator=integ, sot=sot if use_sot else None)
+        sol.field_func = {0: None, 1: ff, 2: site_field_func(cparams, s.N)}[use_ff]
         sol.extra_field = xf if use_xf else None
         e = s.init_spins("random", seed=4)
         out[f"callables/{tag}/e0"] = e.copy()
@@ -190,7 +196,8 @@ def main(ref_root):
         out[f"callables/{tag}/torque"] = np.array(sol.max_torque(e))
         models["callables"]["cases"][tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], B=list(B),
                                                   alpha=alpha, dt=dt, steps=steps, keep=sorted(keep),
-                                                  field_func=use_ff, extra_field=use_xf, integrator=integ)
+                                                  field_func=use_ff, extra_field=use_xf, sot=use_sot,
+                                                  integrator=integ)
 
     # Larmor precession of one free spin (magex tests/test_spindyn.py:36-45)
     s = RS.SpinSystem(uc_of("free", RM.make_model("sc", J=[0.0])), (1, 1, 1), field=(0, 0, 2.0))

@@ -123,3 +123,15 @@ def callable_fields(p):
         return c * np.cross(e, k) + 0.5 * c * e[:, [1, 2, 0]]
 
     return field_func, extra_field
+
+
+def site_field_func(p, N):
+    """A field_func(t) that returns an (N, 3) field (magex allows either shape, magex/llg.py:87): a
+    fixed site pattern times a slow oscillation."""
+    amp, w = float(p["amp"]), float(p["w"])
+    pattern = np.linspace(-1.0, 1.0, N)[:, None] * np.array([0.5, -0.2, 0.3])
+
+    def field_func(t):
+        return amp * np.cos(w * t) * pattern
+
+    return field_func

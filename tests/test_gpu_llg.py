@@ -344,14 +344,15 @@ def test_site_relabelling_gives_the_same_spins(cuda, golden, golden_models, tag)
     assert b.energy(eb) == pytest.approx(a.energy(ea), rel=1e-13, abs=1e-12)
 
 
-@pytest.mark.parametrize("tag", ["pulse", "extra", "both"])
+@pytest.mark.parametrize("tag", ["pulse", "extra", "both", "sot", "sot_site"])
 def test_field_hooks_match_reference(cuda, golden, golden_models, tag):
     """magex's field hooks on the solver (magex/llg.py:124-137), as magex's FMR program and spin-lattice
     coupling use them (magex/programs.py:131, magex/sld.py:171): a uniform field_func(t) whose pulse
-    ends between a predictor (t) and its corrector (t + dt), plus a rotating part, and a per-site
-    extra_field(e) evaluated at e and at the predicted spins; Heun and Depondt.  Trajectories and the
-    max torque (field of LLGSolver.field) against the reference's; run() equals the step loop."""
-    from helpers import callable_fields
+    ends between a predictor (t) and its corrector (t + dt), plus a rotating part; an (N, 3)
+    field_func(t); a per-site extra_field(e) evaluated at e and at the predicted spins; the spin-orbit
+    torque fields (sot=, in-kernel); Heun and Depondt.  Trajectories and the max torque against the
+    reference's; run() equals the step loop."""
+    from helpers import callable_fields, site_field_func
     from magex_gb300.lattice import Supercell
     from magex_gb300.llg import GB300LLG
     from magex_gb300.spinmodel import load_results
@@ -361,8 +362,9 @@ def test_field_hooks_match_reference(cuda, golden, golden_models, tag):
     sc = Supercell(load_results(golden_models[case["model"]]["model"]), case["L"], case["pbc"], case["B"])
 
     def solver():
-        sol = GB300LLG(sc, case["alpha"], case["dt"], 0.0, 3, integrator=case["integrator"])
-        sol.field_func = ff if case["field_func"] else None
+        sol = GB300LLG(sc, case["alpha"], case["dt"], 0.0, 3, integrator=case["integrator"],
+                       sot=cal["sot"] if case["sot"] else None)
+        sol.field_func = {0: None, 1: ff, 2: site_field_func(cal["params"], sc.N)}[int(case["field_func"])]
         sol.extra_field = xf if case["extra_field"] else None
         return sol
 
