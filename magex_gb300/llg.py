@@ -49,6 +49,17 @@ def _philox_key(seed):
 
 
 
+def llg_rhs(e, B, alpha, precession=True):
+    """de/dt (1/ps) = -gamma / (1 + alpha^2) [e x B + alpha e x (e x B)] for (N, 3) spins and fields
+    (host NumPy, magex/llg.py:21-28; the kernels evaluate the same expression per site)."""
+    pre = -GAMMA / (1.0 + alpha * alpha)
+    exB = np.cross(e, B)
+    out = alpha * np.cross(e, exB)
+    if precession:
+        out = out + exB
+    return pre * out
+
+
 #: arithmetic forms of the step (precision=...), see the module docstring
 PRECISIONS = {"fp64": _lib.PRECISION_FP64, "df32": _lib.PRECISION_DF32_GATHER, "int48": _lib.PRECISION_INT48_GATHER,
               "fp64_fixed": _lib.PRECISION_FP64_FIXED_GATHER}
@@ -332,6 +343,50 @@ class GB300LLG:
         if src.shape != (N, 3):
             raise ValueError(f"spins have shape {tuple(src.shape)}, expected {(N, 3)}")
         return self.step_host(src, torch.empty((N, 3), dtype=torch.float64)).numpy()
+
+    # ------------------------------------------------------------------ magex's host-side pieces
+    @property
+    def _a(self):
+        return self.alpha[:, None] if self.alpha.ndim else self.alpha
+
+    def thermal_field(self):
+        """One draw of the thermal field b (N, 3) in tesla from the solver's NumPy generator, 0.0 at
+        T = 0 (magex/llg.py:106-122): sigma = sqrt(2 alpha k_B T_i / (gamma mu_i mu_B dt)), zero on
+        pinned sites.  The steps themselves draw their noise inside the kernels or, with noise="host",
+        from this same generator."""
+        sT = self._site_T()
+        if self.T <= 0 and sT is None:
+            return 0.0
+        T = self.T if sT is None else sT
+        sigma2 = 2.0 * self.alpha * K_B * T / (GAMMA * self.sc.mu * MU_B * self.dt)
+        b = np.sqrt(sigma2)[:, None] * self.rng.normal(size=(self.sc.N, 3))
+        pinned = getattr(self.sc, "pinned", None)
+        if pinned is not None:
+            b[np.asarray(pinned, bool)] = 0.0
+        return b
+
+    def field(self, e, t):
+        """B (N, 3) in tesla at spins e and time t (magex/llg.py:124-137): the effective field (on the
+        device) plus the spin-orbit torque fields, field_func(t) and extra_field(e); zero on pinned
+        sites when any of those is present."""
+        e = np.asarray(e, float)
+        B = self.effective_field(e)
+        extras = self.sot is not None or self._has_callables()
+        if self.sot is not None:
+            p, bdl, bfl = self.sot
+            B = B + bdl * np.cross(e, p[None, :]) + bfl * p[None, :]
+        if self.field_func is not None:
+            B = B + self.field_func(t)
+        if self.extra_field is not None:
+            B = B + self.extra_field(e)
+        pinned = getattr(self.sc, "pinned", None)
+        if pinned is not None and extras:
+            B[np.asarray(pinned, bool)] = 0.0
+        return B
+
+    def rhs(self, e, b, t):
+        """Tangent de/dt (1/ps) at spins e, thermal field b and time t (magex/llg.py:138-151)."""
+        return llg_rhs(np.asarray(e, float), self.field(e, t) + b, self._a, self.precession)
 
     # ------------------------------------------------------------------ checkpoint / resume
     def checkpoint(self, e, path):

@@ -189,6 +189,8 @@ def main(ref_root):
         sol.extra_field = xf if use_xf else None
         e = s.init_spins("random", seed=4)
         out[f"callables/{tag}/e0"] = e.copy()
+        out[f"callables/{tag}/field0"] = sol.field(e, 0.0)
+        out[f"callables/{tag}/rhs0"] = sol.rhs(e, 0.0, 0.0)
         for n in range(1, steps + 1):
             e = sol.step(e)
             if n in keep:
@@ -198,6 +200,10 @@ def main(ref_root):
                                                   alpha=alpha, dt=dt, steps=steps, keep=sorted(keep),
                                                   field_func=use_ff, extra_field=use_xf, sot=use_sot,
                                                   integrator=integ)
+
+    # one draw of LLGSolver.thermal_field (magex/llg.py:106-122) of the sc6_thermal system
+    s = RS.SpinSystem(ucs["sc_dmi"], (6, 6, 6), (1, 1, 1), (0.1, 0, 0.5))
+    out["thermal_field/b"] = LLGSolver(s, 0.2, 1e-3, 50.0, 5).thermal_field()
 
     # Larmor precession of one free spin (magex tests/test_spindyn.py:36-45)
     s = RS.SpinSystem(uc_of("free", RM.make_model("sc", J=[0.0])), (1, 1, 1), field=(0, 0, 2.0))

@@ -380,3 +380,38 @@ def test_field_hooks_match_reference(cuda, golden, golden_models, tag):
     e_run, table, _ = solver().run(golden[f"callables/{tag}/e0"].copy(), case["steps"], output_every=case["steps"])
     assert np.array_equal(e_run, e)
     assert table[-1, 6] == pytest.approx(tq, rel=1e-10, abs=1e-10)
+
+
+@pytest.mark.parametrize("tag", ["pulse", "extra", "both", "sot", "sot_site"])
+def test_field_and_rhs_match_reference(cuda, golden, golden_models, tag):
+    """LLGSolver.field(e, t) and .rhs(e, b, t) (magex/llg.py:124-151) with every hook, against the
+    reference's values at the initial spins."""
+    from helpers import callable_fields, site_field_func
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    cal = golden_models["callables"]
+    case = cal["cases"][tag]
+    ff, xf = callable_fields(cal["params"])
+    sc = Supercell(load_results(golden_models[case["model"]]["model"]), case["L"], case["pbc"], case["B"])
+    sol = GB300LLG(sc, case["alpha"], case["dt"], 0.0, 3, integrator=case["integrator"],
+                   sot=cal["sot"] if case["sot"] else None)
+    sol.field_func = {0: None, 1: ff, 2: site_field_func(cal["params"], sc.N)}[int(case["field_func"])]
+    sol.extra_field = xf if case["extra_field"] else None
+    e0 = golden[f"callables/{tag}/e0"]
+    B, ref_B = sol.field(e0, 0.0), golden[f"callables/{tag}/field0"]
+    assert np.abs(B - ref_B).max() <= 1e-12 * max(1.0, np.abs(ref_B).max())
+    f, ref_f = sol.rhs(e0, 0.0, 0.0), golden[f"callables/{tag}/rhs0"]
+    assert np.abs(f - ref_f).max() <= 1e-12 * max(1.0, np.abs(ref_f).max())
+
+
+def test_thermal_field_matches_reference(cuda, golden, golden_models):
+    """One LLGSolver.thermal_field() draw (magex/llg.py:106-122): same generator, same amplitudes."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    sc = Supercell(load_results(golden_models["sc_dmi"]["model"]), (6, 6, 6), (True, True, True), (0.1, 0, 0.5))
+    b = GB300LLG(sc, 0.2, 1e-3, 50.0, 5).thermal_field()
+    ref = golden["thermal_field/b"]
+    assert np.abs(b - ref).max() <= 1e-14 * np.abs(ref).max()
+    assert GB300LLG(sc, 0.2, 1e-3, 0.0, 5).thermal_field() == 0.0
