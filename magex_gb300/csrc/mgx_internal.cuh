@@ -99,9 +99,9 @@ struct DevLLG {
   // caller-supplied per-site field added to the effective field of both stages ([3][N], lattice
   // layout; mgx_llg_set_extra_field), or nullptr
   const double* B_add = nullptr;
-  // spin-orbit torque as effective fields B_DL e x p + B_FL p (mgx_llg_set_sot); sot = 0: none
-  int sot = 0;
-  double sot_p0 = 0.0, sot_p1 = 0.0, sot_p2 = 0.0, sot_dl = 0.0, sot_fl = 0.0;
+  // spin-orbit torque as effective fields B_DL e x p + B_FL p (mgx_llg_set_sot): device
+  // [p0, p1, p2, B_DL, B_FL], or nullptr
+  const double* sot = nullptr;
 };
 
 // Tables of the compensated-FP32 gather (MGX_PRECISION_DF32_GATHER): every coupling as 9 (hi, lo)
@@ -165,6 +165,7 @@ struct LLGPlan {
   double* host_lat = nullptr;    // [3][N] lattice layout
   double* host_aos = nullptr;    // [N][3] magex order (staging of the copies)
   cudaEvent_t host_ev[2 * MGX_HOST_CHUNKS + 4] = {};  // in[c] | out[c] | start | done | joined aux | joined main
+  double* sot_block = nullptr;   // device [5] spin-orbit torque parameters
 };
 
 // Threads per block of the one-site-per-thread kernels: 256, or fewer for small lattices so that the

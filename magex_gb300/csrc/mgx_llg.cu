@@ -15,23 +15,23 @@ namespace mgx {
 
 // Sites begin + i (i < count) of sublattice blockIdx.y: the whole lattice is one row of N sites
 // (gridDim.y = 1, begin = 0), a range of cells one row of `count` cells per sublattice.
-template <int W, int NOISE, int INTEG>
+template <int W, int NOISE, int INTEG, bool EXTRA>
 __global__ void __launch_bounds__(256) k_predict(const DevLattice L, const DevLLG P, const double* __restrict__ e,
                                                  const double* __restrict__ noise, uint64_t step, long long begin,
                                                  long long count) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
-    predict_site<W, NOISE, INTEG>(L, P, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+    predict_site<W, NOISE, INTEG, EXTRA>(L, P, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
                                   P.step_base ? *P.step_base + step : step);
 }
 
-template <int W, int NOISE, int INTEG>
+template <int W, int NOISE, int INTEG, bool EXTRA>
 __global__ void __launch_bounds__(256) k_correct(const DevLattice L, const DevLLG P, double* __restrict__ e,
                                                  const double* __restrict__ noise, uint64_t step, long long begin,
                                                  long long count) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
-    correct_site<W, NOISE, INTEG>(L, P, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+    correct_site<W, NOISE, INTEG, EXTRA>(L, P, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
                                   P.step_base ? *P.step_base + step : step);
 }
 
@@ -49,8 +49,13 @@ static void launch_step(const LLGPlan* pl, double* e, const double* noise, uint6
   const long long count = whole ? L.N : r.cn;
   const int tpb = site_block_size(whole ? L.N : r.cn * L.ns);
   const dim3 grid((unsigned)((count + tpb - 1) / tpb), whole ? 1u : (unsigned)L.ns);
-  if (stages & 1) k_predict<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
-  if (stages & 2) k_correct<W, NOISE, INTEG><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
+  if (pl->p.sot || pl->p.B_add) {
+    if (stages & 1) k_predict<W, NOISE, INTEG, true><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
+    if (stages & 2) k_correct<W, NOISE, INTEG, true><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
+  } else {
+    if (stages & 1) k_predict<W, NOISE, INTEG, false><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
+    if (stages & 2) k_correct<W, NOISE, INTEG, false><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
+  }
 }
 
 template <int W, int NOISE>
@@ -277,14 +282,15 @@ mgx_status mgx_llg_set_sot(mgx_llg* pp, const double p[3], double B_DL, double B
     return set_error(MGX_ERR_INVALID, "mgx_llg_set_sot: p must be a finite non-zero vector, B_DL and B_FL finite");
   if (on && pl->precision != MGX_PRECISION_FP64)
     return set_error(MGX_ERR_UNSUPPORTED, "spin-orbit torque needs an FP64 plan");
-  drop_llg_graph(pl);                                 // captured launches hold the parameters by value
-  DevLLG& d = pl->p;
-  d.sot = on ? 1 : 0;
-  d.sot_p0 = on ? p[0] / n : 0.0;
-  d.sot_p1 = on ? p[1] / n : 0.0;
-  d.sot_p2 = on ? p[2] / n : 0.0;
-  d.sot_dl = B_DL;
-  d.sot_fl = B_FL;
+  drop_llg_graph(pl);                                 // captured launches hold the pointer by value
+  if (!on) {
+    pl->p.sot = nullptr;
+    return MGX_OK;
+  }
+  if (!pl->sot_block) MGX_CUDA_TRY(cudaMalloc(&pl->sot_block, 5 * sizeof(double)));
+  const double v[5] = {p[0] / n, p[1] / n, p[2] / n, B_DL, B_FL};
+  MGX_CUDA_TRY(cudaMemcpy(pl->sot_block, v, sizeof(v), cudaMemcpyHostToDevice));
+  pl->p.sot = pl->sot_block;
   return MGX_OK;
 }
 
@@ -317,6 +323,7 @@ mgx_status mgx_llg_destroy(mgx_llg* pp) {
   if (pl->cap_stream) cudaStreamDestroy(pl->cap_stream);
   cudaFree(pl->d_step);
   drop_host_buffers(pl);
+  cudaFree(pl->sot_block);
   delete pl;
   return MGX_OK;
 }

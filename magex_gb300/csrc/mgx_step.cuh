@@ -46,9 +46,11 @@ __device__ __forceinline__ void add_extra(const DevLLG& P, long long N, long lon
 __device__ __forceinline__ void add_sot(const DevLLG& P, double x, double y, double z, double& bx, double& by,
                                         double& bz) {
   if (!P.sot) return;
-  bx += fma(P.sot_dl, y * P.sot_p2 - z * P.sot_p1, P.sot_fl * P.sot_p0);
-  by += fma(P.sot_dl, z * P.sot_p0 - x * P.sot_p2, P.sot_fl * P.sot_p1);
-  bz += fma(P.sot_dl, x * P.sot_p1 - y * P.sot_p0, P.sot_fl * P.sot_p2);
+  const double p0 = __ldg(P.sot), p1 = __ldg(P.sot + 1), p2 = __ldg(P.sot + 2);
+  const double dl = __ldg(P.sot + 3), fl = __ldg(P.sot + 4);
+  bx += fma(dl, y * p2 - z * p1, fl * p0);
+  by += fma(dl, z * p0 - x * p2, fl * p1);
+  bz += fma(dl, x * p1 - y * p0, fl * p2);
 }
 
 template <int NOISE>
@@ -70,8 +72,10 @@ __device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P
 }
 
 // Predictor of site q (0 <= q < L.N): writes P.ep and P.k1 at q.  With Hout != nullptr the total
-// field (effective + thermal) of the site is stored there too (adjoint recomputation).
-template <int W, int NOISE, int INTEG>
+// field (effective + thermal) of the site is stored there too (adjoint recomputation).  EXTRA adds the
+// spin-orbit torque fields and the caller's per-site field (a separate instantiation, so the plain
+// kernels carry neither).
+template <int W, int NOISE, int INTEG, bool EXTRA = false>
 __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& P, const double* __restrict__ e,
                                              const double* __restrict__ noise, long long q, uint64_t step,
                                              double* __restrict__ Hout = nullptr, double* __restrict__ rout = nullptr) {
@@ -89,8 +93,10 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
   site_coords(L, q, s, c0, c1, c2);
   double bx, by, bz;
   effective_field<W>(L, e, q, s, c0, c1, c2, ex, ey, ez, bx, by, bz);
-  add_sot(P, ex, ey, ez, bx, by, bz);
-  add_extra(P, N, q, bx, by, bz);
+  if (EXTRA) {
+    add_sot(P, ex, ey, ez, bx, by, bz);
+    add_extra(P, N, q, bx, by, bz);
+  }
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
   if (Hout) {
     Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
@@ -120,7 +126,7 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
 
 // Corrector of site q (0 <= q < L.N): reads P.ep (neighbours), P.k1 and e at q, writes e at q
 // (or eout at q when given; the adjoint recomputation keeps e).  Hout as in predict_site.
-template <int W, int NOISE, int INTEG>
+template <int W, int NOISE, int INTEG, bool EXTRA = false>
 __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& P, double* __restrict__ e,
                                              const double* __restrict__ noise, long long q, uint64_t step,
                                              double* __restrict__ Hout = nullptr, double* __restrict__ eout = nullptr,
@@ -143,8 +149,10 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
   const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
   double bx, by, bz;
   effective_field<W>(L, P.ep, q, s, c0, c1, c2, px, py, pz, bx, by, bz);
-  add_sot(P, px, py, pz, bx, by, bz);
-  add_extra(P, N, q, bx, by, bz);
+  if (EXTRA) {
+    add_sot(P, px, py, pz, bx, by, bz);
+    add_extra(P, N, q, bx, by, bz);
+  }
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
   if (Hout) {
     Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
