@@ -201,6 +201,27 @@ def main(ref_root):
                                                   field_func=use_ff, extra_field=use_xf, sot=use_sot,
                                                   integrator=integ)
 
+    # run() loop semantics (magex/llg.py:254-283): early stop on torque_tol (T = 0), and a callback that
+    # changes the temperature every step (the two-temperature hook of magex/llg.py:337-341) with snapshots
+    s = RS.SpinSystem(ucs["sc_afm"], (3, 3, 3), (1, 1, 1), (0, 0, 0))
+    e0 = s.init_spins("reference", cone=0.3, seed=2)
+    sol = LLGSolver(s, 0.5, 2e-3, 0.0, 2)
+    e, tab, _ = sol.run(e0.copy(), 4000, output_every=100, torque_tol=1e-3)
+    out["run_tol/e0"], out["run_tol/e"], out["run_tol/table"] = e0, e, tab
+    s = RS.SpinSystem(ucs["sc_dmi"], (4, 4, 4), (1, 1, 1), (0.0, 0.0, 0.5))
+    e0 = s.init_spins("random", seed=6)
+    sol = LLGSolver(s, 0.1, 1e-3, 20.0, 8)
+    seen = []
+
+    def cool(n, e_, solver=sol):
+        seen.append([n, float(e_[0, 2])])
+        solver.T = 20.0 * np.exp(-0.05 * n)
+    e, tab, snaps = sol.run(e0.copy(), 40, output_every=10, snapshots=4, callback=cool)
+    out["run_cb/e0"], out["run_cb/e"], out["run_cb/table"] = e0, e, tab
+    out["run_cb/seen"] = np.array(seen)
+    out["run_cb/snap_t"] = np.array([t for t, _ in snaps])
+    out["run_cb/snap_last"] = snaps[-1][1]
+
     # one draw of LLGSolver.thermal_field (magex/llg.py:106-122) of the sc6_thermal system
     s = RS.SpinSystem(ucs["sc_dmi"], (6, 6, 6), (1, 1, 1), (0.1, 0, 0.5))
     out["thermal_field/b"] = LLGSolver(s, 0.2, 1e-3, 50.0, 5).thermal_field()

@@ -415,3 +415,45 @@ def test_thermal_field_matches_reference(cuda, golden, golden_models):
     ref = golden["thermal_field/b"]
     assert np.abs(b - ref).max() <= 1e-14 * np.abs(ref).max()
     assert GB300LLG(sc, 0.2, 1e-3, 0.0, 5).thermal_field() == 0.0
+
+
+def test_run_stops_on_torque_tol_like_reference(cuda, golden, golden_models):
+    """run(torque_tol=...) at T = 0 stops at the first output row whose max torque is below the
+    tolerance (magex/llg.py:271-274): same rows, same final spins (AFM relaxation, sc 3^3)."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    sc = Supercell(load_results(golden_models["sc_afm"]["model"]), (3, 3, 3), (True, True, True), (0, 0, 0))
+    sol = GB300LLG(sc, 0.5, 2e-3, 0.0, 2)
+    e, table, _ = sol.run(golden["run_tol/e0"].copy(), 4000, output_every=100, torque_tol=1e-3)
+    ref = golden["run_tol/table"]
+    assert table.shape == ref.shape
+    assert np.allclose(table[:, :6], ref[:, :6], rtol=1e-9, atol=1e-10)
+    assert np.allclose(table[:, 6], ref[:, 6], rtol=1e-6, atol=1e-9)
+    assert np.abs(e - golden["run_tol/e"]).max() <= 1e-9
+
+
+def test_run_callback_and_snapshots_like_reference(cuda, golden, golden_models):
+    """A callback sees (n, spins) after every step and may change the temperature for the next one
+    (magex's two-temperature hook, magex/llg.py:337-341); snapshots every steps // snapshots.  With
+    the reference's noise stream ("host") the table, the callback's view and the final spins equal
+    the reference run's."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.spinmodel import load_results
+    sc = Supercell(load_results(golden_models["sc_dmi"]["model"]), (4, 4, 4), (True, True, True), (0.0, 0.0, 0.5))
+    sol = GB300LLG(sc, 0.1, 1e-3, 20.0, 8, noise="host")
+    seen = []
+
+    def cool(n, e_):
+        seen.append([n, float(e_[0, 2])])
+        sol.T = 20.0 * np.exp(-0.05 * n)
+
+    e, table, snaps = sol.run(golden["run_cb/e0"].copy(), 40, output_every=10, snapshots=4, callback=cool)
+    ref = golden["run_cb/table"]
+    assert table.shape == ref.shape
+    assert np.allclose(table, ref, rtol=1e-10, atol=1e-11)
+    assert np.abs(np.array(seen) - golden["run_cb/seen"]).max() <= 1e-11
+    assert np.allclose([t for t, _ in snaps], golden["run_cb/snap_t"], rtol=0, atol=1e-15)
+    assert np.abs(snaps[-1][1] - golden["run_cb/snap_last"]).max() <= 1e-11
+    assert np.abs(e - golden["run_cb/e"]).max() <= 1e-11
