@@ -244,14 +244,16 @@ def test_graph_replayed_run_equals_direct_launches(cuda, precision):
     assert torch.equal(la, lb)
 
 
-@pytest.mark.parametrize("shells,pbc0,noise,precision", [
-    ((20.0, 10.0, -1.0), True, "philox", "fp64"),
-    ((20.0, 10.0, -1.0, 1.0), True, "philox", "fp64"),      # 4th shell: couplings reach 2 layers
-    ((20.0, 10.0, -1.0), False, "philox", "fp64"),          # open along the slab axis
-    ((20.0, 10.0, -1.0), True, "host", "fp64"),
-    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed"),     # one piece (reduced split refreshed)
+@pytest.mark.parametrize("shells,pbc0,noise,precision,L", [
+    ((20.0, 10.0, -1.0), True, "philox", "fp64", (96, 76, 76)),
+    ((20.0, 10.0, -1.0, 1.0), True, "philox", "fp64", (96, 76, 76)),   # 4th shell: couplings reach 2 layers
+    ((20.0, 10.0, -1.0), False, "philox", "fp64", (96, 76, 76)),        # open along the slab axis
+    ((20.0, 10.0, -1.0), True, "host", "fp64", (96, 76, 76)),
+    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76)),  # one piece (reduced split refreshed)
+    ((20.0, 10.0, -1.0), True, "philox", "fp64", (4, 512, 256)),      # four slabs of one layer
+    ((20.0, 10.0, -1.0), False, "philox", "fp64", (2, 512, 512)),     # too thin to split: one piece
 ])
-def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precision):
+def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precision, L):
     """mgx_llg_step_host (pinned host buffers; copies in axis-0 slabs overlapping the stages for FP64
     plans of >= 2^20 sites) gives the same bits as the step on device spins: also in place, and for
     pageable numpy input (one piece)."""
@@ -259,7 +261,7 @@ def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precisio
     from magex_gb300.llg import GB300LLG
     from magex_gb300.spinmodel import load_results
     from magex_gb300.workloads import bcc_two_site_model
-    sc = Supercell(load_results(bcc_two_site_model(J=shells)), (96, 76, 76), (pbc0, True, True), (0.0, 0.0, 0.5))
+    sc = Supercell(load_results(bcc_two_site_model(J=shells)), L, (pbc0, True, True), (0.0, 0.0, 0.5))
     assert sc.N >= 1 << 20
     a = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision)
     b = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision)
@@ -457,3 +459,29 @@ def test_run_callback_and_snapshots_like_reference(cuda, golden, golden_models):
     assert np.allclose([t for t, _ in snaps], golden["run_cb/snap_t"], rtol=0, atol=1e-15)
     assert np.abs(snaps[-1][1] - golden["run_cb/snap_last"]).max() <= 1e-11
     assert np.abs(e - golden["run_cb/e"]).max() <= 1e-11
+
+
+@pytest.mark.parametrize("noise", ["philox", "host"])
+def test_every_site_pinned_keeps_the_spins(cuda, golden_models, noise):
+    """Edge case: a lattice whose sites are all pinned (magex/structure.py:198-207) keeps its spins bit
+    for bit at T > 0, in the step, the graph-replayed run and the host-buffer step; a Monte Carlo plan
+    on it has no colour class to update."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.spinmodel import load_results
+    sc = Supercell(load_results(golden_models["sc_dmi"]["model"]), (6, 6, 6), (True, True, True), (0.1, 0.0, 0.5))
+    sc.pinned = np.ones(sc.N, bool)
+    e0 = sc.init_spins("random", seed=2)
+    sol = GB300LLG(sc, 0.1, 1e-3, 300.0, 4, noise=noise)
+    e = e0.copy()
+    for _ in range(3):
+        e = sol.step(e)
+    assert np.array_equal(e, e0)
+    lat = sol.model.to_lattice(e0)
+    sol.run_lattice(lat, 70)
+    assert np.array_equal(sol.model.from_lattice(lat).cpu().numpy(), e0)
+    mc = MetropolisMC(sc, 20.0, seed=1)
+    assert mc.ncolors == 0
+    f = mc.sweep(e0.copy())
+    assert np.array_equal(f, e0) and mc.acceptance() == 0.0
