@@ -376,6 +376,18 @@ static int32_t first_fit(int64_t N, Nbrs nbrs, int32_t* colour) {
   return ncol;
 }
 
+// sigma <- clip(sigma * 0.5 / max(1 - a, 0.05), 0.02, 4) with a = accepted / tried, counts reset: the
+// arithmetic of magex's adaptation (magex/montecarlo.py:257-261), operation for operation
+__global__ void k_mc_adapt(double* __restrict__ sigma, unsigned long long* __restrict__ acc, int n,
+                           unsigned long long tried) {
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const double a = (double)acc[k] / (double)(tried > 0 ? tried : 1ull);
+    const double x = sigma[k] * 0.5 / fmax(1.0 - a, 0.05);
+    sigma[k] = fmin(fmax(x, 0.02), 4.0);
+    acc[k] = 0;
+  }
+}
+
 }  // namespace mgx
 
 using namespace mgx;
@@ -626,18 +638,6 @@ extern "C" mgx_status mgx_mc_counts(mgx_mc* h, uint64_t* accepted, uint64_t* tri
   return MGX_OK;
 }
 
-// sigma <- clip(sigma * 0.5 / max(1 - a, 0.05), 0.02, 4) with a = accepted / tried, counts reset: the
-// arithmetic of magex's adaptation (magex/montecarlo.py:257-261), operation for operation
-__global__ void k_mc_adapt(double* __restrict__ sigma, unsigned long long* __restrict__ acc, int n,
-                           unsigned long long tried) {
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    const double a = (double)acc[k] / (double)(tried > 0 ? tried : 1ull);
-    const double x = sigma[k] * 0.5 / fmax(1.0 - a, 0.05);
-    sigma[k] = fmin(fmax(x, 0.02), 4.0);
-    acc[k] = 0;
-  }
-}
-
 extern "C" mgx_status mgx_mc_set_chains(mgx_mc* h, int32_t nchains, const uint64_t* seeds, const double* beta,
                                         const double* sigma) {
   McPlan* mc = reinterpret_cast<McPlan*>(h);
@@ -706,7 +706,7 @@ extern "C" mgx_status mgx_mc_adapt_sigma(mgx_mc* h, void* stream) {
   McPlan* mc = reinterpret_cast<McPlan*>(h);
   if (!mc) return set_error(MGX_ERR_INVALID, "mgx_mc_adapt_sigma: null plan");
   if (!mc->chain_block) return set_error(MGX_ERR_INVALID, "mgx_mc_adapt_sigma: no chains set");
-  k_mc_adapt<<<1, 256, 0, (cudaStream_t)stream>>>(const_cast<double*>(mc->chains.sigma), mc->chains.acc, mc->nchains,
+  mgx::k_mc_adapt<<<1, 256, 0, (cudaStream_t)stream>>>(const_cast<double*>(mc->chains.sigma), mc->chains.acc, mc->nchains,
                                                   (unsigned long long)mc->tried);
   MGX_CUDA_TRY(cudaGetLastError());
   mc->tried = 0;
