@@ -375,32 +375,39 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0, precision="fp64")
                         "grad_norm_per_shell": [float(x) for x in g.reshape(4, -1).norm(dim=1)]}}
 
 
-def bench_mc_points(L=16, npts=16, therm=1000, meas=4000):
-    """Monte Carlo T scan of magex's mc workflow: npts temperatures of an sc L^3 ferromagnet (J = 1 meV),
-    therm + meas sweeps each (Gaussian moves + over-relaxation, sigma adapted every 50 sweeps, E and
-    the order vector sampled every 5 sweeps): wall time of points() (one ensemble) against one point()
-    (magex runs each point as its own process, magex/montecarlo.py:390-401)."""
+def bench_mc_points(sizes=(8, 16), npts=16, therm=1000, meas=4000):
+    """Monte Carlo T scan of magex's mc workflow (the input of a T_c estimate): npts temperatures for
+    each sc L^3 ferromagnet size (J = 1 meV), therm + meas sweeps each (Gaussian moves +
+    over-relaxation, sigma adapted every 50 sweeps, E and the order vector sampled every 5 sweeps):
+    wall time of points() (one ensemble per size, the sizes on concurrent streams) against the points
+    run one by one with point() (magex runs each point as its own process, magex/montecarlo.py:390-401)."""
     import numpy as np
     from magex_gb300.mc import point, points
     from magex_gb300.spinmodel import load_results, make_model
     uc = load_results(make_model("sc", J=[1.0]))
     c = dict(sigma=0.6, overrelax=1, move="gaussian", init="random", init_axis=(0.0, 0.0, 1.0),
              therm_sweeps=therm, meas_sweeps=meas, sample_every=5)
+    Ts = np.linspace(10.0, 40.0, npts)
     jobs = [(uc, (L, L, L), (True,) * 3, (0.0, 0.0, 0.0), float(T), c, 100 + i)
-            for i, T in enumerate(np.linspace(10.0, 40.0, npts))]
+            for L in sizes for i, T in enumerate(Ts)]
     point(jobs[0])
-    t0 = time.perf_counter()
-    one = point(jobs[0])
-    t_one = time.perf_counter() - t0
+    t_one = {}
+    for L in sizes:
+        job = next(j for j in jobs if j[1][0] == L)
+        t0 = time.perf_counter()
+        one = point(job)
+        t_one[L] = time.perf_counter() - t0
     t0 = time.perf_counter()
     rows = points(jobs)
     t_all = time.perf_counter() - t0
-    assert rows[0]["E"] == one["E"]
-    N = L ** 3
-    return {"workload": f"sc {L}^3 ({N} spins), {npts} temperatures 10..40 K, {therm} + {meas} sweeps each, "
+    assert rows[-npts]["E"] == one["E"]
+    spins = sum(L ** 3 for L in sizes) * npts
+    seq = sum(t_one[L] * npts for L in sizes)
+    return {"workload": f"sc L^3 for L in {list(sizes)}, {npts} temperatures 10..40 K each, {therm} + {meas} sweeps, "
                         "Gaussian moves + 1 over-relaxation pass, Philox, FP64",
-            "points_s": t_all, "one_point_s": t_one, "speedup_vs_points_one_by_one": t_one * npts / t_all,
-            "site_updates_per_s": 2 * N * npts * (therm + meas) / t_all, "unit": "site-updates/s",
+            "points_s": t_all, "one_point_s": {str(L): t_one[L] for L in sizes},
+            "speedup_vs_points_one_by_one": seq / t_all,
+            "site_updates_per_s": 2 * spins * (therm + meas) / t_all, "unit": "site-updates/s",
             "rows_equal_point": True}
 
 

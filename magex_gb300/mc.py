@@ -337,8 +337,10 @@ def points(jobs, max_chains=4096):
     differ) run as one ensemble (``mgx_mc_set_chains``): every pass of a sweep is one launch over the
     class's sites of all chains, the cone widths adapt on the device every 50 thermalisation sweeps,
     and the samples of E and the order vector are reduced into a device buffer, read once at the end.
-    Each chain's trajectory is that of its own ``point``.  Points with T = 0 or structure edits run one
-    by one.  ``seconds`` of an ensemble's rows is its wall time divided by its number of chains."""
+    The ensembles of different lattices (e.g. the sizes of a T_c scan) run concurrently, each on its
+    own CUDA stream.  Each chain's trajectory is that of its own ``point``.  Points with T = 0 or
+    structure edits run one by one.  ``seconds`` of an ensemble's rows is its wall time divided by its
+    number of chains."""
     from .lattice import Supercell
     jobs = list(jobs)
     rows = [None] * len(jobs)
@@ -349,15 +351,26 @@ def points(jobs, max_chains=4096):
             rows[i] = point(job)
             continue
         groups.setdefault(_ensemble_key(job), []).append(i)
-    for idxs in groups.values():
-        for k0 in range(0, len(idxs), max_chains):
-            part = idxs[k0:k0 + max_chains]
-            for i, row in zip(part, _ensemble([jobs[i] for i in part], Supercell)):
-                rows[i] = row
+    parts = [idxs[k:k + max_chains] for idxs in groups.values() for k in range(0, len(idxs), max_chains)]
+    runs = [(part, _ensemble([jobs[i] for i in part], Supercell), torch.cuda.Stream()) for part in parts]
+    # round-robin: each generator enqueues a batch of sweeps on its stream and yields
+    while runs:
+        left = []
+        for part, gen, stream in runs:
+            with torch.cuda.stream(stream):
+                try:
+                    next(gen)
+                    left.append((part, gen, stream))
+                except StopIteration as done:
+                    for i, row in zip(part, done.value):
+                        rows[i] = row
+        runs = left
     return rows
 
 
 def _ensemble(jobs, Supercell):
+    """Generator running one ensemble on the current stream; yields after each batch of enqueued
+    work and returns the rows."""
     uc, L, pbc, B, _, c, _ = jobs[0]
     n = len(jobs)
     Ts = [float(j[4]) for j in jobs]
@@ -373,26 +386,27 @@ def _ensemble(jobs, Supercell):
                "mgx_mc_set_chains")
     lat = torch.stack([mc.model.to_lattice(system.init_spins(c["init"], c["init_axis"], s)) for s in seeds])
     mc.model.sync_field()
-    st = stream_ptr()
     ptr = C.c_void_p(lat.data_ptr())
 
     def sweep(k):
         if k > 0:
-            _lib.check(lib.mgx_mc_sweep(h, ptr, int(k), None, st), "mgx_mc_sweep")
+            _lib.check(lib.mgx_mc_sweep(h, ptr, int(k), None, stream_ptr()), "mgx_mc_sweep")
 
     def counts(reset):
         acc = np.zeros(n, np.uint64)
         tried = C.c_uint64()
         sig = np.zeros(n, np.float64)
         _lib.check(lib.mgx_mc_chain_counts(h, acc.ctypes.data_as(C.c_void_p), C.byref(tried), _lib.dptr(sig),
-                                           int(reset), st), "mgx_mc_chain_counts")
+                                           int(reset), stream_ptr()), "mgx_mc_chain_counts")
         return acc, int(tried.value), sig
 
     t0 = time.time()
+    yield
     therm = int(c["therm_sweeps"])
     for _ in range(therm // 50):                 # sigma adapts after sweeps 50, 100, ... (as point())
         sweep(50)
-        _lib.check(lib.mgx_mc_adapt_sigma(h, st), "mgx_mc_adapt_sigma")
+        _lib.check(lib.mgx_mc_adapt_sigma(h, stream_ptr()), "mgx_mc_adapt_sigma")
+        yield
     sweep(therm % 50)
     counts(True)
     meas, every = int(c["meas_sweeps"]), int(c["sample_every"])
@@ -402,8 +416,10 @@ def _ensemble(jobs, Supercell):
     for j in range(nsamp):                       # samples after sweeps 1, 1 + every, 1 + 2 every, ...
         sweep(j * every + 1 - done)
         done = j * every + 1
-        _lib.check(lib.mgx_observables_n(mc.model.handle, ptr, n, C.c_void_p(obs[j].data_ptr()), st),
+        _lib.check(lib.mgx_observables_n(mc.model.handle, ptr, n, C.c_void_p(obs[j].data_ptr()), stream_ptr()),
                    "mgx_observables_n")
+        if j % 10 == 9:
+            yield
     sweep(meas - done)
     acc, tried, sig = counts(True)
     o = obs[:nsamp].cpu().numpy()
