@@ -7,7 +7,7 @@
 // w_a(c) = exp(-2 pi i f_a c) (f = fractional coordinates of q), so the projection is a pruned
 // separable DFT evaluated only at the requested wave vectors:
 //   stage 1 (k_fourier_rows): P[v][comp][row] = sum_c2 e[comp][row, c2] w2_v(c2) for every distinct
-//            f_2 value v, one thread per (row, comp) with the twiddles broadcast across the warp;
+//            f_2 value v, one thread per (chunk of f_2 values, row, comp), twiddles broadcast;
 //   stage 2 (k_fourier_q):    m_q[comp] = N^-1/2 sum_{s, c0, c1} exp(-i q.p_s) w0(c0) w1(c1)
 //            P[v2(q)][comp][s, c0, c1], one block per q.
 // Spins never leave HBM; a sample costs one read of e plus O(nq ns L0 L1) work.
@@ -34,35 +34,37 @@ struct FourierPlan {
 
 constexpr int kVChunk = 8;      // f_2 values per pass of stage 1 (accumulators held in registers)
 
-// Stage 1: one thread per (component, row) walks the row's L2 spins once per chunk of f_2 values.
-// The twiddles w2[v][c] are the same for every thread of a warp (one broadcast load); the row's
-// spins come from L1 after the first chunk.  No cross-lane reduction: two FMAs per (spin, f_2).
+// Stage 1: one thread per (chunk of f_2 values, component, row) walks the row's L2 spins once.  The
+// twiddles w2[v][c] are the same for every thread of a warp (one broadcast load); the other chunks'
+// threads read the row again from L2.  No cross-lane reduction: two FMAs per (spin, f_2).
 __global__ void __launch_bounds__(128) k_fourier_rows(const double* __restrict__ e, long long N, int rows, int L2,
                                                       const double2* __restrict__ w2, int nv2,
                                                       double2* __restrict__ P) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 3LL * rows) return;
-  const int comp = (int)(t / rows), row = (int)(t - (long long)comp * rows);
+  const long long per_chunk = 3LL * rows;
+  const int chunk = (int)(t / per_chunk);
+  const int v0 = chunk * kVChunk;
+  if (v0 >= nv2) return;
+  const long long r = t - (long long)chunk * per_chunk;
+  const int comp = (int)(r / rows), row = (int)(r - (long long)comp * rows);
   const double* x = e + (long long)comp * N + (long long)row * L2;
-  for (int v0 = 0; v0 < nv2; v0 += kVChunk) {
-    double re[kVChunk], im[kVChunk];
+  double re[kVChunk], im[kVChunk];
 #pragma unroll
-    for (int k = 0; k < kVChunk; ++k) re[k] = im[k] = 0.0;
-    for (int c = 0; c < L2; ++c) {
-      const double xv = __ldg(x + c);
+  for (int k = 0; k < kVChunk; ++k) re[k] = im[k] = 0.0;
+  for (int c = 0; c < L2; ++c) {
+    const double xv = __ldg(x + c);
 #pragma unroll
-      for (int k = 0; k < kVChunk; ++k) {
-        if (v0 + k < nv2) {
-          const double2 w = __ldg(w2 + (long long)(v0 + k) * L2 + c);
-          re[k] = fma(xv, w.x, re[k]);
-          im[k] = fma(xv, w.y, im[k]);
-        }
+    for (int k = 0; k < kVChunk; ++k) {
+      if (v0 + k < nv2) {
+        const double2 w = __ldg(w2 + (long long)(v0 + k) * L2 + c);
+        re[k] = fma(xv, w.x, re[k]);
+        im[k] = fma(xv, w.y, im[k]);
       }
     }
-#pragma unroll
-    for (int k = 0; k < kVChunk; ++k)
-      if (v0 + k < nv2) P[((long long)(v0 + k) * 3 + comp) * rows + row] = make_double2(re[k], im[k]);
   }
+#pragma unroll
+  for (int k = 0; k < kVChunk; ++k)
+    if (v0 + k < nv2) P[((long long)(v0 + k) * 3 + comp) * rows + row] = make_double2(re[k], im[k]);
 }
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
@@ -202,8 +204,9 @@ extern "C" mgx_status mgx_fourier_project(mgx_fourier* h, const double* e, doubl
   const DevLattice& d = f->model->d;
   const int rows = d.ns * d.L0 * d.L1;
   cudaStream_t st = (cudaStream_t)stream;
-  const long long threads = 3LL * rows;
-  k_fourier_rows<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(e, d.N, rows, d.L2, f->w2, f->nv2, f->P);
+  const long long threads = 3LL * rows * ((f->nv2 + kVChunk - 1) / kVChunk);
+  if (threads > 0)
+    k_fourier_rows<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(e, d.N, rows, d.L2, f->w2, f->nv2, f->P);
   k_fourier_q<<<f->nq, 256, 0, st>>>(f->P, rows, d.ns, d.L0, d.L1, f->w0, f->w1, f->qidx, f->sub,
                                      1.0 / std::sqrt((double)d.N), mq);
   MGX_CUDA_TRY(cudaGetLastError());
