@@ -205,14 +205,28 @@ def bench_batched(K_batch=200, K_plain=20, nsys=256, log=None, precision="fp64")
     b.record(stream)
     b.synchronize()
     t_plain = a.elapsed_time(b) * 1e-3
+    # the same per-system plans with their step loops replayed from CUDA graphs (runs of >= 64 steps of
+    # lattices up to 2^21 sites); the graphs are captured in a first, untimed run
+    K_graph = 64
+    for sol, lat in zip(sols, lats):
+        sol.run_lattice(lat, K_graph)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for sol, lat in zip(sols, lats):
+        sol.run_lattice(lat, K_graph)
+    b.record(stream)
+    b.synchronize()
+    t_graph = a.elapsed_time(b) * 1e-3
     v_batch = ntot * K_batch / t_batch
     v_plain = ntot * K_plain / t_plain
+    v_graph = ntot * K_graph / t_graph
     return {"workload": f"{nsys} triangular films, L in {{32,48,...,256}} (uneven, {ntot:,} spins in total), "
                         "J1=1 meV, interfacial DMI D/J=0.3, K=0.05 meV, B_z~U[0,3] T, T~U[0,20] K, alpha 0.1, "
                         "dt 0.1 fs, Philox, FP64" + (" with the exact fixed-point exchange sum (batched and plain)"
                                                      if precision == "fp64_fixed" else ""),
             "value": v_batch, "unit": UNIT, "steps": K_batch, "plain_value": v_plain, "plain_steps": K_plain,
-            "speedup_vs_plain": v_batch / v_plain, "launch": {"threads": best[0], "ctas_per_sm": best[1]},
+            "speedup_vs_plain": v_batch / v_plain, "plain_graph_value": v_graph, "plain_graph_steps": K_graph,
+            "speedup_vs_plain_graphs": v_batch / v_graph, "launch": {"threads": best[0], "ctas_per_sm": best[1]},
             "autotune_ms_per_step": {f"{t}x{c}": round(v, 4) for (t, c), v in timings.items()},
             "ms_per_step": 1e3 * t_batch / K_batch, "gpu_launches_per_step": 2,
             "plain_gpu_launches_per_step": 2 * nsys,
