@@ -182,7 +182,7 @@ mgx_status mgx_llg_set_sigma(mgx_llg* plan, const double* sigma_sub, const doubl
 mgx_status mgx_llg_set_extra_field(mgx_llg* plan, const double* B_add);
 /* Spin-orbit torque as effective fields B_DL e x p + B_FL p at each stage's spins, p normalised here
  * (LLGSolver(sot={p, B_DL, B_FL}), magex/llg.py:84-86,126-128); B_DL = B_FL = 0 removes it.  FP64
- * plans (MGX_ERR_UNSUPPORTED otherwise). */
+ * plans (MGX_ERR_UNSUPPORTED otherwise).  Synchronous: call it while no step of the plan is in flight. */
 mgx_status mgx_llg_set_sot(mgx_llg* plan, const double p[3], double B_DL, double B_FL);
 
 /* One stochastic Heun step in place on e (device, lattice layout):
