@@ -433,6 +433,86 @@ def _ensemble(jobs, Supercell):
     return rows
 
 
+def parallel_tempering(system, temperatures, therm_sweeps=2000, meas_sweeps=4000, sample_every=2, swap_every=5,
+                       seed=1, init="reference", init_axis=(0, 0, 1), sigma=0.6, overrelax=1, log=None):
+    """Replica exchange with the arguments and return value of magex/advanced_mc.py:38-95: replicas at
+    temperatures T_1 < ... < T_M sweep, every ``swap_every`` sweeps neighbouring pairs (even pairs,
+    then odd, alternating) exchange configurations with probability min(1, exp[(b_k - b_k+1)
+    (E_k - E_k+1)]) drawn from ``default_rng(seed)`` as magex does; returns (rows like point(),
+    swap acceptance per neighbouring pair).
+
+    The replicas are the chains of one ensemble (``mgx_mc_set_chains``, Philox key of seed + 17 k as
+    magex seeds replica k): every pass of a sweep is one launch for all of them, cone widths adapt on
+    the device, a swap exchanges the two chains' spin blocks on the device, and the replica energies
+    for the swap decisions come back in one ``mgx_observables_n`` read."""
+    Ts = np.array(sorted(float(t) for t in temperatures))
+    M = len(Ts)
+    if M < 1 or not np.all(Ts > 0):
+        raise ValueError("parallel tempering needs temperatures > 0")
+    rng = np.random.default_rng(seed)
+    mc = MetropolisMC(system, Ts[0], seed, sigma, overrelax)
+    sc, lib, h = mc.sc, mc.lib, mc.handle
+    N = sc.N
+    keys = np.array([np.random.SeedSequence(seed + 17 * k).generate_state(1, np.uint64)[0] for k in range(M)],
+                    np.uint64)
+    beta = np.array([1.0 / (K_B * T) for T in Ts], np.float64)
+    _lib.check(lib.mgx_mc_set_chains(h, M, keys.ctypes.data_as(C.c_void_p), _lib.dptr(beta),
+                                     _lib.dptr(np.full(M, float(sigma)))), "mgx_mc_set_chains")
+    lat = torch.stack([mc.model.to_lattice(sc.init_spins(init, init_axis, seed + k)) for k in range(M)])
+    mc.model.sync_field()
+    st = stream_ptr()
+    ptr = C.c_void_p(lat.data_ptr())
+    total = int(therm_sweeps) + int(meas_sweeps)
+    nsamp = len(range(0, int(meas_sweeps), int(sample_every)))
+    samples = torch.empty((max(nsamp, 1), M, 8), dtype=torch.float64, device=lat.device)
+    energies = torch.empty((M, 8), dtype=torch.float64, device=lat.device)
+    swaps_try, swaps_acc = np.zeros(max(M - 1, 0)), np.zeros(max(M - 1, 0))
+    t0 = time.time()
+    j = 0
+    for n in range(total):
+        _lib.check(lib.mgx_mc_sweep(h, ptr, 1, None, st), "mgx_mc_sweep")
+        if n < therm_sweeps and (n + 1) % 50 == 0:
+            _lib.check(lib.mgx_mc_adapt_sigma(h, st), "mgx_mc_adapt_sigma")
+        if (n + 1) % swap_every == 0 and M > 1:
+            _lib.check(lib.mgx_observables_n(mc.model.handle, ptr, M, C.c_void_p(energies.data_ptr()), st),
+                       "mgx_observables_n")
+            E = energies[:, 0].cpu().numpy().copy()
+            perm = list(range(M))
+            for k in range((n // swap_every) % 2, M - 1, 2):
+                d = (1 / (K_B * Ts[k]) - 1 / (K_B * Ts[k + 1])) * (E[k] - E[k + 1])
+                swaps_try[k] += 1
+                if d >= 0 or rng.random() < np.exp(d):
+                    perm[k], perm[k + 1] = perm[k + 1], perm[k]
+                    E[k], E[k + 1] = E[k + 1], E[k]
+                    swaps_acc[k] += 1
+            if perm != list(range(M)):
+                lat.copy_(lat[perm])                 # configurations change places, temperatures stay
+        if n >= therm_sweeps and (n - therm_sweeps) % sample_every == 0:
+            _lib.check(lib.mgx_observables_n(mc.model.handle, ptr, M, C.c_void_p(samples[j].data_ptr()), st),
+                       "mgx_observables_n")
+            j += 1
+    acc = np.zeros(M, np.uint64)
+    tried = C.c_uint64()
+    sig = np.zeros(M, np.float64)
+    _lib.check(lib.mgx_mc_chain_counts(h, acc.ctypes.data_as(C.c_void_p), C.byref(tried), _lib.dptr(sig), 0, st),
+               "mgx_mc_chain_counts")
+    o = samples[:nsamp].cpu().numpy()
+    L = list(getattr(system, "L", sc.L))
+    rows = []
+    for k, T in enumerate(Ts):
+        v = o[:, k, 4:7] / N
+        row = _row_of(L, N, float(T), list(o[:, k, 0]), [np.linalg.norm(x) for x in v], list(v),
+                      int(acc[k]) / max(int(tried.value), 1), float(sig[k]), mc.ncolors, time.time() - t0, None)
+        row["mvec"] = [0, 0, 0]                     # as magex/advanced_mc.py:88
+        row.pop("spins")
+        rows.append(row)
+    swap = (swaps_acc / np.maximum(swaps_try, 1)).tolist()
+    if log:
+        log(f"  parallel tempering L={L}: {M} replicas, swap acceptance {np.round(swap, 2).tolist()}, "
+            f"{time.time() - t0:.1f} s")
+    return rows, swap
+
+
 def _peak(T, y):
     """Peak of y(T): vertex of the parabola through the maximum and its neighbours when it lies
     between them, else the sampled maximum."""

@@ -304,6 +304,19 @@ def main(ref_root):
                               row={k: (float(v) if np.isscalar(v) else v) for k, v in row.items()
                                    if k not in ("spins", "seconds", "mvec")})
 
+    # parallel tempering (magex/advanced_mc.py:38-95): sc 6^3 replicas around T_c, the reference's rows
+    # and swap acceptances (compared within statistical errors: the sweeps draw other random numbers)
+    from magex.advanced_mc import parallel_tempering
+    pt = dict(L=[6, 6, 6], T=[32.0, 34.0, 36.0, 38.0, 40.0], therm=1000, meas=4000, sample_every=2, swap_every=5,
+              seed=3)
+    rows, swap = parallel_tempering(RS.SpinSystem(ucs["sc"], tuple(pt["L"]), (1, 1, 1), (0, 0, 0)), pt["T"],
+                                    therm_sweeps=pt["therm"], meas_sweeps=pt["meas"], sample_every=pt["sample_every"],
+                                    swap_every=pt["swap_every"], seed=pt["seed"])
+    pt["rows"] = [{k: (float(v) if isinstance(v, (float, np.floating)) else v) for k, v in r.items()
+                   if k in ("T", "E", "dE", "m", "dm", "C", "U4", "acceptance", "ncolors")} for r in rows]
+    pt["swap"] = [float(x) for x in swap]
+    models["parallel_tempering"] = pt
+
     # T_c estimation from rows of two sizes (synthetic rows with a Binder crossing)
     Ts = np.linspace(20.0, 40.0, 9)
     rows = []

@@ -216,3 +216,28 @@ def test_points_ensemble_equals_single_points(cuda, golden_models, move, overrel
         for key in ROW_KEYS:       # NaN == NaN: C and chi of the T = 0 job divide by k_B T
             assert np.array_equal(np.asarray(row[key]), np.asarray(ref[key]), equal_nan=True), \
                 (key, job[4], job[6], row[key], ref[key])
+
+
+def test_parallel_tempering_matches_reference_within_3_sigma(cuda, golden_models):
+    """Replica exchange (magex/advanced_mc.py:38-95) on an sc 6^3 ferromagnet with five replicas around
+    T_c: E/N and m of every replica, the Metropolis acceptance and the swap acceptance of every
+    neighbouring pair agree with the reference's run within statistical errors (mean of 4 seeds here;
+    the reference's sweeps and ours draw different random numbers)."""
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.mc import parallel_tempering
+    from magex_gb300.spinmodel import load_results
+    pt = golden_models["parallel_tempering"]
+    sc = Supercell(load_results(golden_models["sc"]["model"]), tuple(pt["L"]), (True, True, True), (0, 0, 0))
+    runs = [parallel_tempering(sc, pt["T"], therm_sweeps=pt["therm"], meas_sweeps=pt["meas"],
+                               sample_every=pt["sample_every"], swap_every=pt["swap_every"], seed=s)
+            for s in (11, 12, 13, 14)]
+    for k, ref in enumerate(pt["rows"]):
+        rows = [r[k] for r, _ in runs]
+        assert all(r["T"] == ref["T"] and r["ncolors"] == ref["ncolors"] for r in rows)
+        for key, err in (("E", "dE"), ("m", "dm")):
+            x = np.mean([r[key] for r in rows])
+            sem = np.sqrt(np.mean([r[err] ** 2 for r in rows]) / len(rows))
+            assert abs(x - ref[key]) <= 3.0 * np.hypot(ref[err], sem), (ref["T"], key, x, ref[key])
+        assert abs(np.mean([r["acceptance"] for r in rows]) - ref["acceptance"]) < 0.03
+    swap = np.mean([s for _, s in runs], axis=0)
+    assert np.all(np.abs(swap - np.array(pt["swap"])) < 0.08), (swap, pt["swap"])
