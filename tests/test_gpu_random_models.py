@@ -58,10 +58,12 @@ def _fixed_eligible(sc):
     return getattr(sc, "A_site", None) is None and getattr(sc, "mu_site", None) is None
 
 
+@pytest.mark.parametrize("precision", ["fp64_fixed", "int48", "df32"])
 @pytest.mark.parametrize("seed", range(24))
-def test_random_model_fixed_point_gather_matches_oracle(cuda, seed):
-    """The FP64 step with the exact fixed-point exchange sum on the same random models (the per-sublattice
-    models it accepts), at the FP64 bar."""
+def test_random_model_fixed_point_gather_matches_oracle(cuda, seed, precision):
+    """The FP64 step with the exact fixed-point exchange sum, and the 48-bit integer and FP32-pair
+    forms, on the same random models (the per-sublattice stencil models they accept), at the FP64
+    plan's per-step bar."""
     from magex_gb300.llg import GB300LLG
     from oracle import OracleLLG
     try:
@@ -70,7 +72,7 @@ def test_random_model_fixed_point_gather_matches_oracle(cuda, seed):
         pytest.skip(f"model not buildable: {err}")
     if not _fixed_eligible(sc):
         pytest.skip("per-site tensors: the fixed-point form takes per-sublattice models")
-    gpu = GB300LLG(sc, 0.1, 1e-3, meta["T"], 7, integrator=meta["integrator"], noise="host", precision="fp64_fixed")
+    gpu = GB300LLG(sc, 0.1, 1e-3, meta["T"], 7, integrator=meta["integrator"], noise="host", precision=precision)
     ora = OracleLLG(sc, 0.1, 1e-3, meta["T"], 7, integrator=meta["integrator"])
     e0 = sc.init_spins("random", seed=seed)
     a, b = e0.copy(), e0.copy()
