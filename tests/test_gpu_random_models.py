@@ -104,3 +104,37 @@ def test_random_model_monte_carlo_matches_oracle(cuda, seed):
         ora.sweep(b)
         assert np.abs(a - b).max() <= 1e-11, (meta, move)
         assert gpu.counts() == (ora.accepted, ora.tried), (meta, move)
+
+
+def test_random_models_as_one_batch(cuda):
+    """The random models that take uniform per-sublattice parameters, stepped together as one batched
+    ensemble (mixed lattices, sublattice counts, coupling widths, sizes and boundaries; per-system T
+    and seed, Philox and Depondt / Heun as drawn per batch), equal their own plans to 1e-12 per step
+    and their energies to 1e-12."""
+    from magex_gb300.batched import BatchedLLG
+    from magex_gb300.llg import GB300LLG
+    systems, Ts, seeds = [], [], []
+    for seed in range(24):
+        try:
+            sc, meta = _draw(seed)
+        except (ValueError, NotImplementedError):
+            continue
+        if sc.alpha_site is None and sc.site_T is None and sc.mu_site is None and len(sc.bond_src):
+            systems.append(sc)
+            Ts.append(meta["T"])
+            seeds.append(100 + seed)
+    assert len(systems) >= 12
+    for integ in ("heun", "depondt"):
+        ens = BatchedLLG(systems, 0.1, 1e-3, Ts, seeds, integrator=integ)
+        e0 = [sc.init_spins("random", seed=300 + k) for k, sc in enumerate(systems)]
+        ens.set_spins(e0)
+        ens.run(8, graph_chunk=0)
+        obs = ens.observables()
+        for k, sc in enumerate(systems):
+            sol = GB300LLG(sc, 0.1, 1e-3, Ts[k], seeds[k], integrator=integ)
+            lat = sol.model.to_lattice(e0[k])
+            sol.run_lattice(lat, 8)
+            err = float((ens.spins(k) - sol.model.from_lattice(lat)).abs().max())
+            assert err <= 1e-12 * 8, (k, integ, err)
+            E = sol.energy(ens.spins(k).cpu().numpy())
+            assert abs(obs[k, 0] - E) <= 1e-12 * max(1.0, abs(E))
