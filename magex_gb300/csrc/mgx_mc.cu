@@ -53,6 +53,7 @@ struct McPlan {
   bool fixed = false;                      // exchange field from the exact 56-bit fixed-point gather
   DevFX fx{};
   void* fx_block = nullptr;
+  bool share = false;                      // small classes split a site over kShare lanes (see launch_pass)
   // ensemble (mgx_mc_set_chains): nchains > 1 or chain_block set
   int nchains = 1;
   void* chain_block = nullptr;             // device: seed | beta | sigma | acc, nchains each
@@ -125,10 +126,52 @@ __device__ __forceinline__ double onsite(const DevLattice& L, long long q, int s
 
 enum { MC_GAUSSIAN = 0, MC_UNIFORM = 1, MC_HEATBATH = 2, MC_HINZKE = 3, MC_OVERRELAX = 4 };
 
+// This lane's share of the exchange field h = sum_j J_ij x_j when LANES lanes split a site's
+// couplings: couplings lane, lane + LANES, ... (the shares are summed by the caller).  Same per-coupling
+// arithmetic and open-boundary skips as exchange_field.
+template <int W, int LANES>
+__device__ __forceinline__ void exchange_field_share(const DevLattice& L, const double* __restrict__ x, int s, int c0,
+                                                     int c1, int c2, int lane, double& hx, double& hy, double& hz) {
+  hx = hy = hz = 0.0;
+  const long long N = L.N;
+  const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
+  for (int b = b0 + lane; b < b1; b += LANES) {
+    const int4 g = __ldg(L.bond_geo + b);
+    int n0 = c0 + g.y, n1 = c1 + g.z, n2 = c2 + g.w;
+    bool ok = true;
+    if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
+    if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
+    if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
+    if (!ok) continue;
+    const long long j = (long long)g.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
+    const double ex = __ldg(x + j), ey = __ldg(x + N + j), ez = __ldg(x + 2 * N + j);
+    const double* T = L.bond_J + (long long)b * W;
+    if (W == 1) {
+      const double J = __ldg(T);
+      hx = fma(J, ex, hx);
+      hy = fma(J, ey, hy);
+      hz = fma(J, ez, hz);
+    } else if (W == 4) {
+      const double J = __ldg(T), Dx = __ldg(T + 1), Dy = __ldg(T + 2), Dz = __ldg(T + 3);
+      hx = fma(J, ex, hx); hx = fma(ey, Dz, hx); hx = fma(-ez, Dy, hx);
+      hy = fma(J, ey, hy); hy = fma(ez, Dx, hy); hy = fma(-ex, Dz, hy);
+      hz = fma(J, ez, hz); hz = fma(ex, Dy, hz); hz = fma(-ey, Dx, hz);
+    } else {
+      hx = fma(__ldg(T + 0), ex, hx); hx = fma(__ldg(T + 1), ey, hx); hx = fma(__ldg(T + 2), ez, hx);
+      hy = fma(__ldg(T + 3), ex, hy); hy = fma(__ldg(T + 4), ey, hy); hy = fma(__ldg(T + 5), ez, hy);
+      hz = fma(__ldg(T + 6), ex, hz); hz = fma(__ldg(T + 7), ey, hz); hz = fma(__ldg(T + 8), ez, hz);
+    }
+  }
+}
+
 // One pass over the n sites of a colour class (of chain blockIdx.y of an ensemble).  hr: host-supplied
 // draws of this pass (RNG_HOST), laid out as documented at mgx_mc_sweep; otherwise Philox with counter
 // (site, sweep, pass).
-template <int W, int MOVE, bool HOSTRNG, bool FIXED>
+// LANES > 1 (stencil FP64 plans, small classes): LANES consecutive lanes share one site; each sums its
+// share of the couplings, the shares are added across the group, every lane of the group then runs the
+// same move and test and lane 0 writes the site.  This shortens each thread's serial chain when a class
+// is too small to fill the GPU with one thread per site.
+template <int W, int MOVE, bool HOSTRNG, bool FIXED, int LANES>
 __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __restrict__ e,
                                                  const long long* __restrict__ sites, long long n,
                                                  const double* __restrict__ beta_sub,
@@ -136,7 +179,8 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
                                                  const double* __restrict__ hr, uint64_t seed, uint64_t sweep,
                                                  int pass, unsigned long long* acc, const DevFX F,
                                                  const McChains chains) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / LANES;
+  const int lane = (int)(threadIdx.x % LANES);
   double chain_beta = 0.0;
   if (chains.seed) {
     const int k = blockIdx.y;
@@ -147,24 +191,41 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
     acc = chains.acc + k;
   }
   bool ok = false;
-  if (t < n) {
-    const long long N = L.N;
-    const long long q = __ldg(sites + t);
-    int s, c0, c1, c2;
-    site_coords(L, q, s, c0, c1, c2);
-    const long long m = (L.layout == 1) ? q : (long long)(q - (long long)s * L.ncell) * L.ns + s;
-    double hx, hy, hz;
-    if (FIXED) {
-      // exact 56-bit fixed-point sum h = sum_j J_ij e_j, rounded once to FP64
-      FxAcc a;
-      fx_accumulate(L, F, F.es, q, s, c0, c1, c2, a);
-      const double sc = F.scale[s];
-      hx = fma((double)a.x[0], 3.7252902984619141e-9, (double)a.hh[0]) * sc;
-      hy = fma((double)a.x[1], 3.7252902984619141e-9, (double)a.hh[1]) * sc;
-      hz = fma((double)a.x[2], 3.7252902984619141e-9, (double)a.hh[2]) * sc;
-    } else {
-      exchange_field<W>(L, e, s, c0, c1, c2, hx, hy, hz);
+  const bool active = t < n;
+  long long q = 0;
+  int s = 0, c0 = 0, c1 = 0, c2 = 0;
+  double hx = 0.0, hy = 0.0, hz = 0.0;
+  if (LANES > 1) {
+    if (active) {
+      q = __ldg(sites + t);
+      site_coords(L, q, s, c0, c1, c2);
+      exchange_field_share<W, LANES>(L, e, s, c0, c1, c2, lane, hx, hy, hz);
     }
+#pragma unroll
+    for (int o = LANES / 2; o > 0; o >>= 1) {          // every lane of the warp takes part
+      hx += __shfl_xor_sync(0xffffffffu, hx, o);
+      hy += __shfl_xor_sync(0xffffffffu, hy, o);
+      hz += __shfl_xor_sync(0xffffffffu, hz, o);
+    }
+  }
+  if (active) {
+    const long long N = L.N;
+    if (LANES == 1) {
+      q = __ldg(sites + t);
+      site_coords(L, q, s, c0, c1, c2);
+      if (FIXED) {
+        // exact 56-bit fixed-point sum h = sum_j J_ij e_j, rounded once to FP64
+        FxAcc a;
+        fx_accumulate(L, F, F.es, q, s, c0, c1, c2, a);
+        const double sc = F.scale[s];
+        hx = fma((double)a.x[0], 3.7252902984619141e-9, (double)a.hh[0]) * sc;
+        hy = fma((double)a.x[1], 3.7252902984619141e-9, (double)a.hh[1]) * sc;
+        hz = fma((double)a.x[2], 3.7252902984619141e-9, (double)a.hh[2]) * sc;
+      } else {
+        exchange_field<W>(L, e, s, c0, c1, c2, hx, hy, hz);
+      }
+    }
+    const long long m = (L.layout == 1) ? q : (long long)(q - (long long)s * L.ncell) * L.ns + s;
     const double ox = e[q], oy = e[N + q], oz = e[2 * N + q];
     const double mu = L.mu_site ? __ldg(L.mu_site + q) : __ldg(L.mu_sub + s);
     const double bt = chains.seed ? chain_beta : (beta_site ? __ldg(beta_site + q) : __ldg(beta_sub + s));
@@ -279,7 +340,7 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
       const double a = dE * bt;
       ok = below_exp(ua, -(a < 700.0 ? a : 700.0));
     }
-    if (ok) {
+    if (ok && lane == 0) {
       e[q] = nx;
       e[N + q] = ny;
       e[2 * N + q] = nz;
@@ -290,35 +351,55 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
       }
     }
   }
-  const int cnt = __syncthreads_count(ok);
+  const int cnt = __syncthreads_count(ok && lane == 0);
   if (MOVE != MC_OVERRELAX && threadIdx.x == 0 && cnt) atomicAdd(acc, (unsigned long long)cnt);
 }
+
+// Classes of at most kShareMaxSites sites of stencil FP64 plans with many couplings per site run with
+// kShare lanes per site (the choice depends on the class alone, so a chain's trajectory is the same in
+// an ensemble and on its own).  Measured on bcc (26 couplings): a single chain gains 2x at every class
+// size up to ~1000 sites, a 16-chain ensemble gains 2x at ~60 sites per class, 1.2x at ~200 and
+// loses beyond (the lanes repeat the move's arithmetic), so sharing stops at 256.
+constexpr long long kShareMaxSites = 256;
+constexpr int kShare = 16;
 
 template <int W, int MOVE>
 static void launch_pass(const McPlan* mc, double* e, int g, const double* hr, int pass, cudaStream_t st) {
   const DevLattice& L = mc->model->d;
   const long long n = mc->gsize[g];
   if (n == 0) return;
-  // small classes in small blocks, so that they still spread over the SMs
-  const int tpb = n > 152LL * 128 ? 128 : (n > 152LL * 64 ? 64 : 32);
-  const dim3 grid((unsigned)((n + tpb - 1) / tpb), (unsigned)mc->nchains);
   const long long* sites = mc->sites + mc->goff[g];
-  if (mc->fixed) {
+  const bool share = mc->share && n <= kShareMaxSites;
+  const long long threads = n * (share ? kShare : 1);
+  // small classes in small blocks, so that they still spread over the SMs
+  const int tpb = threads > 152LL * 128 ? 128 : (threads > 152LL * 64 ? 64 : 32);
+  const dim3 grid((unsigned)((threads + tpb - 1) / tpb), (unsigned)mc->nchains);
+  if (share) {
     if (hr)
-      k_mc_pass<W, MOVE, true, true><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
-                                                           mc->seed, mc->sweep, pass, mc->acc, mc->fx, mc->chains);
+      k_mc_pass<W, MOVE, true, false, kShare><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site,
+                                                                     mc->sigma, hr, mc->seed, mc->sweep, pass,
+                                                                     mc->acc, mc->fx, mc->chains);
     else
-      k_mc_pass<W, MOVE, false, true><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
-                                                            nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
-                                                            mc->chains);
+      k_mc_pass<W, MOVE, false, false, kShare><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site,
+                                                                      mc->sigma, nullptr, mc->seed, mc->sweep,
+                                                                      pass, mc->acc, mc->fx, mc->chains);
+  } else if (mc->fixed) {
+    if (hr)
+      k_mc_pass<W, MOVE, true, true, 1><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
+                                                              mc->seed, mc->sweep, pass, mc->acc, mc->fx, mc->chains);
+    else
+      k_mc_pass<W, MOVE, false, true, 1><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
+                                                               nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
+                                                               mc->chains);
   } else {
     if (hr)
-      k_mc_pass<W, MOVE, true, false><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma, hr,
-                                                            mc->seed, mc->sweep, pass, mc->acc, mc->fx, mc->chains);
+      k_mc_pass<W, MOVE, true, false, 1><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
+                                                               hr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
+                                                               mc->chains);
     else
-      k_mc_pass<W, MOVE, false, false><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
-                                                             nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
-                                                             mc->chains);
+      k_mc_pass<W, MOVE, false, false, 1><<<grid, tpb, 0, st>>>(L, e, sites, n, mc->beta, mc->beta_site, mc->sigma,
+                                                                nullptr, mc->seed, mc->sweep, pass, mc->acc, mc->fx,
+                                                                mc->chains);
   }
 }
 
@@ -528,6 +609,9 @@ extern "C" mgx_status mgx_mc_create(const mgx_model* mm, const mgx_mc_params* p,
     mc_free(mc);
     return cuda_error(err, "mgx_mc_create");
   }
+  // many couplings per site (at least 12 per cell and sublattice) on the stencil layout: sites of small
+  // classes are shared by kShare lanes
+  mc->share = d.layout == 0 && p->precision == MGX_PRECISION_FP64 && m->nbond >= 12 * d.ns;
   if (p->precision == MGX_PRECISION_FP64_FIXED_GATHER) {
     const mgx_status st = fx_build(m, 28, false, 1, &mc->fx, &mc->fx_block);
     if (st != MGX_OK) {
