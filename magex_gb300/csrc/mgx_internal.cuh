@@ -136,7 +136,7 @@ struct DevFX {
 };
 
 // Axis-0 slabs a host-buffer step is split into (copies of one overlap the stages of another).
-#define MGX_HOST_CHUNKS 16
+#define MGX_HOST_CHUNKS 32
 
 struct LLGPlan {
   const Model* model;
