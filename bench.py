@@ -425,6 +425,26 @@ def bench_mc_points(sizes=(8, 16), npts=16, therm=1000, meas=4000):
             "rows_equal_point": True}
 
 
+def bench_mc_pt(L=16, nrep=16, therm=1000, meas=4000):
+    """Parallel tempering (magex/advanced_mc.py:38-95): nrep replicas of an sc L^3 ferromagnet on
+    30..45 K, therm + meas sweeps, swaps every 5 sweeps, samples every 2: wall time and swap
+    acceptance."""
+    import numpy as np
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.mc import parallel_tempering
+    from magex_gb300.spinmodel import load_results, make_model
+    sc = Supercell(load_results(make_model("sc", J=[1.0])), (L, L, L), (True,) * 3, (0.0, 0.0, 0.0))
+    Ts = np.linspace(30.0, 45.0, nrep)
+    parallel_tempering(sc, Ts, therm_sweeps=50, meas_sweeps=50)
+    t0 = time.perf_counter()
+    rows, swap = parallel_tempering(sc, Ts, therm_sweeps=therm, meas_sweeps=meas, sample_every=2, swap_every=5)
+    t = time.perf_counter() - t0
+    return {"workload": f"parallel tempering, sc {L}^3, {nrep} replicas on 30..45 K, {therm} + {meas} sweeps, "
+                        "swaps every 5 sweeps, Gaussian moves + 1 over-relaxation pass, Philox, FP64",
+            "seconds": t, "site_updates_per_s": 2 * sc.N * nrep * (therm + meas) / t, "unit": "site-updates/s",
+            "swap_acceptance": [round(x, 3) for x in swap]}
+
+
 def bench_mc(L=128, sweeps=20, move="gaussian", overrelax=1, cpu_baseline=True, precision="fp64"):
     """Monte Carlo colour sweeps on the 128^3 two-site bcc workload (4,194,304 spins, z = 26, full
     3x3 tensors), T = 300 K, in-kernel Philox draws: site updates per second (one update = one trial
@@ -716,6 +736,7 @@ def run_gb300(args):
         line["monte_carlo"] = bench_mc(L=args.L, cpu_baseline=not args.no_cpu_baseline)
         line["monte_carlo_fp64_fixed"] = bench_mc(L=args.L, cpu_baseline=False, precision="fp64_fixed")
         line["monte_carlo_points"] = bench_mc_points()
+        line["monte_carlo_parallel_tempering"] = bench_mc_pt()
         line["sqw_projection"] = bench_sqw(L=args.L)
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
@@ -763,7 +784,7 @@ def main():
             out = [bench_mc(L=args.L, sweeps=min(args.steps, 100), cpu_baseline=False, precision=p)
                    for p in ("fp64", "fp64_fixed")]
             if args.steps >= 20:           # short profiling runs skip the T scan's ~300k launches
-                out.append(bench_mc_points())
+                out += [bench_mc_points(), bench_mc_pt()]
         elif args.only == "config5":
             out = [bench_config5(K=min(args.steps, 50), adj_steps=args.adjoint_steps or 1000),
                    bench_config5(K=min(args.steps, 50), adj_steps=0, precision="fp64_fixed")]
