@@ -485,3 +485,41 @@ def test_every_site_pinned_keeps_the_spins(cuda, golden_models, noise):
     assert mc.ncolors == 0
     f = mc.sweep(e0.copy())
     assert np.array_equal(f, e0) and mc.acceptance() == 0.0
+
+
+def test_new_entry_points_reject_bad_arguments(cuda, golden_models):
+    """Errors of the newer calls surface as the exceptions magex raises (ValueError for bad values,
+    NotImplementedError for what the kernels do not offer), with nothing launched."""
+    import ctypes as C
+    from magex_gb300 import _lib
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.mc import MetropolisMC
+    from magex_gb300.spinmodel import load_results
+    sc = Supercell(load_results(golden_models["sc_dmi"]["model"]), (4, 4, 4), (True, True, True), (0.0, 0.0, 0.5))
+    with pytest.raises(NotImplementedError):
+        GB300LLG(sc, 0.1, 1e-3, sot=dict(p=[0, 1, 0], B_DL=0.1), precision="fp64_fixed")
+    with pytest.raises(NotImplementedError):
+        GB300LLG(sc, 0.1, 1e-3, stt=dict(u=[1, 0, 0], beta=0.1))
+    sol = GB300LLG(sc, 0.1, 1e-3)
+    lib = sol.model.lib
+    with pytest.raises(ValueError):                       # p must be a non-zero vector
+        _lib.check(lib.mgx_llg_set_sot(sol.handle, _lib.dptr(np.zeros(3)), 0.1, 0.0), "mgx_llg_set_sot")
+    fixed = GB300LLG(sc, 0.1, 1e-3, precision="fp64_fixed")
+    field = torch.zeros(3 * sc.N, dtype=torch.float64, device="cuda")
+    with pytest.raises(NotImplementedError):              # per-site fields: FP64 plans only
+        _lib.check(lib.mgx_llg_set_extra_field(fixed.handle, C.c_void_p(field.data_ptr())), "mgx_llg_set_extra_field")
+    sol.field_func = lambda t: np.zeros(5)                # neither (3,) nor (N, 3)
+    with pytest.raises(ValueError):
+        sol.step(sc.init_spins("random", seed=1))
+    mc = MetropolisMC(sc, 10.0, seed=1)
+    keys = np.array([1, 2], np.uint64)
+    with pytest.raises(ValueError):                       # beta must be finite and > 0
+        _lib.check(lib.mgx_mc_set_chains(mc.handle, 2, keys.ctypes.data_as(C.c_void_p), _lib.dptr(np.array([1.0, 0.0])),
+                                         _lib.dptr(np.array([0.5, 0.5]))), "mgx_mc_set_chains")
+    host = MetropolisMC(sc, 10.0, seed=1, rng="host")
+    with pytest.raises(NotImplementedError):              # ensembles draw Philox numbers
+        _lib.check(lib.mgx_mc_set_chains(host.handle, 2, keys.ctypes.data_as(C.c_void_p), _lib.dptr(np.array([1.0, 1.0])),
+                                         _lib.dptr(np.array([0.5, 0.5]))), "mgx_mc_set_chains")
+    with pytest.raises(ValueError):
+        _lib.check(lib.mgx_mc_chain_counts(mc.handle, C.c_void_p(0), None, None, 0, None), "mgx_mc_chain_counts")
