@@ -526,6 +526,39 @@ def bench_sqw(L=128, reps=20):
                     f"case would hold {16 * sc.N * len(q) / 1e9:.0f} GB"}
 
 
+def bench_texture(L=256, reps=20):
+    """Topological charge of a triangular L x L film through magex_gb300.texture (the drop-in for
+    magex/texture.py:30-63): the first call builds and keeps the periodic Delaunay triangulation,
+    later calls are one device pass over the triangles.  magex repeats the triangulation and the
+    NumPy solid-angle sum on every call; both are timed here on the host beside the device call."""
+    import time
+    import torch
+    from magex_gb300 import texture
+    from magex_gb300.workloads import triangular_film
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import solid_angle_charge
+    sc = triangular_film(L=L, field=(0, 0, 0))
+    e = torch.as_tensor(sc.init_spins("random", seed=3), device="cuda")
+    t0 = time.perf_counter()
+    tri, sign = texture.layer_triangles(sc)
+    t_tri = time.perf_counter() - t0
+    texture.topological_charge(sc, e)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        Q = texture.topological_charge(sc, e)
+    t_dev = (time.perf_counter() - t0) / reps
+    e_host = e.cpu().numpy()
+    t0 = time.perf_counter()
+    Q_host = solid_angle_charge(e_host, tri, sign)
+    t_sum = time.perf_counter() - t0
+    return {"workload": f"triangular {L} x {L} film ({sc.N:,} spins, {len(tri):,} triangles), random spins",
+            "ms_per_call": t_dev * 1e3, "host_triangulation_ms": t_tri * 1e3, "host_solid_angle_sum_ms": t_sum * 1e3,
+            "abs_diff_vs_host": abs(Q - Q_host),
+            "note": "ms_per_call is the wall time of texture.topological_charge on a device tensor after the first "
+                    "call (which also triangulates); magex pays triangulation + sum on every call"}
+
+
 def bench_config1(steps=1000, cpu=True):
     """Plain FP64 workload of the reference's CPU-runnable case: simple-cubic 16^3 (4,096 spins), 6
     neighbours, J = 1 meV, mu = 2 mu_B, alpha 0.1, B = 0, T = 0, dt 0.1 fs, 1000 Heun steps from
@@ -738,6 +771,7 @@ def run_gb300(args):
         line["monte_carlo_points"] = bench_mc_points()
         line["monte_carlo_parallel_tempering"] = bench_mc_pt()
         line["sqw_projection"] = bench_sqw(L=args.L)
+        line["topological_charge"] = bench_texture()
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -759,7 +793,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
     ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "fp64_fixed", "config1", "config5", "mc",
-                                       "sqw"],
+                                       "sqw", "texture"],
                     default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
@@ -780,6 +814,8 @@ def main():
             out = bench_config1()
         elif args.only == "sqw":
             out = bench_sqw(L=args.L)
+        elif args.only == "texture":
+            out = bench_texture()
         elif args.only == "mc":
             out = [bench_mc(L=args.L, sweeps=min(args.steps, 100), cpu_baseline=False, precision=p)
                    for p in ("fp64", "fp64_fixed")]

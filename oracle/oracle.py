@@ -302,3 +302,15 @@ class OracleMC:
             for idx in self.groups:
                 self._group(e, idx, 4, rng.random(len(idx)), beta)
         return e
+
+
+def solid_angle_charge(e, tri, sign):
+    """Skyrmion number (1/4 pi) sum_t sign_t * 2 atan2(s1.(s2 x s3), 1 + s1.s2 + s2.s3 + s3.s1) over
+    triangles tri ((T, 3) site indices of spins e, (N, 3)), the Berg-Luscher solid angle of
+    magex/texture.py:53-62 with the plane's handedness folded into sign."""
+    e = np.asarray(e, np.float64)
+    tri = np.asarray(tri, np.int64).reshape(-1, 3)
+    s1, s2, s3 = e[tri[:, 0]], e[tri[:, 1]], e[tri[:, 2]]
+    num = np.einsum("ij,ij->i", s1, np.cross(s2, s3))
+    den = 1 + np.einsum("ij,ij->i", s1, s2) + np.einsum("ij,ij->i", s2, s3) + np.einsum("ij,ij->i", s3, s1)
+    return float((2 * np.arctan2(num, den) * np.asarray(sign, np.float64)).sum() / (4 * np.pi))

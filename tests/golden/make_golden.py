@@ -393,6 +393,29 @@ def main(ref_root):
     out["topo/random_e"] = e2
     out["topo/random_Q"] = np.array(RT.topological_charge(s, e2))
 
+    # the same charge on other lattices and planes, open and periodic in-plane axes (periodic Delaunay
+    # of magex/texture.py:30-63): a Gaussian bubble texture and random spins
+    topo_cases = {}
+    ucs_topo = dict(ucs, sq=uc_of("sq", RM.make_model(lattice="square", J=[1.0], D=0.2)))
+    for tag, model, L, pbc, plane, layer in (("square", "sq", (24, 24, 1), (1, 1, 0), "xy", 0),
+                                             ("honeycomb", "honeycomb_bulk", (12, 12, 1), (1, 1, 0), "xy", 0),
+                                             ("kagome", "kagome", (10, 10, 1), (1, 0, 0), "xy", 0),
+                                             ("sc_xz", "sc", (8, 4, 8), (1, 1, 1), "xz", 2),
+                                             ("sc_open", "sc", (10, 10, 3), (0, 0, 0), "xy", 1)):
+        s = RS.SpinSystem(ucs_topo[model], L, pbc)
+        ax, bx, _ = RT.PLANES[plane]
+        r = s.positions[:, [ax, bx]] - s.positions[:, [ax, bx]].mean(0)
+        R = np.linalg.norm(r, axis=1)
+        th = np.pi * np.exp(-(R / (0.3 * R.max())) ** 2)
+        ph = np.arctan2(r[:, 1], r[:, 0])
+        e = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)
+        e2 = s.init_spins("random", seed=13)
+        out[f"topo2/{tag}/bubble_e"], out[f"topo2/{tag}/random_e"] = e, e2
+        out[f"topo2/{tag}/bubble_Q"] = np.array(RT.topological_charge(s, e, plane, layer))
+        out[f"topo2/{tag}/random_Q"] = np.array(RT.topological_charge(s, e2, plane, layer))
+        topo_cases[tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], plane=plane, layer=layer)
+    models["topo2"] = topo_cases
+
     np.savez_compressed(os.path.join(HERE, "llg_golden.npz"), **out)
     with open(os.path.join(HERE, "models.json"), "w") as f:
         json.dump(models, f)
