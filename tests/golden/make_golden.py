@@ -415,6 +415,16 @@ def main(ref_root):
         out[f"topo2/{tag}/random_Q"] = np.array(RT.topological_charge(s, e2, plane, layer))
         topo_cases[tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], plane=plane, layer=layer)
     models["topo2"] = topo_cases
+    # magex's own texture initialisers on a 40 x 40 triangular film (the charges of
+    # tests/test_universal.py:81-91): one and two skyrmions, helicity 0 with vorticity +1 and -1
+    s = RS.SpinSystem(ucs["tri"], (40, 40, 1), (1, 1, 0), (0, 0, 1.0))
+    for tag, kw in (("skyrmion", dict(kind="skyrmion", radius=8.0)),
+                    ("skyrmions", dict(kind="skyrmions", centers=[[30, 30], [80, 60]], radius=6.0)),
+                    ("helicity0", dict(kind="skyrmion", radius=8.0, helicity=0.0)),
+                    ("antiskyrmion", dict(kind="skyrmion", radius=8.0, helicity=0.0, vorticity=-1))):
+        e = s.init_spins(**kw)
+        out[f"topo3/{tag}_e"] = e
+        out[f"topo3/{tag}_Q"] = np.array(RT.topological_charge(s, e, "xy", 0))
 
     np.savez_compressed(os.path.join(HERE, "llg_golden.npz"), **out)
     with open(os.path.join(HERE, "models.json"), "w") as f:

@@ -67,3 +67,32 @@ def test_device_charge(cuda, golden, golden_models, tag):
             assert abs(Q - float(golden[f"topo2/{tag}/{k}_Q"])) < 1e-9, (tag, k)
         # a device tensor, and the kept triangulation on the second call
         assert texture.topological_charge(sc, torch.as_tensor(e, device="cuda"), plane, layer) == Q
+
+
+TEXTURES = ("skyrmion", "skyrmions", "helicity0", "antiskyrmion")
+
+
+def _film40(golden_models):
+    return Supercell(load_results(golden_models["tri"]["model"]), (40, 40, 1), (True, True, False), (0, 0, 1.0))
+
+
+def test_texture_charges_match_reference(golden, golden_models):
+    from oracle import solid_angle_charge
+    sc = _film40(golden_models)
+    tri, sign = texture.layer_triangles(sc)
+    for k in TEXTURES:
+        Q = solid_angle_charge(golden[f"topo3/{k}_e"], tri, sign)
+        assert abs(Q - float(golden[f"topo3/{k}_Q"])) < 1e-12, k
+
+
+@pytest.mark.gpu
+def test_texture_charges_on_device(cuda, golden, golden_models):
+    """The assertions of tests/test_universal.py:81-91 on magex's own textures, through the drop-in."""
+    sc = _film40(golden_models)
+    Q = {k: texture.topological_charge(sc, golden[f"topo3/{k}_e"], "xy", 0) for k in TEXTURES}
+    for k in TEXTURES:
+        assert abs(Q[k] - float(golden[f"topo3/{k}_Q"])) < 1e-9, k
+    assert abs(abs(Q["skyrmion"]) - 1) < 1e-6
+    assert abs(abs(Q["skyrmions"]) - 2) < 1e-6
+    assert abs(Q["helicity0"] + Q["antiskyrmion"]) < 1e-6
+    assert abs(texture.topological_charge(sc, np.tile([0, 0, 1.0], (sc.N, 1)))) < 1e-9
