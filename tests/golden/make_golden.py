@@ -415,6 +415,27 @@ def main(ref_root):
         out[f"topo2/{tag}/random_Q"] = np.array(RT.topological_charge(s, e2, plane, layer))
         topo_cases[tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], plane=plane, layer=layer)
     models["topo2"] = topo_cases
+    # damped-LLG relaxation of magex/minimize.py:168-181 (alpha 1, dt 2 fs, no precession, torque
+    # checked every 50 steps): to a torque tolerance, with a pinned layer, and stopped by max_iter
+    from magex.minimize import minimize as RMIN
+    relax_cases = {}
+    for tag, model, L, pbc, B, tol, max_iter, structure, seed in (
+            ("tri", "tri", (12, 12, 1), (1, 1, 0), (0.0, 0.0, 1.0), 1e-4, None, None, 21),
+            ("sc_pinned", "sc_dmi", (4, 4, 4), (1, 1, 0), (0.2, 0.0, 0.3), 1e-5, 20000,
+             dict(pinned=[dict(region="bottom", layers=1, direction=[1, 0, 0])]), 22),
+            ("max_iter", "bcc2", (3, 3, 3), (1, 1, 1), (0.0, 0.0, 0.5), 1e-12, 120, None, 23)):
+        s = RS.SpinSystem(ucs_topo[model], L, pbc, B)
+        if structure:
+            apply_structure(s, structure)
+        e0 = s.init_spins("random", seed=seed)
+        e, info = RMIN(s, e0.copy(), "llg", tol=tol, max_iter=max_iter)
+        out[f"relax/{tag}/e0"], out[f"relax/{tag}/e"] = e0, e
+        out[f"relax/{tag}/iterations"] = np.array(info["iterations"])
+        out[f"relax/{tag}/energy"] = np.array(info["energy"])
+        relax_cases[tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], B=list(B), tol=tol,
+                                max_iter=max_iter, structure=structure)
+    models["relax"] = relax_cases
+
     # magex's own texture initialisers on a 40 x 40 triangular film (the charges of
     # tests/test_universal.py:81-91): one and two skyrmions, helicity 0 with vorticity +1 and -1
     s = RS.SpinSystem(ucs["tri"], (40, 40, 1), (1, 1, 0), (0, 0, 1.0))
