@@ -248,7 +248,10 @@ class GB300LLG:
 
     def _advance(self, nsteps=1):
         self._step_index += int(nsteps)
-        self.time += self.dt * int(nsteps)
+        t, dt = self.time, self.dt
+        for _ in range(int(nsteps)):         # one addition per step, as magex/llg.py:196,213,247 accumulate
+            t += dt
+        self.time = t
 
     def step_lattice(self, lat, stream=None):
         """One step on device spins in the lattice layout ((3, N) float64, in place)."""

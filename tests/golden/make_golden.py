@@ -436,6 +436,24 @@ def main(ref_root):
                                 max_iter=max_iter, structure=structure)
     models["relax"] = relax_cases
 
+    # FMR ring-down of magex/programs.py:124-150 from states relaxed to 1e-11 (so that magex's own
+    # L-BFGS relaxation inside fmr returns at once)
+    from magex.programs import fmr as RFMR
+    fmr_cases = {}
+    for tag, model, L, pbc, B, kw in (
+            ("tri_heun", "tri", (8, 8, 1), (1, 1, 0), (0.0, 0.0, 1.0),
+             dict(B_pulse=0.05, alpha=0.01, dt=2e-3, steps=3000, every=5)),
+            ("sc_depondt", "sc_dmi", (4, 4, 4), (1, 1, 1), (0.0, 0.0, 2.0),
+             dict(B_pulse=0.02, direction=(0, 1, 1), alpha=0.005, dt=1e-3, steps=2002, every=7,
+                  integrator="depondt"))):
+        s = RS.SpinSystem(ucs_topo[model], L, pbc, B)
+        e_rel, _ = RMIN(s, s.init_spins("ferro", (0, 0, 1)), "lbfgs", tol=1e-11)
+        (f, F), fpk, table = RFMR(s, e_rel.copy(), **kw)
+        out[f"fmr/{tag}/e"], out[f"fmr/{tag}/f"], out[f"fmr/{tag}/F"] = e_rel, f, F
+        out[f"fmr/{tag}/fpk"], out[f"fmr/{tag}/table"] = np.array(fpk), table
+        fmr_cases[tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], B=list(B), kw=kw)
+    models["fmr"] = fmr_cases
+
     # magex's own texture initialisers on a 40 x 40 triangular film (the charges of
     # tests/test_universal.py:81-91): one and two skyrmions, helicity 0 with vorticity +1 and -1
     s = RS.SpinSystem(ucs["tri"], (40, 40, 1), (1, 1, 0), (0, 0, 1.0))
