@@ -559,6 +559,55 @@ def bench_texture(L=256, reps=20):
                     "call (which also triangulates); magex pays triangulation + sum on every call"}
 
 
+def bench_callers(L=128, fmr_steps=20000, relax_L=64, cpu_steps=400):
+    """Two callers of the step on a triangular film (J = 1 meV, D = 0.3 meV interfacial, K = 0.05
+    meV, mu = 2 mu_B, B_z = 1 T): the FMR ring-down of magex/programs.py:124-150 (L x L, fmr_steps
+    steps, a sample every 5 steps) and the damped-LLG relaxation of magex/minimize.py:168-181 from
+    random spins (relax_L x relax_L, tol 1e-4 meV).  Wall time of the whole call; beside each, the
+    oracle's step loop on the host cores for cpu_steps steps of the same system."""
+    import torch
+    from magex_gb300.minimize import minimize
+    from magex_gb300.programs import fmr
+    from magex_gb300.workloads import triangular_film
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import OracleLLG, max_threads
+
+    def cpu_rate(sc, alpha, dt, precession):
+        ora = OracleLLG(sc, alpha, dt, 0.0, precession=precession, csr="stencil")
+        e = sc.init_spins("random", seed=2)
+        t0 = time.perf_counter()
+        for _ in range(cpu_steps):
+            ora.step_inplace(e)
+        return sc.N * cpu_steps / (time.perf_counter() - t0)
+
+    out = {}
+    sc = triangular_film(L=L, field=(0, 0, 1.0))
+    e0 = sc.init_spins("ferro", (0, 0, 1))
+    fmr(sc, e0, steps=200)                                   # warm-up (graphs, buffers)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, fpk, table = fmr(sc, e0, steps=fmr_steps)
+    el = time.perf_counter() - t0
+    out["fmr"] = {"workload": f"triangular {L} x {L} film ({sc.N:,} spins), {fmr_steps} steps, a sample every 5",
+                  "seconds": el, "value": sc.N * fmr_steps / el, "unit": UNIT, "f_peak_GHz": fpk,
+                  "cpu_baseline": {"value": cpu_rate(sc, 0.001, 2e-3, True), "unit": UNIT, "cores": max_threads(),
+                                   "kind": "port", "sample": f"{cpu_steps} oracle steps of the same film"}}
+    sc = triangular_film(L=relax_L, field=(0, 0, 1.0))
+    e0 = sc.init_spins("random", seed=5)
+    minimize(sc, e0, "llg", tol=1e-4, max_iter=200)        # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, info = minimize(sc, e0, "llg", tol=1e-4)
+    el = time.perf_counter() - t0
+    out["relax"] = {"workload": f"triangular {relax_L} x {relax_L} film ({sc.N:,} spins) from random spins, "
+                                "tol 1e-4 meV",
+                    "iterations": info["iterations"], "seconds": el, "value": sc.N * info["iterations"] / el,
+                    "unit": UNIT,
+                    "cpu_baseline": {"value": cpu_rate(sc, 1.0, 2e-3, False), "unit": UNIT, "cores": max_threads(),
+                                     "kind": "port", "sample": f"{cpu_steps} oracle steps of the same film"}}
+    return out
+
+
 def bench_config1(steps=1000, cpu=True):
     """Plain FP64 workload of the reference's CPU-runnable case: simple-cubic 16^3 (4,096 spins), 6
     neighbours, J = 1 meV, mu = 2 mu_B, alpha 0.1, B = 0, T = 0, dt 0.1 fs, 1000 Heun steps from
@@ -772,6 +821,7 @@ def run_gb300(args):
         line["monte_carlo_parallel_tempering"] = bench_mc_pt()
         line["sqw_projection"] = bench_sqw(L=args.L)
         line["topological_charge"] = bench_texture()
+        line["callers"] = bench_callers()
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -793,7 +843,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
     ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "fp64_fixed", "config1", "config5", "mc",
-                                       "sqw", "texture"],
+                                       "sqw", "texture", "callers"],
                     default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
@@ -816,6 +866,8 @@ def main():
             out = bench_sqw(L=args.L)
         elif args.only == "texture":
             out = bench_texture()
+        elif args.only == "callers":
+            out = bench_callers()
         elif args.only == "mc":
             out = [bench_mc(L=args.L, sweeps=min(args.steps, 100), cpu_baseline=False, precision=p)
                    for p in ("fp64", "fp64_fixed")]

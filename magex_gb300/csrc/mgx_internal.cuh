@@ -137,6 +137,18 @@ struct DevFX {
 
 // Axis-0 slabs a host-buffer step is split into (copies of one overlap the stages of another).
 #define MGX_HOST_CHUNKS 32
+#define MGX_LLG_GRAPHS 4
+
+// one captured loop of `steps` Heun steps, valid for the spin buffer, noise mode, external field and
+// cell offset it was captured with (kernel parameters are captured by value)
+struct LLGGraph {
+  cudaGraphExec_t exec = nullptr;
+  int steps = 0, mode = -1;
+  const double* e = nullptr;
+  double B[3] = {0.0, 0.0, 0.0};
+  long long offset = 0;
+  unsigned long long used = 0;
+};
 
 struct LLGPlan {
   const Model* model;
@@ -151,14 +163,13 @@ struct LLGPlan {
   double* site_block = nullptr;  // alpha_site | pre_site
   double* sigma_site = nullptr;
   double* scratch = nullptr;     // ep | k1
-  // captured step loop of mgx_llg_run (small lattices, where launches dominate)
+  // captured step loops of mgx_llg_run (small lattices, where launches dominate): a few graphs of
+  // different step counts, the least recently used one replaced
   cudaStream_t cap_stream = nullptr;
-  cudaGraphExec_t graph = nullptr;
+  LLGGraph graphs[MGX_LLG_GRAPHS];
+  unsigned long long graph_clock = 0;
+  long long last_tail = -1;      // step count of the previous call's ungraphed tail
   unsigned long long* d_step = nullptr;
-  int graph_chunk = 0, graph_mode = -1;
-  const double* graph_e = nullptr;
-  double graph_B[3] = {0.0, 0.0, 0.0};
-  long long graph_offset = 0;
   // step on host buffers (mgx_llg_step_host): device copies of the spins, the copy stream and a
   // second compute stream (consecutive slabs run on alternate streams so each fills the other's tail)
   cudaStream_t copy_stream = nullptr, aux_stream = nullptr;

@@ -114,51 +114,78 @@ static std::vector<T> site_to_lattice(const T* src, int ns, int ncell) {
   return out;
 }
 
-// Small lattices are launch-bound: mgx_llg_run replays a CUDA graph of kGraphChunk steps whose kernels
+// Small lattices are launch-bound: mgx_llg_run replays CUDA graphs of kGraphChunk steps whose kernels
 // read the Philox step index from a device counter (advanced by a one-thread kernel at the end of the
-// chunk), so every replay draws fresh noise and the trajectory equals the directly launched one.
+// graph), so every replay draws fresh noise and the trajectory equals the directly launched one.  A
+// shorter tail of k >= kGraphMinTail steps is captured as a graph of its own once the same k comes
+// twice in a row (callers that step in fixed chunks of a few steps between checks or samples).
 constexpr long long kGraphMaxSites = 1LL << 21;
 constexpr int kGraphChunk = 32;
+constexpr int kGraphMinTail = 4;
 
 __global__ void k_llg_step_set(unsigned long long* c, unsigned long long v) { *c = v; }
 __global__ void k_llg_step_advance(unsigned long long* c, unsigned long long n) { *c += n; }
 
 static void drop_llg_graph(LLGPlan* pl) {
-  if (pl->graph) cudaGraphExecDestroy(pl->graph);
-  pl->graph = nullptr;
-  pl->graph_e = nullptr;
-  pl->graph_mode = -1;
+  for (LLGGraph& g : pl->graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = LLGGraph{};
+  }
+  pl->last_tail = -1;
 }
 
-static mgx_status llg_graph(LLGPlan* pl, double* e) {
+static bool graph_matches(const LLGGraph& g, int steps, const double* e, int mode, const DevLattice& L) {
+  return g.exec && g.steps == steps && g.e == e && g.mode == mode && g.B[0] == L.B0 && g.B[1] == L.B1 &&
+         g.B[2] == L.B2 && g.offset == L.cell_offset;
+}
+
+static const LLGGraph* find_llg_graph(LLGPlan* pl, int steps, const double* e) {
+  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
+  for (LLGGraph& g : pl->graphs)
+    if (graph_matches(g, steps, e, mode, pl->model->d)) return &g;
+  return nullptr;
+}
+
+// the graph of `steps` steps on spins e (captured now if no current one matches)
+static mgx_status llg_graph(LLGPlan* pl, double* e, int steps, cudaGraphExec_t* out) {
   const DevLattice& L = pl->model->d;
   const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
-  if (pl->graph && pl->graph_e == e && pl->graph_mode == mode && pl->graph_B[0] == L.B0 && pl->graph_B[1] == L.B1 &&
-      pl->graph_B[2] == L.B2 && pl->graph_offset == L.cell_offset)
-    return MGX_OK;
-  drop_llg_graph(pl);
+  LLGGraph* slot = nullptr;
+  for (LLGGraph& g : pl->graphs) {
+    if (graph_matches(g, steps, e, mode, L)) {
+      g.used = ++pl->graph_clock;
+      *out = g.exec;
+      return MGX_OK;
+    }
+    if (!slot || !g.exec || (slot->exec && g.used < slot->used)) slot = &g;
+  }
+  if (slot->exec) cudaGraphExecDestroy(slot->exec);
+  *slot = LLGGraph{};
   if (!pl->d_step) MGX_CUDA_TRY(cudaMalloc(&pl->d_step, sizeof(unsigned long long)));
   if (!pl->cap_stream) MGX_CUDA_TRY(cudaStreamCreateWithFlags(&pl->cap_stream, cudaStreamNonBlocking));
   MGX_CUDA_TRY(cudaStreamBeginCapture(pl->cap_stream, cudaStreamCaptureModeThreadLocal));
   pl->p.step_base = pl->d_step;
-  for (int k = 0; k < kGraphChunk; ++k) enqueue_llg_step(pl, e, nullptr, (uint64_t)k, pl->cap_stream, 3);
+  for (int k = 0; k < steps; ++k) enqueue_llg_step(pl, e, nullptr, (uint64_t)k, pl->cap_stream, 3);
   pl->p.step_base = nullptr;
-  k_llg_step_advance<<<1, 1, 0, pl->cap_stream>>>(pl->d_step, (unsigned long long)kGraphChunk);
+  k_llg_step_advance<<<1, 1, 0, pl->cap_stream>>>(pl->d_step, (unsigned long long)steps);
   cudaGraph_t g = nullptr;
   cudaError_t err = cudaStreamEndCapture(pl->cap_stream, &g);
   if (err != cudaSuccess) return cuda_error(err, "mgx_llg_run capture");
-  err = cudaGraphInstantiate(&pl->graph, g, 0);
+  err = cudaGraphInstantiate(&slot->exec, g, 0);
   cudaGraphDestroy(g);
   if (err != cudaSuccess) {
-    pl->graph = nullptr;
+    slot->exec = nullptr;
     return cuda_error(err, "mgx_llg_run instantiate");
   }
-  pl->graph_e = e;
-  pl->graph_mode = mode;
-  pl->graph_B[0] = L.B0;
-  pl->graph_B[1] = L.B1;
-  pl->graph_B[2] = L.B2;
-  pl->graph_offset = L.cell_offset;
+  slot->steps = steps;
+  slot->e = e;
+  slot->mode = mode;
+  slot->B[0] = L.B0;
+  slot->B[1] = L.B1;
+  slot->B[2] = L.B2;
+  slot->offset = L.cell_offset;
+  slot->used = ++pl->graph_clock;
+  *out = slot->exec;
   return MGX_OK;
 }
 
@@ -507,11 +534,26 @@ mgx_status mgx_llg_run(mgx_llg* pp, double* e, int64_t nsteps, uint64_t step0, v
   cudaStream_t st = (cudaStream_t)stream;
   if (nsteps > 0) enqueue_reduced_split(pl, e, st);
   int64_t done = 0;
-  if (pl->model->d.N <= kGraphMaxSites && nsteps >= 2 * kGraphChunk) {
-    const mgx_status gs = llg_graph(pl, e);
-    if (gs != MGX_OK) return gs;
-    k_llg_step_set<<<1, 1, 0, st>>>(pl->d_step, (unsigned long long)step0);
-    for (; done + kGraphChunk <= nsteps; done += kGraphChunk) MGX_CUDA_TRY(cudaGraphLaunch(pl->graph, st));
+  if (pl->model->d.N <= kGraphMaxSites) {
+    bool counter_set = false;
+    cudaGraphExec_t exec = nullptr;
+    if (nsteps >= 2 * kGraphChunk) {
+      const mgx_status gs = llg_graph(pl, e, kGraphChunk, &exec);
+      if (gs != MGX_OK) return gs;
+      k_llg_step_set<<<1, 1, 0, st>>>(pl->d_step, (unsigned long long)step0);
+      counter_set = true;
+      for (; done + kGraphChunk <= nsteps; done += kGraphChunk) MGX_CUDA_TRY(cudaGraphLaunch(exec, st));
+    }
+    const long long tail = nsteps - done;
+    if (tail >= kGraphMinTail && tail < 2 * kGraphChunk &&
+        (tail == pl->last_tail || find_llg_graph(pl, (int)tail, e))) {
+      const mgx_status gs = llg_graph(pl, e, (int)tail, &exec);
+      if (gs != MGX_OK) return gs;
+      if (!counter_set) k_llg_step_set<<<1, 1, 0, st>>>(pl->d_step, (unsigned long long)(step0 + done));
+      MGX_CUDA_TRY(cudaGraphLaunch(exec, st));
+      done = nsteps;
+    }
+    pl->last_tail = tail;
   }
   for (; done < nsteps; ++done) enqueue_llg_step(pl, e, nullptr, step0 + (uint64_t)done, st, 3);
   MGX_CUDA_TRY(cudaGetLastError());

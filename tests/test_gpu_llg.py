@@ -242,6 +242,13 @@ def test_graph_replayed_run_equals_direct_launches(cuda, precision):
     for _ in range(64):
         b.run_lattice(lb, 1)
     assert torch.equal(la, lb)
+    # repeated short chunks (tails of 4..63 steps become graphs of their own from the second call on),
+    # more step counts than cached graphs, and tails after 32-step replays
+    for n in (5, 5, 5, 50, 50, 7, 5, 50, 9, 11, 13, 5, 70, 70, 6, 4, 4, 3, 3):
+        a.run_lattice(la, n)
+        for _ in range(n):
+            b.run_lattice(lb, 1)
+        assert torch.equal(la, lb), n
 
 
 @pytest.mark.parametrize("shells,pbc0,noise,precision,L", [
