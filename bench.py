@@ -105,7 +105,7 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------------------ CPU (oracle) timing
-def cpu_oracle_timing(L, min_seconds=10.0, max_steps=40, steps=None, warmup=1):
+def cpu_oracle_timing(L, min_seconds=10.0, max_steps=400, steps=None, warmup=1):
     """The reference's CPU algorithm on the same workload: returns (spin-steps/s, steps, threads, seconds)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
