@@ -454,6 +454,21 @@ def main(ref_root):
         fmr_cases[tag] = dict(model=model, L=list(L), pbc=[bool(x) for x in pbc], B=list(B), kw=kw)
     models["fmr"] = fmr_cases
 
+    # the Python-API tutorial of magex (docs/tutorials/07_python_api.md:18-26): write_model ->
+    # load_results -> SpinSystem -> LLGSolver.run (20,000 steps, rows every 200, 10 snapshots) -> Q
+    from magex.models import write_model as RWM
+    from magex.llg import LLGSolver as RLLG
+    p = os.path.join(tmp, "tutorial_tri.json")
+    RWM(p, lattice="triangular", J=[2.0], D=1.0, moment=3.0)
+    s = RS.SpinSystem(RS.load_results(p), supercell=(48, 48, 1), pbc=(True, True, False), field=(0, 0, 2.0))
+    e0 = s.init_spins("random", seed=1)
+    e, table, snaps = RLLG(s, alpha=0.5, dt=2e-3, temperature=0.0).run(e0.copy(), steps=20000, output_every=200,
+                                                                        snapshots=10)
+    out["tutorial/e"], out["tutorial/table"] = e, table
+    out["tutorial/snap_t"] = np.array([t for t, _ in snaps])
+    out["tutorial/snap5"] = snaps[5][1]
+    out["tutorial/Q"] = np.array(RT.topological_charge(s, e))
+
     # magex's own texture initialisers on a 40 x 40 triangular film (the charges of
     # tests/test_universal.py:81-91): one and two skyrmions, helicity 0 with vorticity +1 and -1
     s = RS.SpinSystem(ucs["tri"], (40, 40, 1), (1, 1, 0), (0, 0, 1.0))
