@@ -58,6 +58,8 @@ class Supercell:
     ``B`` / ``set_field``, ``mu``, ``A``, ``signs``, ``pinned``, ``site_T``, ``alpha_site``,
     ``positions``, ``sublattice``, ``init_spins``), with per-site arrays created lazily; per-site
     overrides (``A_site``, ``mu_site``, ``pinned``, ``site_T``, ``alpha_site``) may be assigned.
+    ``energy``, ``gradient`` and ``effective_field`` are evaluated on the GPU; ``order_parameter``
+    and ``magnetization`` on the host arrays, as magex computes them.
     """
 
     def __init__(self, uc: UnitCellModel, supercell=(10, 10, 10), pbc=(True, True, True),
@@ -190,6 +192,38 @@ class Supercell:
     def order_parameter(self, e):
         """|sum_i s_i e_i| / N on host spins (magex ``magex/spinmodel.py:517-519``)."""
         return float(np.linalg.norm((self.signs[:, None] * e).sum(0)) / self.N)
+
+    def magnetization(self, e, weighted=False):
+        """Mean spin, or the moment-weighted mean (magex/spinmodel.py:521-524)."""
+        e = np.asarray(e, float)
+        return (self.mu[:, None] * e).sum(0) / self.mu.sum() if weighted else e.mean(0)
+
+    # ------------------------------------------------------------------ energy terms, on the GPU
+    def device_model(self):
+        """The DeviceModel that ``energy`` / ``gradient`` / ``effective_field`` evaluate on, created
+        on first use with the couplings and per-site terms of that moment; the external field follows
+        ``set_field``."""
+        dm = getattr(self, "_device_model", None)
+        if dm is None:
+            from .device import DeviceModel
+            dm = self._device_model = DeviceModel(self)
+        return dm
+
+    def energy(self, e, per_spin=False):
+        """Total energy (meV) of spins e ((N, 3), magex order), as magex/spinmodel.py:475-484."""
+        dm = self.device_model()
+        E = float(dm.observables(dm.to_lattice(e))[0].item())
+        return E / self.N if per_spin else E
+
+    def effective_field(self, e):
+        """B_eff = -(dE/de) / (mu_B mu) in tesla, (N, 3) numpy (magex/spinmodel.py:471-473); zero
+        on pinned sites."""
+        dm = self.device_model()
+        return dm.from_lattice(dm.effective_field(dm.to_lattice(e))).cpu().numpy()
+
+    def gradient(self, e):
+        """dE/de (meV), (N, 3) numpy (magex/spinmodel.py:458-469)."""
+        return -MU_B * self.mu[:, None] * self.effective_field(e)
 
     # ------------------------------------------------------------------ host CSR (reference order)
     def neighbour_csr(self):

@@ -9,6 +9,7 @@ import pytest
 import torch
 
 from helpers import golden_supercell
+from magex_gb300.constants import MU_B
 
 pytestmark = pytest.mark.gpu
 
@@ -37,6 +38,12 @@ def test_trajectory_matches_reference(cuda, golden, golden_models, tag):
     B = sol.effective_field(e)
     ref_B = golden[f"{tag}/field"]
     assert np.abs(B - ref_B).max() <= 1e-12 * max(1.0, np.abs(ref_B).max())
+    # the same terms through the system object, as magex's SpinSystem methods
+    E = float(golden[f"{tag}/energy"])
+    assert abs(sc.energy(e) - E) <= 1e-12 * max(1.0, abs(E))
+    assert np.abs(sc.effective_field(e) - ref_B).max() <= 1e-12 * max(1.0, np.abs(ref_B).max())
+    ref_g = -MU_B * sc.mu[:, None] * ref_B
+    assert np.abs(sc.gradient(e) - ref_g).max() <= 1e-12 * max(1.0, np.abs(ref_g).max())
 
 
 def test_sc16_1000_steps_device_resident(cuda, golden, golden_models):
