@@ -51,7 +51,44 @@ def compress_tensors(tensors):
     return WIDTH_FULL, M.reshape(-1, 9).copy()
 
 
-class Supercell:
+class _SpinTerms:
+    """magex SpinSystem's energy terms for a lattice description (``N``, ``mu``): ``energy``,
+    ``gradient`` and ``effective_field`` evaluated on the GPU, ``magnetization`` on the host."""
+
+    def magnetization(self, e, weighted=False):
+        """Mean spin, or the moment-weighted mean (magex/spinmodel.py:521-524)."""
+        e = np.asarray(e, float)
+        return (self.mu[:, None] * e).sum(0) / self.mu.sum() if weighted else e.mean(0)
+
+    # ------------------------------------------------------------------ energy terms, on the GPU
+    def device_model(self):
+        """The DeviceModel that ``energy`` / ``gradient`` / ``effective_field`` evaluate on, created
+        on first use with the couplings and per-site terms of that moment; the external field follows
+        ``set_field``."""
+        dm = getattr(self, "_device_model", None)
+        if dm is None:
+            from .device import DeviceModel
+            dm = self._device_model = DeviceModel(self)
+        return dm
+
+    def energy(self, e, per_spin=False):
+        """Total energy (meV) of spins e ((N, 3), magex order), as magex/spinmodel.py:475-484."""
+        dm = self.device_model()
+        E = float(dm.observables(dm.to_lattice(e))[0].item())
+        return E / self.N if per_spin else E
+
+    def effective_field(self, e):
+        """B_eff = -(dE/de) / (mu_B mu) in tesla, (N, 3) numpy (magex/spinmodel.py:471-473); zero
+        on pinned sites."""
+        dm = self.device_model()
+        return dm.from_lattice(dm.effective_field(dm.to_lattice(e))).cpu().numpy()
+
+    def gradient(self, e):
+        """dE/de (meV), (N, 3) numpy (magex/spinmodel.py:458-469)."""
+        return -MU_B * self.mu[:, None] * self.effective_field(e)
+
+
+class Supercell(_SpinTerms):
     """Supercell of a UnitCellModel: the state the LLG kernels need, O(ns + couplings) in size.
 
     Mirrors the parts of magex ``SpinSystem`` that the LLG path reads (``N``, ``L``, ``pbc``,
@@ -193,38 +230,6 @@ class Supercell:
         """|sum_i s_i e_i| / N on host spins (magex ``magex/spinmodel.py:517-519``)."""
         return float(np.linalg.norm((self.signs[:, None] * e).sum(0)) / self.N)
 
-    def magnetization(self, e, weighted=False):
-        """Mean spin, or the moment-weighted mean (magex/spinmodel.py:521-524)."""
-        e = np.asarray(e, float)
-        return (self.mu[:, None] * e).sum(0) / self.mu.sum() if weighted else e.mean(0)
-
-    # ------------------------------------------------------------------ energy terms, on the GPU
-    def device_model(self):
-        """The DeviceModel that ``energy`` / ``gradient`` / ``effective_field`` evaluate on, created
-        on first use with the couplings and per-site terms of that moment; the external field follows
-        ``set_field``."""
-        dm = getattr(self, "_device_model", None)
-        if dm is None:
-            from .device import DeviceModel
-            dm = self._device_model = DeviceModel(self)
-        return dm
-
-    def energy(self, e, per_spin=False):
-        """Total energy (meV) of spins e ((N, 3), magex order), as magex/spinmodel.py:475-484."""
-        dm = self.device_model()
-        E = float(dm.observables(dm.to_lattice(e))[0].item())
-        return E / self.N if per_spin else E
-
-    def effective_field(self, e):
-        """B_eff = -(dE/de) / (mu_B mu) in tesla, (N, 3) numpy (magex/spinmodel.py:471-473); zero
-        on pinned sites."""
-        dm = self.device_model()
-        return dm.from_lattice(dm.effective_field(dm.to_lattice(e))).cpu().numpy()
-
-    def gradient(self, e):
-        """dE/de (meV), (N, 3) numpy (magex/spinmodel.py:458-469)."""
-        return -MU_B * self.mu[:, None] * self.effective_field(e)
-
     # ------------------------------------------------------------------ host CSR (reference order)
     def neighbour_csr(self):
         """Per-site neighbour list in magex site order: (ptr int64 (N+1), nbr int32, typ int32,
@@ -282,7 +287,7 @@ class Supercell:
                 f"B = {self.B.tolist()} T, mu_B = {MU_B}")
 
 
-class NeighbourList:
+class NeighbourList(_SpinTerms):
     """Arbitrary spin system as per-site neighbour lists (carved shapes, vacancies, edited exchange).
 
     Built from a 3N x 3N coupling matrix the way magex builds its kernel tables

@@ -192,6 +192,7 @@ def test_irregular_lattice_matches_reference(cuda, golden, golden_models, tag):
     assert np.abs(e - golden[f"{tag}/e{meta['steps']}"]).max() <= 1e-12 * meta["steps"]
     E = float(golden[f"{tag}/energy"])
     assert abs(sol.energy(e) - E) <= 1e-12 * abs(E)
+    assert abs(nl.energy(e) - E) <= 1e-12 * abs(E)
     assert abs(sol.max_torque(e) - float(golden[f"{tag}/torque"])) <= 1e-10 * max(1.0, float(golden[f"{tag}/torque"]))
 
 
