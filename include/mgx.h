@@ -144,6 +144,15 @@ int64_t mgx_model_nsites(const mgx_model* m);
  * parameters (magex rebuilds FastModel after editing couplings, magex/fast.py:631). */
 mgx_status mgx_model_set_couplings(mgx_model* m, const double* bond_table);
 mgx_status mgx_model_set_onsite(mgx_model* m, const double* A_sub);
+/* Cubic anisotropy E_i = Kc_i (a1^2 a2^2 + a2^2 a3^2 + a3^2 a1^2), a = C e_i (C: 3x3 axes, rows), and
+ * higher uniaxial anisotropy E_i = -K2_i (e_i.u)^4 - K3_i (e_i.u)^6: the Kc, C, K2, K3, u, has_c, has_u
+ * members of magex's kernel arguments (magex/fast.py:640-672, magex/terms.py:35-75, from
+ * magex/structure.py:188-193).  Host per-site arrays [N] in magex site order (NULL: term absent; K3
+ * NULL with K2: zeros); synchronous; call before creating plans.  The FP64 LLG step, the field and
+ * the observables include them; reduced forms, batched systems, the adjoint and Monte Carlo refuse
+ * such a model with MGX_ERR_UNSUPPORTED. */
+mgx_status mgx_model_set_onsite_higher(mgx_model* m, const double* Kc, const double* C, const double* K2,
+                                       const double* K3, const double* u);
 /* Slab decomposition of one supercell along axis 0 (the halo-exchange path of magex/mpi_spin.py:
  * 150-180): this model is a slab of the whole lattice.  In-kernel Philox counters use local cell +
  * cell_offset as the cell index of the whole lattice (so the noise equals the unsplit run's), and

@@ -120,6 +120,7 @@ SIGNATURES = {
     "mgx_batch_topological_charge": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_model_set_couplings": (C.c_int32, [C.c_void_p, _dp]),
     "mgx_model_set_onsite": (C.c_int32, [C.c_void_p, _dp]),
+    "mgx_model_set_onsite_higher": (C.c_int32, [C.c_void_p, _dp, _dp, _dp, _dp, _dp]),
     "mgx_adjoint_create": (C.c_int32, [C.c_void_p, C.c_void_p, _ip, _ip, C.c_int32, C.POINTER(LLGParams), C.c_int32,
                                        C.POINTER(C.c_void_p)]),
     "mgx_adjoint_destroy": (C.c_int32, [C.c_void_p]),

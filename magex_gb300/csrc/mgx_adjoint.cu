@@ -418,6 +418,8 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   *out = nullptr;
   if (F->d.layout != 0 || R->d.layout != 0)
     return set_error(MGX_ERR_UNSUPPORTED, "the adjoint is implemented for lattice stencils, not neighbour lists");
+  if (has_higher_onsite(F->d) || has_higher_onsite(R->d))
+    return set_error(MGX_ERR_UNSUPPORTED, "the adjoint does not include cubic / higher uniaxial anisotropy");
   if (F->d.width != 9 || R->d.width != 9)
     return set_error(MGX_ERR_INVALID, "the adjoint needs full-tensor (width 9) forward and reverse models");
   if (F->d.ns != R->d.ns || F->d.L0 != R->d.L0 || F->d.L1 != R->d.L1 || F->d.L2 != R->d.L2 ||

@@ -278,6 +278,9 @@ mgx_status mgx_batch_create(const mgx_model* const* models, const mgx_llg_params
   *out = nullptr;
   for (int k = 0; k < nsys; ++k) {
     if (!models[k]) return set_error(MGX_ERR_INVALID, "mgx_batch_create: model %d is null", k);
+    if (has_higher_onsite(reinterpret_cast<const Model*>(models[k])->d))
+      return set_error(MGX_ERR_UNSUPPORTED, "system %d: batched systems do not include cubic / higher uniaxial "
+                       "anisotropy", k);
     const mgx_llg_params& p = params[k];
     if (!(p.dt > 0.0)) return set_error(MGX_ERR_INVALID, "system %d: dt must be positive", k);
     if (p.alpha_site) return set_error(MGX_ERR_INVALID, "system %d: batched systems take a uniform alpha", k);

@@ -60,6 +60,14 @@ struct DevLattice {
   // the cell of the whole lattice; observables sum only cells with own0_begin <= c0 < own0_end
   long long cell_offset;
   int own0_begin, own0_end;
+  // cubic anisotropy E = Kc (a1^2 a2^2 + a2^2 a3^2 + a3^2 a1^2), a = C e (magex/terms.py:35-55), and
+  // higher uniaxial anisotropy E = -K2 (e.u)^4 - K3 (e.u)^6 (magex/terms.py:58-75): per-site
+  // constants in the lattice layout, nullptr when the model has none
+  const double* Kc_site;         // [N] or nullptr
+  const double* K2_site;         // [N] or nullptr (with K3_site)
+  const double* K3_site;         // [N]
+  double C[9];                   // cubic axes, rows
+  double u[3];                   // uniaxial axis (unit)
 };
 
 struct Model {
@@ -71,6 +79,7 @@ struct Model {
   double* inv_mu_site = nullptr;
   double* mu_site = nullptr;
   uint8_t* pinned = nullptr;
+  double* higher_site = nullptr; // Kc | K2 | K3 (lattice layout) of the higher on-site terms
   double* partials = nullptr;    // reduction scratch for observables
   int partial_cap = 0;           // number of 8-double slots
   int* slot_of_bond = nullptr;   // host [nbond]: position of input coupling b in the device table
@@ -319,6 +328,45 @@ __device__ __forceinline__ void effective_field(const DevLattice& L, const doubl
   bx = fma(fma(2.0, hx, -gx), inv, L.B0);
   by = fma(fma(2.0, hy, -gy), inv, L.B1);
   bz = fma(fma(2.0, hz, -gz), inv, L.B2);
+}
+
+inline bool has_higher_onsite(const DevLattice& L) { return L.Kc_site || L.K2_site; }
+
+// dE/de of the higher on-site terms at site q (magex/fast.py:39-64 order: cubic, then uniaxial)
+__device__ __forceinline__ void higher_onsite_grad(const DevLattice& L, long long q, double x, double y, double z,
+                                                   double& gx, double& gy, double& gz) {
+  gx = gy = gz = 0.0;
+  if (L.Kc_site) {
+    const double a1 = L.C[0] * x + L.C[1] * y + L.C[2] * z;
+    const double a2 = L.C[3] * x + L.C[4] * y + L.C[5] * z;
+    const double a3 = L.C[6] * x + L.C[7] * y + L.C[8] * z;
+    const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
+    const double kc = L.Kc_site[q];
+    const double d1 = 2.0 * a1 * (q2 + q3) * kc, d2 = 2.0 * a2 * (q1 + q3) * kc, d3 = 2.0 * a3 * (q1 + q2) * kc;
+    gx += d1 * L.C[0] + d2 * L.C[3] + d3 * L.C[6];
+    gy += d1 * L.C[1] + d2 * L.C[4] + d3 * L.C[7];
+    gz += d1 * L.C[2] + d2 * L.C[5] + d3 * L.C[8];
+  }
+  if (L.K2_site) {
+    const double c = x * L.u[0] + y * L.u[1] + z * L.u[2];
+    const double c2 = c * c;
+    const double f = -4.0 * L.K2_site[q] * c2 * c - 6.0 * L.K3_site[q] * c2 * c2 * c;
+    gx += f * L.u[0];
+    gy += f * L.u[1];
+    gz += f * L.u[2];
+  }
+}
+
+// B -= dE_higher/de / (mu mu_B) at site q of sublattice s
+__device__ __forceinline__ void add_higher_onsite(const DevLattice& L, long long q, int s, double x, double y,
+                                                  double z, double& bx, double& by, double& bz) {
+  if (!L.Kc_site && !L.K2_site) return;
+  double gx, gy, gz;
+  higher_onsite_grad(L, q, x, y, z, gx, gy, gz);
+  const double inv = L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s];
+  bx -= gx * inv;
+  by -= gy * inv;
+  bz -= gz * inv;
 }
 
 // LLG right-hand side f = pre [e x B + alpha e x (e x B)], pre = -gamma / (1 + alpha^2)

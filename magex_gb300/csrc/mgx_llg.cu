@@ -49,7 +49,7 @@ static void launch_step(const LLGPlan* pl, double* e, const double* noise, uint6
   const long long count = whole ? L.N : r.cn;
   const int tpb = site_block_size(whole ? L.N : r.cn * L.ns);
   const dim3 grid((unsigned)((count + tpb - 1) / tpb), whole ? 1u : (unsigned)L.ns);
-  if (pl->p.sot || pl->p.B_add) {
+  if (pl->p.sot || pl->p.B_add || has_higher_onsite(L)) {
     if (stages & 1) k_predict<W, NOISE, INTEG, true><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
     if (stages & 2) k_correct<W, NOISE, INTEG, true><<<grid, tpb, 0, st>>>(L, pl->p, e, noise, step, r.cb, count);
   } else {
@@ -229,6 +229,8 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
   if (p->precision < MGX_PRECISION_FP64 || p->precision > MGX_PRECISION_FP64_FIXED_GATHER)
     return set_error(MGX_ERR_INVALID, "precision %d is not fp64 (0), df32-gather (1), int48-gather (2) or "
                      "fp64-fixed-gather (3)", p->precision);
+  if (has_higher_onsite(m->d) && p->precision != MGX_PRECISION_FP64)
+    return set_error(MGX_ERR_UNSUPPORTED, "cubic / higher uniaxial anisotropy need the FP64 form (precision 0)");
   const int ns = m->d.ns;
   const long long N = m->d.N;
   LLGPlan* pl = new LLGPlan();

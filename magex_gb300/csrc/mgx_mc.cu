@@ -560,6 +560,8 @@ extern "C" mgx_status mgx_mc_create(const mgx_model* mm, const mgx_mc_params* p,
     return set_error(MGX_ERR_INVALID, "mgx_mc_create: move %d is not gaussian (0), uniform (1), heatbath (2) or "
                                       "hinzke (3)", p->move);
   if (p->overrelax < 0) return set_error(MGX_ERR_INVALID, "mgx_mc_create: overrelax must be >= 0");
+  if (has_higher_onsite(m->d))
+    return set_error(MGX_ERR_UNSUPPORTED, "mgx_mc_create: cubic / higher uniaxial anisotropy are not in the sweep");
   if (p->rng != MGX_MC_RNG_PHILOX && p->rng != MGX_MC_RNG_HOST)
     return set_error(MGX_ERR_INVALID, "mgx_mc_create: rng %d is not philox (0) or host (1)", p->rng);
   if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_FP64_FIXED_GATHER)

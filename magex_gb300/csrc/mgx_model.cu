@@ -378,6 +378,43 @@ mgx_status mgx_model_create_csr(const mgx_csr_desc* c, mgx_model** out) {
   return MGX_OK;
 }
 
+mgx_status mgx_model_set_onsite_higher(mgx_model* mm, const double* Kc, const double* C, const double* K2,
+                                       const double* K3, const double* u) {
+  Model* m = reinterpret_cast<Model*>(mm);
+  if (!m) return set_error(MGX_ERR_INVALID, "mgx_model_set_onsite_higher: null model");
+  if ((Kc && !C) || (K2 && !u))
+    return set_error(MGX_ERR_INVALID, "mgx_model_set_onsite_higher: Kc needs the cubic axes C, K2 the axis u");
+  DevLattice& d = m->d;
+  const long long N = d.N, ncell = d.ncell;
+  const int ns = d.ns;
+  cudaFree(m->higher_site);
+  m->higher_site = nullptr;
+  d.Kc_site = d.K2_site = d.K3_site = nullptr;
+  if (!Kc && !K2) return MGX_OK;
+  // magex site i = cell * ns + s  ->  lattice index s * ncell + cell
+  std::vector<double> h(3 * (size_t)N, 0.0);
+  for (long long i = 0; i < N; ++i) {
+    const long long q = (i % ns) * ncell + i / ns;
+    if (Kc) h[q] = Kc[i];
+    if (K2) {
+      h[N + q] = K2[i];
+      h[2 * N + q] = K3 ? K3[i] : 0.0;
+    }
+  }
+  MGX_CUDA_TRY(cudaMalloc(&m->higher_site, sizeof(double) * 3 * N));
+  MGX_CUDA_TRY(cudaMemcpy(m->higher_site, h.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice));
+  if (Kc) {
+    d.Kc_site = m->higher_site;
+    for (int k = 0; k < 9; ++k) d.C[k] = C[k];
+  }
+  if (K2) {
+    d.K2_site = m->higher_site + N;
+    d.K3_site = m->higher_site + 2 * N;
+    for (int k = 0; k < 3; ++k) d.u[k] = u[k];
+  }
+  return MGX_OK;
+}
+
 mgx_status mgx_model_destroy(mgx_model* mm) {
   Model* m = reinterpret_cast<Model*>(mm);
   if (!m) return MGX_OK;
@@ -389,6 +426,7 @@ mgx_status mgx_model_destroy(mgx_model* mm) {
   cudaFree(m->partials);
   cudaFree(m->csr_block);
   cudaFree(m->sign_site);
+  cudaFree(m->higher_site);
   delete[] m->slot_of_bond;
   delete m;
   return MGX_OK;

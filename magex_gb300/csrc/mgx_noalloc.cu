@@ -75,6 +75,8 @@ extern "C" mgx_status mgx_llg_step_noalloc(const mgx_model* mm, const mgx_llg_pa
                      "mgx_llg_step_noalloc: %lld sites exceed the fixed scratch of %lld sites "
                      "(MGX_NOALLOC_MAX_SITES); use mgx_llg_create / mgx_llg_step for larger models",
                      N, kNoallocMaxSites);
+  if (has_higher_onsite(m->d))
+    return set_error(MGX_ERR_UNSUPPORTED, "mgx_llg_step_noalloc: cubic / higher uniaxial anisotropy need a plan");
   if (p->alpha_site)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: per-site damping (alpha_site) needs a plan; "
                                       "pass a uniform alpha");

@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(256) k_field(const DevLattice L, const double*
   site_coords(L, q, s, c0, c1, c2);
   double bx, by, bz;
   effective_field<W>(L, e, q, s, c0, c1, c2, e[q], e[N + q], e[2 * N + q], bx, by, bz);
+  add_higher_onsite(L, q, s, e[q], e[N + q], e[2 * N + q], bx, by, bz);
   B[q] = bx; B[N + q] = by; B[2 * N + q] = bz;
 }
 

@@ -94,6 +94,7 @@ __device__ __forceinline__ void predict_site(const DevLattice& L, const DevLLG& 
   double bx, by, bz;
   effective_field<W>(L, e, q, s, c0, c1, c2, ex, ey, ez, bx, by, bz);
   if (EXTRA) {
+    add_higher_onsite(L, q, s, ex, ey, ez, bx, by, bz);
     add_sot(P, ex, ey, ez, bx, by, bz);
     add_extra(P, N, q, bx, by, bz);
   }
@@ -150,6 +151,7 @@ __device__ __forceinline__ void correct_site(const DevLattice& L, const DevLLG& 
   double bx, by, bz;
   effective_field<W>(L, P.ep, q, s, c0, c1, c2, px, py, pz, bx, by, bz);
   if (EXTRA) {
+    add_higher_onsite(L, q, s, px, py, pz, bx, by, bz);
     add_sot(P, px, py, pz, bx, by, bz);
     add_extra(P, N, q, bx, by, bz);
   }

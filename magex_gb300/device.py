@@ -50,10 +50,7 @@ def supercell_from_system(system):
                 v = getattr(system, name, None)
                 if v is not None:
                     setattr(sc, name, np.array(v))
-            sc.terms = list(getattr(system, "terms", []) or [])
-            if sc.terms:
-                raise NotImplementedError("extra energy terms (dipolar, cubic, higher uniaxial, quadruplets) "
-                                          "are not supported by the GB300 kernels")
+            _take_onsite_terms(sc, getattr(system, "terms", []))
             return sc
         A = np.asarray(system.A, float).reshape(sc.N, 3, 3)
         if not np.array_equal(A, np.tile(sc.A_sub, (sc.ncell, 1, 1))):
@@ -65,13 +62,30 @@ def supercell_from_system(system):
             v = getattr(system, name, None)
             if v is not None:
                 setattr(sc, name, np.array(v))
-        sc.terms = list(getattr(system, "terms", []) or [])
-    if sc.terms:
-        raise NotImplementedError("extra energy terms (dipolar, cubic, higher uniaxial, quadruplets) "
-                                  "are not supported by the GB300 kernels")
+        _take_onsite_terms(sc, getattr(system, "terms", []))
+    if getattr(sc, "terms", None):
+        raise NotImplementedError("extra energy terms (dipolar, quadruplets) are not supported by the GB300 kernels")
     if sc.has_higher:
         raise NotImplementedError("biquadratic / four-spin couplings are not supported by the GB300 kernels")
     return sc
+
+
+def _take_onsite_terms(sc, terms):
+    """The first cubic (Kc, C) and the first higher uniaxial (K2, K3, u) term of a magex system go to the
+    kernels, as magex/fast.py:647-652 splits them off; anything else (dipolar, quadruplets, a second
+    term of either kind) raises NotImplementedError, as magex/cuda_backend.py:315-316 does."""
+    rest = []
+    for t in terms or []:
+        kind = type(t).__name__
+        if kind == "CubicAnisotropy" and getattr(sc, "cubic", None) is None:
+            sc.cubic = (np.array(t.Kc, float), np.array(t.C, float))
+        elif kind == "UniaxialHigher" and getattr(sc, "uniaxial_higher", None) is None:
+            sc.uniaxial_higher = (np.array(t.K2, float), np.array(t.K3, float), np.array(t.u, float))
+        else:
+            rest.append(t)
+    sc.terms = []
+    if rest:
+        raise NotImplementedError("extra energy terms (dipolar, quadruplets) are not supported by the GB300 kernels")
 
 
 def _stencil_matches(sc, Jsp):
@@ -126,6 +140,7 @@ class DeviceModel:
         self._keep = []
         if isinstance(sc, NeighbourList):
             self._create_csr(sc)
+            self._set_higher_onsite(sc)
             return
         nb = len(sc.bond_src)
         if nb > _lib.MAX_BONDS:
@@ -155,6 +170,24 @@ class DeviceModel:
         self._obs = torch.empty(8, dtype=torch.float64, device=self.device)
         self._tri = None
         self.field_owner = None
+        self._set_higher_onsite(sc)
+
+    def _set_higher_onsite(self, sc):
+        """Cubic and higher uniaxial anisotropy of the lattice (mgx_model_set_onsite_higher)."""
+        cub, uni = getattr(sc, "cubic", None), getattr(sc, "uniaxial_higher", None)
+        if cub is None and uni is None:
+            return
+        N = sc.N
+        arr = lambda x, n: np.ascontiguousarray(np.broadcast_to(np.asarray(x, float), (n,)), np.float64)  # noqa: E731
+        Kc = Cm = K2 = K3 = u = None
+        if cub is not None:
+            Kc, Cm = arr(cub[0], N), np.ascontiguousarray(np.asarray(cub[1], float).reshape(9))
+        if uni is not None:
+            K2, K3, u = arr(uni[0], N), arr(uni[1], N), np.ascontiguousarray(np.asarray(uni[2], float).reshape(3))
+        p = lambda a: None if a is None else _lib.dptr(a)                                              # noqa: E731
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.mgx_model_set_onsite_higher(self.handle, p(Kc), p(Cm), p(K2), p(K3), p(u)),
+                       "mgx_model_set_onsite_higher")
 
     def _create_csr(self, sc):
         c = _lib.CSRDesc()

@@ -53,7 +53,14 @@ def compress_tensors(tensors):
 
 class _SpinTerms:
     """magex SpinSystem's energy terms for a lattice description (``N``, ``mu``): ``energy``,
-    ``gradient`` and ``effective_field`` evaluated on the GPU, ``magnetization`` on the host."""
+    ``gradient`` and ``effective_field`` evaluated on the GPU, ``magnetization`` on the host.
+
+    ``cubic = (Kc, C)`` (per-site Kc, 3x3 axes) and ``uniaxial_higher = (K2, K3, u)`` (per-site K2, K3,
+    axis) are the cubic and higher uniaxial anisotropies of magex/terms.py:35-75 (None: absent).
+    """
+
+    cubic = None
+    uniaxial_higher = None
 
     def magnetization(self, e, weighted=False):
         """Mean spin, or the moment-weighted mean (magex/spinmodel.py:521-524)."""

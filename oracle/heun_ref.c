@@ -44,6 +44,13 @@ typedef struct oracle_model {
   const double* mu;       /* N */
   double B[3];
   const uint8_t* pinned;  /* N or NULL */
+  /* cubic anisotropy Kc (N or NULL) with axes C (rows), higher uniaxial K2, K3 (N or NULL) along u:
+   * the Kc, C, K2, K3, u, has_c, has_u kernel arguments of magex/fast.py:640-672 */
+  const double* Kc;
+  double C[9];
+  const double* K2;
+  const double* K3;
+  double u[3];
 } oracle_model;
 
 static void hfield(const oracle_model* m, int64_t i, const double* e, double* h) {
@@ -81,11 +88,53 @@ static void onsite_grad(const oracle_model* m, int64_t i, const double* v, doubl
   g[2] = 2.0 * (A[6] * v[0] + A[7] * v[1] + A[8] * v[2]);
 }
 
+/* adds dE/de of the cubic and higher uniaxial terms (magex/fast.py:50-63, magex/terms.py:45-49,65-67) */
+static void higher_grad(const oracle_model* m, int64_t i, const double* v, double* g) {
+  if (m->Kc) {
+    const double* C = m->C;
+    const double a1 = C[0] * v[0] + C[1] * v[1] + C[2] * v[2];
+    const double a2 = C[3] * v[0] + C[4] * v[1] + C[5] * v[2];
+    const double a3 = C[6] * v[0] + C[7] * v[1] + C[8] * v[2];
+    const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
+    const double d1 = 2 * a1 * (q2 + q3) * m->Kc[i], d2 = 2 * a2 * (q1 + q3) * m->Kc[i],
+                 d3 = 2 * a3 * (q1 + q2) * m->Kc[i];
+    g[0] += d1 * C[0] + d2 * C[3] + d3 * C[6];
+    g[1] += d1 * C[1] + d2 * C[4] + d3 * C[7];
+    g[2] += d1 * C[2] + d2 * C[5] + d3 * C[8];
+  }
+  if (m->K2) {
+    const double c = v[0] * m->u[0] + v[1] * m->u[1] + v[2] * m->u[2];
+    const double f = -4.0 * m->K2[i] * c * c * c - 6.0 * m->K3[i] * c * c * c * c * c;
+    g[0] += f * m->u[0];
+    g[1] += f * m->u[1];
+    g[2] += f * m->u[2];
+  }
+}
+
+/* energy of the cubic and higher uniaxial terms at site i (magex/terms.py:41-43,61-63) */
+static double higher_energy(const oracle_model* m, int64_t i, const double* v) {
+  double E = 0.0;
+  if (m->Kc) {
+    const double* C = m->C;
+    const double a1 = C[0] * v[0] + C[1] * v[1] + C[2] * v[2];
+    const double a2 = C[3] * v[0] + C[4] * v[1] + C[5] * v[2];
+    const double a3 = C[6] * v[0] + C[7] * v[1] + C[8] * v[2];
+    const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
+    E += m->Kc[i] * (q1 * q2 + q2 * q3 + q3 * q1);
+  }
+  if (m->K2) {
+    const double c = v[0] * m->u[0] + v[1] * m->u[1] + v[2] * m->u[2];
+    E += -m->K2[i] * c * c * c * c - m->K3[i] * c * c * c * c * c * c;
+  }
+  return E;
+}
+
 /* B_eff of site i for spins e (T) */
 static void bloc(const oracle_model* m, int64_t i, const double* e, double* B) {
   double h[3], g[3];
   hfield(m, i, e, h);
   onsite_grad(m, i, e + 3 * i, g);
+  higher_grad(m, i, e + 3 * i, g);
   const double inv = 1.0 / (m->mu[i] * MU_B);
   B[0] = (2 * h[0] - g[0]) * inv + m->B[0];
   B[1] = (2 * h[1] - g[1]) * inv + m->B[1];
@@ -241,7 +290,8 @@ void oracle_observables(const oracle_model* m, const double* e, const double* si
     hfield(m, i, e, h);
     onsite_grad(m, i, v, g);
     E += 0.5 * (v[0] * g[0] + v[1] * g[1] + v[2] * g[2]) - (v[0] * h[0] + v[1] * h[1] + v[2] * h[2]) -
-         MU_B * m->mu[i] * (v[0] * m->B[0] + v[1] * m->B[1] + v[2] * m->B[2]);
+         MU_B * m->mu[i] * (v[0] * m->B[0] + v[1] * m->B[1] + v[2] * m->B[2]) + higher_energy(m, i, v);
+    higher_grad(m, i, v, g);
     mx += v[0];
     my += v[1];
     mz += v[2];

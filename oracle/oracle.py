@@ -35,7 +35,8 @@ _dp = C.POINTER(C.c_double)
 class _Model(C.Structure):
     _fields_ = [("N", C.c_int64), ("ptr", C.POINTER(C.c_int64)), ("nbr", C.POINTER(C.c_int32)),
                 ("typ", C.POINTER(C.c_int32)), ("table", _dp), ("width", C.c_int32), ("A", _dp), ("mu", _dp),
-                ("B", C.c_double * 3), ("pinned", C.POINTER(C.c_uint8))]
+                ("B", C.c_double * 3), ("pinned", C.POINTER(C.c_uint8)),
+                ("Kc", _dp), ("C", C.c_double * 9), ("K2", _dp), ("K3", _dp), ("u", C.c_double * 3)]
 
 
 _lib = None
@@ -141,6 +142,16 @@ class OracleLLG:
         m.mu = _p(self._arrays["mu"])
         m.B[:] = [float(x) for x in sc.B]
         m.pinned = _p(pin, C.POINTER(C.c_uint8))
+        cub, uni = getattr(sc, "cubic", None), getattr(sc, "uniaxial_higher", None)
+        if cub is not None:
+            self._arrays["Kc"] = np.ascontiguousarray(np.broadcast_to(np.asarray(cub[0], float), (N,)))
+            m.Kc = _p(self._arrays["Kc"])
+            m.C[:] = [float(x) for x in np.asarray(cub[1], float).reshape(9)]
+        if uni is not None:
+            self._arrays["K2"] = np.ascontiguousarray(np.broadcast_to(np.asarray(uni[0], float), (N,)))
+            self._arrays["K3"] = np.ascontiguousarray(np.broadcast_to(np.asarray(uni[1], float), (N,)))
+            m.K2, m.K3 = _p(self._arrays["K2"]), _p(self._arrays["K3"])
+            m.u[:] = [float(x) for x in np.asarray(uni[2], float).reshape(3)]
         self._m = m
         a = getattr(sc, "alpha_site", None)
         al = np.asarray(a if (a is not None and np.isscalar(alpha)) else alpha, float)

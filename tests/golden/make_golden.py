@@ -132,6 +132,13 @@ def main(ref_root):
               temperature_profile=dict(axis="x", T0=5.0, T1=30.0))
     traj("sc_structure", ucs["sc_dmi"], (6, 6, 4), (1, 1, 1), (0, 0, 0.5), 0.1, 1e-3, 10.0, 6, 10, {10},
          structure=st)
+    # cubic and higher uniaxial anisotropy (magex/terms.py:35-75, added by magex/structure.py:163-193)
+    c30, s30 = float(np.cos(np.pi / 6)), float(np.sin(np.pi / 6))
+    traj("sc_cubic", ucs["sc_dmi"], (5, 5, 4), (1, 1, 1), (0.1, 0, 0.3), 0.1, 1e-3, 0.0, 3, 20, {1, 20},
+         structure=dict(materials=[dict(name="bulk", Kc=0.3, K2=0.2, K3=0.1, K_axis=[1, 1, 1])]), run_every=5)
+    traj("tri_cubic_thermal", ucs["tri"], (6, 6, 1), (1, 1, 0), (0, 0, 0.5), 0.2, 1e-3, 5.0, 4, 20, {20},
+         integrator="depondt", structure=dict(materials=[dict(
+             name="bulk", Kc=-0.2, cubic_axes=[[c30, -s30, 0.0], [s30, c30, 0.0], [0.0, 0.0, 1.0]], K2=0.1)]))
     # arbitrary lattices (per-site neighbour lists): a carved sphere with vacancies, and two materials
     # with interface exchange scaling; the reference's coupling matrix and per-site arrays are stored
     def irregular(tag, uc, L, pbc, B, structure, alpha, dt, T, seed, steps):

@@ -12,6 +12,7 @@ def golden_supercell(golden_models, tag):
         "sc16": "sc", "sc6_thermal": "sc_dmi", "bcc2_thermal": "bcc2", "bcc2_T0": "bcc2", "bcc2_shell4": "bcc2_shell4",
         "tri16": "tri", "sc_depondt": "sc_dmi", "tri_depondt_thermal": "tri", "sc_open": "sc_open",
         "sc_tiny_fold": "sc_two_shell", "sc_afm": "sc_afm", "honeycomb": "honeycomb_bulk", "sc_structure": "sc_dmi",
+        "sc_cubic": "sc_dmi", "tri_cubic_thermal": "tri",
     }[tag]
     uc = load_results(golden_models[model_name]["model"])
     sc = Supercell(uc, meta["L"], meta["pbc"], meta["B"])
@@ -25,6 +26,13 @@ def apply_structure_subset(sc, st):
     one bulk material with alpha and T (:172-179), a pinned bottom layer with a direction (:198-207)
     and a linear temperature profile along x that fills sites without a material T (:208-225)."""
     for m in st.get("materials", []):
+        if "Kc" in m:                     # magex/structure.py:163-165,190-191 (one material covers every site)
+            axes = m.get("cubic_axes")
+            sc.cubic = (np.full(sc.N, float(m["Kc"])), np.eye(3) if axes is None else np.asarray(axes, float))
+        if "K2" in m or "K3" in m:        # magex/structure.py:166-169,192-193 and magex/terms.py:59-63
+            u = np.asarray(m.get("K_axis", (0, 0, 1)), float)
+            sc.uniaxial_higher = (np.full(sc.N, float(m.get("K2", 0.0))), np.full(sc.N, float(m.get("K3", 0.0))),
+                                  u / np.linalg.norm(u))
         if "alpha" in m:
             sc.alpha_site = np.full(sc.N, float(m["alpha"]))
         if "T" in m:

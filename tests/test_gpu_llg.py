@@ -14,7 +14,7 @@ from magex_gb300.constants import MU_B
 pytestmark = pytest.mark.gpu
 
 TRAJ = ["sc16", "sc6_thermal", "bcc2_thermal", "bcc2_T0", "bcc2_shell4", "tri16", "sc_depondt", "tri_depondt_thermal",
-        "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb", "sc_structure"]
+        "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb", "sc_structure", "sc_cubic", "tri_cubic_thermal"]
 
 
 def _solver(golden_models, tag, noise="host"):
@@ -538,3 +538,20 @@ def test_new_entry_points_reject_bad_arguments(cuda, golden_models):
                                          _lib.dptr(np.array([0.5, 0.5]))), "mgx_mc_set_chains")
     with pytest.raises(ValueError):
         _lib.check(lib.mgx_mc_chain_counts(mc.handle, C.c_void_p(0), None, None, 0, None), "mgx_mc_chain_counts")
+
+
+def test_higher_onsite_terms_outside_the_fp64_step_are_refused(cuda, golden_models):
+    """Cubic / higher uniaxial anisotropy are in the FP64 step, field and observables only; the forms
+    that do not evaluate them refuse such a model instead of dropping the terms."""
+    from magex_gb300.batched import BatchedLLG
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.mc import MetropolisMC
+    sc, _ = golden_supercell(golden_models, "sc_cubic")
+    GB300LLG(sc, 0.1, 1e-3)
+    for precision in ("df32", "int48", "fp64_fixed"):
+        with pytest.raises(NotImplementedError):
+            GB300LLG(sc, 0.1, 1e-3, precision=precision)
+    with pytest.raises(NotImplementedError):
+        BatchedLLG([sc], 0.1, 1e-3, [0.0], [1])
+    with pytest.raises(NotImplementedError):
+        MetropolisMC(sc, 10.0, 1)

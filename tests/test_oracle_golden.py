@@ -11,7 +11,7 @@ from helpers import golden_supercell
 from oracle import OracleLLG
 
 TRAJ = ["sc16", "sc6_thermal", "bcc2_thermal", "bcc2_T0", "bcc2_shell4", "tri16", "sc_depondt", "tri_depondt_thermal",
-        "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb", "sc_structure"]
+        "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb", "sc_structure", "sc_cubic", "tri_cubic_thermal"]
 
 
 def _oracle(golden_models, tag, csr="blocks"):
