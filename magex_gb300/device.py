@@ -31,9 +31,10 @@ def supercell_from_system(system):
     The coupling stencil is rebuilt from ``system.uc`` and checked against ``system.Jsp`` so that a
     system whose exchange was edited after construction (carving, interface scaling) is refused
     instead of being integrated with the wrong couplings.  Per-site single-ion tensors, moments,
-    pinning, site temperatures and damping set by ``magex.structure`` are carried over.  Terms the
-    kernels do not implement (biquadratic, four-spin, dipolar, cubic / higher uniaxial, quadruplets)
-    raise NotImplementedError, as ``magex/cuda_backend.py:315-316`` does.
+    pinning, site temperatures and damping set by ``magex.structure`` are carried over, and so are the
+    first cubic and higher uniaxial anisotropy terms (the on-site terms of magex's fused kernels).  Terms
+    the kernels do not implement (biquadratic, four-spin, dipolar, quadruplets) raise
+    NotImplementedError, as ``magex/cuda_backend.py:315-316`` does.
     """
     if isinstance(system, (Supercell, NeighbourList)):
         sc = system
