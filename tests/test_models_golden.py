@@ -88,3 +88,33 @@ def test_init_spins_matches_reference(golden, golden_models):
         sc, meta = golden_supercell(golden_models, tag)
         e0 = sc.init_spins("random", seed=meta["init_seed"])
         assert np.array_equal(e0, golden[f"{tag}/e0"]), tag
+
+
+def test_onsite_terms_of_a_magex_system_are_carried(golden_models):
+    """The first cubic and the first higher-uniaxial term of a magex system go to the kernels (as
+    magex/fast.py:647-652 splits them off); other terms are refused."""
+    import numpy as np
+    import pytest
+    from magex_gb300.device import _take_onsite_terms
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.spinmodel import load_results
+
+    class CubicAnisotropy:
+        def __init__(self, Kc, C):
+            self.Kc, self.C = Kc, C
+
+    class UniaxialHigher:
+        def __init__(self, K2, K3, u):
+            self.K2, self.K3, self.u = K2, K3, u
+
+    class Dipolar:
+        pass
+
+    sc = Supercell(load_results(golden_models["sc"]["model"]), (2, 2, 2))
+    Kc = np.linspace(0.1, 0.8, sc.N)
+    _take_onsite_terms(sc, [CubicAnisotropy(Kc, np.eye(3)), UniaxialHigher(np.ones(sc.N), np.zeros(sc.N), [0, 0, 1.0])])
+    assert np.array_equal(sc.cubic[0], Kc) and np.array_equal(sc.cubic[1], np.eye(3))
+    assert np.array_equal(sc.uniaxial_higher[2], [0, 0, 1.0]) and sc.terms == []
+    sc2 = Supercell(load_results(golden_models["sc"]["model"]), (2, 2, 2))
+    with pytest.raises(NotImplementedError):
+        _take_onsite_terms(sc2, [Dipolar()])
