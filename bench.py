@@ -608,6 +608,31 @@ def bench_callers(L=128, fmr_steps=20000, relax_L=64, cpu_steps=400):
     return out
 
 
+def bench_onsite_higher(L=128, steps=50):
+    """The headline step with magex's cubic (Kc = 0.02 meV, axes along x, y, z) and higher uniaxial
+    (K2 = 0.01, K3 = 0.005 meV along z) anisotropy on every site: the EXTRA kernels that evaluate them
+    beside the plain ones, on the same two-site bcc L^3 lattice."""
+    import torch
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=L, field=FIELD)
+    sc.cubic = (np.full(sc.N, 0.02), np.eye(3))
+    sc.uniaxial_higher = (np.full(sc.N, 0.01), np.full(sc.N, 0.005), np.array([0.0, 0.0, 1.0]))
+    sol = GB300LLG(sc, ALPHA, DT, TEMP, 3)
+    lat = sol.model.to_lattice(sc.init_spins("random", seed=1))
+    sol.run_lattice(lat, 3)
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    sol.run_lattice(lat, steps)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / steps
+    return {"workload": f"two-site bcc {L}^3 ({sc.N:,} spins) with cubic and higher uniaxial anisotropy on every site",
+            "value": sc.N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": steps}
+
+
 def bench_config1(steps=1000, cpu=True):
     """Plain FP64 workload of the reference's CPU-runnable case: simple-cubic 16^3 (4,096 spins), 6
     neighbours, J = 1 meV, mu = 2 mu_B, alpha 0.1, B = 0, T = 0, dt 0.1 fs, 1000 Heun steps from
@@ -822,6 +847,7 @@ def run_gb300(args):
         line["sqw_projection"] = bench_sqw(L=args.L)
         line["topological_charge"] = bench_texture()
         line["callers"] = bench_callers()
+        line["onsite_higher"] = bench_onsite_higher()
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -843,7 +869,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-ensemble measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint / forward timing")
     ap.add_argument("--only", choices=["adjoint", "batched", "df32", "int48", "fp64_fixed", "config1", "config5", "mc",
-                                       "sqw", "texture", "callers"],
+                                       "sqw", "texture", "callers", "onsite_higher"],
                     default=None,
                     help="run only one of the secondary measurements and print its JSON (for profiling)")
     ap.add_argument("--adjoint-steps", type=int, default=None)
@@ -868,6 +894,8 @@ def main():
             out = bench_texture()
         elif args.only == "callers":
             out = bench_callers()
+        elif args.only == "onsite_higher":
+            out = bench_onsite_higher()
         elif args.only == "mc":
             out = [bench_mc(L=args.L, sweeps=min(args.steps, 100), cpu_baseline=False, precision=p)
                    for p in ("fp64", "fp64_fixed")]
