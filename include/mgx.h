@@ -149,8 +149,8 @@ mgx_status mgx_model_set_onsite(mgx_model* m, const double* A_sub);
  * members of magex's kernel arguments (magex/fast.py:640-672, magex/terms.py:35-75, from
  * magex/structure.py:188-193).  Host per-site arrays [N] in magex site order (NULL: term absent; K3
  * NULL with K2: zeros); synchronous; call before creating plans.  The FP64 LLG step, the field and
- * the observables include them; reduced forms, batched systems, the adjoint and Monte Carlo refuse
- * such a model with MGX_ERR_UNSUPPORTED. */
+ * the observables and the Monte Carlo sweep include them; the reduced LLG forms, batched systems and
+ * the adjoint refuse such a model with MGX_ERR_UNSUPPORTED. */
 mgx_status mgx_model_set_onsite_higher(mgx_model* m, const double* Kc, const double* C, const double* K2,
                                        const double* K3, const double* u);
 /* Slab decomposition of one supercell along axis 0 (the halo-exchange path of magex/mpi_spin.py:

@@ -332,6 +332,22 @@ __device__ __forceinline__ void effective_field(const DevLattice& L, const doubl
 
 inline bool has_higher_onsite(const DevLattice& L) { return L.Kc_site || L.K2_site; }
 
+// energies of the cubic and the higher uniaxial term at site q (magex/terms.py:41-43,61-63)
+__device__ __forceinline__ double cubic_energy(const DevLattice& L, long long q, double x, double y, double z) {
+  const double a1 = L.C[0] * x + L.C[1] * y + L.C[2] * z;
+  const double a2 = L.C[3] * x + L.C[4] * y + L.C[5] * z;
+  const double a3 = L.C[6] * x + L.C[7] * y + L.C[8] * z;
+  const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
+  return L.Kc_site[q] * (q1 * q2 + q2 * q3 + q3 * q1);
+}
+
+__device__ __forceinline__ double uniaxial_higher_energy(const DevLattice& L, long long q, double x, double y,
+                                                         double z) {
+  const double c = x * L.u[0] + y * L.u[1] + z * L.u[2];
+  const double c2 = c * c;
+  return -L.K2_site[q] * c2 * c2 - L.K3_site[q] * c2 * c2 * c2;
+}
+
 // dE/de of the higher on-site terms at site q (magex/fast.py:39-64 order: cubic, then uniaxial)
 __device__ __forceinline__ void higher_onsite_grad(const DevLattice& L, long long q, double x, double y, double z,
                                                    double& gx, double& gy, double& gz) {

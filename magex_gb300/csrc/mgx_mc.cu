@@ -333,6 +333,8 @@ __global__ void __launch_bounds__(128) k_mc_pass(const DevLattice L, double* __r
     const double dx = nx - ox, dy = ny - oy, dz = nz - oz;
     double dE = -2.0 * (dx * hx + dy * hy + dz * hz) - kMuB * mu * (dx * L.B0 + dy * L.B1 + dz * L.B2);
     if (L.has_A) dE += onsite(L, q, s, nx, ny, nz) - onsite(L, q, s, ox, oy, oz);
+    if (L.Kc_site) dE += cubic_energy(L, q, nx, ny, nz) - cubic_energy(L, q, ox, oy, oz);
+    if (L.K2_site) dE += uniaxial_higher_energy(L, q, nx, ny, nz) - uniaxial_higher_energy(L, q, ox, oy, oz);
     dE += extra;
     const double thr = (MOVE == MC_OVERRELAX) ? 1e-12 : 0.0;
     ok = dE <= thr;
@@ -560,8 +562,6 @@ extern "C" mgx_status mgx_mc_create(const mgx_model* mm, const mgx_mc_params* p,
     return set_error(MGX_ERR_INVALID, "mgx_mc_create: move %d is not gaussian (0), uniform (1), heatbath (2) or "
                                       "hinzke (3)", p->move);
   if (p->overrelax < 0) return set_error(MGX_ERR_INVALID, "mgx_mc_create: overrelax must be >= 0");
-  if (has_higher_onsite(m->d))
-    return set_error(MGX_ERR_UNSUPPORTED, "mgx_mc_create: cubic / higher uniaxial anisotropy are not in the sweep");
   if (p->rng != MGX_MC_RNG_PHILOX && p->rng != MGX_MC_RNG_HOST)
     return set_error(MGX_ERR_INVALID, "mgx_mc_create: rng %d is not philox (0) or host (1)", p->rng);
   if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_FP64_FIXED_GATHER)

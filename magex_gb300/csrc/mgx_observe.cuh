@@ -59,18 +59,8 @@ __device__ __forceinline__ void observe_site(const DevLattice& L, const double* 
   const double eB = ex * L.B0 + ey * L.B1 + ez * L.B2;
   v[0] = eAe - eh - 5.7883818060e-2 * mu * eB;
   double Ghx = 0.0, Ghy = 0.0, Ghz = 0.0;       // higher on-site terms (magex/terms.py:41-43,66-68)
-  if (L.Kc_site) {
-    const double a1 = L.C[0] * ex + L.C[1] * ey + L.C[2] * ez;
-    const double a2 = L.C[3] * ex + L.C[4] * ey + L.C[5] * ez;
-    const double a3 = L.C[6] * ex + L.C[7] * ey + L.C[8] * ez;
-    const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
-    v[0] += L.Kc_site[q] * (q1 * q2 + q2 * q3 + q3 * q1);
-  }
-  if (L.K2_site) {
-    const double c = ex * L.u[0] + ey * L.u[1] + ez * L.u[2];
-    const double c2 = c * c;
-    v[0] -= L.K2_site[q] * c2 * c2 + L.K3_site[q] * c2 * c2 * c2;
-  }
+  if (L.Kc_site) v[0] += cubic_energy(L, q, ex, ey, ez);
+  if (L.K2_site) v[0] += uniaxial_higher_energy(L, q, ex, ey, ez);
   if (L.Kc_site || L.K2_site) higher_onsite_grad(L, q, ex, ey, ez, Ghx, Ghy, Ghz);
   v[1] = ex;
   v[2] = ey;

@@ -111,22 +111,23 @@ static void higher_grad(const oracle_model* m, int64_t i, const double* v, doubl
   }
 }
 
-/* energy of the cubic and higher uniaxial terms at site i (magex/terms.py:41-43,61-63) */
+/* energies of the cubic and the higher uniaxial term at site i (magex/terms.py:41-43,61-63) */
+static double cubic_energy(const oracle_model* m, int64_t i, const double* v) {
+  const double* C = m->C;
+  const double a1 = C[0] * v[0] + C[1] * v[1] + C[2] * v[2];
+  const double a2 = C[3] * v[0] + C[4] * v[1] + C[5] * v[2];
+  const double a3 = C[6] * v[0] + C[7] * v[1] + C[8] * v[2];
+  const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
+  return m->Kc[i] * (q1 * q2 + q2 * q3 + q3 * q1);
+}
+
+static double uniaxial_energy(const oracle_model* m, int64_t i, const double* v) {
+  const double c = v[0] * m->u[0] + v[1] * m->u[1] + v[2] * m->u[2];
+  return -m->K2[i] * c * c * c * c - m->K3[i] * c * c * c * c * c * c;
+}
+
 static double higher_energy(const oracle_model* m, int64_t i, const double* v) {
-  double E = 0.0;
-  if (m->Kc) {
-    const double* C = m->C;
-    const double a1 = C[0] * v[0] + C[1] * v[1] + C[2] * v[2];
-    const double a2 = C[3] * v[0] + C[4] * v[1] + C[5] * v[2];
-    const double a3 = C[6] * v[0] + C[7] * v[1] + C[8] * v[2];
-    const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
-    E += m->Kc[i] * (q1 * q2 + q2 * q3 + q3 * q1);
-  }
-  if (m->K2) {
-    const double c = v[0] * m->u[0] + v[1] * m->u[1] + v[2] * m->u[2];
-    E += -m->K2[i] * c * c * c * c - m->K3[i] * c * c * c * c * c * c;
-  }
-  return E;
+  return (m->Kc ? cubic_energy(m, i, v) : 0.0) + (m->K2 ? uniaxial_energy(m, i, v) : 0.0);
 }
 
 /* B_eff of site i for spins e (T) */
@@ -580,6 +581,8 @@ int64_t oracle_mc_group(const oracle_model* m, const int64_t* idx, int64_t n, in
     double dE = -2.0 * (d[0] * h[0] + d[1] * h[1] + d[2] * h[2]) -
                 MU_B * mu * (d[0] * m->B[0] + d[1] * m->B[1] + d[2] * m->B[2]);
     if (m->A) dE += eAe(m, i, v) - eAe(m, i, eo);
+    if (m->Kc) dE += cubic_energy(m, i, v) - cubic_energy(m, i, eo);      /* magex/montecarlo.py:136-137 */
+    if (m->K2) dE += uniaxial_energy(m, i, v) - uniaxial_energy(m, i, eo);
     dE += extra;
     int ok = dE <= (move == 4 ? 1e-12 : 0.0);
     if (!ok) {

@@ -299,6 +299,10 @@ def main(ref_root):
             structure=st)
     mc_traj("bcc2_shell4", ucs["bcc2_shell4"], (3, 3, 3), (1, 1, 1), (0.0, 0.0, 0.2), 150.0, 10, "gaussian", 1,
             0.3, 3, 8)
+    mc_traj("cubic", ucs["sc_dmi"], (4, 4, 4), (1, 1, 1), (0.0, 0.1, 0.3), 8.0, 12, "gaussian", 1, 0.6, 4, 10,
+            structure=dict(materials=[dict(name="bulk", Kc=0.4, K2=0.3, K3=0.1, K_axis=[0, 1, 1])]))
+    mc_traj("cubic_heatbath", ucs["sc_dmi"], (4, 4, 4), (1, 1, 1), (0.0, 0.1, 0.3), 8.0, 13, "heatbath", 1, 0.6, 4,
+            11, structure=dict(materials=[dict(name="bulk", Kc=-0.3)]))
     # carved sphere with vacancies (neighbour lists): the structure of the sc_sphere LLG case
     mc_traj("sphere", ucs["sc_dmi"], (9, 9, 9), (0, 0, 0), (0.1, 0.0, 0.4), 6.0, 11, "gaussian", 1, 0.6, 3, 9,
             structure=dict(shape="sphere", size=11.0, vacancies=dict(fraction=0.1, seed=3)))

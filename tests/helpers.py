@@ -97,7 +97,8 @@ def assert_within_3_sigma(golden, key, mean, sem):
 
 
 UC_OF = {"gauss_dmi": "sc_dmi", "uniform_sc": "sc", "heatbath_tri": "tri", "hinzke_bcc2": "bcc2",
-         "T0_afm": "sc_afm", "open_kagome": "kagome", "structure": "sc_dmi", "bcc2_shell4": "bcc2_shell4"}
+         "T0_afm": "sc_afm", "open_kagome": "kagome", "structure": "sc_dmi", "bcc2_shell4": "bcc2_shell4",
+         "cubic": "sc_dmi", "cubic_heatbath": "sc_dmi"}
 MC_TAGS = list(UC_OF) + ["sphere"]
 
 

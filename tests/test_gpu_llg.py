@@ -541,11 +541,10 @@ def test_new_entry_points_reject_bad_arguments(cuda, golden_models):
 
 
 def test_higher_onsite_terms_outside_the_fp64_step_are_refused(cuda, golden_models):
-    """Cubic / higher uniaxial anisotropy are in the FP64 step, field and observables only; the forms
-    that do not evaluate them refuse such a model instead of dropping the terms."""
+    """Cubic / higher uniaxial anisotropy are in the FP64 step, field, observables and Monte Carlo
+    sweep; the forms that do not evaluate them refuse such a model instead of dropping the terms."""
     from magex_gb300.batched import BatchedLLG
     from magex_gb300.llg import GB300LLG
-    from magex_gb300.mc import MetropolisMC
     sc, _ = golden_supercell(golden_models, "sc_cubic")
     GB300LLG(sc, 0.1, 1e-3)
     for precision in ("df32", "int48", "fp64_fixed"):
@@ -553,5 +552,3 @@ def test_higher_onsite_terms_outside_the_fp64_step_are_refused(cuda, golden_mode
             GB300LLG(sc, 0.1, 1e-3, precision=precision)
     with pytest.raises(NotImplementedError):
         BatchedLLG([sc], 0.1, 1e-3, [0.0], [1])
-    with pytest.raises(NotImplementedError):
-        MetropolisMC(sc, 10.0, 1)
