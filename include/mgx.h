@@ -284,16 +284,20 @@ mgx_status mgx_adjoint_grads(mgx_adjoint* a, double* out, void* stream);
 /* ---------------------------------------------------------------- step without allocation
  * No counterpart in the reference.  One Heun / Depondt step like mgx_llg_step, for callers that
  * cannot allocate GPU memory while they step: a host framework that owns all device memory through
- * its own pool and only hands the plugin its input and output buffers, a loop captured into a CUDA
- * graph in global capture mode (where cudaMalloc is not allowed), or a real-time loop that must not
- * wait on the allocator.  It needs no plan: the predictor scratch (ep, k1) and the per-sublattice
- * constants live in one static device array of 64 + 6 * MGX_NOALLOC_MAX_SITES doubles (12 MiB) that
- * every GPU loading the library holds until the process exits; the call itself allocates nothing.
+ * its own pool and only hands the plugin its input and output buffers, or a real-time loop that must
+ * never wait on the allocator.  It needs no plan: the predictor scratch (ep, k1) and the
+ * per-sublattice constants live in one static device array of 64 + 6 * MGX_NOALLOC_MAX_SITES doubles
+ * (12 MiB) that every GPU loading the library holds until the process exits; the call itself
+ * allocates nothing.
  *   - m: a model from mgx_model_create (created beforehand) with at most MGX_NOALLOC_MAX_SITES sites;
- *     larger models are rejected with MGX_ERR_INVALID.
- *   - p: dt, uniform alpha (p->alpha_site must be NULL), precession, integrator, noise mode, seed.
- *   - sigma_sub: host [ns] thermal amplitudes (read during the call), required unless p->noise is
- *     MGX_NOISE_NONE; e, noise and step as for mgx_llg_step.
+ *     larger models are rejected with MGX_ERR_INVALID.  Cubic and higher uniaxial on-site terms of
+ *     the model are stepped as in mgx_llg_step.
+ *   - p: dt (finite, > 0), uniform alpha (finite, >= 0; p->alpha_site must be NULL), precession,
+ *     integrator, noise mode, seed; p->precision must be MGX_PRECISION_FP64.
+ *   - sigma_sub: host [ns] thermal amplitudes (finite, >= 0; read during the call), required unless
+ *     p->noise is MGX_NOISE_NONE; e, noise and step as for mgx_llg_step.  A model whose moments differ
+ *     site by site has per-site amplitudes, which only a plan carries: with noise it is rejected
+ *     with MGX_ERR_UNSUPPORTED.
  * The first call on a device looks up the array's device address (cudaGetSymbolAddress, with that
  * device current); make that first call before any stream capture begins.  All calls on a device
  * share the array, which keeps the last call's contents: calls whose GPU work overlaps (other

@@ -1,22 +1,25 @@
 // mgx_llg_step_noalloc: the stochastic Heun step without any device allocation.
 //
 // Why it exists: some callers of this library cannot allocate GPU memory when they step the spins.
-// A host framework that owns every byte of the device through its own pool allocator (and hands a
-// plugin only the input and output buffers), a solver loop that runs while a CUDA graph is being
-// captured in global mode (where cudaMalloc is not permitted), or a real-time driver that must not
-// block on the allocator all need a step that only reads its inputs and writes its outputs.
-// mgx_llg_step needs a plan from mgx_llg_create, which allocates the predictor scratch
-// (ep and k1, 6 doubles per site) with cudaMalloc; this entry point keeps that scratch in one
-// file-scope device array instead, allocated by the CUDA runtime when the library's device code is
-// loaded on a GPU and held until the process exits.
+// A host framework that owns every byte of the device through its own pool allocator and hands a
+// plugin only the input and output buffers, or a real-time driver loop that must never block on
+// the allocator, needs a step that only reads its inputs and writes its outputs.  mgx_llg_step
+// needs a plan from mgx_llg_create, which allocates the predictor scratch (ep and k1, 6 doubles per
+// site) with cudaMalloc; this entry point keeps that scratch in one file-scope device array
+// instead, allocated by the CUDA runtime when the library's device code is loaded on a GPU and held
+// until the process exits.
 //
 // Rules for callers (also in include/mgx.h):
 //   - at most MGX_NOALLOC_MAX_SITES sites; larger models are rejected with MGX_ERR_INVALID;
 //   - uniform damping only (params->alpha_site must be NULL);
+//   - thermal noise only with one moment per sublattice: a model whose moments differ site by site
+//     (per-site mu from a structure edit) needs per-site amplitudes, which only a plan carries, and
+//     is rejected with MGX_ERR_UNSUPPORTED unless the noise mode is none;
 //   - every call on a device shares the same array: calls whose work overlaps on that GPU (other
 //     streams, other host threads) race and must be serialised by the caller;
 //   - the first call on a device looks the array's device address up with cudaGetSymbolAddress
 //     (with that device current); make that first call before any stream capture begins.
+#include <cmath>
 #include <mutex>
 
 #include "mgx_internal.cuh"
@@ -75,14 +78,14 @@ extern "C" mgx_status mgx_llg_step_noalloc(const mgx_model* mm, const mgx_llg_pa
                      "mgx_llg_step_noalloc: %lld sites exceed the fixed scratch of %lld sites "
                      "(MGX_NOALLOC_MAX_SITES); use mgx_llg_create / mgx_llg_step for larger models",
                      N, kNoallocMaxSites);
-  if (has_higher_onsite(m->d))
-    return set_error(MGX_ERR_UNSUPPORTED, "mgx_llg_step_noalloc: cubic / higher uniaxial anisotropy need a plan");
   if (p->alpha_site)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: per-site damping (alpha_site) needs a plan; "
                                       "pass a uniform alpha");
   if (p->precision != MGX_PRECISION_FP64)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: only the FP64 gather (precision 0) is available");
-  if (!(p->dt > 0.0)) return set_error(MGX_ERR_INVALID, "dt must be a positive number");
+  if (!(p->dt > 0.0) || !std::isfinite(p->dt)) return set_error(MGX_ERR_INVALID, "dt must be a positive number");
+  if (!std::isfinite(p->alpha) || p->alpha < 0.0)
+    return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: alpha must be finite and >= 0");
   if (p->integrator != MGX_INTEGRATOR_HEUN && p->integrator != MGX_INTEGRATOR_DEPONDT)
     return set_error(MGX_ERR_INVALID, "integrator %d is not heun (0) or depondt (1)", p->integrator);
   if (p->noise < MGX_NOISE_NONE || p->noise > MGX_NOISE_PHILOX)
@@ -91,6 +94,14 @@ extern "C" mgx_status mgx_llg_step_noalloc(const mgx_model* mm, const mgx_llg_pa
     return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: host-noise mode needs a noise buffer");
   if (p->noise != MGX_NOISE_NONE && !sigma_sub)
     return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: thermal noise needs sigma_sub");
+  if (p->noise != MGX_NOISE_NONE && m->d.inv_mu_site)
+    return set_error(MGX_ERR_UNSUPPORTED,
+                     "mgx_llg_step_noalloc: the model's moments differ site by site, so the thermal amplitude "
+                     "does too; per-site amplitudes need a plan (mgx_llg_create + mgx_llg_set_sigma)");
+  if (p->noise != MGX_NOISE_NONE)
+    for (int s = 0; s < ns; ++s)
+      if (!std::isfinite(sigma_sub[s]) || sigma_sub[s] < 0.0)
+        return set_error(MGX_ERR_INVALID, "mgx_llg_step_noalloc: sigma_sub must be finite and >= 0");
 
   double* base = nullptr;
   mgx_status st = scratch_address(&base);

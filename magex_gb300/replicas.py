@@ -3,9 +3,9 @@
 The LLG step of one lattice needs no communication; an ensemble of independent systems (replicas,
 temperature / field scans, uneven films) is split across ranks by system, each rank steps its share
 with its own BatchedLLG, and only the per-system observables are gathered at the end.  This is the
-GPU analogue of magex running one process per temperature or per replica; the slab decomposition of
-one lattice with a halo exchange per stage (magex/mpi_spin.py:160-174) is not needed on one-GPU
-boxes and is left to ``mgx_llg_stage`` callers.
+GPU analogue of magex running one process per temperature or per replica.  One lattice too large
+for one GPU is split into slabs with a halo exchange per Heun stage instead (magex/mpi_spin.py:160-174):
+that path is ``magex_gb300.slab``.
 
 All functions work with any torch.distributed backend (nccl on GPUs, gloo on CPU) or without one.
 """

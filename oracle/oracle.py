@@ -25,6 +25,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
+# the same source built at -O3 with host-CPU tuning: only the CPU-baseline timing loads it
+LIB_TUNED = os.path.join(HERE, "liboracle_tuned.so")
 MU_B = 5.7883818060e-2
 K_B = 8.617333262e-2
 GAMMA = 0.1760859630
@@ -43,39 +45,60 @@ _lib = None
 
 
 def build(force=False):
-    """Compile liboracle.so with the Makefile next to this file (gcc, OpenMP)."""
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "heun_ref.c")):
+    """Compile liboracle.so and liboracle_tuned.so with the Makefile next to this file (gcc, OpenMP)."""
+    src = os.path.getmtime(os.path.join(HERE, "heun_ref.c"))
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < src for p in (LIB, LIB_TUNED)):
         r = subprocess.run(["make", "-C", HERE, "-B" if force else "all"], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
-def load():
-    global _lib
+def tuned_flags():
+    """Compiler flags of liboracle_tuned.so (recorded by the Makefile when it built the library)."""
+    build()
+    with open(os.path.join(HERE, "liboracle_tuned.flags")) as f:
+        return f.read().strip()
+
+
+_lib_tuned = None
+
+
+def load(tuned=False):
+    """The parity oracle (liboracle.so), or with tuned=True its -O3 host-tuned build for timing."""
+    global _lib, _lib_tuned
+    if tuned:
+        if _lib_tuned is None:
+            build()
+            _lib_tuned = _bind(C.CDLL(LIB_TUNED))
+        return _lib_tuned
     if _lib is None:
         build()
-        lib = C.CDLL(LIB)
-        lib.oracle_step.argtypes = [C.POINTER(_Model), _dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
-        lib.oracle_step.restype = None
-        lib.oracle_stage.argtypes = [C.POINTER(_Model), _dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int,
-                                     C.c_int]
-        lib.oracle_stage.restype = None
-        lib.oracle_observables.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, C.c_int]
-        lib.oracle_observables.restype = None
-        lib.oracle_gauss3.argtypes = [_dp, C.POINTER(C.c_uint64), C.c_int, _dp, C.POINTER(C.c_uint8), C.c_int64, C.c_int]
-        lib.oracle_gauss3.restype = None
-        lib.oracle_max_threads.restype = C.c_int
-        ip = C.POINTER(C.c_int32)
-        lib.oracle_stencil_csr.argtypes = [C.c_int, ip, ip, C.c_int, ip, ip, ip, ip, C.POINTER(C.c_int64), ip, ip]
-        lib.oracle_stencil_csr.restype = C.c_int64
-        lib.oracle_greedy_colour.argtypes = [C.c_int64, C.POINTER(C.c_int64), ip, ip]
-        lib.oracle_greedy_colour.restype = C.c_int32
-        lib.oracle_mc_group.argtypes = [C.POINTER(_Model), C.POINTER(C.c_int64), C.c_int64, C.c_int, _dp, C.c_double,
-                                        _dp, _dp, C.c_int]
-        lib.oracle_mc_group.restype = C.c_int64
-        _lib = lib
+        _lib = _bind(C.CDLL(LIB))
     return _lib
+
+
+def _bind(lib):
+    """Argument and result types of the oracle's exported functions."""
+    lib.oracle_step.argtypes = [C.POINTER(_Model), _dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
+    lib.oracle_step.restype = None
+    lib.oracle_stage.argtypes = [C.POINTER(_Model), _dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int,
+                                 C.c_int]
+    lib.oracle_stage.restype = None
+    lib.oracle_observables.argtypes = [C.POINTER(_Model), _dp, _dp, _dp, C.c_int]
+    lib.oracle_observables.restype = None
+    lib.oracle_gauss3.argtypes = [_dp, C.POINTER(C.c_uint64), C.c_int, _dp, C.POINTER(C.c_uint8), C.c_int64, C.c_int]
+    lib.oracle_gauss3.restype = None
+    lib.oracle_max_threads.restype = C.c_int
+    ip = C.POINTER(C.c_int32)
+    lib.oracle_stencil_csr.argtypes = [C.c_int, ip, ip, C.c_int, ip, ip, ip, ip, C.POINTER(C.c_int64), ip, ip]
+    lib.oracle_stencil_csr.restype = C.c_int64
+    lib.oracle_greedy_colour.argtypes = [C.c_int64, C.POINTER(C.c_int64), ip, ip]
+    lib.oracle_greedy_colour.restype = C.c_int32
+    lib.oracle_mc_group.argtypes = [C.POINTER(_Model), C.POINTER(C.c_int64), C.c_int64, C.c_int, _dp, C.c_double,
+                                    _dp, _dp, C.c_int]
+    lib.oracle_mc_group.restype = C.c_int64
+    return lib
 
 
 def max_threads():
@@ -115,8 +138,8 @@ class OracleLLG:
     """
 
     def __init__(self, sc, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
-                 integrator="heun", noise="host", threads=0, csr="blocks"):
-        self.lib = load()
+                 integrator="heun", noise="host", threads=0, csr="blocks", tuned=False):
+        self.lib = load(tuned)
         self.sc = sc
         N = sc.N
         if csr == "blocks":

@@ -9,6 +9,13 @@ It imports magex from that tree and writes, next to this file:
   llg_golden.npz   LLGSolver trajectories (NumPy Heun / Depondt path, the reference's own stream of
                    thermal noise), observables, run() tables and topological charges
 
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/magex --thermal-bcc2
+
+writes only thermal_bcc2.npz: the equilibrium statistics of magex's own Langevin run of the
+benchmark Hamiltonian (two-site bcc, full 3x3 tensors with DMI, SIA, B_z = 0.5 T, 300 K) at 8^3
+cells (about 4 minutes on one core);  --adversarial writes only adversarial.npz: T = 0
+trajectories of models whose couplings span eight decades in one stencil, in a 100 T field.
+
 The fixtures are inputs and outputs of the reference, not data of any public benchmark; every model
 is a seeded synthetic lattice.  numpy / scipy versions are recorded in the npz.
 """
@@ -497,5 +504,106 @@ def main(ref_root):
     print("wrote", os.path.join(HERE, "llg_golden.npz"), os.path.join(HERE, "models.json"))
 
 
+def thermal_bcc2(ref_root):
+    """Equilibrium statistics of the benchmark Hamiltonian from magex's own Langevin run.
+
+    Two-site bcc 8^3 (1,024 spins), shells 8+6+12 with per-bond full 3x3 tensors (isotropic
+    20/10/-1 meV, 1 % symmetric anisotropic part, DMI |D| = 1 meV), SIA K = 0.01 meV along z,
+    B = (0, 0, 0.5) T, T = 300 K, alpha 0.05, dt 0.1 fs: LLGSolver (NumPy Heun, noise
+    default_rng(seed).normal per step, magex/llg.py:106-122,216-227) from the ferromagnetic state,
+    `equil` steps discarded, then E/N (magex/spinmodel.py:475-484) and |M| = |mean e| sampled every
+    `every` steps over `sample` steps.  20 block means give each mean and its standard error; the
+    block length (10,000 steps) is several times the autocorrelation time of |M| (about 1,600 steps
+    at this size and temperature)."""
+    sys.path.insert(0, ref_root)
+    import scipy
+    from magex import spinmodel as RS
+    from magex.llg import LLGSolver
+    from magex_gb300.workloads import bcc_two_site_model
+
+    th = dict(L=8, alpha=0.05, dt=1e-4, T=300.0, Bz=0.5, seed=31, equil=20000, sample=200000, every=20,
+              model="bcc2", model_kwargs=dict(J=[20.0, 10.0, -1.0], seed=0))
+    tmp = tempfile.mkdtemp()
+    path = os.path.join(tmp, "bcc2.json")
+    with open(path, "w") as f:
+        json.dump(bcc_two_site_model(J=(20.0, 10.0, -1.0), seed=0), f)
+    s = RS.SpinSystem(RS.load_results(path), (th["L"],) * 3, (1, 1, 1), (0.0, 0.0, th["Bz"]))
+    sol = LLGSolver(s, alpha=th["alpha"], dt=th["dt"], temperature=th["T"], seed=th["seed"])
+    e = s.init_spins("ferro")
+    for _ in range(th["equil"]):
+        e = sol.step(e)
+    Es, Ms = [], []
+    for k in range(th["sample"]):
+        e = sol.step(e)
+        if k % th["every"] == th["every"] - 1:
+            Es.append(s.energy(e, per_spin=True))
+            Ms.append(np.linalg.norm(e.mean(0)))
+    out = {"numpy_version": np.array(np.__version__), "scipy_version": np.array(scipy.__version__),
+           "params": np.array(json.dumps(th)), "E_series": np.array(Es), "M_series": np.array(Ms)}
+    for key, x in (("E", np.array(Es)), ("M", np.array(Ms))):
+        blocks = x.reshape(20, -1).mean(1)
+        out[f"{key}_mean"] = np.array(blocks.mean())
+        out[f"{key}_sem"] = np.array(blocks.std(ddof=1) / np.sqrt(20))
+    np.savez_compressed(os.path.join(HERE, "thermal_bcc2.npz"), **out)
+    print("wrote", os.path.join(HERE, "thermal_bcc2.npz"), {k: float(out[k]) for k in ("E_mean", "E_sem", "M_mean",
+                                                                                          "M_sem")})
+
+
+def adversarial(ref_root):
+    """T = 0 trajectories of models built to stress a fixed-point exchange sum (adversarial.npz).
+
+    sc_decades: simple cubic 6^3 with three shells J = 100, 1e-3 and 1e-6 meV (eight decades in one
+    stencil), nearest-neighbour DMI 5 meV and an anisotropic part of 1e-2 meV, a near-zero single-ion
+    constant K = 1e-9 meV, |B| = 100 T along an oblique axis.  bcc2_decades: two-site bcc 4^3, four
+    shells 20 / 10 / -1 / 1e-6 meV with per-shell full tensors (1 % anisotropic, DMI 5 %), K = 1e-10
+    meV, the same 100 T field.  magex's LLGSolver (NumPy Heun, magex/llg.py:216-227), alpha 0.1,
+    dt 0.1 fs, 1000 steps from random spins; spins kept after 1, 10, 100 and 1000 steps, final
+    energy and effective field."""
+    sys.path.insert(0, ref_root)
+    import scipy
+    from magex import models as RM
+    from magex import spinmodel as RS
+    from magex.llg import LLGSolver
+    from magex_gb300.workloads import bcc_two_site_model
+
+    B = 100.0 * np.array([0.3, -0.6, 0.75]) / np.linalg.norm([0.3, -0.6, 0.75])
+    cases = {
+        "sc_decades": (RM.make_model(lattice="sc", J=[100.0, 1e-3, 1e-6], D=5.0,
+                                     Jani=[[1e-2, 0, 0], [0, -2e-2, 0], [0, 0, 1e-2]], K=1e-9, moment=2.0),
+                       (6, 6, 6)),
+        "bcc2_decades": (bcc_two_site_model(J=(20.0, 10.0, -1.0, 1e-6), dmi_frac=0.05, per="shell", K=1e-10, seed=5),
+                         (4, 4, 4)),
+    }
+    tmp = tempfile.mkdtemp()
+    out = {"numpy_version": np.array(np.__version__), "scipy_version": np.array(scipy.__version__)}
+    meta = {}
+    keep = (1, 10, 100, 1000)
+    for tag, (d, L) in cases.items():
+        path = os.path.join(tmp, tag + ".json")
+        with open(path, "w") as f:
+            json.dump(d, f)
+        s = RS.SpinSystem(RS.load_results(path), L, (1, 1, 1), tuple(B))
+        e = s.init_spins("random", seed=11)
+        sol = LLGSolver(s, 0.1, 1e-4, 0.0, 1)
+        out[f"{tag}/e0"] = e.copy()
+        for n in range(1, keep[-1] + 1):
+            e = sol.step(e)
+            if n in keep:
+                out[f"{tag}/e{n}"] = e.copy()
+        out[f"{tag}/energy"] = np.array(s.energy(e))
+        out[f"{tag}/field"] = s.effective_field(e)
+        meta[tag] = dict(model=d, L=list(L), B=list(map(float, B)), alpha=0.1, dt=1e-4, keep=list(keep))
+    out["meta"] = np.array(json.dumps(meta))
+    np.savez_compressed(os.path.join(HERE, "adversarial.npz"), **out)
+    print("wrote", os.path.join(HERE, "adversarial.npz"))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--thermal-bcc2" in sys.argv:
+        thermal_bcc2(root)
+    elif "--adversarial" in sys.argv:
+        adversarial(root)
+    else:
+        main(root)

@@ -138,3 +138,43 @@ def test_oracle_mc_sweeps_match_reference(golden, golden_models, tag):
         mc.sweep(e)
         assert np.abs(e - golden[f"mc/{tag}/e{k}"]).max() <= 1e-12, (tag, k)
         assert (mc.accepted, mc.tried) == tuple(int(x) for x in counts[k - 1])
+
+
+@pytest.mark.parametrize("tag", ["sc_decades", "bcc2_decades"])
+def test_oracle_adversarial_trajectory(tag):
+    """The adversarial T = 0 fixtures (couplings over eight decades in one stencil, |B| = 100 T, a
+    near-zero single-ion term; make_golden.py --adversarial): the oracle follows magex's trajectory
+    to 1e-12 per step over 1000 steps, so the fixture is a sound target for the fixed-point sum."""
+    import json
+    import os
+    from magex_gb300.lattice import Supercell
+    from magex_gb300.spinmodel import load_results
+    adv = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "adversarial.npz"))
+    meta = json.loads(str(adv["meta"]))[tag]
+    sc = Supercell(load_results(meta["model"]), tuple(meta["L"]), (True, True, True), tuple(meta["B"]))
+    ora = OracleLLG(sc, meta["alpha"], meta["dt"], 0.0, 1, csr="stencil", threads=1)
+    e = adv[f"{tag}/e0"].copy()
+    for n in range(1, meta["keep"][-1] + 1):
+        ora.step_inplace(e)
+        if n in meta["keep"]:
+            err = np.abs(e - adv[f"{tag}/e{n}"]).max()
+            assert err <= 1e-12 * n, (tag, n, err)
+    E = float(adv[f"{tag}/energy"])
+    assert abs(ora.observables(e)[0] - E) <= 1e-12 * abs(E)
+
+
+def test_config2_thermal_fixture_is_consistent():
+    """The reference's config-2 Langevin statistics (make_golden.py --thermal-bcc2): the stored means
+    and standard errors are the 20-block statistics of the stored series, and the run is in the
+    ordered phase it was chosen for (|M| ~ 0.9 at 300 K, well below T_c)."""
+    import json
+    import os
+    from helpers import block_stats
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "thermal_bcc2.npz"))
+    th = json.loads(str(ref["params"]))
+    assert len(ref["E_series"]) == th["sample"] // th["every"]
+    for key in ("E", "M"):
+        m, s = block_stats(ref[f"{key}_series"])
+        assert abs(m - float(ref[f"{key}_mean"])) <= 1e-12 * abs(m)
+        assert abs(s - float(ref[f"{key}_sem"])) <= 1e-9 * s
+    assert 0.85 < float(ref["M_mean"]) < 0.97

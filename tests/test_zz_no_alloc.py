@@ -1,11 +1,12 @@
 """mgx_llg_step_noalloc: the Heun step for callers that cannot allocate GPU memory.
 
-Such callers (a framework that owns all device memory through its own pool, a step loop being
-captured into a CUDA graph in global mode, a real-time loop) get a step whose scratch lives in a
-fixed static device array.  These tests call it through the C ABI and compare it with the planned
-entry point (mgx_llg_create + mgx_llg_step, via GB300LLG) on the same spins and the same noise, for
-two calls in a row, to the 1e-12 tolerance of the other GPU tests.  The file is named so that pytest
-collects it last.
+Such callers (a framework that owns all device memory through its own pool and hands a plugin only
+its input and output buffers, a real-time loop that must not wait on the allocator) get a step whose
+scratch lives in a fixed static device array.  These tests call it through the C ABI and compare it
+with the planned entry point (mgx_llg_create + mgx_llg_step, via GB300LLG) on the same spins and the
+same noise, and with the reference's own trajectories (golden fixtures made by running magex), for
+two or more calls in a row, to the 1e-12 per-step tolerance of the other GPU tests.  The file is named
+so that pytest collects it last.
 """
 import ctypes as C
 
@@ -64,14 +65,20 @@ def test_noalloc_matches_planned_step_host_noise(cuda):
     _noalloc_step(model, params, sigma, lat, noise[0], 0)
     out1 = model.from_lattice(lat).cpu().numpy()
     assert np.abs(out1 - ref1).max() <= 1e-12
+    # after the first call (which loads the module and looks the array up), further calls change
+    # neither the device's free memory nor anything held by torch's caching allocator
+    spare = lat.clone()
     torch.cuda.synchronize()
     free_before = torch.cuda.mem_get_info()[0]
+    torch_before = (torch.cuda.memory_allocated(), torch.cuda.memory_reserved())
+    _noalloc_step(model, params, sigma, spare, noise[1], 1)
     _noalloc_step(model, params, sigma, lat, noise[1], 1)
     torch.cuda.synchronize()
-    free_after = torch.cuda.mem_get_info()[0]
+    assert torch.cuda.mem_get_info()[0] == free_before, "the no-allocation step changed the free device memory"
+    assert (torch.cuda.memory_allocated(), torch.cuda.memory_reserved()) == torch_before
     out2 = model.from_lattice(lat).cpu().numpy()
     assert np.abs(out2 - ref2).max() <= 1e-12
-    assert free_after == free_before, "the no-allocation step changed the free device memory"
+    assert torch.equal(spare, lat)
 
 
 def test_noalloc_matches_planned_step_philox(cuda):
@@ -111,3 +118,87 @@ def test_noalloc_rejects_oversized_and_per_site_damping(cuda):
     lat = torch.zeros((3, small.N), dtype=torch.float64, device=small.device)
     with pytest.raises(ValueError, match="alpha_site"):
         _noalloc_step(small, p, None, lat, None, 0)
+
+
+def test_noalloc_follows_reference_trajectory_host_noise(cuda, golden, golden_models):
+    """Pinned to the reference directly: the config-2 Hamiltonian (two-site bcc 4^3, full tensors +
+    DMI + SIA, B_z = 0.5 T, 300 K) stepped with the reference's own noise stream
+    (default_rng(seed).normal per step, magex/llg.py:106-122) through 20 consecutive calls equals
+    magex's LLGSolver trajectory after 1 and 20 steps."""
+    from helpers import golden_supercell
+    from magex_gb300 import _lib
+    from magex_gb300.device import DeviceModel
+    from magex_gb300.constants import GAMMA, K_B, MU_B
+    sc, meta = golden_supercell(golden_models, "bcc2_thermal")
+    model = DeviceModel(sc)
+    rng = np.random.default_rng(meta["seed"])
+    lat = model.to_lattice(golden["bcc2_thermal/e0"])
+    params = _params(_lib.NOISE_HOST, 0, alpha=meta["alpha"])
+    params.dt = meta["dt"]
+    sigma = np.ascontiguousarray(np.sqrt(2.0 * meta["alpha"] * K_B * meta["T"] / (GAMMA * sc.mu_sub * MU_B * meta["dt"])))
+    for n in range(1, meta["steps"] + 1):
+        noise = model.to_lattice(rng.normal(size=(sc.N, 3)))
+        _noalloc_step(model, params, sigma, lat, noise, n - 1)
+        if n in meta["keep"]:
+            got = model.from_lattice(lat).cpu().numpy()
+            assert np.abs(got - golden[f"bcc2_thermal/e{n}"]).max() <= 1e-12 * n, n
+
+
+@pytest.mark.parametrize("tag", ["sc_cubic", "tri_cubic_thermal"])
+def test_noalloc_higher_onsite_terms_follow_reference(cuda, golden, golden_models, tag):
+    """Cubic (Kc, rotated axes) and higher uniaxial (K2, K3) anisotropy are stepped as in the planned
+    step: the reference's trajectories (Heun at T = 0; Depondt at 5 K with its noise stream)."""
+    from helpers import golden_supercell
+    from magex_gb300 import _lib
+    from magex_gb300.device import DeviceModel
+    from magex_gb300.constants import GAMMA, K_B, MU_B
+    sc, meta = golden_supercell(golden_models, tag)
+    model = DeviceModel(sc)
+    thermal = meta["T"] > 0
+    rng = np.random.default_rng(meta["seed"])
+    lat = model.to_lattice(golden[f"{tag}/e0"])
+    params = _params(_lib.NOISE_HOST if thermal else _lib.NOISE_NONE, 0, alpha=meta["alpha"])
+    params.dt = meta["dt"]
+    params.integrator = _lib.DEPONDT if meta["integrator"] == "depondt" else _lib.HEUN
+    sigma = np.ascontiguousarray(np.sqrt(2.0 * meta["alpha"] * K_B * meta["T"] / (GAMMA * sc.mu_sub * MU_B * meta["dt"])))
+    for n in range(1, meta["steps"] + 1):
+        noise = model.to_lattice(rng.normal(size=(sc.N, 3))) if thermal else None
+        _noalloc_step(model, params, sigma if thermal else None, lat, noise, n - 1)
+        if n in meta["keep"]:
+            got = model.from_lattice(lat).cpu().numpy()
+            assert np.abs(got - golden[f"{tag}/e{n}"]).max() <= 1e-12 * n, (tag, n)
+
+
+def test_noalloc_rejects_per_site_moments_with_noise_and_bad_numbers(cuda):
+    """A model whose moments differ site by site has per-site thermal amplitudes, which the
+    per-sublattice sigma_sub cannot carry: refused with noise, stepped without.  Non-finite dt,
+    negative or non-finite alpha and bad amplitudes are refused as by the planned path."""
+    from magex_gb300 import _lib
+    from magex_gb300.device import DeviceModel
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=4)
+    sc.mu_site = sc.mu * (1.0 + 0.1 * np.random.default_rng(3).random(sc.N))
+    model = DeviceModel(sc)
+    e0 = sc.init_spins("random", seed=2)
+    lat = model.to_lattice(e0)
+    sigma = _sigma_sub(sc)
+    with pytest.raises(NotImplementedError, match="moments differ"):
+        _noalloc_step(model, _params(_lib.NOISE_PHILOX, 1), sigma, lat, None, 0)
+    # without noise the per-site moments enter the field as in the planned step
+    planned = GB300LLG(sc, ALPHA, DT, 0.0, seed=1)
+    ref = planned.step(planned.step(e0))
+    for k in range(2):
+        _noalloc_step(model, _params(_lib.NOISE_NONE, 0), None, lat, None, k)
+    assert np.abs(model.from_lattice(lat).cpu().numpy() - ref).max() <= 1e-12
+    small = DeviceModel(bcc_two_site(L=4))
+    lat = small.to_lattice(e0)
+    for bad in (float("nan"), float("inf"), -1.0):
+        p = _params(_lib.NOISE_NONE, 0)
+        p.dt = bad
+        with pytest.raises(ValueError, match="dt"):
+            _noalloc_step(small, p, None, lat, None, 0)
+        with pytest.raises(ValueError, match="alpha"):
+            _noalloc_step(small, _params(_lib.NOISE_NONE, 0, alpha=bad), None, lat, None, 0)
+        with pytest.raises(ValueError, match="sigma_sub"):
+            _noalloc_step(small, _params(_lib.NOISE_PHILOX, 1), np.full(2, bad), lat, None, 0)
