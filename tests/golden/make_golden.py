@@ -13,7 +13,7 @@ It imports magex from that tree and writes, next to this file:
 
 writes only thermal_bcc2.npz: the equilibrium statistics of magex's own Langevin run of the
 benchmark Hamiltonian (two-site bcc, full 3x3 tensors with DMI, SIA, B_z = 0.5 T, 300 K) at 8^3
-cells (about 4 minutes on one core);  --adversarial writes only adversarial.npz: T = 0
+cells (eight runs in parallel processes, about 5 minutes on 8 cores);  --adversarial writes only adversarial.npz: T = 0
 trajectories of models whose couplings span eight decades in one stencil, in a 100 T field.
 
 The fixtures are inputs and outputs of the reference, not data of any public benchmark; every model
@@ -504,31 +504,19 @@ def main(ref_root):
     print("wrote", os.path.join(HERE, "llg_golden.npz"), os.path.join(HERE, "models.json"))
 
 
-def thermal_bcc2(ref_root):
-    """Equilibrium statistics of the benchmark Hamiltonian from magex's own Langevin run.
-
-    Two-site bcc 8^3 (1,024 spins), shells 8+6+12 with per-bond full 3x3 tensors (isotropic
-    20/10/-1 meV, 1 % symmetric anisotropic part, DMI |D| = 1 meV), SIA K = 0.01 meV along z,
-    B = (0, 0, 0.5) T, T = 300 K, alpha 0.05, dt 0.1 fs: LLGSolver (NumPy Heun, noise
-    default_rng(seed).normal per step, magex/llg.py:106-122,216-227) from the ferromagnetic state,
-    `equil` steps discarded, then E/N (magex/spinmodel.py:475-484) and |M| = |mean e| sampled every
-    `every` steps over `sample` steps.  20 block means give each mean and its standard error; the
-    block length (10,000 steps) is several times the autocorrelation time of |M| (about 1,600 steps
-    at this size and temperature)."""
+def _thermal_bcc2_run(ref_root, th, seed):
+    """One Langevin run of magex's LLGSolver on the config-2 Hamiltonian: E/N and |M| samples."""
     sys.path.insert(0, ref_root)
-    import scipy
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
     from magex import spinmodel as RS
     from magex.llg import LLGSolver
     from magex_gb300.workloads import bcc_two_site_model
-
-    th = dict(L=8, alpha=0.05, dt=1e-4, T=300.0, Bz=0.5, seed=31, equil=20000, sample=200000, every=20,
-              model="bcc2", model_kwargs=dict(J=[20.0, 10.0, -1.0], seed=0))
     tmp = tempfile.mkdtemp()
     path = os.path.join(tmp, "bcc2.json")
     with open(path, "w") as f:
         json.dump(bcc_two_site_model(J=(20.0, 10.0, -1.0), seed=0), f)
     s = RS.SpinSystem(RS.load_results(path), (th["L"],) * 3, (1, 1, 1), (0.0, 0.0, th["Bz"]))
-    sol = LLGSolver(s, alpha=th["alpha"], dt=th["dt"], temperature=th["T"], seed=th["seed"])
+    sol = LLGSolver(s, alpha=th["alpha"], dt=th["dt"], temperature=th["T"], seed=seed)
     e = s.init_spins("ferro")
     for _ in range(th["equil"]):
         e = sol.step(e)
@@ -538,15 +526,45 @@ def thermal_bcc2(ref_root):
         if k % th["every"] == th["every"] - 1:
             Es.append(s.energy(e, per_spin=True))
             Ms.append(np.linalg.norm(e.mean(0)))
+    return np.array(Es), np.array(Ms)
+
+
+def thermal_bcc2(ref_root):
+    """Equilibrium statistics of the benchmark Hamiltonian from magex's own Langevin runs.
+
+    Two-site bcc 8^3 (1,024 spins), shells 8+6+12 with per-bond full 3x3 tensors (isotropic
+    20/10/-1 meV, 1 % symmetric anisotropic part, DMI |D| = 1 meV), SIA K = 0.01 meV along z,
+    B = (0, 0, 0.5) T, T = 300 K, alpha 0.05, dt 0.1 fs: `nruns` independent LLGSolver runs (NumPy
+    Heun, noise default_rng(seed).normal per step, magex/llg.py:106-122,216-227; seeds seed0,
+    seed0 + 1, ...) from the ferromagnetic state, `equil` steps discarded, then E/N
+    (magex/spinmodel.py:475-484) and |M| = |mean e| sampled every `every` steps over `sample` steps.
+
+    Each run gives one mean per observable.  The energy has slow components (its autocorrelation
+    still reads a few per cent after 10,000 steps), so 20-block errors of one run understate the
+    scatter between runs; the standard error used is that of the run means (sem_runs), together
+    with the scatter of one run (sd_run), which a run of the same length on the GPU shares."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    import scipy
+
+    th = dict(L=8, alpha=0.05, dt=1e-4, T=300.0, Bz=0.5, seed0=31, nruns=8, equil=20000, sample=200000, every=20,
+              model="bcc2", model_kwargs=dict(J=[20.0, 10.0, -1.0], seed=0))
+    seeds = [th["seed0"] + k for k in range(th["nruns"])]
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    with ProcessPoolExecutor(max_workers=min(8, len(seeds)), mp_context=mp.get_context("spawn")) as ex:
+        runs = list(ex.map(_thermal_bcc2_run, [ref_root] * len(seeds), [th] * len(seeds), seeds))
     out = {"numpy_version": np.array(np.__version__), "scipy_version": np.array(scipy.__version__),
-           "params": np.array(json.dumps(th)), "E_series": np.array(Es), "M_series": np.array(Ms)}
-    for key, x in (("E", np.array(Es)), ("M", np.array(Ms))):
-        blocks = x.reshape(20, -1).mean(1)
-        out[f"{key}_mean"] = np.array(blocks.mean())
-        out[f"{key}_sem"] = np.array(blocks.std(ddof=1) / np.sqrt(20))
+           "params": np.array(json.dumps(th)), "E_series0": runs[0][0], "M_series0": runs[0][1]}
+    for key, col in (("E", 0), ("M", 1)):
+        means = np.array([r[col].mean() for r in runs])
+        out[f"{key}_run_means"] = means
+        out[f"{key}_mean"] = np.array(means.mean())
+        out[f"{key}_sd_run"] = np.array(means.std(ddof=1))
+        out[f"{key}_sem"] = np.array(means.std(ddof=1) / np.sqrt(len(means)))
     np.savez_compressed(os.path.join(HERE, "thermal_bcc2.npz"), **out)
-    print("wrote", os.path.join(HERE, "thermal_bcc2.npz"), {k: float(out[k]) for k in ("E_mean", "E_sem", "M_mean",
-                                                                                          "M_sem")})
+    print("wrote", os.path.join(HERE, "thermal_bcc2.npz"),
+          {k: out[k].tolist() for k in ("E_mean", "E_sem", "E_sd_run", "M_mean", "M_sem", "M_sd_run")})
 
 
 def adversarial(ref_root):

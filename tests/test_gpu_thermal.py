@@ -1,13 +1,16 @@
-"""Thermal equilibrium of the benchmark Hamiltonian against the reference's own Langevin run.
+"""Thermal equilibrium of the benchmark Hamiltonian against the reference's own Langevin runs.
 
 The fixture (tests/golden/thermal_bcc2.npz, written by make_golden.py --thermal-bcc2) holds the
-equilibrium <E>/N and <|M|> of magex's LLGSolver (NumPy Heun, its default_rng noise stream,
-magex/llg.py:106-122,216-227) on the two-site bcc model with full 3x3 tensors, DMI, SIA and
-B_z = 0.5 T at 300 K (8^3 cells), from 20 block means.  The GPU runs the same model, parameters and
+equilibrium <E>/N and <|M|> of eight independent runs of magex's LLGSolver (NumPy Heun, its
+default_rng noise stream, magex/llg.py:106-122,216-227) on the two-site bcc model with full 3x3
+tensors, DMI, SIA and B_z = 0.5 T at 300 K (8^3 cells): per run the mean over 10,000 samples, and
+the scatter of those run means (sd_run).  The GPU runs the same model, parameters, run length and
 sampling with in-kernel Philox noise (FP32 Box-Muller of Philox4x32-10 draws), in every step form,
-and must land within 3 combined standard errors; magex checks its own thermostat the same way against
-a known law (tests/test_spindyn.py:79-89).  A run at a temperature 10 % off must fail the same bound,
-so the check can tell a wrong noise amplitude from a right one.
+with four seeds; under the hypothesis that it samples the same distribution its run means scatter
+like the reference's, so the difference of the two averages is compared with
+3 sd_run sqrt(1/8 + 1/4).  magex checks its own thermostat the same way against a known law
+(tests/test_spindyn.py:79-89).  Runs at a temperature 10 % off must fail the same bound, so the
+check tells a wrong noise amplitude from a right one.
 """
 import json
 import os
@@ -31,12 +34,11 @@ def _system(th):
     return bcc_two_site(L=th["L"], field=(0.0, 0.0, th["Bz"]))
 
 
-def _stats(sc, th, precision, seeds, T=None):
-    """Means and standard errors of E/N and |M| over `seeds` independent Philox runs, each sampled
-    as the reference run was (ferromagnetic start, equil steps, then every `every` steps)."""
-    from helpers import block_stats
+def _run_means(sc, th, precision, seeds, T=None):
+    """Per-seed means of E/N and |M| of Philox runs sampled as the reference runs were
+    (ferromagnetic start, `equil` steps, then a sample every `every` steps over `sample` steps)."""
     from magex_gb300.llg import GB300LLG
-    out = {"E": [], "M": []}
+    E, M = [], []
     for seed in seeds:
         sol = GB300LLG(sc, th["alpha"], th["dt"], th["T"] if T is None else T, seed, precision=precision)
         lat = sol.model.to_lattice(sc.init_spins("ferro"))
@@ -46,36 +48,38 @@ def _stats(sc, th, precision, seeds, T=None):
             sol.run_lattice(lat, th["every"])
             obs.append(sol.model.observables(lat).clone())
         o = torch.stack(obs).cpu().numpy()
-        out["E"].append(block_stats(o[:, 0] / sc.N))
-        out["M"].append(block_stats(np.linalg.norm(o[:, 1:4], axis=1) / sc.N))
-    res = {}
-    for key, st in out.items():
-        mean = float(np.mean([m for m, _ in st]))
-        sem = float(np.sqrt(np.sum([s ** 2 for _, s in st]))) / len(st)
-        res[key] = (mean, sem)
-    return res
+        E.append(float(np.mean(o[:, 0] / sc.N)))
+        M.append(float(np.mean(np.linalg.norm(o[:, 1:4], axis=1) / sc.N)))
+    return {"E": np.array(E), "M": np.array(M)}
 
 
-def _sigmas(ref, key, mean, sem):
-    return abs(mean - float(ref[f"{key}_mean"])) / np.hypot(float(ref[f"{key}_sem"]), sem)
+SEEDS = (101, 202, 303, 404)
+
+
+def _z(ref, key, means):
+    """Difference of the GPU and reference averages in units of its standard error (the run-mean
+    scatter sd_run of the reference runs, shared by runs of the same length)."""
+    n_ref = len(ref[f"{key}_run_means"])
+    se = float(ref[f"{key}_sd_run"]) * np.sqrt(1.0 / n_ref + 1.0 / len(means))
+    return abs(float(np.mean(means)) - float(ref[f"{key}_mean"])) / se
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp64_fixed", "int48", "df32"])
 def test_config2_thermal_equilibrium_within_3_sigma_of_reference(cuda, ref, precision):
     th = json.loads(str(ref["params"]))
     sc = _system(th)
-    res = _stats(sc, th, precision, seeds=(101, 202))
+    means = _run_means(sc, th, precision, SEEDS)
     for key in ("E", "M"):
-        z = _sigmas(ref, key, *res[key])
-        assert z <= 3.0, (precision, key, res[key], float(ref[f"{key}_mean"]), float(ref[f"{key}_sem"]), z)
+        z = _z(ref, key, means[key])
+        assert z <= 3.0, (precision, key, means[key].tolist(), float(ref[f"{key}_mean"]), z)
 
 
 def test_config2_thermal_check_fails_at_10_percent_wrong_temperature(cuda, ref):
-    """The same comparison at 0.9 T and 1.1 T: <E>/N moves by tens of standard errors, far outside
-    the 3-sigma bound, so a noise amplitude off by 5 % (T off by 10 %) cannot pass."""
+    """The same comparison at 0.9 T and 1.1 T: <E>/N moves by about 2.8 meV, tens of standard errors,
+    far outside the 3-sigma bound, so a noise amplitude off by 5 % (T off by 10 %) cannot pass."""
     th = json.loads(str(ref["params"]))
     sc = _system(th)
     for factor in (0.9, 1.1):
-        res = _stats(sc, th, "fp64", seeds=(101, 202), T=factor * th["T"])
-        z = _sigmas(ref, "E", *res["E"])
-        assert z > 10.0, (factor, res["E"], z)
+        means = _run_means(sc, th, "fp64", SEEDS, T=factor * th["T"])
+        z = _z(ref, "E", means["E"])
+        assert z > 10.0, (factor, means["E"].tolist(), z)

@@ -164,17 +164,18 @@ def test_oracle_adversarial_trajectory(tag):
 
 
 def test_config2_thermal_fixture_is_consistent():
-    """The reference's config-2 Langevin statistics (make_golden.py --thermal-bcc2): the stored means
-    and standard errors are the 20-block statistics of the stored series, and the run is in the
-    ordered phase it was chosen for (|M| ~ 0.9 at 300 K, well below T_c)."""
+    """The reference's config-2 Langevin statistics (make_golden.py --thermal-bcc2): the stored mean
+    and errors are those of the stored run means, the first run's stored series gives its run mean,
+    and the runs are in the ordered phase they were chosen for (|M| ~ 0.9 at 300 K, below T_c)."""
     import json
     import os
-    from helpers import block_stats
     ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "thermal_bcc2.npz"))
     th = json.loads(str(ref["params"]))
-    assert len(ref["E_series"]) == th["sample"] // th["every"]
+    assert len(ref["E_series0"]) == th["sample"] // th["every"]
     for key in ("E", "M"):
-        m, s = block_stats(ref[f"{key}_series"])
-        assert abs(m - float(ref[f"{key}_mean"])) <= 1e-12 * abs(m)
-        assert abs(s - float(ref[f"{key}_sem"])) <= 1e-9 * s
+        runs = ref[f"{key}_run_means"]
+        assert len(runs) == th["nruns"]
+        assert abs(runs.mean() - float(ref[f"{key}_mean"])) <= 1e-12 * abs(runs.mean())
+        assert abs(runs.std(ddof=1) - float(ref[f"{key}_sd_run"])) <= 1e-9 * runs.std(ddof=1)
+        assert abs(ref[f"{key}_series0"].mean() - runs[0]) <= 1e-12 * abs(runs[0])
     assert 0.85 < float(ref["M_mean"]) < 0.97
