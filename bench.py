@@ -725,16 +725,52 @@ def _r(x, n=4):
     return None if x is None else float(f"{x:.{n}g}")
 
 
+def bench_fp64_plan(sc, e0, K, warmup, peak64, flops_step, hbm_peak):
+    """The all-FP64 plan (precision="fp64") on the same workload: K steps through mgx_llg_run, its
+    per-kernel times and both roofline fractions (HBM at 72 / 96 B per site; FP64 pipe at
+    flops_step per spin-step against the live-measured DFMA peak)."""
+    import torch
+    from magex_gb300.llg import GB300LLG
+    sol = GB300LLG(sc, ALPHA, DT, TEMP, seed=3000, precision="fp64")
+    lat = sol.model.to_lattice(e0)
+    stream = torch.cuda.current_stream()
+    sol.run_lattice(lat, warmup)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    sol.stage_lattice(lat, 0)
+    ev[1].record(stream)
+    sol.stage_lattice(lat, 1)
+    ev[2].record(stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    sol.run_lattice(lat, K)
+    b.record(stream)
+    b.synchronize()
+    ms = a.elapsed_time(b) / K
+    pm, cm = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    N = sc.N
+    return {"value": N / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": K,
+            "kernels_ms": {"k_predict": pm, "k_correct": cm},
+            "hbm_roofline_frac": 96.0 * N / (cm * 1e-3) / 1e9 / hbm_peak,
+            "fp64_roofline": {"achieved": flops_step * N / (ms * 1e-3) / 1e12, "peak": peak64 / 1e12,
+                              "unit": "TFLOP/s", "frac": flops_step * N / (ms * 1e-3) / peak64,
+                              "flops_per_spin_step": flops_step,
+                              "peak_source": "measured live (mgx_measure_fp64_peak, DFMA loop)"}}
+
+
 def north_star_summary(line):
     """The figures the benchmark targets grade, compact: spin-steps/s and roofline fractions of the
     FP64 step and of its exact fixed-point-sum form, batched / per-system speed-ups, adjoint / forward
     time ratios (recompute and resident), and the large batched + adjoint workload."""
-    out = {"fp64": {"value": _r(line["value"]), "hbm_frac": _r(line["roofline"]["frac"], 3),
-                    "fp64_pipe_frac": _r(line["fp64_roofline"]["frac"], 3)}}
+    fp = line["fp64_plan"]
+    out = {"default": {"precision": line["config"]["precision"], "value": _r(line["value"]),
+                       "hbm_frac": _r(line["roofline"]["frac"], 3)},
+           "fp64": {"value": _r(fp["value"]), "hbm_frac": _r(fp["hbm_roofline_frac"], 3),
+                    "fp64_pipe_frac": _r(fp["fp64_roofline"]["frac"], 3)}}
     fx = line.get("fp64_fixed_gather_variant")
     if fx:
-        out["fp64_fixed"] = {"value": _r(fx["value"]), "hbm_frac": _r(fx["hbm_roofline_frac"], 3),
-                             "dev_vs_fp64": _r(fx["max_abs_deviation_from_fp64_plan"], 2)}
+        out["fp64_fixed_dev_vs_fp64"] = _r(fx["max_abs_deviation_from_fp64_plan"], 2)
     for key in ("batched", "batched_fp64_fixed"):
         b = line.get(key)
         if b:
@@ -781,30 +817,41 @@ def run_gb300(args):
     N = sc.N
     z = len(sc.bond_src) / sc.ns
     e0 = sc.init_spins("random", seed=1 + rank)
+    # the default solver: precision "auto" is the FP64 step with the exact fixed-point exchange sum
+    # for this model (every floating-point operation FP64)
     sol = GB300LLG(sc, ALPHA, DT, TEMP, seed=1000 + rank)
+    prec = sol.precision
     lat = sol.model.to_lattice(e0)
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        sol.stage_lattice(lat, 0)
-        sol.stage_lattice(lat, 1)
+    sol.run_lattice(lat, args.warmup)
     K = args.steps
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * K + 1)]
+    # per-kernel durations: CUDA events around each stage call on the launching stream (the stage-0
+    # call of a fixed-point plan also refreshes the fixed-point copy of the spins: one split kernel)
+    Kk = min(K, 50)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * Kk + 1)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for k in range(Kk):
+        sol.stage_lattice(lat, 0)
+        ev[2 * k + 1].record(stream)
+        sol.stage_lattice(lat, 1)
+        ev[2 * k + 2].record(stream)
+    torch.cuda.synchronize()
+    pred_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(Kk)]
+    corr_ms = [ev[2 * k + 1].elapsed_time(ev[2 * k + 2]) for k in range(Kk)]
+    # the timed region: K steps through one public call (mgx_llg_run)
+    a_ev, b_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        ev[0].record(stream)
-        for k in range(K):
-            sol.stage_lattice(lat, 0)
-            ev[2 * k + 1].record(stream)
-            sol.stage_lattice(lat, 1)
-            ev[2 * k + 2].record(stream)
+        a_ev.record(stream)
+        sol.run_lattice(lat, K)
+        b_ev.record(stream)
         torch.cuda.synchronize()
         if ws > 1:
             dist.barrier()
-    total_ms = ev[0].elapsed_time(ev[2 * K])
-    pred_ms = [ev[2 * k].elapsed_time(ev[2 * k + 1]) for k in range(K)]
-    corr_ms = [ev[2 * k + 1].elapsed_time(ev[2 * k + 2]) for k in range(K)]
+    total_ms = a_ev.elapsed_time(b_ev)
     norm_err = float((torch.linalg.vector_norm(lat, dim=0) - 1).abs().max())
     if not (norm_err < 1e-12):
         raise RuntimeError(f"spins lost unit norm during the benchmark: {norm_err}")
@@ -833,9 +880,15 @@ def run_gb300(args):
 
     value = N * K * ws / (total_ms * 1e-3)
     pm, cm = statistics.mean(pred_ms), statistics.mean(corr_ms)
-    dominant, dom_ms = ("k_correct", cm) if cm >= pm else ("k_predict", pm)
-    # algorithmic HBM bytes per spin: predictor reads e, writes ep, k1; corrector reads ep, k1, e, writes e
-    bytes_per_spin = {"k_predict": 72.0, "k_correct": 96.0}[dominant]
+    fixed = prec == "fp64_fixed"
+    names = ("k_fx_split + k_predict_fx", "k_correct_fx") if fixed else ("k_predict", "k_correct")
+    dominant, dom_ms = (names[1], cm) if cm >= pm else (names[0], pm)
+    # algorithmic HBM bytes per site.  FP64 plan: predictor reads e, writes ep, k1 (72); corrector reads
+    # ep, k1, e, writes e (96).  Fixed-point plan: the split reads e and writes its 56-bit copy es (48);
+    # the predictor reads e, es and writes ep, k1 and the copy eps (120); the corrector reads eps, k1,
+    # ep, e and writes e, es (144).  Neighbour rows come from L1 / L2 (the stencil re-reads them).
+    bytes_per_spin = {"k_predict": 72.0, "k_correct": 96.0, "k_fx_split + k_predict_fx": 168.0,
+                      "k_correct_fx": 144.0}[dominant]
     hbm_peak = None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
@@ -844,15 +897,20 @@ def run_gb300(args):
     else:
         hbm_peak, peak_src = 6800.0, "fallback"
     achieved = bytes_per_spin * N / (dom_ms * 1e-3) / 1e9
-    traffic = read_ncu_traffic().get(dominant)
+    traffic = read_ncu_traffic().get(dominant.split(" + ")[-1])
     flops_step = fp64_flops_per_spin_step(z)
-    fp64_achieved = flops_step * N * K / (total_ms * 1e-3)
     clocks = clk.summary()
+    # the all-FP64 plan on the same workload, beside the default
+    plain = bench_fp64_plan(sc, e0, min(K, 200), args.warmup, peak64.value, flops_step, hbm_peak)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
         "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded two-site bcc model, random initial spins)",
-        "config": workload_config(args.L), "gpu_launches": 2 * K,
+        "config": {**workload_config(args.L), "precision": prec,
+                   "arithmetic": ("every floating-point operation FP64; exchange and on-site sums exact on 56-bit "
+                                  "fixed-point spins and couplings (INT32 pipe), rounded once" if fixed else
+                                  "all FP64")},
+        "gpu_launches": 2 * K + (1 if fixed else 0),
     }
     # secondary measurements first (bulky), the graded figures last: a reader of the line's tail sees
     # the roofline, the CPU baseline, e2e and the compact spec summary
@@ -882,10 +940,8 @@ def run_gb300(args):
         # free HBM (2000 steps x 14 N doubles = 3.7 GB here), so nothing is recomputed
         line["adjoint_resident"] = bench_adjoint(cache_bytes="auto")
         line["adjoint_large"] = bench_adjoint(L=1024, nsteps=200, seg=50)
-    line["kernels_ms"] = {"k_predict": pm, "k_correct": cm}
-    line["fp64_roofline"] = {"achieved": fp64_achieved / 1e12, "peak": peak64.value / 1e12, "unit": "TFLOP/s",
-                             "frac": fp64_achieved / peak64.value, "flops_per_spin_step": flops_step,
-                             "peak_source": "measured live (mgx_measure_fp64_peak, DFMA loop)"}
+    line["kernels_ms"] = {names[0]: pm, names[1]: cm}
+    line["fp64_plan"] = plain
     if ws == 1 and not args.no_cpu_baseline:
         v, n, cores, el = cpu_oracle_timing(args.L)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",

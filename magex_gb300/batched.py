@@ -24,7 +24,7 @@ import torch
 from . import _lib
 from .constants import GAMMA, K_B, MU_B
 from .device import DeviceModel, stream_ptr, supercell_from_system
-from .llg import _SUPPORTED, _philox_key
+from .llg import _SUPPORTED, _philox_key, fixed_point_eligible
 
 
 def _per_system(x, n, name):
@@ -40,15 +40,20 @@ class BatchedLLG:
     """An ensemble of independent Heun / Depondt LLG systems stepped by shared launches."""
 
     def __init__(self, systems, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
-                 integrator="heun", noise="philox", precision="fp64", device=None):
+                 integrator="heun", noise="philox", precision="auto", device=None):
         if integrator not in _SUPPORTED:
             raise NotImplementedError(f"integrator '{integrator}' is not implemented by the GB300 kernels")
         if noise not in ("philox", "host"):
             raise ValueError("noise must be 'philox' or 'host'")
-        if precision not in ("fp64", "fp64_fixed"):
-            raise ValueError("batched systems use precision 'fp64' or 'fp64_fixed'")
-        self.precision = precision
+        if precision not in ("fp64", "fp64_fixed", "auto"):
+            raise ValueError("batched systems use precision 'auto', 'fp64' or 'fp64_fixed'")
         self.systems = [supercell_from_system(s) for s in systems]
+        if precision == "auto":
+            # the exact fixed-point sum form when every system supports it (as GB300LLG's "auto")
+            ok = all(fixed_point_eligible(sc, a) for sc, a in zip(self.systems, _per_system(alpha, len(self.systems),
+                                                                                              "alpha")))
+            precision = "fp64_fixed" if ok else "fp64"
+        self.precision = precision
         n = len(self.systems)
         if n == 0:
             raise ValueError("empty ensemble")

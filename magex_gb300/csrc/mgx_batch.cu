@@ -71,13 +71,17 @@ struct Batch {
   int graph_threads = 0, graph_grid = 0;
   // exact fixed-point exchange sums (every system of the batch, or none)
   bool fixed = false;
+  // cubic / higher-uniaxial terms in at least one system: the HIGHER stage instantiation
+  bool higher = false;
   std::vector<void*> fx_blocks;
   int2* fx_split = nullptr;           // es | eps of all systems (2 * 3 * ntot)
 };
 
 constexpr int BATCH_MAX_THREADS = 512;
 
-template <int STAGE, int NOISE, int INTEG, bool FIXED>
+// HIGHER: a separate instantiation for batches with cubic / higher-uniaxial terms (in any system), so
+// that the plain stage kernels keep their registers.
+template <int STAGE, int NOISE, int INTEG, bool FIXED, bool HIGHER>
 __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch_stage(const BatchSys* __restrict__ sys,
                                                                    const int2* __restrict__ tiles, int ntiles,
                                                                    double* __restrict__ e,
@@ -91,19 +95,23 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS) k_batch_stage(const BatchSy
     double* es = e + S.off3;
     const double* ns = noise ? noise + S.off3 : nullptr;
     if (FIXED) {
-      if (STAGE == 0) fx_predict_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER>(S.L, S.P, S.F, es, ns, q, st);
-      else fx_correct_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER>(S.L, S.P, S.F, es, ns, q, st);
+      if (STAGE == 0)
+        fx_predict_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(S.L, S.P, S.F, es, ns, q, st);
+      else
+        fx_correct_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(S.L, S.P, S.F, es, ns, q, st);
       continue;
     }
+    // the EXTRA bodies add the higher on-site fields (the spin-orbit torque and per-site extra field
+    // pointers of a batched system are null)
     const int W = S.L.width;
     if (STAGE == 0) {
-      if (W == 1) predict_site<1, NOISE, INTEG>(S.L, S.P, es, ns, q, st);
-      else if (W == 4) predict_site<4, NOISE, INTEG>(S.L, S.P, es, ns, q, st);
-      else predict_site<9, NOISE, INTEG>(S.L, S.P, es, ns, q, st);
+      if (W == 1) predict_site<1, NOISE, INTEG, HIGHER>(S.L, S.P, es, ns, q, st);
+      else if (W == 4) predict_site<4, NOISE, INTEG, HIGHER>(S.L, S.P, es, ns, q, st);
+      else predict_site<9, NOISE, INTEG, HIGHER>(S.L, S.P, es, ns, q, st);
     } else {
-      if (W == 1) correct_site<1, NOISE, INTEG>(S.L, S.P, es, ns, q, st);
-      else if (W == 4) correct_site<4, NOISE, INTEG>(S.L, S.P, es, ns, q, st);
-      else correct_site<9, NOISE, INTEG>(S.L, S.P, es, ns, q, st);
+      if (W == 1) correct_site<1, NOISE, INTEG, HIGHER>(S.L, S.P, es, ns, q, st);
+      else if (W == 4) correct_site<4, NOISE, INTEG, HIGHER>(S.L, S.P, es, ns, q, st);
+      else correct_site<9, NOISE, INTEG, HIGHER>(S.L, S.P, es, ns, q, st);
     }
   }
 }
@@ -224,15 +232,23 @@ static int grid_size(const Batch* b) {
   return std::max(1, std::min(b->ntiles, b->ctas_per_sm * b->sms));
 }
 
+template <int NOISE, int INTEG, bool FIXED, bool HIGHER>
+static void enqueue_batch_form(const Batch* b, double* e, const double* noise, StepArg step, cudaStream_t st) {
+  const int grid = grid_size(b);
+  k_batch_stage<0, NOISE, INTEG, FIXED, HIGHER><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e,
+                                                                             noise, step);
+  k_batch_stage<1, NOISE, INTEG, FIXED, HIGHER><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e,
+                                                                             noise, step);
+}
+
 template <int NOISE, int INTEG>
 static void enqueue_batch(const Batch* b, double* e, const double* noise, StepArg step, cudaStream_t st) {
-  const int grid = grid_size(b);
   if (b->fixed) {
-    k_batch_stage<0, NOISE, INTEG, true><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
-    k_batch_stage<1, NOISE, INTEG, true><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
+    if (b->higher) enqueue_batch_form<NOISE, INTEG, true, true>(b, e, noise, step, st);
+    else enqueue_batch_form<NOISE, INTEG, true, false>(b, e, noise, step, st);
   } else {
-    k_batch_stage<0, NOISE, INTEG, false><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
-    k_batch_stage<1, NOISE, INTEG, false><<<grid, b->threads, 0, st>>>(b->d_sys, b->d_tiles, b->ntiles, e, noise, step);
+    if (b->higher) enqueue_batch_form<NOISE, INTEG, false, true>(b, e, noise, step, st);
+    else enqueue_batch_form<NOISE, INTEG, false, false>(b, e, noise, step, st);
   }
 }
 
@@ -278,9 +294,6 @@ mgx_status mgx_batch_create(const mgx_model* const* models, const mgx_llg_params
   *out = nullptr;
   for (int k = 0; k < nsys; ++k) {
     if (!models[k]) return set_error(MGX_ERR_INVALID, "mgx_batch_create: model %d is null", k);
-    if (has_higher_onsite(reinterpret_cast<const Model*>(models[k])->d))
-      return set_error(MGX_ERR_UNSUPPORTED, "system %d: batched systems do not include cubic / higher uniaxial "
-                       "anisotropy", k);
     const mgx_llg_params& p = params[k];
     if (!(p.dt > 0.0)) return set_error(MGX_ERR_INVALID, "system %d: dt must be positive", k);
     if (p.alpha_site) return set_error(MGX_ERR_INVALID, "system %d: batched systems take a uniform alpha", k);
@@ -307,6 +320,7 @@ mgx_status mgx_batch_create(const mgx_model* const* models, const mgx_llg_params
     const Model* m = reinterpret_cast<const Model*>(models[k]);
     b->models.push_back(m);
     b->offset[k + 1] = b->offset[k] + m->d.N;
+    b->higher |= has_higher_onsite(m->d);
   }
   b->ntot = b->offset[nsys];
   const double gamma = 0.1760859630;

@@ -86,12 +86,15 @@ __device__ __forceinline__ void fx_rhs(const DevLattice& L, const DevLLG& P, con
 }
 
 // FP64 field of the site from the integer gather (+ Zeeman and thermal): the 56-bit form's field, and
-// the field of the Depondt integrator for both forms
-template <int NOISE, int PREC>
+// the field of the Depondt integrator for both forms.  HIGHER (56-bit form only, a separate
+// instantiation) adds the cubic and higher-uniaxial fields at the site's FP64 spin (sx, sy, sz), in the
+// place the FP64 kernels add them: after the effective field, before the thermal field.
+template <int NOISE, int PREC, bool HIGHER = false>
 __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                            const int2* __restrict__ xs, const double* __restrict__ noise,
                                            long long q, int s, int c0, int c1, int c2, uint64_t step, double& bx,
-                                           double& by, double& bz) {
+                                           double& by, double& bz, double sx = 0.0, double sy = 0.0,
+                                           double sz = 0.0) {
   double h[3];
   if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
     fx_gather64(L, F, xs, q, s, c0, c1, c2, h);
@@ -105,11 +108,13 @@ __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P,
   bx = h[0] + L.B0;
   by = h[1] + L.B1;
   bz = h[2] + L.B2;
+  if (HIGHER) add_higher_onsite(L, q, s, sx, sy, sz, bx, by, bz);
   add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
 }
 
 // Predictor of site q (0 <= q < L.N) of the fixed-point forms: writes P.ep, P.k1 and the split F.eps at q.
-template <int NOISE, int INTEG, int PREC>
+// HIGHER: the 56-bit form with the model's cubic / higher-uniaxial terms.
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
 __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 const double* __restrict__ e, const double* __restrict__ noise,
                                                 long long q, uint64_t step) {
@@ -128,7 +133,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
   if (INTEG == MGX_INTEGRATOR_HEUN) {
     if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
       double bx, by, bz;
-      fx_field64<NOISE, PREC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
+      fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
       llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
               f[2]);
     } else {
@@ -141,7 +146,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
     x *= r; y *= r; z *= r;
   } else {
     double bx, by, bz;
-    fx_field64<NOISE, PREC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
     double fx, fy, fz;
     llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     f[0] = ey * fz - ez * fy; f[1] = ez * fx - ex * fz; f[2] = ex * fy - ey * fx;
@@ -154,7 +159,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
 }
 
 // Corrector of site q: reads the neighbours' F.eps, P.k1 and e at q, writes e and its split F.es at q.
-template <int NOISE, int INTEG, int PREC>
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
 __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 double* __restrict__ e, const double* __restrict__ noise, long long q,
                                                 uint64_t step) {
@@ -170,7 +175,7 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
     if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
       const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
       double bx, by, bz;
-      fx_field64<NOISE, PREC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
+      fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
       llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
               f[2]);
     } else {
@@ -182,7 +187,7 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
   } else {
     const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
     double bx, by, bz;
-    fx_field64<NOISE, PREC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz);
+    fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
     double fx, fy, fz;
     llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     const double wx = py * fz - pz * fy, wy = pz * fx - px * fz, wz = px * fy - py * fx;

@@ -216,6 +216,11 @@ void enqueue_df_step(const LLGPlan* pl, double* e, const double* noise, uint64_t
 mgx_status build_fx_tables(LLGPlan* pl);
 void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st);
 void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
+// The same stages on cells [cb, cb + cn) of every sublattice, and the split of those cells only
+// (the slabs of mgx_llg_step_host).
+void enqueue_fx_range(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages,
+                      long long cb, long long cn);
+void enqueue_fx_split_cells(const LLGPlan* pl, const double* e, cudaStream_t st, long long cb, long long cn);
 
 // Host-side NVTX range over one library call (named in profiler timelines; a no-op without a tool).
 struct NvtxRange {

@@ -229,8 +229,9 @@ mgx_status mgx_llg_create(const mgx_model* mm, const mgx_llg_params* p, mgx_llg*
   if (p->precision < MGX_PRECISION_FP64 || p->precision > MGX_PRECISION_FP64_FIXED_GATHER)
     return set_error(MGX_ERR_INVALID, "precision %d is not fp64 (0), df32-gather (1), int48-gather (2) or "
                      "fp64-fixed-gather (3)", p->precision);
-  if (has_higher_onsite(m->d) && p->precision != MGX_PRECISION_FP64)
-    return set_error(MGX_ERR_UNSUPPORTED, "cubic / higher uniaxial anisotropy need the FP64 form (precision 0)");
+  if (has_higher_onsite(m->d) && p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_FP64_FIXED_GATHER)
+    return set_error(MGX_ERR_UNSUPPORTED, "cubic / higher uniaxial anisotropy need the FP64 form (precision 0) or "
+                     "the FP64 form with the fixed-point exchange sum (precision 3)");
   const int ns = m->d.ns;
   const long long N = m->d.N;
   LLGPlan* pl = new LLGPlan();
@@ -416,7 +417,8 @@ mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t st
 }
 
 // Copies of host buffers inside one step.  The input goes to the device in axis-0 slabs on the plan's
-// copy stream (each packed into the lattice layout as it lands); the predictor of a slab starts once
+// copy stream (each packed into the lattice layout as it lands, and for the fixed-point-gather forms
+// split into its fixed-point copy); the predictor of a slab starts once
 // the slabs it gathers from (its own and its neighbours', every slab at least as thick as the
 // couplings' reach) are in; the corrector runs slab by slab and each finished slab goes back to the
 // host while the next ones are computed.  Consecutive slabs alternate between the caller's stream and
@@ -452,9 +454,11 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
   cudaEvent_t* ev_out = pl->host_ev + MGX_HOST_CHUNKS;
   cudaEvent_t ev_start = pl->host_ev[2 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[2 * MGX_HOST_CHUNKS + 1];
   cudaEvent_t ev_join_aux = pl->host_ev[2 * MGX_HOST_CHUNKS + 2], ev_join_main = pl->host_ev[2 * MGX_HOST_CHUNKS + 3];
-  // slabs: FP64 stencil plans of at least 2^20 sites with both buffers page-locked; otherwise one piece
+  // slabs: FP64 and fixed-point-gather stencil plans of at least 2^20 sites with both buffers
+  // page-locked; otherwise one piece
+  const bool fx = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER || pl->precision == MGX_PRECISION_INT48_GATHER;
   int nc = 1;
-  if (pl->precision == MGX_PRECISION_FP64 && L.layout == 0 && m->reach0 >= 0 && N >= (1LL << 20) &&
+  if ((pl->precision == MGX_PRECISION_FP64 || fx) && L.layout == 0 && m->reach0 >= 0 && N >= (1LL << 20) &&
       pinned_host(e_in) && pinned_host(e_out)) {
     nc = std::min(MGX_HOST_CHUNKS, L.L0 / std::max(m->reach0, 1));
     if (nc < 3) nc = 1;
@@ -468,6 +472,7 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
     MGX_CUDA_TRY(cudaMemcpyAsync(pl->host_aos + 3 * sb, e_in + 3 * sb, sizeof(double) * 3 * (se - sb),
                                  cudaMemcpyDefault, cs));
     enqueue_pack(m, pl->host_aos, pl->host_lat, sb, se - sb, cs);
+    if (fx && nc > 1) enqueue_fx_split_cells(pl, pl->host_lat, cs, cell0(c), cell0(c + 1) - cell0(c));
     MGX_CUDA_TRY(cudaEventRecord(ev_in[c], cs));
   }
   double* lat = pl->host_lat;
@@ -489,7 +494,10 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
       const int c = ring ? (k + 1) % nc : k;
       cudaStream_t st = run[k & 1];
       MGX_CUDA_TRY(cudaStreamWaitEvent(st, ev_in[c == 0 && ring ? nc - 1 : std::min(c + 1, nc - 1)], 0));
-      enqueue_fp64_range(pl, lat, noise, step, st, 1, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
+      if (fx)
+        enqueue_fx_range(pl, lat, noise, step, st, 1, cell0(c), cell0(c + 1) - cell0(c));
+      else
+        enqueue_fp64_range(pl, lat, noise, step, st, 1, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
     }
     // every corrector gathers the predicted spins of its neighbours: both streams pass all predictors
     MGX_CUDA_TRY(cudaEventRecord(ev_join_aux, run[1]));
@@ -498,7 +506,10 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
     MGX_CUDA_TRY(cudaStreamWaitEvent(run[1], ev_join_main, 0));
     for (int c = 0; c < nc; ++c) {
       cudaStream_t st = run[c & 1];
-      enqueue_fp64_range(pl, lat, noise, step, st, 2, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
+      if (fx)
+        enqueue_fx_range(pl, lat, noise, step, st, 2, cell0(c), cell0(c + 1) - cell0(c));
+      else
+        enqueue_fp64_range(pl, lat, noise, step, st, 2, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
       const long long sb = cell0(c) * L.ns, se = cell0(c + 1) * L.ns;
       enqueue_unpack(m, lat, pl->host_aos, sb, se - sb, st);
       MGX_CUDA_TRY(cudaEventRecord(ev_out[c], st));

@@ -31,58 +31,92 @@ __global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, 
   if (i < n) xs[i] = fx_split<PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24>(x[i]);
 }
 
-template <int NOISE, int INTEG, int PREC>
+// The split of cells [cb, cb + cn) of every sublattice (blockIdx.y) and component (blockIdx.z).
+template <int PREC>
+__global__ void __launch_bounds__(256) k_fx_split_cells(const double* __restrict__ x, int2* __restrict__ xs,
+                                                        long long N, int ncell, long long cb, long long cn) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cn) return;
+  const long long q = (long long)blockIdx.z * N + (long long)blockIdx.y * ncell + cb + i;
+  xs[q] = fx_split<PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24>(x[q]);
+}
+
+// Sites begin + i (i < count) of sublattice blockIdx.y: the whole lattice is one row of N sites
+// (gridDim.y = 1, begin = 0), a range of cells one row of `count` cells per sublattice.
+template <int NOISE, int INTEG, int PREC, bool HIGHER>
 __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                        const double* __restrict__ e, const double* __restrict__ noise,
-                                                       uint64_t step) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) fx_predict_site<NOISE, INTEG, PREC>(L, P, F, e, noise, q, P.step_base ? *P.step_base + step : step);
+                                                       uint64_t step, long long begin, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count)
+    fx_predict_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+                                                P.step_base ? *P.step_base + step : step);
 }
 
-template <int NOISE, int INTEG, int PREC>
+template <int NOISE, int INTEG, int PREC, bool HIGHER>
 __global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                        double* __restrict__ e, const double* __restrict__ noise,
-                                                       uint64_t step) {
-  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) fx_correct_site<NOISE, INTEG, PREC>(L, P, F, e, noise, q, P.step_base ? *P.step_base + step : step);
+                                                       uint64_t step, long long begin, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count)
+    fx_correct_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+                                                P.step_base ? *P.step_base + step : step);
 }
 
 template <int NOISE, int INTEG, int PREC>
-static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
+static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st,
+                      long long cb, long long cn) {
   const DevLattice& L = pl->model->d;
   DevFX F = pl->fx;
   F.B[0] = split_host(L.B0);
   F.B[1] = split_host(L.B1);
   F.B[2] = split_host(L.B2);
-  const int tpb = site_block_size(L.N);
-  const unsigned grid = (unsigned)((L.N + tpb - 1) / tpb);
-  if (stages & 1) k_predict_fx<NOISE, INTEG, PREC><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
-  if (stages & 2) k_correct_fx<NOISE, INTEG, PREC><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step);
-}
-
-template <int NOISE, int PREC>
-static void fx_integ(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
-  if (pl->p.integrator == MGX_INTEGRATOR_DEPONDT)
-    launch_fx<NOISE, MGX_INTEGRATOR_DEPONDT, PREC>(pl, e, noise, step, stages, st);
-  else
-    launch_fx<NOISE, MGX_INTEGRATOR_HEUN, PREC>(pl, e, noise, step, stages, st);
-}
-
-template <int PREC>
-static void fx_noise(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st) {
-  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
-  switch (mode) {
-    case MGX_NOISE_HOST: fx_integ<MGX_NOISE_HOST, PREC>(pl, e, noise, step, stages, st); break;
-    case MGX_NOISE_PHILOX: fx_integ<MGX_NOISE_PHILOX, PREC>(pl, e, noise, step, stages, st); break;
-    default: fx_integ<MGX_NOISE_NONE, PREC>(pl, e, noise, step, stages, st); break;
+  const bool whole = cb == 0 && cn == L.ncell;
+  const long long count = whole ? L.N : cn;
+  const int tpb = site_block_size(whole ? L.N : cn * L.ns);
+  const dim3 grid((unsigned)((count + tpb - 1) / tpb), whole ? 1u : (unsigned)L.ns);
+  // cubic / higher-uniaxial terms (56-bit form only): a separate instantiation, so that the plain
+  // kernels keep their registers
+  constexpr bool H = PREC == MGX_PRECISION_FP64_FIXED_GATHER;
+  if (H && has_higher_onsite(L)) {
+    if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+    if (stages & 2) k_correct_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+  } else {
+    if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+    if (stages & 2) k_correct_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
   }
 }
 
-void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages) {
-  if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
-    fx_noise<MGX_PRECISION_FP64_FIXED_GATHER>(pl, e, noise, step, stages, st);
+template <int NOISE, int PREC>
+static void fx_integ(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st,
+                     long long cb, long long cn) {
+  if (pl->p.integrator == MGX_INTEGRATOR_DEPONDT)
+    launch_fx<NOISE, MGX_INTEGRATOR_DEPONDT, PREC>(pl, e, noise, step, stages, st, cb, cn);
   else
-    fx_noise<MGX_PRECISION_INT48_GATHER>(pl, e, noise, step, stages, st);
+    launch_fx<NOISE, MGX_INTEGRATOR_HEUN, PREC>(pl, e, noise, step, stages, st, cb, cn);
+}
+
+template <int PREC>
+static void fx_noise(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st,
+                     long long cb, long long cn) {
+  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
+  switch (mode) {
+    case MGX_NOISE_HOST: fx_integ<MGX_NOISE_HOST, PREC>(pl, e, noise, step, stages, st, cb, cn); break;
+    case MGX_NOISE_PHILOX: fx_integ<MGX_NOISE_PHILOX, PREC>(pl, e, noise, step, stages, st, cb, cn); break;
+    default: fx_integ<MGX_NOISE_NONE, PREC>(pl, e, noise, step, stages, st, cb, cn); break;
+  }
+}
+
+void enqueue_fx_range(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages,
+                      long long cb, long long cn) {
+  if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
+    fx_noise<MGX_PRECISION_FP64_FIXED_GATHER>(pl, e, noise, step, stages, st, cb, cn);
+  else
+    fx_noise<MGX_PRECISION_INT48_GATHER>(pl, e, noise, step, stages, st, cb, cn);
+}
+
+void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages) {
+  enqueue_fx_range(pl, e, noise, step, st, stages, 0, pl->model->d.ncell);
 }
 
 void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st) {
@@ -92,6 +126,16 @@ void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st) {
     k_fx_split<MGX_PRECISION_FP64_FIXED_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, n);
   else
     k_fx_split<MGX_PRECISION_INT48_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, n);
+}
+
+void enqueue_fx_split_cells(const LLGPlan* pl, const double* e, cudaStream_t st, long long cb, long long cn) {
+  const DevLattice& L = pl->model->d;
+  if (cn <= 0) return;
+  const dim3 grid((unsigned)((cn + 255) / 256), (unsigned)L.ns, 3u);
+  if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
+    k_fx_split_cells<MGX_PRECISION_FP64_FIXED_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, L.N, L.ncell, cb, cn);
+  else
+    k_fx_split_cells<MGX_PRECISION_INT48_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, L.N, L.ncell, cb, cn);
 }
 
 // balanced (hi, lo) int32 halves of round(v 2^(2 limb - sigma)), |v| <= 2^sigma

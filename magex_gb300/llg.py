@@ -9,15 +9,19 @@ columns as magex ``magex/llg.py:48-283``.  The spins stay on the GPU for the who
 Heun step is two fused sm_103a kernels (libmgx: ``mgx_llg_step`` / ``mgx_llg_run``); observables
 rows are computed on the device by ``mgx_observables``.
 
-Arithmetic (``precision=``): "fp64" (default) runs everything in FP64.  GB300's FP64 units run at
-1/61 of its FP32 rate, so two reduced forms keep the spins, the integration and the renormalisation
-in FP64 and move the rest off the FP64 pipe (Heun: field and right-hand side on compensated FP32
-pairs): "df32" evaluates the exchange sum on compensated FP32 pairs (~44 significant bits), "int48"
-as exact integer products and sums of 48-bit fixed-point couplings and spins on the INT32 pipe.
-Both stay within the per-step parity tolerance against magex (tests/test_gpu_df.py).  "fp64_fixed"
-keeps every floating-point operation FP64 and evaluates the exchange and on-site sums exactly on
-56-bit fixed-point spins and couplings (INT32 pipe): its only extra error, the 2^-57 quantisation of
-the inputs, is below the rounding of an FP64 multiply-add chain.
+Arithmetic (``precision=``): "fp64" runs everything in FP64.  "fp64_fixed" keeps every
+floating-point operation FP64 and evaluates the exchange and on-site sums exactly on 56-bit
+fixed-point spins and couplings (INT32 pipe): its only extra error, the 2^-57 quantisation of the
+inputs, is below the rounding of an FP64 multiply-add chain, and it is 3.5x faster on GB300, whose
+FP64 units run at 1/61 of its FP32 rate.  "auto" (default) is "fp64_fixed" for the models that form
+supports (lattice stencils with per-sublattice moments and single-ion tensors, uniform damping and
+temperature, no spin-orbit torque) and "fp64" otherwise; a
+solver on "auto" moves to an FP64 plan when field hooks (field_func, extra_field) are first used.
+Two reduced forms keep the spins, the integration and the renormalisation in FP64 and move the rest
+off the FP64 pipe (Heun: field and right-hand side on compensated FP32 pairs): "df32" evaluates the
+exchange sum on compensated FP32 pairs (~44 significant bits), "int48" as exact integer products and
+sums of 48-bit fixed-point couplings and spins.  Every form stays within the per-step parity
+tolerance against magex (tests/test_gpu_df.py, tests/test_gpu_fixed_adversarial.py).
 
 Thermal noise (``noise=``):
   "philox"  counter-based Philox4x32-10 keyed by (seed, site, step), generated inside the kernels
@@ -64,12 +68,27 @@ def llg_rhs(e, B, alpha, precession=True):
 PRECISIONS = {"fp64": _lib.PRECISION_FP64, "df32": _lib.PRECISION_DF32_GATHER, "int48": _lib.PRECISION_INT48_GATHER,
               "fp64_fixed": _lib.PRECISION_FP64_FIXED_GATHER}
 
+
+def fixed_point_eligible(sc, alpha=0.1, sot=None):
+    """True when the exact fixed-point sum form (fp64_fixed) supports the system: a lattice stencil
+    of fewer than 2^31 sites with per-sublattice moments and single-ion tensors, uniform damping and
+    temperature, no extra energy terms (biquadratic, four-spin) and no spin-orbit torque.  Cubic and
+    higher-uniaxial anisotropy are evaluated in FP64 beside the fixed-point sum."""
+    from .lattice import Supercell
+    if not isinstance(sc, Supercell) or sc.N >= 2 ** 31 or sot:
+        return False
+    if np.ndim(alpha) or getattr(sc, "alpha_site", None) is not None or getattr(sc, "site_T", None) is not None:
+        return False
+    if sc.A_site is not None or sc.mu_site is not None or getattr(sc, "terms", None):
+        return False
+    return not sc.has_higher
+
 class GB300LLG:
     """Stochastic Heun / Depondt LLG on one GB300, with the API of magex ``LLGSolver``."""
 
     def __init__(self, system, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
                  thermostat="classical", integrator="heun", stt=None, sot=None, backend="gb300",
-                 noise="philox", precision="fp64", device=None):
+                 noise="philox", precision="auto", device=None):
         if integrator not in INTEGRATORS:
             raise ValueError(f"integrator must be one of {INTEGRATORS}")
         if integrator not in _SUPPORTED:
@@ -85,11 +104,14 @@ class GB300LLG:
             raise ValueError("backend must be 'gb300'")
         if noise not in ("philox", "host"):
             raise ValueError("noise must be 'philox' or 'host'")
-        if precision not in PRECISIONS:
-            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}")
-        self.precision = precision
+        if precision not in PRECISIONS and precision != "auto":
+            raise ValueError(f"precision must be 'auto' or one of {sorted(PRECISIONS)}")
         self.sys = system
         self.sc = supercell_from_system(system)
+        self.auto_precision = precision == "auto"
+        if self.auto_precision:
+            precision = "fp64_fixed" if fixed_point_eligible(self.sc, alpha, sot) else "fp64"
+        self.precision = precision
         self.model = DeviceModel(self.sc, device)
         if system is not self.sc:
             self.model.field_owner = system          # follow SpinSystem.set_field (magex/llg.py:327)
@@ -126,11 +148,8 @@ class GB300LLG:
         p.noise = _lib.NOISE_HOST if noise == "host" else _lib.NOISE_PHILOX
         p.seed = _philox_key(seed)
         p.precision = PRECISIONS[precision]
-        h = C.c_void_p()
-        with torch.cuda.device(self.device):
-            _lib.check(self.model.lib.mgx_llg_create(self.model.handle, C.byref(p), C.byref(h)), "mgx_llg_create")
-        del al
-        self.handle = h
+        self._params, self._alpha_keep = p, al
+        self.handle = self._create_plan(p)
         self.sot = None
         if sot:
             # magex/llg.py:84-86: p normalised, damping-like and field-like amplitudes in tesla
@@ -142,6 +161,25 @@ class GB300LLG:
         self._noisy = False
         self._noise_lat = None
         self._lat = None
+
+    def _create_plan(self, p):
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(self.model.lib.mgx_llg_create(self.model.handle, C.byref(p), C.byref(h)), "mgx_llg_create")
+        return h
+
+    def _ensure_fp64_plan(self):
+        """A solver on precision "auto" with the fixed-point form moves to an FP64 plan (same seed,
+        parameters and step counter) the first time field hooks are used: the per-site hook field
+        is an input of the FP64 kernels only."""
+        if self.precision == "fp64" or not self.auto_precision:
+            return
+        self._params.precision = PRECISIONS["fp64"]
+        h = self._create_plan(self._params)
+        old, self.handle = self.handle, h
+        self.model.lib.mgx_llg_destroy(old)
+        self.precision = "fp64"
+        self._sigma_key = None
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -255,6 +293,8 @@ class GB300LLG:
 
     def step_lattice(self, lat, stream=None):
         """One step on device spins in the lattice layout ((3, N) float64, in place)."""
+        if self._has_callables():
+            self._ensure_fp64_plan()
         noise_ptr = self._prepare_step(stream)
         if self._has_callables():
             self._step_callables(lat, noise_ptr, stream)

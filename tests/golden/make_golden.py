@@ -574,7 +574,8 @@ def adversarial(ref_root):
     stencil), nearest-neighbour DMI 5 meV and an anisotropic part of 1e-2 meV, a near-zero single-ion
     constant K = 1e-9 meV, |B| = 100 T along an oblique axis.  bcc2_decades: two-site bcc 4^3, four
     shells 20 / 10 / -1 / 1e-6 meV with per-shell full tensors (1 % anisotropic, DMI 5 %), K = 1e-10
-    meV, the same 100 T field.  magex's LLGSolver (NumPy Heun, magex/llg.py:216-227), alpha 0.1,
+    meV, the same 100 T field.  The models are read with jtol = 1e-12 (magex's default 1e-4 would drop the
+    1e-6 meV shells).  magex's LLGSolver (NumPy Heun, magex/llg.py:216-227), alpha 0.1,
     dt 0.1 fs, 1000 steps from random spins; spins kept after 1, 10, 100 and 1000 steps, final
     energy and effective field."""
     sys.path.insert(0, ref_root)
@@ -600,7 +601,7 @@ def adversarial(ref_root):
         path = os.path.join(tmp, tag + ".json")
         with open(path, "w") as f:
             json.dump(d, f)
-        s = RS.SpinSystem(RS.load_results(path), L, (1, 1, 1), tuple(B))
+        s = RS.SpinSystem(RS.load_results(path, jtol=1e-12), L, (1, 1, 1), tuple(B))
         e = s.init_spins("random", seed=11)
         sol = LLGSolver(s, 0.1, 1e-4, 0.0, 1)
         out[f"{tag}/e0"] = e.copy()
@@ -610,7 +611,8 @@ def adversarial(ref_root):
                 out[f"{tag}/e{n}"] = e.copy()
         out[f"{tag}/energy"] = np.array(s.energy(e))
         out[f"{tag}/field"] = s.effective_field(e)
-        meta[tag] = dict(model=d, L=list(L), B=list(map(float, B)), alpha=0.1, dt=1e-4, keep=list(keep))
+        meta[tag] = dict(model=d, L=list(L), B=list(map(float, B)), alpha=0.1, dt=1e-4, keep=list(keep), jtol=1e-12,
+                         ncouplings=len(s.bonds) if hasattr(s, "bonds") else None)
     out["meta"] = np.array(json.dumps(meta))
     np.savez_compressed(os.path.join(HERE, "adversarial.npz"), **out)
     print("wrote", os.path.join(HERE, "adversarial.npz"))

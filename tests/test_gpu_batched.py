@@ -160,3 +160,35 @@ def test_batch_fp64_fixed_equals_single_system_plans_and_fp64(cuda):
     g.set_spins(e0)
     g.run(10, graph_chunk=5)
     assert torch.equal(g.e, fx.e)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fixed"])
+def test_batch_with_higher_onsite_terms_follows_reference(cuda, golden, golden_models, precision):
+    """Cubic (rotated axes) and higher uniaxial anisotropy in batched systems (the HIGHER stage
+    instantiation), in both forms: the sc_cubic system (Heun, T = 0) batched with the config-2
+    Hamiltonian follows the reference's trajectory and the bcc system its single-system plan; the
+    tri_cubic_thermal system (Depondt, 5 K, the reference's noise stream) follows its trajectory."""
+    from helpers import golden_supercell
+    from magex_gb300.batched import BatchedLLG
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc, meta = golden_supercell(golden_models, "sc_cubic")
+    bcc = bcc_two_site(L=4)
+    ens = BatchedLLG([sc, bcc], [meta["alpha"], 0.05], [meta["dt"], 1e-4], [0.0, 0.0], [meta["seed"], 7],
+                     precision=precision)
+    e_bcc = bcc.init_spins("random", seed=5)
+    ens.set_spins([golden["sc_cubic/e0"], e_bcc])
+    ens.run(meta["steps"], graph_chunk=0)
+    err = float(np.abs(ens.spins(0).cpu().numpy() - golden[f"sc_cubic/e{meta['steps']}"]).max())
+    assert err <= 1e-12 * meta["steps"], err
+    single = GB300LLG(bcc, 0.05, 1e-4, 0.0, 7, precision=precision)
+    lat = single.model.to_lattice(e_bcc)
+    single.run_lattice(lat, meta["steps"])
+    assert float((ens.spins(1) - single.model.from_lattice(lat)).abs().max()) <= 1e-12 * meta["steps"]
+    sc2, meta2 = golden_supercell(golden_models, "tri_cubic_thermal")
+    ens2 = BatchedLLG([sc2], meta2["alpha"], meta2["dt"], meta2["T"], meta2["seed"], integrator="depondt",
+                      noise="host", precision=precision)
+    ens2.set_spins([golden["tri_cubic_thermal/e0"]])
+    ens2.run(meta2["steps"], graph_chunk=0)
+    err2 = float(np.abs(ens2.spins(0).cpu().numpy() - golden[f"tri_cubic_thermal/e{meta2['steps']}"]).max())
+    assert err2 <= 1e-12 * meta2["steps"], err2

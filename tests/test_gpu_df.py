@@ -93,3 +93,21 @@ def test_fixed_point_forms_against_fp64_one_step(cuda):
     d_fx = float((out["int48"] - out["fp64"]).abs().max())
     d_64 = float((out["fp64_fixed"] - out["fp64"]).abs().max())
     assert d_64 <= 1e-15 and d_fx <= 2e-15 and d_df <= 2e-14, (d_64, d_fx, d_df)
+
+
+@pytest.mark.parametrize("tag", ["sc_cubic", "tri_cubic_thermal"])
+def test_fixed_point_sum_with_higher_onsite_terms_matches_reference(cuda, golden, golden_models, tag):
+    """The exact fixed-point sum form with cubic (rotated axes) and higher uniaxial anisotropy (its
+    HIGHER instantiation: the terms added in FP64 at the site's spin): the reference's trajectories,
+    Heun at T = 0 and Depondt at 5 K with the reference's noise stream, at the FP64 bars."""
+    from magex_gb300.llg import GB300LLG
+    sc, meta = golden_supercell(golden_models, tag)
+    sol = GB300LLG(sc, meta["alpha"], meta["dt"], meta["T"], meta["seed"], integrator=meta["integrator"],
+                   noise="host", precision="fp64_fixed")
+    e = golden[f"{tag}/e0"].copy()
+    for n in range(1, meta["steps"] + 1):
+        e = sol.step(e)
+        if n in meta["keep"]:
+            err = np.abs(e - golden[f"{tag}/e{n}"]).max()
+            assert err <= min(1e-9, 1e-12 * n + 1e-13), (tag, n, err)
+    assert abs(sol.energy(e) - float(golden[f"{tag}/energy"])) <= 1e-12 * abs(float(golden[f"{tag}/energy"]))

@@ -29,7 +29,7 @@ def adv():
 def _system(meta):
     from magex_gb300.lattice import Supercell
     from magex_gb300.spinmodel import load_results
-    return Supercell(load_results(meta["model"]), tuple(meta["L"]), (True, True, True), tuple(meta["B"]))
+    return Supercell(load_results(meta["model"], jtol=meta["jtol"]), tuple(meta["L"]), (True, True, True), tuple(meta["B"]))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp64_fixed"])
@@ -68,7 +68,7 @@ def test_fixed_point_scale_resolves_the_smallest_shell(cuda, adv):
     for j3 in (1e-6, 2e-6):
         model = make_model("sc", J=[100.0, 1e-3, j3], D=5.0, Jani=[[1e-2, 0, 0], [0, -2e-2, 0], [0, 0, 1e-2]],
                            K=1e-9, moment=2.0)
-        sc = Supercell(load_results(model), tuple(meta["L"]), (True, True, True), tuple(meta["B"]))
+        sc = Supercell(load_results(model, jtol=meta["jtol"]), tuple(meta["L"]), (True, True, True), tuple(meta["B"]))
         for prec in ("fp64", "fp64_fixed"):
             steps[j3, prec] = GB300LLG(sc, meta["alpha"], meta["dt"], 0.0, 1, precision=prec).step(e0)
     assert np.abs(steps[1e-6, "fp64"] - steps[1e-6, "fp64_fixed"]).max() <= 1e-15

@@ -17,16 +17,20 @@ TRAJ = ["sc16", "sc6_thermal", "bcc2_thermal", "bcc2_T0", "bcc2_shell4", "tri16"
         "sc_open", "sc_tiny_fold", "sc_afm", "honeycomb", "sc_structure", "sc_cubic", "tri_cubic_thermal"]
 
 
-def _solver(golden_models, tag, noise="host"):
+def _solver(golden_models, tag, noise="host", precision="auto"):
     from magex_gb300.llg import GB300LLG
     sc, meta = golden_supercell(golden_models, tag)
-    sol = GB300LLG(sc, meta["alpha"], meta["dt"], meta["T"], meta["seed"], integrator=meta["integrator"], noise=noise)
+    sol = GB300LLG(sc, meta["alpha"], meta["dt"], meta["T"], meta["seed"], integrator=meta["integrator"], noise=noise,
+                   precision=precision)
     return sc, meta, sol
 
 
+@pytest.mark.parametrize("precision", ["fp64", "auto"])
 @pytest.mark.parametrize("tag", TRAJ)
-def test_trajectory_matches_reference(cuda, golden, golden_models, tag):
-    sc, meta, sol = _solver(golden_models, tag)
+def test_trajectory_matches_reference(cuda, golden, golden_models, tag, precision):
+    """Every golden trajectory with the all-FP64 plan and with the default ("auto": the exact
+    fixed-point exchange sum where the model allows it, FP64 otherwise)."""
+    sc, meta, sol = _solver(golden_models, tag, precision=precision)
     e = golden[f"{tag}/e0"].copy()
     for n in range(1, meta["steps"] + 1):
         e = sol.step(e)
@@ -264,14 +268,17 @@ def test_graph_replayed_run_equals_direct_launches(cuda, precision):
     ((20.0, 10.0, -1.0, 1.0), True, "philox", "fp64", (96, 76, 76)),   # 4th shell: couplings reach 2 layers
     ((20.0, 10.0, -1.0), False, "philox", "fp64", (96, 76, 76)),        # open along the slab axis
     ((20.0, 10.0, -1.0), True, "host", "fp64", (96, 76, 76)),
-    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76)),  # one piece (reduced split refreshed)
+    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76)),  # slabs, each split as it lands
+    ((20.0, 10.0, -1.0, 1.0), False, "host", "fp64_fixed", (96, 76, 76)),  # open axis 0, reach 2, host noise
+    ((20.0, 10.0, -1.0), True, "philox", "int48", (96, 76, 76)),
+    ((20.0, 10.0, -1.0), True, "philox", "df32", (96, 76, 76)),        # one piece (reduced split refreshed)
     ((20.0, 10.0, -1.0), True, "philox", "fp64", (4, 512, 256)),      # four slabs of one layer
     ((20.0, 10.0, -1.0), False, "philox", "fp64", (2, 512, 512)),     # too thin to split: one piece
 ])
 def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precision, L):
     """mgx_llg_step_host (pinned host buffers; copies in axis-0 slabs overlapping the stages for FP64
-    plans of >= 2^20 sites) gives the same bits as the step on device spins: also in place, and for
-    pageable numpy input (one piece)."""
+    and fixed-point-gather plans of >= 2^20 sites) gives the same bits as the step on device spins:
+    also in place, and for pageable numpy input (one piece)."""
     from magex_gb300.lattice import Supercell
     from magex_gb300.llg import GB300LLG
     from magex_gb300.spinmodel import load_results
@@ -541,14 +548,35 @@ def test_new_entry_points_reject_bad_arguments(cuda, golden_models):
 
 
 def test_higher_onsite_terms_outside_the_fp64_step_are_refused(cuda, golden_models):
-    """Cubic / higher uniaxial anisotropy are in the FP64 step, field, observables and Monte Carlo
-    sweep; the forms that do not evaluate them refuse such a model instead of dropping the terms."""
-    from magex_gb300.batched import BatchedLLG
+    """Cubic / higher uniaxial anisotropy are in the FP64 step and its fixed-point-sum form (also
+    batched), field, observables and Monte Carlo sweep; the reduced forms that do not evaluate them
+    refuse such a model instead of dropping the terms."""
     from magex_gb300.llg import GB300LLG
     sc, _ = golden_supercell(golden_models, "sc_cubic")
-    GB300LLG(sc, 0.1, 1e-3)
-    for precision in ("df32", "int48", "fp64_fixed"):
+    assert GB300LLG(sc, 0.1, 1e-3).precision == "fp64_fixed"
+    GB300LLG(sc, 0.1, 1e-3, precision="fp64")
+    for precision in ("df32", "int48"):
         with pytest.raises(NotImplementedError):
             GB300LLG(sc, 0.1, 1e-3, precision=precision)
-    with pytest.raises(NotImplementedError):
-        BatchedLLG([sc], 0.1, 1e-3, [0.0], [1])
+
+
+def test_auto_precision_moves_to_fp64_for_field_hooks(cuda, golden, golden_models):
+    """A solver on the default precision ("auto") of an eligible model runs the fixed-point-sum form
+    and moves to an FP64 plan, with the same step counter and seed, when a per-site field hook is
+    first used; the trajectory then equals an FP64 solver's that used the hook from the start."""
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=4)
+    e0 = sc.init_spins("random", seed=2)
+    a = GB300LLG(sc, 0.05, 1e-4, 300.0, 9)
+    b = GB300LLG(sc, 0.05, 1e-4, 300.0, 9, precision="fp64")
+    assert a.precision == "fp64_fixed" and b.precision == "fp64"
+    ea, eb = a.step(e0), b.step(e0)
+    assert np.abs(ea - eb).max() <= 1e-12
+    hook = lambda e: 0.3 * np.cross(e, [0.0, 0.0, 1.0])   # noqa: E731  (an extra_field of magex/sld.py:171)
+    a.extra_field = hook
+    b.extra_field = hook
+    for _ in range(3):
+        ea, eb = a.step(ea), b.step(eb)
+    assert a.precision == "fp64" and a._step_index == b._step_index == 4
+    assert np.abs(ea - eb).max() <= 1e-12 * 4

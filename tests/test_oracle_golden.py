@@ -151,7 +151,7 @@ def test_oracle_adversarial_trajectory(tag):
     from magex_gb300.spinmodel import load_results
     adv = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "adversarial.npz"))
     meta = json.loads(str(adv["meta"]))[tag]
-    sc = Supercell(load_results(meta["model"]), tuple(meta["L"]), (True, True, True), tuple(meta["B"]))
+    sc = Supercell(load_results(meta["model"], jtol=meta["jtol"]), tuple(meta["L"]), (True, True, True), tuple(meta["B"]))
     ora = OracleLLG(sc, meta["alpha"], meta["dt"], 0.0, 1, csr="stencil", threads=1)
     e = adv[f"{tag}/e0"].copy()
     for n in range(1, meta["keep"][-1] + 1):
