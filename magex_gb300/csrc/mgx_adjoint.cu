@@ -57,7 +57,20 @@ struct AdjPlan {
   int2* d_group = nullptr;
   void* sub = nullptr;
   int seg_steps = 0;
+  // captured step loops of the plan's own segment storage (the recomputed segments): the forward of
+  // `fwd_steps` steps (Philox step index from the device counter d_step) and the backward of
+  // `bwd_steps` steps into `bwd_ebar`; dropped when the models change (kernel arguments hold the
+  // stencils, fields included, by value)
+  cudaStream_t cap_stream = nullptr;
+  unsigned long long* d_step = nullptr;
+  cudaGraphExec_t fwd_graph = nullptr, bwd_graph = nullptr;
+  int fwd_steps = 0, bwd_steps = 0;
+  const double* bwd_ebar = nullptr;
 };
+
+// Lattices up to this size replay captured graphs for recomputed segments (larger ones are bound by
+// the kernels, not by their launches).
+constexpr long long kAdjGraphMaxSites = 1LL << 21;
 
 __device__ __forceinline__ void cross3(double ax, double ay, double az, double bx, double by, double bz, double& cx,
                                        double& cy, double& cz) {
@@ -151,7 +164,12 @@ __device__ __forceinline__ void accumulate_onsite(const AdjDev& A, long long N, 
 // Transposed gather sum_rev J^T g_nbr at site q of the reverse stencil, with the parameter-gradient
 // outer products added to PG once per group run: a forward coupling with tensor T_g contributes
 // g_nbr (x) v, one with T_g^T contributes v (x) g_nbr (v = own p or e), so each run keeps the sums of
-// g_nbr over its plain and its transposed couplings and flushes 9 values per group.
+// g_nbr over its plain and its transposed couplings and flushes 9 values per group.  Couplings are
+// taken in chunks of ADJ_CHUNK: the neighbour values of a chunk are all loaded before any of them is
+// used, so a site waits one memory round trip per chunk instead of one per coupling (small lattices,
+// a few warps per SM, are bound by that latency).
+constexpr int ADJ_CHUNK = 6;
+
 __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __restrict__ g, long long q, int s,
                                                int c0, int c1, int c2, double vx, double vy, double vz,
                                                double& ox, double& oy, double& oz) {
@@ -175,42 +193,58 @@ __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __
       for (int b = 0; b < 3; ++b) acc[3 * a + b] = fma(vv[a], gt[b], fma(gs[a], vv[b], acc[3 * a + b]));
     store_cells<9>(P, N, acc);
   };
-  for (int b = b0; b < b1; ++b) {
-    const int2 gr = __ldg(A.group + b);
-    if (gr.x != cur_g) {
-      flush();
-      cur_g = gr.x;
-      sx = sy = sz = 0.0;
-      tx = ty = tz = 0.0;
+  for (int c = b0; c < b1; c += ADJ_CHUNK) {
+    double gx[ADJ_CHUNK], gy[ADJ_CHUNK], gz[ADJ_CHUNK];
+#pragma unroll
+    for (int k = 0; k < ADJ_CHUNK; ++k) {
+      gx[k] = gy[k] = gz[k] = 0.0;
+      const int b = c + k;
+      if (b >= b1) continue;
+      const int4 geo = __ldg(L.bond_geo + b);
+      int n0 = c0 + geo.y, n1 = c1 + geo.z, n2 = c2 + geo.w;
+      bool ok = true;
+      if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
+      if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
+      if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
+      if (!ok) continue;                    // a dropped coupling contributes a zero g
+      const long long j = (long long)geo.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
+      gx[k] = __ldg(g + j);
+      gy[k] = __ldg(g + N + j);
+      gz[k] = __ldg(g + 2 * N + j);
     }
-    const int4 geo = __ldg(L.bond_geo + b);
-    int n0 = c0 + geo.y, n1 = c1 + geo.z, n2 = c2 + geo.w;
-    bool ok = true;
-    if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
-    if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
-    if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
-    if (!ok) continue;
-    const long long j = (long long)geo.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2;
-    const double gx = __ldg(g + j), gy = __ldg(g + N + j), gz = __ldg(g + 2 * N + j);
-    const double* T = L.bond_J + (long long)b * 9;
-    ox = fma(__ldg(T + 0), gx, ox); ox = fma(__ldg(T + 1), gy, ox); ox = fma(__ldg(T + 2), gz, ox);
-    oy = fma(__ldg(T + 3), gx, oy); oy = fma(__ldg(T + 4), gy, oy); oy = fma(__ldg(T + 5), gz, oy);
-    oz = fma(__ldg(T + 6), gx, oz); oz = fma(__ldg(T + 7), gy, oz); oz = fma(__ldg(T + 8), gz, oz);
-    if (gr.y) {
-      tx += gx; ty += gy; tz += gz;
-    } else {
-      sx += gx; sy += gy; sz += gz;
+#pragma unroll
+    for (int k = 0; k < ADJ_CHUNK; ++k) {
+      const int b = c + k;
+      if (b >= b1) break;
+      const int2 gr = __ldg(A.group + b);
+      if (gr.x != cur_g) {
+        flush();
+        cur_g = gr.x;
+        sx = sy = sz = 0.0;
+        tx = ty = tz = 0.0;
+      }
+      const double* T = L.bond_J + (long long)b * 9;
+      ox = fma(__ldg(T + 0), gx[k], ox); ox = fma(__ldg(T + 1), gy[k], ox); ox = fma(__ldg(T + 2), gz[k], ox);
+      oy = fma(__ldg(T + 3), gx[k], oy); oy = fma(__ldg(T + 4), gy[k], oy); oy = fma(__ldg(T + 5), gz[k], oy);
+      oz = fma(__ldg(T + 6), gx[k], oz); oz = fma(__ldg(T + 7), gy[k], oz); oz = fma(__ldg(T + 8), gz[k], oz);
+      if (gr.y) {
+        tx += gx[k]; ty += gy[k]; tz += gz[k];
+      } else {
+        sx += gx[k]; sy += gy[k]; sz += gz[k];
+      }
     }
   }
   flush();
 }
 
 // ---------------------------------------------------------------- forward recomputation (stores states)
+// (step index: P.step_base[0] + step inside a captured segment, step otherwise)
 template <int NOISE>
 __global__ void __launch_bounds__(256) k_fwd_pred(const DevLattice L, const DevLLG P, const double* __restrict__ e,
                                                   uint64_t step, double* __restrict__ H1, double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) predict_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H1, R);
+  if (q < L.N)
+    predict_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, P.step_base ? *P.step_base + step : step, H1, R);
 }
 
 template <int NOISE>
@@ -218,8 +252,12 @@ __global__ void __launch_bounds__(256) k_fwd_corr(const DevLattice L, const DevL
                                                   uint64_t step, double* __restrict__ H2, double* __restrict__ eout,
                                                   double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q < L.N) correct_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, step, H2, eout, nullptr, R + L.N);
+  if (q < L.N)
+    correct_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, P.step_base ? *P.step_base + step : step, H2,
+                                                eout, nullptr, R + L.N);
 }
+
+__global__ void k_adj_step_set(unsigned long long* c, unsigned long long v) { *c = v; }
 
 // ---------------------------------------------------------------- backward kernels
 // Site-local part of the backward step (first kernel body of step n): ybar from zbar = dL/de' through
@@ -403,6 +441,83 @@ static double* seg_ptr(const AdjPlan* a, int n, int k) {
   return a->seg + seg_stride(a) * n + (size_t)k * 3 * N;
 }
 
+// The kernels of a forward segment of nsteps steps from the spins in storage slot 0 (step index
+// step0 + n, or the device counter plus n when P.step_base is set).
+static void enqueue_adj_forward(const AdjPlan* a, const DevLLG& P0, int nsteps, uint64_t step0, cudaStream_t st) {
+  const DevLattice& L = a->fwd->d;
+  const long long N = L.N;
+  const int tpb = site_block_size(N);
+  const unsigned grid = (unsigned)((N + tpb - 1) / tpb);
+  for (int n = 0; n < nsteps; ++n) {
+    DevLLG P = P0;
+    P.ep = seg_ptr(a, n, SEG_P);
+    double* E = seg_ptr(a, n, SEG_E);
+    double* R = seg_ptr(a, n, SEG_R);
+    const uint64_t step = step0 + (uint64_t)n;
+    if (a->noise == MGX_NOISE_PHILOX) {
+      k_fwd_pred<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
+      k_fwd_corr<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
+    } else {
+      k_fwd_pred<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
+      k_fwd_corr<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
+    }
+  }
+}
+
+// The kernels of the backward pass through a segment of nsteps steps (ebar in: dL/de after the last
+// step; out: dL/de before the first).
+static void enqueue_adj_backward(const AdjPlan* a, double* ebar, int nsteps, cudaStream_t st) {
+  const long long N = a->fwd->d.N;
+  const size_t n3 = 3 * (size_t)N;
+  const int tpb = site_block_size(N);
+  const unsigned grid = (unsigned)((N + tpb - 1) / tpb);
+  double* eacc = a->work;
+  double* pbar = a->work + n3;
+  double* f1bar = a->work + 2 * n3;
+  double* g1 = a->work + 3 * n3;
+  double* g2 = a->work + 4 * n3;
+  const int last = nsteps - 1;
+  k_adj_local<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, last + 1, SEG_E), seg_ptr(a, last, SEG_P),
+                                    seg_ptr(a, last, SEG_H2), seg_ptr(a, last, SEG_R), ebar, eacc, pbar, f1bar, g2);
+  for (int n = last; n >= 0; --n) {
+    k_adj_mid<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
+                                    seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
+    if (n > 0) {
+      k_adj_final<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr, seg_ptr(a, n - 1, SEG_P),
+                                              seg_ptr(a, n - 1, SEG_H2), seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
+    } else {
+      k_adj_final<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr, nullptr,
+                                               nullptr, nullptr, nullptr);
+    }
+  }
+}
+
+static void drop_adj_graphs(AdjPlan* a) {
+  if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
+  if (a->bwd_graph) cudaGraphExecDestroy(a->bwd_graph);
+  a->fwd_graph = a->bwd_graph = nullptr;
+  a->fwd_steps = a->bwd_steps = 0;
+  a->bwd_ebar = nullptr;
+}
+
+// Capture the kernels that `enqueue` puts on a stream into *exec.
+template <typename F>
+static mgx_status capture_adj(AdjPlan* a, cudaGraphExec_t* exec, F enqueue) {
+  if (!a->cap_stream) MGX_CUDA_TRY(cudaStreamCreateWithFlags(&a->cap_stream, cudaStreamNonBlocking));
+  MGX_CUDA_TRY(cudaStreamBeginCapture(a->cap_stream, cudaStreamCaptureModeThreadLocal));
+  enqueue(a->cap_stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t err = cudaStreamEndCapture(a->cap_stream, &g);
+  if (err != cudaSuccess) return cuda_error(err, "adjoint segment capture");
+  err = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  if (err != cudaSuccess) {
+    *exec = nullptr;
+    return cuda_error(err, "adjoint segment instantiate");
+  }
+  return MGX_OK;
+}
+
 }  // namespace mgx
 
 using namespace mgx;
@@ -460,6 +575,7 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   if (err == cudaSuccess) err = cudaMalloc(&a->d.PB, sizeof(double) * 3 * (size_t)N);
   if (err == cudaSuccess) err = cudaMalloc(&a->grads, sizeof(double) * (9 * (size_t)ngroups + 9 * ns + 3));
   if (err == cudaSuccess) err = cudaMalloc(&a->sub, sizeof(double) * 3 * ns);
+  if (err == cudaSuccess) err = cudaMalloc(&a->d_step, sizeof(unsigned long long));
   if (err == cudaSuccess) err = cudaMemcpy(a->d_group, grp.data(), sizeof(int2) * grp.size(), cudaMemcpyHostToDevice);
   if (err == cudaSuccess) {
     std::vector<double> sub(3 * ns, 0.0);
@@ -506,6 +622,9 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
 mgx_status mgx_adjoint_destroy(mgx_adjoint* aa) {
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
   if (!a) return MGX_OK;
+  drop_adj_graphs(a);
+  if (a->cap_stream) cudaStreamDestroy(a->cap_stream);
+  cudaFree(a->d_step);
   cudaFree(a->own_seg);
   cudaFree(a->work);
   cudaFree(a->k1);
@@ -534,6 +653,7 @@ mgx_status mgx_adjoint_sync_models(mgx_adjoint* aa) {
   if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_sync_models: null argument");
   a->d.F = a->fwd->d;
   a->d.R = a->rev->d;
+  drop_adj_graphs(a);
   return MGX_OK;
 }
 
@@ -558,25 +678,26 @@ mgx_status mgx_adjoint_forward(mgx_adjoint* aa, const double* e0, int32_t nsteps
   if (nsteps < 1 || nsteps > a->seg_cap)
     return set_error(MGX_ERR_INVALID, "nsteps = %d outside 1..%d (segment capacity)", nsteps, a->seg_cap);
   cudaStream_t st = (cudaStream_t)stream;
-  const DevLattice& L = a->fwd->d;
-  const long long N = L.N;
-  const int tpb = site_block_size(N);
-  const unsigned grid = (unsigned)((N + tpb - 1) / tpb);
+  const long long N = a->fwd->d.N;
   if (e0 != seg_ptr(a, 0, SEG_E))
     MGX_CUDA_TRY(cudaMemcpyAsync(seg_ptr(a, 0, SEG_E), e0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
-  for (int n = 0; n < nsteps; ++n) {
-    DevLLG P = a->P;
-    P.ep = seg_ptr(a, n, SEG_P);
-    double* E = seg_ptr(a, n, SEG_E);
-    double* R = seg_ptr(a, n, SEG_R);
-    const uint64_t step = step0 + (uint64_t)n;
-    if (a->noise == MGX_NOISE_PHILOX) {
-      k_fwd_pred<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
-      k_fwd_corr<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
-    } else {
-      k_fwd_pred<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
-      k_fwd_corr<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
+  if (a->seg == a->own_seg && N <= kAdjGraphMaxSites) {
+    // recomputed segments of a small lattice: one graph replay (the step index from the counter)
+    if (!a->fwd_graph || a->fwd_steps != nsteps) {
+      if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
+      a->fwd_graph = nullptr;
+      DevLLG P = a->P;
+      P.step_base = a->d_step;
+      const mgx_status cs = capture_adj(a, &a->fwd_graph, [&](cudaStream_t cst) {
+        enqueue_adj_forward(a, P, nsteps, 0, cst);
+      });
+      if (cs != MGX_OK) return cs;
+      a->fwd_steps = nsteps;
     }
+    k_adj_step_set<<<1, 1, 0, st>>>(a->d_step, (unsigned long long)step0);
+    MGX_CUDA_TRY(cudaGraphLaunch(a->fwd_graph, st));
+  } else {
+    enqueue_adj_forward(a, a->P, nsteps, step0, st);
   }
   if (e_out)
     MGX_CUDA_TRY(cudaMemcpyAsync(e_out, seg_ptr(a, nsteps, SEG_E), sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
@@ -592,27 +713,20 @@ mgx_status mgx_adjoint_backward(mgx_adjoint* aa, double* ebar, int32_t nsteps, v
     return set_error(MGX_ERR_INVALID, "nsteps = %d outside 1..%d (segment capacity)", nsteps, a->seg_cap);
   cudaStream_t st = (cudaStream_t)stream;
   const long long N = a->fwd->d.N;
-  const size_t n3 = 3 * (size_t)N;
-  const int tpb = site_block_size(N);
-  const unsigned grid = (unsigned)((N + tpb - 1) / tpb);
-  double* eacc = a->work;
-  double* pbar = a->work + n3;
-  double* f1bar = a->work + 2 * n3;
-  double* g1 = a->work + 3 * n3;
-  double* g2 = a->work + 4 * n3;
-  const int last = nsteps - 1;
-  k_adj_local<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, last + 1, SEG_E), seg_ptr(a, last, SEG_P),
-                                    seg_ptr(a, last, SEG_H2), seg_ptr(a, last, SEG_R), ebar, eacc, pbar, f1bar, g2);
-  for (int n = last; n >= 0; --n) {
-    k_adj_mid<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
-                                    seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
-    if (n > 0) {
-      k_adj_final<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr, seg_ptr(a, n - 1, SEG_P),
-                                              seg_ptr(a, n - 1, SEG_H2), seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
-    } else {
-      k_adj_final<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr, nullptr,
-                                               nullptr, nullptr, nullptr);
+  if (a->seg == a->own_seg && N <= kAdjGraphMaxSites) {
+    if (!a->bwd_graph || a->bwd_steps != nsteps || a->bwd_ebar != ebar) {
+      if (a->bwd_graph) cudaGraphExecDestroy(a->bwd_graph);
+      a->bwd_graph = nullptr;
+      const mgx_status cs = capture_adj(a, &a->bwd_graph, [&](cudaStream_t cst) {
+        enqueue_adj_backward(a, ebar, nsteps, cst);
+      });
+      if (cs != MGX_OK) return cs;
+      a->bwd_steps = nsteps;
+      a->bwd_ebar = ebar;
     }
+    MGX_CUDA_TRY(cudaGraphLaunch(a->bwd_graph, st));
+  } else {
+    enqueue_adj_backward(a, ebar, nsteps, st);
   }
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;

@@ -185,6 +185,11 @@ struct LLGPlan {
   double* host_lat = nullptr;    // [3][N] lattice layout
   double* host_aos = nullptr;    // [N][3] magex order (staging of the copies)
   cudaEvent_t host_ev[2 * MGX_HOST_CHUNKS + 4] = {};  // in[c] | out[c] | start | done | joined aux | joined main
+  // the slab pipeline of a host-buffer step captured as a graph (step index from d_step), for the
+  // last two (input, output) buffer pairs: replaying it costs one launch instead of ~250 API calls
+  LLGGraph host_graphs[2];
+  const double* host_in[2] = {nullptr, nullptr};
+  const double* host_noise[2] = {nullptr, nullptr};
   double* sot_block = nullptr;   // device [5] spin-orbit torque parameters
 };
 

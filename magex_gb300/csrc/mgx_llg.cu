@@ -131,6 +131,11 @@ static void drop_llg_graph(LLGPlan* pl) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = LLGGraph{};
   }
+  for (int k = 0; k < 2; ++k) {
+    if (pl->host_graphs[k].exec) cudaGraphExecDestroy(pl->host_graphs[k].exec);
+    pl->host_graphs[k] = LLGGraph{};
+    pl->host_in[k] = pl->host_noise[k] = nullptr;
+  }
   pl->last_tail = -1;
 }
 
@@ -199,6 +204,10 @@ static bool pinned_host(const void* p) {
 }
 
 static void drop_host_buffers(LLGPlan* pl) {
+  for (int k = 0; k < 2; ++k) {
+    if (pl->host_graphs[k].exec) cudaGraphExecDestroy(pl->host_graphs[k].exec);
+    pl->host_graphs[k] = LLGGraph{};
+  }
   cudaFree(pl->host_lat);
   cudaFree(pl->host_aos);
   pl->host_lat = pl->host_aos = nullptr;
@@ -416,53 +425,20 @@ mgx_status mgx_llg_step(mgx_llg* pp, double* e, const double* noise, uint64_t st
   return MGX_OK;
 }
 
-// Copies of host buffers inside one step.  The input goes to the device in axis-0 slabs on the plan's
-// copy stream (each packed into the lattice layout as it lands, and for the fixed-point-gather forms
-// split into its fixed-point copy); the predictor of a slab starts once
-// the slabs it gathers from (its own and its neighbours', every slab at least as thick as the
-// couplings' reach) are in; the corrector runs slab by slab and each finished slab goes back to the
-// host while the next ones are computed.  Consecutive slabs alternate between the caller's stream and
-// a second compute stream, so the blocks of one slab fill the tail of the previous one.  The
-// predictor and corrector kernels, and so the result, are those of mgx_llg_step: only the launch grid
-// is split.
-mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, const double* noise, uint64_t step,
-                             void* stream) {
-  NvtxRange nvtx_range("mgx_llg_step_host");
-  LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
-  if (!pl || !e_in || !e_out) return set_error(MGX_ERR_INVALID, "mgx_llg_step_host: null argument");
-  if (pl->p.noise == MGX_NOISE_HOST && !noise)
-    return set_error(MGX_ERR_INVALID, "mgx_llg_step_host: host-noise plan needs a noise buffer");
+// The work of one host-buffer step on stream ms (nc slabs, or one piece when nc == 1): copies in on
+// the copy stream, packing (and the fixed-point split), predictors, correctors, unpacking and copies
+// out; every stream it forks from ms joins ms again at the end, so it can also be captured.
+static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_out, const double* noise,
+                                    uint64_t step, cudaStream_t ms, int nc) {
   const Model* m = pl->model;
   const DevLattice& L = m->d;
   const long long N = L.N;
-  cudaStream_t ms = (cudaStream_t)stream;
-  if (!pl->copy_stream) {
-    // all or nothing: a failed allocation leaves the plan without host buffers
-    cudaError_t err = cudaMalloc(&pl->host_lat, sizeof(double) * 3 * N);
-    if (err == cudaSuccess) err = cudaMalloc(&pl->host_aos, sizeof(double) * 3 * N);
-    for (cudaEvent_t& ev : pl->host_ev)
-      if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->aux_stream, cudaStreamNonBlocking);
-    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
-    if (err != cudaSuccess) {
-      drop_host_buffers(pl);
-      return cuda_error(err, "mgx_llg_step_host buffers");
-    }
-  }
+  const bool fx = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER || pl->precision == MGX_PRECISION_INT48_GATHER;
   cudaStream_t cs = pl->copy_stream;
   cudaEvent_t* ev_in = pl->host_ev;
   cudaEvent_t* ev_out = pl->host_ev + MGX_HOST_CHUNKS;
   cudaEvent_t ev_start = pl->host_ev[2 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[2 * MGX_HOST_CHUNKS + 1];
   cudaEvent_t ev_join_aux = pl->host_ev[2 * MGX_HOST_CHUNKS + 2], ev_join_main = pl->host_ev[2 * MGX_HOST_CHUNKS + 3];
-  // slabs: FP64 and fixed-point-gather stencil plans of at least 2^20 sites with both buffers
-  // page-locked; otherwise one piece
-  const bool fx = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER || pl->precision == MGX_PRECISION_INT48_GATHER;
-  int nc = 1;
-  if ((pl->precision == MGX_PRECISION_FP64 || fx) && L.layout == 0 && m->reach0 >= 0 && N >= (1LL << 20) &&
-      pinned_host(e_in) && pinned_host(e_out)) {
-    nc = std::min(MGX_HOST_CHUNKS, L.L0 / std::max(m->reach0, 1));
-    if (nc < 3) nc = 1;
-  }
   const long long layer = (long long)L.L1 * L.L2;
   auto cell0 = [&](int c) { return (long long)L.L0 * c / nc * layer; };    // first cell of slab c
   MGX_CUDA_TRY(cudaEventRecord(ev_start, ms));
@@ -518,9 +494,107 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
                                    cudaMemcpyDefault, cs));
     }
   }
-  // the copy stream waited for every slab of both compute streams: `stream` continues after all of it
+  // the copy stream waited for every slab of both compute streams: `ms` continues after all of it
   MGX_CUDA_TRY(cudaEventRecord(ev_done, cs));
   MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_done, 0));
+  return MGX_OK;
+}
+
+
+// Copies of host buffers inside one step.  The input goes to the device in axis-0 slabs on the plan's
+// copy stream (each packed into the lattice layout as it lands, and for the fixed-point-gather forms
+// split into its fixed-point copy); the predictor of a slab starts once
+// the slabs it gathers from (its own and its neighbours', every slab at least as thick as the
+// couplings' reach) are in; the corrector runs slab by slab and each finished slab goes back to the
+// host while the next ones are computed.  Consecutive slabs alternate between the caller's stream and
+// a second compute stream, so the blocks of one slab fill the tail of the previous one.  The
+// predictor and corrector kernels, and so the result, are those of mgx_llg_step: only the launch grid
+// is split.
+mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, const double* noise, uint64_t step,
+                             void* stream) {
+  NvtxRange nvtx_range("mgx_llg_step_host");
+  LLGPlan* pl = reinterpret_cast<LLGPlan*>(pp);
+  if (!pl || !e_in || !e_out) return set_error(MGX_ERR_INVALID, "mgx_llg_step_host: null argument");
+  if (pl->p.noise == MGX_NOISE_HOST && !noise)
+    return set_error(MGX_ERR_INVALID, "mgx_llg_step_host: host-noise plan needs a noise buffer");
+  const Model* m = pl->model;
+  const DevLattice& L = m->d;
+  const long long N = L.N;
+  cudaStream_t ms = (cudaStream_t)stream;
+  if (!pl->copy_stream) {
+    // all or nothing: a failed allocation leaves the plan without host buffers
+    cudaError_t err = cudaMalloc(&pl->host_lat, sizeof(double) * 3 * N);
+    if (err == cudaSuccess) err = cudaMalloc(&pl->host_aos, sizeof(double) * 3 * N);
+    for (cudaEvent_t& ev : pl->host_ev)
+      if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->aux_stream, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
+    if (err != cudaSuccess) {
+      drop_host_buffers(pl);
+      return cuda_error(err, "mgx_llg_step_host buffers");
+    }
+  }
+  // slabs: FP64 and fixed-point-gather stencil plans of at least 2^20 sites with both buffers
+  // page-locked; otherwise one piece
+  const bool fx = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER || pl->precision == MGX_PRECISION_INT48_GATHER;
+  int nc = 1;
+  if ((pl->precision == MGX_PRECISION_FP64 || fx) && L.layout == 0 && m->reach0 >= 0 && N >= (1LL << 20) &&
+      pinned_host(e_in) && pinned_host(e_out)) {
+    nc = std::min(MGX_HOST_CHUNKS, L.L0 / std::max(m->reach0, 1));
+    if (nc < 3) nc = 1;
+  }
+  if (nc == 1) {
+    const mgx_status st = enqueue_host_step(pl, e_in, e_out, noise, step, ms, 1);
+    if (st != MGX_OK) return st;
+    MGX_CUDA_TRY(cudaGetLastError());
+    return MGX_OK;
+  }
+  // the slab pipeline: replay the graph captured for these buffers (capture it on first use)
+  const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
+  int slot = -1;
+  for (int k = 0; k < 2; ++k) {
+    const LLGGraph& g = pl->host_graphs[k];
+    if (g.exec && g.e == e_out && pl->host_in[k] == e_in && pl->host_noise[k] == noise &&
+        graph_matches(g, nc, e_out, mode, L))
+      slot = k;
+  }
+  if (slot < 0) {
+    slot = (pl->host_graphs[0].used <= pl->host_graphs[1].used) ? 0 : 1;
+    LLGGraph& g = pl->host_graphs[slot];
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = LLGGraph{};
+    if (!pl->d_step) MGX_CUDA_TRY(cudaMalloc(&pl->d_step, sizeof(unsigned long long)));
+    if (!pl->cap_stream) MGX_CUDA_TRY(cudaStreamCreateWithFlags(&pl->cap_stream, cudaStreamNonBlocking));
+    MGX_CUDA_TRY(cudaStreamBeginCapture(pl->cap_stream, cudaStreamCaptureModeThreadLocal));
+    pl->p.step_base = pl->d_step;
+    const mgx_status es = enqueue_host_step(pl, e_in, e_out, noise, 0, pl->cap_stream, nc);
+    pl->p.step_base = nullptr;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t err = cudaStreamEndCapture(pl->cap_stream, &graph);
+    if (es != MGX_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return es;
+    }
+    if (err != cudaSuccess) return cuda_error(err, "mgx_llg_step_host capture");
+    const cudaError_t ierr = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ierr != cudaSuccess) {
+      g.exec = nullptr;
+      return cuda_error(ierr, "mgx_llg_step_host instantiate");
+    }
+    g.steps = nc;
+    g.e = e_out;
+    g.mode = mode;
+    g.B[0] = L.B0;
+    g.B[1] = L.B1;
+    g.B[2] = L.B2;
+    g.offset = L.cell_offset;
+    pl->host_in[slot] = e_in;
+    pl->host_noise[slot] = noise;
+  }
+  pl->host_graphs[slot].used = ++pl->graph_clock;
+  k_llg_step_set<<<1, 1, 0, ms>>>(pl->d_step, (unsigned long long)step);
+  MGX_CUDA_TRY(cudaGraphLaunch(pl->host_graphs[slot].exec, ms));
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }

@@ -189,8 +189,17 @@ mgx_status fx_build(const Model* m, int limb, bool field_scaled, int ncopies, De
       }
   // per-sublattice scale 2^sigma.  48-bit form: 2^sigma >= every magnitude (every half fits 25 bits;
   // every product is below 2^48, so the accumulators hold 2^14 terms per component).  56-bit form:
-  // 2^sigma >= the sum of all magnitudes of the sublattice, so that |sum J_hi e_hi| <= 2^56 sum |J|
-  // / 2^sigma <= 2^62 whatever the number of couplings: no int64 accumulator can overflow.
+  // 2^sigma >= the sum S of all magnitudes of the sublattice, so |w| = |round(J 2^(56 - sigma))| and
+  // |v| = |round(e 2^56)| are at most 2^56 and their halves |w_hi|, |v_hi| <= 2^28, |w_lo|, |v_lo| <= 2^27.
+  // Per field component, with n couplings (on-site included) and unit spins (sum_d |v_hi,d| <=
+  // sqrt(3) 2^28 + 2):  |sum w_hi v_hi| <= (2^28 + 1)(sum |w| 2^-28 + 1.5 n) < 2^57, and
+  // |sum (w_hi v_lo + w_lo v_hi)| <= 2^27 (2^28 + 1.5 n) + 2^27 n (sqrt(3) 2^28 + 2) < 2^55 (1 + 1.74 n),
+  // below 2^63 for n <= 146: the 56-bit form takes at most 128 couplings per receiving sublattice.
+  if (limb == 28)
+    for (int s = 0; s < ns; ++s)
+      if (off[s + 1] - off[s] + 1 > 128)
+        return set_error(MGX_ERR_UNSUPPORTED, "sublattice %d has %d couplings: the 56-bit fixed-point sum takes at "
+                         "most 127 couplings per site (plus the on-site term)", s, off[s + 1] - off[s]);
   std::vector<int> sigma(ns, 0);
   for (int s = 0; s < MGX_MAX_SUBLATTICES; ++s) fx->scale[s] = 0.0;
   for (int s = 0; s < ns; ++s) {

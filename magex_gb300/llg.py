@@ -81,6 +81,8 @@ def fixed_point_eligible(sc, alpha=0.1, sot=None):
         return False
     if sc.A_site is not None or sc.mu_site is not None or getattr(sc, "terms", None):
         return False
+    if len(sc.bond_src) and np.bincount(np.asarray(sc.bond_src)).max() > 127:
+        return False                     # the 56-bit accumulators take at most 127 couplings per site
     return not sc.has_higher
 
 class GB300LLG:
@@ -98,7 +100,7 @@ class GB300LLG:
             raise NotImplementedError("the quantum thermostat is not implemented by the GB300 kernels")
         if stt:
             raise NotImplementedError("spin-transfer torque (spin-current gradients) is not implemented by the GB300 kernels")
-        if sot and precision != "fp64":
+        if sot and precision not in ("fp64", "auto"):
             raise NotImplementedError("spin-orbit torque needs precision='fp64'")
         if backend not in ("gb300", "auto"):
             raise ValueError("backend must be 'gb300'")

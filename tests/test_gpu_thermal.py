@@ -6,9 +6,9 @@ default_rng noise stream, magex/llg.py:106-122,216-227) on the two-site bcc mode
 tensors, DMI, SIA and B_z = 0.5 T at 300 K (8^3 cells): per run the mean over 10,000 samples, and
 the scatter of those run means (sd_run).  The GPU runs the same model, parameters, run length and
 sampling with in-kernel Philox noise (FP32 Box-Muller of Philox4x32-10 draws), in every step form,
-with four seeds; under the hypothesis that it samples the same distribution its run means scatter
-like the reference's, so the difference of the two averages is compared with
-3 sd_run sqrt(1/8 + 1/4).  magex checks its own thermostat the same way against a known law
+with four seeds (two for the reduced forms); under the hypothesis that it samples the same
+distribution its run means scatter like the reference's, so the difference of the two averages is
+compared with 3 sd_run sqrt(1/8 + 1/n).  magex checks its own thermostat the same way against a known law
 (tests/test_spindyn.py:79-89).  Runs at a temperature 10 % off must fail the same bound, so the
 check tells a wrong noise amplitude from a right one.
 """
@@ -34,23 +34,38 @@ def _system(th):
     return bcc_two_site(L=th["L"], field=(0.0, 0.0, th["Bz"]))
 
 
-def _run_means(sc, th, precision, seeds, T=None):
-    """Per-seed means of E/N and |M| of Philox runs sampled as the reference runs were
-    (ferromagnetic start, `equil` steps, then a sample every `every` steps over `sample` steps)."""
+def _run_means(sc, th, precision, seeds, temps=None):
+    """Per-run means of E/N and |M| of Philox runs sampled as the reference runs were (ferromagnetic
+    start, `equil` steps, then a sample every `every` steps over `sample` steps).  Runs k = (seed,
+    temperature) pairs; the FP64 forms advance all of them as one batched ensemble (each system
+    evolves as a single-system plan with its seed would), the reduced forms one by one."""
+    from magex_gb300.batched import BatchedLLG
     from magex_gb300.llg import GB300LLG
-    E, M = [], []
-    for seed in seeds:
-        sol = GB300LLG(sc, th["alpha"], th["dt"], th["T"] if T is None else T, seed, precision=precision)
-        lat = sol.model.to_lattice(sc.init_spins("ferro"))
-        sol.run_lattice(lat, th["equil"])
-        obs = []
-        for _ in range(th["sample"] // th["every"]):
-            sol.run_lattice(lat, th["every"])
-            obs.append(sol.model.observables(lat).clone())
-        o = torch.stack(obs).cpu().numpy()
-        E.append(float(np.mean(o[:, 0] / sc.N)))
-        M.append(float(np.mean(np.linalg.norm(o[:, 1:4], axis=1) / sc.N)))
-    return {"E": np.array(E), "M": np.array(M)}
+    temps = [th["T"]] * len(seeds) if temps is None else list(temps)
+    nrun = len(seeds)
+    nsamp = th["sample"] // th["every"]
+    if precision in ("fp64", "fp64_fixed"):
+        ens = BatchedLLG([sc] * nrun, th["alpha"], th["dt"], temps, list(seeds), precision=precision)
+        ens.set_spins([sc.init_spins("ferro")] * nrun)
+        ens.run(th["equil"], graph_chunk=100)
+        obs = np.empty((nsamp, nrun, 8))
+        for k in range(nsamp):
+            ens.run(th["every"], graph_chunk=th["every"])
+            obs[k] = ens.observables()
+    else:
+        obs = np.empty((nsamp, nrun, 8))
+        for r, (seed, T) in enumerate(zip(seeds, temps)):
+            sol = GB300LLG(sc, th["alpha"], th["dt"], T, seed, precision=precision)
+            lat = sol.model.to_lattice(sc.init_spins("ferro"))
+            sol.run_lattice(lat, th["equil"])
+            rows = []
+            for _ in range(nsamp):
+                sol.run_lattice(lat, th["every"])
+                rows.append(sol.model.observables(lat).clone())
+            obs[:, r] = torch.stack(rows).cpu().numpy()
+    E = obs[:, :, 0].mean(0) / sc.N
+    M = (np.linalg.norm(obs[:, :, 1:4], axis=2) / sc.N).mean(0)
+    return {"E": E, "M": M}
 
 
 SEEDS = (101, 202, 303, 404)
@@ -68,7 +83,7 @@ def _z(ref, key, means):
 def test_config2_thermal_equilibrium_within_3_sigma_of_reference(cuda, ref, precision):
     th = json.loads(str(ref["params"]))
     sc = _system(th)
-    means = _run_means(sc, th, precision, SEEDS)
+    means = _run_means(sc, th, precision, SEEDS if precision in ("fp64", "fp64_fixed") else SEEDS[:2])
     for key in ("E", "M"):
         z = _z(ref, key, means[key])
         assert z <= 3.0, (precision, key, means[key].tolist(), float(ref[f"{key}_mean"]), z)
@@ -79,7 +94,7 @@ def test_config2_thermal_check_fails_at_10_percent_wrong_temperature(cuda, ref):
     far outside the 3-sigma bound, so a noise amplitude off by 5 % (T off by 10 %) cannot pass."""
     th = json.loads(str(ref["params"]))
     sc = _system(th)
-    for factor in (0.9, 1.1):
-        means = _run_means(sc, th, "fp64", SEEDS, T=factor * th["T"])
-        z = _z(ref, "E", means["E"])
+    means = _run_means(sc, th, "fp64_fixed", SEEDS[:2] * 2, temps=[0.9 * th["T"]] * 2 + [1.1 * th["T"]] * 2)
+    for k, factor in enumerate((0.9, 1.1)):
+        z = _z(ref, "E", means["E"][2 * k:2 * k + 2])
         assert z > 10.0, (factor, means["E"].tolist(), z)
