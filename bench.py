@@ -259,7 +259,8 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
             S[adj.groups.group[b]] = torch.as_tensor(S_bond[b])
     e0 = sc.init_spins("random", seed=1)
     target = torch.as_tensor(sc.init_spins("random", seed=2), device=adj.device)
-    plain = GB300LLG(sc, 0.3, 1e-4, 0.0, 1)
+    plain = GB300LLG(sc, 0.3, 1e-4, 0.0, 1, precision="fp64")      # the all-FP64 forward
+    default = GB300LLG(sc, 0.3, 1e-4, 0.0, 1)                      # the default solver ("auto")
     stream = torch.cuda.current_stream()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
 
@@ -283,6 +284,10 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
         loss.backward()
         if record:
             ev[3].record(stream)
+            lat2 = default.model.to_lattice(e0)
+            ev[4].record(stream)
+            default.run_lattice(lat2, nsteps)
+            ev[5].record(stream)
         torch.cuda.synchronize()
         return theta.grad
 
@@ -291,12 +296,15 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
     t_plain = ev[0].elapsed_time(ev[1])
     t_fwd = ev[1].elapsed_time(ev[2])
     t_bwd = ev[2].elapsed_time(ev[3])
+    t_default = ev[4].elapsed_time(ev[5])
     return {"workload": f"triangular {L}x{L} film, J1=1 meV, D/J=0.3, K=0.05 meV, B_z=2 T, T=0, alpha 0.3, "
                         f"dt 0.1 fs, {nsteps} Heun steps, checkpoint every {seg}, loss sum|e(T)-target|^2, FP64",
             "cache_bytes": cache_bytes,
             "resident_segments": min(len(adj._segments(nsteps)), adj._cache_budget() // (8 * adj.storage_doubles)),
             "forward_plain_ms": t_plain, "forward_checkpointed_ms": t_fwd, "backward_ms": t_bwd,
             "adjoint_over_forward": t_bwd / t_plain, "gradient_total_over_forward": (t_fwd + t_bwd) / t_plain,
+            "default_forward": {"precision": default.precision, "ms": t_default,
+                                "adjoint_over_forward": t_bwd / t_default},
             "grad_J1_D": [float(x) for x in g]}
 
 
@@ -780,6 +788,9 @@ def north_star_summary(line):
         a = line.get(key)
         if a:
             out[key + "_bwd_over_fwd"] = _r(a["adjoint_over_forward"], 3)
+            d = a.get("default_forward")
+            if d and d["precision"] != "fp64":
+                out[key + "_bwd_over_default_fwd"] = _r(d["adjoint_over_forward"], 3)
     c5 = line.get("large_batched_adjoint")
     if c5:
         out["config5"] = {"batched_value": _r(c5["batched_value"]), "speedup_vs_plain": _r(c5["speedup_vs_plain"], 3),

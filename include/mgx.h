@@ -280,6 +280,11 @@ mgx_status mgx_adjoint_forward(mgx_adjoint* a, const double* e0, int32_t nsteps,
 mgx_status mgx_adjoint_backward(mgx_adjoint* a, double* ebar, int32_t nsteps, void* stream);
 mgx_status mgx_adjoint_zero_grads(mgx_adjoint* a, void* stream);
 mgx_status mgx_adjoint_grads(mgx_adjoint* a, double* out, void* stream);
+/* Cubic and higher-uniaxial terms (magex/terms.py:35-75, magex/fast.py:39-64) enter the adjoint
+ * through their Hessian; their parameter gradients, summed over the sites, go to out (device) [3]:
+ * dL/dKc, dL/dK2, dL/dK3 (derivatives with respect to a change of every site's constant by the same
+ * amount; zero when the model has none of those terms). */
+mgx_status mgx_adjoint_grads_onsite_higher(mgx_adjoint* a, double* out, void* stream);
 
 /* ---------------------------------------------------------------- step without allocation
  * No counterpart in the reference.  One Heun / Depondt step like mgx_llg_step, for callers that

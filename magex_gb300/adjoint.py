@@ -18,6 +18,9 @@ kernels (libmgx ``mgx_adjoint_*``) back through the segment.  The last segments 
 to the memory one grants it ("auto", the default: half of the free device memory; 0: recompute every
 segment).  Thermal (Philox) noise is regenerated bit-identically
 from (seed, site, step), so the gradient is the pathwise derivative of the same noisy trajectory.
+The forward and its recomputation run in the form GB300LLG's default would use for the system
+(``precision="auto"``: the exact 56-bit fixed-point exchange sum on lattices where it is faster, FP64
+otherwise); the adjoint kernels themselves are FP64.
 magex itself has no gradients; parity of this module is pinned against central finite differences
 and against torch autograd of a dense FP64 restatement (tests/test_gpu_adjoint.py).
 """
@@ -33,7 +36,7 @@ from . import _lib
 from .constants import GAMMA, K_B, MU_B
 from .device import DeviceModel, stream_ptr
 from .lattice import WIDTH_FULL
-from .llg import _philox_key
+from .llg import _philox_key, auto_fixed
 
 
 class CouplingGroups:
@@ -131,7 +134,7 @@ class AdjointLLG:
     """Forward / adjoint engine of Heun trajectories on one supercell (uniform alpha per run)."""
 
     def __init__(self, sc, groups=None, alpha=0.1, dt=1e-3, temperature=0.0, seed=None, precession=True,
-                 seg_steps=100, cache_bytes="auto", device=None):
+                 seg_steps=100, cache_bytes="auto", precision="auto", device=None):
         if sc.alpha_site is not None or sc.site_T is not None or sc.A_site is not None:
             raise NotImplementedError("the adjoint supports uniform damping, temperature and per-sublattice A")
         if sc.terms or sc.has_higher:
@@ -152,6 +155,13 @@ class AdjointLLG:
         p.integrator = _lib.HEUN
         p.noise = _lib.NOISE_PHILOX if self.T > 0 else _lib.NOISE_NONE
         p.seed = _philox_key(seed)
+        # the forward (and its recomputation) in the form GB300LLG's default would step this system
+        # with: the exact fixed-point exchange sum where "auto" picks it; the adjoint kernels are FP64
+        if precision not in ("auto", "fp64", "fp64_fixed"):
+            raise ValueError("precision must be 'auto', 'fp64' or 'fp64_fixed'")
+        fixed = precision == "fp64_fixed" or (precision == "auto" and auto_fixed(sc, alpha))
+        self.precision = "fp64_fixed" if fixed else "fp64"
+        p.precision = _lib.PRECISION_FP64_FIXED_GATHER if fixed else _lib.PRECISION_FP64
         rg = np.ascontiguousarray(self.groups.group[self.rev_order], np.int32)
         rt = np.ascontiguousarray(self.groups.transposed[self.rev_order], np.int32)
         h = C.c_void_p()
@@ -189,6 +199,39 @@ class AdjointLLG:
             self.handle = None
 
     # ------------------------------------------------------------------ parameters
+    @property
+    def has_higher(self):
+        """The system carries cubic and / or higher-uniaxial anisotropy (magex/terms.py:35-75)."""
+        return self.sc.cubic is not None or self.sc.uniaxial_higher is not None
+
+    def set_higher(self, H):
+        """Uniform cubic / higher-uniaxial constants H = (Kc, K2, K3) (meV) on every site of the forward
+        model; the axes stay the system's.  Only the terms the system has are set."""
+        Kc, K2, K3 = (float(x) for x in np.asarray(H, float).reshape(3))
+        sc, N = self.sc, self.sc.N
+        keep = []
+
+        def arr(x):
+            a = np.full(N, x, np.float64)
+            keep.append(a)
+            return _lib.dptr(a)
+        cub, uni = sc.cubic, sc.uniaxial_higher
+        Cm = None if cub is None else np.ascontiguousarray(np.asarray(cub[1], float).reshape(9))
+        u = None if uni is None else np.ascontiguousarray(np.asarray(uni[2], float).reshape(3))
+        _lib.check(self.lib.mgx_model_set_onsite_higher(
+            self.fwd.handle, None if cub is None else arr(Kc), None if Cm is None else _lib.dptr(Cm),
+            None if uni is None else arr(K2), None if uni is None else arr(K3), None if u is None else _lib.dptr(u)),
+            "mgx_model_set_onsite_higher")
+        _lib.check(self.lib.mgx_adjoint_sync_models(self.handle), "sync_models")
+
+    def higher_params(self):
+        """(Kc, K2, K3) of the system's first site (0 for absent terms)."""
+        sc = self.sc
+        Kc = 0.0 if sc.cubic is None else float(np.asarray(sc.cubic[0], float).reshape(-1)[0])
+        K2 = 0.0 if sc.uniaxial_higher is None else float(np.asarray(sc.uniaxial_higher[0], float).reshape(-1)[0])
+        K3 = 0.0 if sc.uniaxial_higher is None else float(np.asarray(sc.uniaxial_higher[1], float).reshape(-1)[0])
+        return np.array([Kc, K2, K3])
+
     def set_params(self, T, A, B):
         """Load parameter tensors T (G,3,3), A (ns,3,3) and field B (3) into both device stencils."""
         T = np.asarray(T, float).reshape(self.groups.ngroups, 3, 3)
@@ -267,36 +310,53 @@ class AdjointLLG:
         gT = g[:9 * G].view(G, 3, 3).clone()
         gA = g[9 * G:9 * G + 9 * ns].view(9, ns).t().reshape(ns, 3, 3).clone()
         gB = g[9 * G + 9 * ns:].clone()
+        gH = torch.zeros(3, dtype=torch.float64, device=self.device)
+        if self.has_higher:
+            _lib.check(self.lib.mgx_adjoint_grads_onsite_higher(self.handle, C.c_void_p(gH.data_ptr()), stream_ptr()),
+                       "mgx_adjoint_grads_onsite_higher")
+        self.last_grad_higher = gH
         return ebar, gT, gA, gB
 
 
 class _Trajectory(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, e0, T, A, B, adj, nsteps):
-        adj.set_params(T.detach().cpu().numpy(), A.detach().cpu().numpy(), B.detach().cpu().numpy())
+    def forward(ctx, e0, T, A, B, H, adj, nsteps):
+        params = (T.detach().cpu().numpy(), A.detach().cpu().numpy(), B.detach().cpu().numpy(),
+                  None if H is None else H.detach().cpu().numpy())
+        _Trajectory._load(adj, params)
         lat0 = adj.fwd.to_lattice(e0.detach())
         eT, ckpts, cache = adj.forward(lat0, nsteps)
         ctx.adj, ctx.nsteps, ctx.ckpts, ctx.cache = adj, nsteps, ckpts, cache
-        ctx.devs = (e0.device, T.device, A.device, B.device)
-        ctx.params = (T.detach().cpu().numpy(), A.detach().cpu().numpy(), B.detach().cpu().numpy())
+        ctx.devs = (e0.device, T.device, A.device, B.device, None if H is None else H.device)
+        ctx.params = params
         out = adj.fwd.from_lattice(eT)
         return out.to(e0.device)
 
     @staticmethod
+    def _load(adj, params):
+        adj.set_params(*params[:3])
+        if params[3] is not None:
+            adj.set_higher(params[3])
+
+    @staticmethod
     def backward(ctx, grad_eT):
         adj = ctx.adj
-        adj.set_params(*ctx.params)                  # the parameters may have changed since the forward
+        _Trajectory._load(adj, ctx.params)           # the parameters may have changed since the forward
         ebar_T = adj.fwd.to_lattice(grad_eT.detach().contiguous())
         ebar0, gT, gA, gB = adj.backward(ctx.ckpts, ebar_T, ctx.nsteps, ctx.cache)
         ctx.cache = ()
         ge0 = adj.fwd.from_lattice(ebar0)
-        d0, dT, dA, dB = ctx.devs
-        return ge0.to(d0), gT.to(dT), gA.to(dA), gB.to(dB), None, None
+        d0, dT, dA, dB, dH = ctx.devs
+        gH = None if dH is None else adj.last_grad_higher.to(dH)
+        return ge0.to(d0), gT.to(dT), gA.to(dA), gB.to(dB), gH, None, None
 
 
-def llg_trajectory(adj, e0, T, A, B, nsteps):
-    """Spins after nsteps Heun steps from e0 ((N,3) tensor), differentiable in e0, T, A and B."""
-    return _Trajectory.apply(e0, T, A, B, adj, int(nsteps))
+def llg_trajectory(adj, e0, T, A, B, nsteps, H=None):
+    """Spins after nsteps Heun steps from e0 ((N,3) tensor), differentiable in e0, T, A and B, and in
+    H = (Kc, K2, K3), uniform cubic / higher-uniaxial constants, when given (systems with those terms)."""
+    if H is not None and not adj.has_higher:
+        raise ValueError("H (Kc, K2, K3) needs a system with cubic or higher-uniaxial anisotropy")
+    return _Trajectory.apply(e0, T, A, B, H, adj, int(nsteps))
 
 
 _BOND_SITES: dict = {}

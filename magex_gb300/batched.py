@@ -24,7 +24,7 @@ import torch
 from . import _lib
 from .constants import GAMMA, K_B, MU_B
 from .device import DeviceModel, stream_ptr, supercell_from_system
-from .llg import _SUPPORTED, _philox_key, fixed_point_eligible
+from .llg import AUTO_FIXED_MIN_SITES, _SUPPORTED, _philox_key, fixed_point_eligible
 
 
 def _per_system(x, n, name):
@@ -49,9 +49,13 @@ class BatchedLLG:
             raise ValueError("batched systems use precision 'auto', 'fp64' or 'fp64_fixed'")
         self.systems = [supercell_from_system(s) for s in systems]
         if precision == "auto":
-            # the exact fixed-point sum form when every system supports it (as GB300LLG's "auto")
-            ok = all(fixed_point_eligible(sc, a) for sc, a in zip(self.systems, _per_system(alpha, len(self.systems),
-                                                                                              "alpha")))
+            # the exact fixed-point sum form when every system supports it, the ensemble holds at least
+            # AUTO_FIXED_MIN_SITES sites and some system has couplings beyond isotropic numbers (the
+            # per-system choice of GB300LLG's "auto" made for the whole launch)
+            alphas = _per_system(alpha, len(self.systems), "alpha")
+            ok = all(fixed_point_eligible(sc, a) for sc, a in zip(self.systems, alphas))
+            ok = ok and sum(sc.N for sc in self.systems) >= AUTO_FIXED_MIN_SITES
+            ok = ok and any(int(sc.width) != 1 for sc in self.systems)
             precision = "fp64_fixed" if ok else "fp64"
         self.precision = precision
         n = len(self.systems)

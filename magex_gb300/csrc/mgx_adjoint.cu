@@ -24,8 +24,8 @@
 #include <cmath>
 #include <vector>
 
+#include "mgx_fx_step.cuh"
 #include "mgx_observe.cuh"
-#include "mgx_step.cuh"
 
 namespace mgx {
 
@@ -40,6 +40,7 @@ struct AdjDev {
   double* PG;             // [ngroups*9][N] coupling-group gradients per site
   double* PA;             // [9][N] single-ion gradients per site
   double* PB;             // [3][N] field gradients per site
+  double* PH;             // [3][N] gradients w.r.t. the sites' Kc, K2, K3 (cubic / higher uniaxial), or nullptr
 };
 
 struct AdjPlan {
@@ -54,6 +55,7 @@ struct AdjPlan {
   double* work = nullptr; // eacc | pbar | f1bar | g1 | g2 (5 x 3N)
   double* k1 = nullptr;
   double* grads = nullptr;  // reduction output on device
+  double* PH = nullptr;     // [3][N] Kc | K2 | K3 gradient accumulators (used when the model has those terms)
   int2* d_group = nullptr;
   void* sub = nullptr;
   int seg_steps = 0;
@@ -66,6 +68,11 @@ struct AdjPlan {
   cudaGraphExec_t fwd_graph = nullptr, bwd_graph = nullptr;
   int fwd_steps = 0, bwd_steps = 0;
   const double* bwd_ebar = nullptr;
+  // forward (and recomputation) with the exact 56-bit fixed-point exchange sum (MGX_PRECISION_FP64_FIXED_GATHER):
+  // tables of the current couplings and the split copies of e / ep
+  bool fixed = false;
+  DevFX fx{};
+  void* fx_block = nullptr;
 };
 
 // Lattices up to this size replay captured graphs for recomputed segments (larger ones are bound by
@@ -161,6 +168,56 @@ __device__ __forceinline__ void accumulate_onsite(const AdjDev& A, long long N, 
   store_cells<3>(A.PB + q, N, pb);
 }
 
+// Adjoint of the cubic and higher-uniaxial fields at a site with spin v (magex/terms.py:35-75):
+// B_h = -grad E_h(v) / (mu mu_B), so with g = 2 Hbar / (mu mu_B) the spin adjoint gains
+// (dB_h/dv)^T Hbar = -Hess E_h(v) g / 2 (returned in ox, oy, oz) and the parameter accumulators
+// PH[Kc | K2 | K3] gain Hbar . dB_h/dK = -(g / 2) . d(grad E_h)/dK.
+//   cubic, a = C v, S = |a|^2:  dE/da_i = 2 Kc a_i (S - a_i^2),
+//     (Hess_a w)_i = 2 Kc [(S - a_i^2) w_i + 2 a_i (a.w - a_i w_i)],  Hess_v = C^T Hess_a C;
+//   uniaxial, c = v.u:  grad E = (-4 K2 c^3 - 6 K3 c^5) u,  Hess = (-12 K2 c^2 - 30 K3 c^4) u u^T.
+__device__ __forceinline__ void higher_onsite_adjoint(const AdjDev& A, long long q, double vx, double vy, double vz,
+                                                      double gx, double gy, double gz, double& ox, double& oy,
+                                                      double& oz) {
+  const DevLattice& L = A.F;
+  const long long N = L.N;
+  ox = oy = oz = 0.0;
+  const double hx = 0.5 * gx, hy = 0.5 * gy, hz = 0.5 * gz;       // Hbar / (mu mu_B)
+  double ph[3];
+  load_cells<3>(A.PH + q, N, ph);
+  if (L.Kc_site) {
+    const double* C = L.C;
+    const double a1 = C[0] * vx + C[1] * vy + C[2] * vz;
+    const double a2 = C[3] * vx + C[4] * vy + C[5] * vz;
+    const double a3 = C[6] * vx + C[7] * vy + C[8] * vz;
+    const double w1 = C[0] * hx + C[1] * hy + C[2] * hz;              // w = C h
+    const double w2 = C[3] * hx + C[4] * hy + C[5] * hz;
+    const double w3 = C[6] * hx + C[7] * hy + C[8] * hz;
+    const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3, S = q1 + q2 + q3;
+    const double aw = a1 * w1 + a2 * w2 + a3 * w3;
+    const double kc = L.Kc_site[q];
+    // -(h . d grad / dKc) = -(w . d), d_i = 2 a_i (S - a_i^2)
+    ph[0] -= 2.0 * (w1 * a1 * (S - q1) + w2 * a2 * (S - q2) + w3 * a3 * (S - q3));
+    const double t1 = 2.0 * kc * ((S - q1) * w1 + 2.0 * a1 * (aw - a1 * w1));
+    const double t2 = 2.0 * kc * ((S - q2) * w2 + 2.0 * a2 * (aw - a2 * w2));
+    const double t3 = 2.0 * kc * ((S - q3) * w3 + 2.0 * a3 * (aw - a3 * w3));
+    ox -= C[0] * t1 + C[3] * t2 + C[6] * t3;                           // -C^T Hess_a C h
+    oy -= C[1] * t1 + C[4] * t2 + C[7] * t3;
+    oz -= C[2] * t1 + C[5] * t2 + C[8] * t3;
+  }
+  if (L.K2_site) {
+    const double* u = L.u;
+    const double c = vx * u[0] + vy * u[1] + vz * u[2], c2 = c * c;
+    const double hu = hx * u[0] + hy * u[1] + hz * u[2];
+    ph[1] += 4.0 * c2 * c * hu;
+    ph[2] += 6.0 * c2 * c2 * c * hu;
+    const double f = -(-12.0 * L.K2_site[q] * c2 - 30.0 * L.K3_site[q] * c2 * c2) * hu;
+    ox += f * u[0];
+    oy += f * u[1];
+    oz += f * u[2];
+  }
+  store_cells<3>(A.PH + q, N, ph);
+}
+
 // Transposed gather sum_rev J^T g_nbr at site q of the reverse stencil, with the parameter-gradient
 // outer products added to PG once per group run: a forward coupling with tensor T_g contributes
 // g_nbr (x) v, one with T_g^T contributes v (x) g_nbr (v = own p or e), so each run keeps the sums of
@@ -239,22 +296,47 @@ __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __
 
 // ---------------------------------------------------------------- forward recomputation (stores states)
 // (step index: P.step_base[0] + step inside a captured segment, step otherwise)
-template <int NOISE>
+// (HIGHER: the EXTRA bodies, which add the cubic / higher-uniaxial fields; the adjoint's forward
+// parameters carry no spin-orbit torque or extra field)
+template <int NOISE, bool HIGHER>
 __global__ void __launch_bounds__(256) k_fwd_pred(const DevLattice L, const DevLLG P, const double* __restrict__ e,
                                                   uint64_t step, double* __restrict__ H1, double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < L.N)
-    predict_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, P.step_base ? *P.step_base + step : step, H1, R);
+    predict_site<9, NOISE, MGX_INTEGRATOR_HEUN, HIGHER>(L, P, e, nullptr, q, P.step_base ? *P.step_base + step : step,
+                                                        H1, R);
 }
 
-template <int NOISE>
+template <int NOISE, bool HIGHER>
 __global__ void __launch_bounds__(256) k_fwd_corr(const DevLattice L, const DevLLG P, double* __restrict__ e,
                                                   uint64_t step, double* __restrict__ H2, double* __restrict__ eout,
                                                   double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < L.N)
-    correct_site<9, NOISE, MGX_INTEGRATOR_HEUN>(L, P, e, nullptr, q, P.step_base ? *P.step_base + step : step, H2,
-                                                eout, nullptr, R + L.N);
+    correct_site<9, NOISE, MGX_INTEGRATOR_HEUN, HIGHER>(L, P, e, nullptr, q, P.step_base ? *P.step_base + step : step,
+                                                        H2, eout, nullptr, R + L.N);
+}
+
+// the same with the exact fixed-point exchange sum: the split of E is in F.es (written by the previous
+// corrector, or by the split kernel before the first step); the corrector writes E_next and its split
+template <int NOISE, bool HIGHER>
+__global__ void __launch_bounds__(256, 4) k_fwd_pred_fx(const DevLattice L, const DevLLG P, const DevFX F,
+                                                        const double* __restrict__ e, uint64_t step,
+                                                        double* __restrict__ H1, double* __restrict__ R) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < L.N)
+    fx_predict_site<NOISE, MGX_INTEGRATOR_HEUN, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(
+        L, P, F, e, nullptr, q, P.step_base ? *P.step_base + step : step, H1, R);
+}
+
+template <int NOISE, bool HIGHER>
+__global__ void __launch_bounds__(256, 4) k_fwd_corr_fx(const DevLattice L, const DevLLG P, const DevFX F,
+                                                        double* __restrict__ e, uint64_t step, double* __restrict__ H2,
+                                                        double* __restrict__ eout, double* __restrict__ R) {
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < L.N)
+    fx_correct_site<NOISE, MGX_INTEGRATOR_HEUN, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(
+        L, P, F, e, nullptr, q, P.step_base ? *P.step_base + step : step, H2, eout, R + L.N);
 }
 
 __global__ void k_adj_step_set(unsigned long long* c, unsigned long long v) { *c = v; }
@@ -297,6 +379,13 @@ __device__ __forceinline__ void adj_local_site(const AdjDev& A, long long q, con
     pbx -= a[0] * gx + a[3] * gy + a[6] * gz;     // -A^T g
     pby -= a[1] * gx + a[4] * gy + a[7] * gz;
     pbz -= a[2] * gx + a[5] * gy + a[8] * gz;
+  }
+  if (A.PH) {
+    double hx, hy, hz;
+    higher_onsite_adjoint(A, q, px, py, pz, gx, gy, gz, hx, hy, hz);
+    pbx += hx;
+    pby += hy;
+    pbz += hz;
   }
   accumulate_onsite(A, N, q, L.has_A != 0, gx, gy, gz, px, py, pz, Hbx, Hby, Hbz);
   store3(eacc, N, q, ybx, yby, ybz);
@@ -376,6 +465,13 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
     ay -= a[1] * gx + a[4] * gy + a[7] * gz;
     az -= a[2] * gx + a[5] * gy + a[8] * gz;
   }
+  if (A.PH) {
+    double hx, hy, hz;
+    higher_onsite_adjoint(A, q, ex, ey, ez, gx, gy, gz, hx, hy, hz);
+    ax += hx;
+    ay += hy;
+    az += hz;
+  }
   accumulate_onsite(A, N, q, L.has_A != 0, gx, gy, gz, ex, ey, ez, Hbx, Hby, Hbz);
   store3(eacc, N, q, ax, ay, az);
   store3(g1, N, q, gx, gy, gz);
@@ -443,23 +539,67 @@ static double* seg_ptr(const AdjPlan* a, int n, int k) {
 
 // The kernels of a forward segment of nsteps steps from the spins in storage slot 0 (step index
 // step0 + n, or the device counter plus n when P.step_base is set).
+template <int NOISE, bool HIGHER>
+static void launch_adj_step_fx(const AdjPlan* a, const DevLLG& P, double* E, uint64_t step, double* H1, double* H2,
+                               double* E1, double* R, unsigned grid, int tpb, cudaStream_t st) {
+  const DevLattice& L = a->fwd->d;
+  k_fwd_pred_fx<NOISE, HIGHER><<<grid, tpb, 0, st>>>(L, P, a->fx, E, step, H1, R);
+  k_fwd_corr_fx<NOISE, HIGHER><<<grid, tpb, 0, st>>>(L, P, a->fx, E, step, H2, E1, R);
+}
+
 static void enqueue_adj_forward(const AdjPlan* a, const DevLLG& P0, int nsteps, uint64_t step0, cudaStream_t st) {
   const DevLattice& L = a->fwd->d;
   const long long N = L.N;
   const int tpb = site_block_size(N);
   const unsigned grid = (unsigned)((N + tpb - 1) / tpb);
+  if (a->fixed) {
+    // the split of the first spins; every corrector then writes the split of the spins it produces
+    enqueue_fx_split_n(seg_ptr(a, 0, SEG_E), a->fx.es, 3 * N, 28, st);
+    const bool hi = has_higher_onsite(L);
+    for (int n = 0; n < nsteps; ++n) {
+      DevLLG P = P0;
+      P.ep = seg_ptr(a, n, SEG_P);
+      double* E = seg_ptr(a, n, SEG_E);
+      double* R = seg_ptr(a, n, SEG_R);
+      double* H1 = seg_ptr(a, n, SEG_H1);
+      double* H2 = seg_ptr(a, n, SEG_H2);
+      double* E1 = seg_ptr(a, n + 1, SEG_E);
+      const uint64_t step = step0 + (uint64_t)n;
+      if (a->noise == MGX_NOISE_PHILOX)
+        hi ? launch_adj_step_fx<MGX_NOISE_PHILOX, true>(a, P, E, step, H1, H2, E1, R, grid, tpb, st)
+           : launch_adj_step_fx<MGX_NOISE_PHILOX, false>(a, P, E, step, H1, H2, E1, R, grid, tpb, st);
+      else
+        hi ? launch_adj_step_fx<MGX_NOISE_NONE, true>(a, P, E, step, H1, H2, E1, R, grid, tpb, st)
+           : launch_adj_step_fx<MGX_NOISE_NONE, false>(a, P, E, step, H1, H2, E1, R, grid, tpb, st);
+    }
+    return;
+  }
   for (int n = 0; n < nsteps; ++n) {
     DevLLG P = P0;
     P.ep = seg_ptr(a, n, SEG_P);
     double* E = seg_ptr(a, n, SEG_E);
     double* R = seg_ptr(a, n, SEG_R);
     const uint64_t step = step0 + (uint64_t)n;
+    double* H1 = seg_ptr(a, n, SEG_H1);
+    double* H2 = seg_ptr(a, n, SEG_H2);
+    double* E1 = seg_ptr(a, n + 1, SEG_E);
+    const bool hi = has_higher_onsite(L);
     if (a->noise == MGX_NOISE_PHILOX) {
-      k_fwd_pred<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
-      k_fwd_corr<MGX_NOISE_PHILOX><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
+      if (hi) {
+        k_fwd_pred<MGX_NOISE_PHILOX, true><<<grid, tpb, 0, st>>>(L, P, E, step, H1, R);
+        k_fwd_corr<MGX_NOISE_PHILOX, true><<<grid, tpb, 0, st>>>(L, P, E, step, H2, E1, R);
+      } else {
+        k_fwd_pred<MGX_NOISE_PHILOX, false><<<grid, tpb, 0, st>>>(L, P, E, step, H1, R);
+        k_fwd_corr<MGX_NOISE_PHILOX, false><<<grid, tpb, 0, st>>>(L, P, E, step, H2, E1, R);
+      }
     } else {
-      k_fwd_pred<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H1), R);
-      k_fwd_corr<MGX_NOISE_NONE><<<grid, tpb, 0, st>>>(L, P, E, step, seg_ptr(a, n, SEG_H2), seg_ptr(a, n + 1, SEG_E), R);
+      if (hi) {
+        k_fwd_pred<MGX_NOISE_NONE, true><<<grid, tpb, 0, st>>>(L, P, E, step, H1, R);
+        k_fwd_corr<MGX_NOISE_NONE, true><<<grid, tpb, 0, st>>>(L, P, E, step, H2, E1, R);
+      } else {
+        k_fwd_pred<MGX_NOISE_NONE, false><<<grid, tpb, 0, st>>>(L, P, E, step, H1, R);
+        k_fwd_corr<MGX_NOISE_NONE, false><<<grid, tpb, 0, st>>>(L, P, E, step, H2, E1, R);
+      }
     }
   }
 }
@@ -490,6 +630,15 @@ static void enqueue_adj_backward(const AdjPlan* a, double* ebar, int nsteps, cud
                                                nullptr, nullptr, nullptr);
     }
   }
+}
+
+// (Re)build the fixed-point tables from the forward model's current couplings and on-site tensors
+// (called at creation and whenever the models change), keeping two split arrays of 3 N.
+static mgx_status build_adj_fx(AdjPlan* a) {
+  if (!a->fixed) return MGX_OK;
+  if (a->fx_block) cudaFree(a->fx_block);
+  a->fx_block = nullptr;
+  return fx_build(a->fwd, 28, true, 2, &a->fx, &a->fx_block);
 }
 
 static void drop_adj_graphs(AdjPlan* a) {
@@ -533,8 +682,6 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   *out = nullptr;
   if (F->d.layout != 0 || R->d.layout != 0)
     return set_error(MGX_ERR_UNSUPPORTED, "the adjoint is implemented for lattice stencils, not neighbour lists");
-  if (has_higher_onsite(F->d) || has_higher_onsite(R->d))
-    return set_error(MGX_ERR_UNSUPPORTED, "the adjoint does not include cubic / higher uniaxial anisotropy");
   if (F->d.width != 9 || R->d.width != 9)
     return set_error(MGX_ERR_INVALID, "the adjoint needs full-tensor (width 9) forward and reverse models");
   if (F->d.ns != R->d.ns || F->d.L0 != R->d.L0 || F->d.L1 != R->d.L1 || F->d.L2 != R->d.L2 ||
@@ -545,7 +692,9 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   if (ngroups < 1 || ngroups > 4096) return set_error(MGX_ERR_INVALID, "ngroups must be in 1..4096");
   if (R->nbond > 0 && (!rev_group || !rev_transposed)) return set_error(MGX_ERR_INVALID, "group arrays are required");
   if (p->alpha_site) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint supports a uniform damping only");
-  if (p->precision != MGX_PRECISION_FP64) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint uses the FP64 gather");
+  if (p->precision != MGX_PRECISION_FP64 && p->precision != MGX_PRECISION_FP64_FIXED_GATHER)
+    return set_error(MGX_ERR_UNSUPPORTED, "the adjoint runs its forward in the FP64 form (0) or the FP64 form with "
+                     "the exact fixed-point exchange sum (3)");
   if (p->integrator != MGX_INTEGRATOR_HEUN) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint is implemented for heun");
   if (p->noise == MGX_NOISE_HOST) return set_error(MGX_ERR_UNSUPPORTED, "the adjoint recomputes noise: use none or philox");
   if (!(p->dt > 0.0)) return set_error(MGX_ERR_INVALID, "dt must be positive");
@@ -560,6 +709,7 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   a->rev = R;
   a->seg_cap = seg_steps;
   a->noise = p->noise;
+  a->fixed = p->precision == MGX_PRECISION_FP64_FIXED_GATHER;
   const long long N = F->d.N;
   const int ns = F->d.ns;
   const double gamma = 0.1760859630;
@@ -573,6 +723,8 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   if (err == cudaSuccess) err = cudaMalloc(&a->d.PG, sizeof(double) * 9 * (size_t)ngroups * N);
   if (err == cudaSuccess) err = cudaMalloc(&a->d.PA, sizeof(double) * 9 * (size_t)N);
   if (err == cudaSuccess) err = cudaMalloc(&a->d.PB, sizeof(double) * 3 * (size_t)N);
+  if (err == cudaSuccess) err = cudaMalloc(&a->PH, sizeof(double) * 3 * (size_t)N);
+  if (err == cudaSuccess) err = cudaMemset(a->PH, 0, sizeof(double) * 3 * (size_t)N);
   if (err == cudaSuccess) err = cudaMalloc(&a->grads, sizeof(double) * (9 * (size_t)ngroups + 9 * ns + 3));
   if (err == cudaSuccess) err = cudaMalloc(&a->sub, sizeof(double) * 3 * ns);
   if (err == cudaSuccess) err = cudaMalloc(&a->d_step, sizeof(unsigned long long));
@@ -595,6 +747,7 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   AdjDev& d = a->d;
   d.F = F->d;
   d.R = R->d;
+  d.PH = has_higher_onsite(F->d) ? a->PH : nullptr;
   d.group = a->d_group;
   d.ngroups = ngroups;
   d.dt = p->dt;
@@ -615,6 +768,11 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   P.alpha_site = P.pre_site = P.sigma_site = nullptr;
   P.ep = nullptr;
   P.k1 = a->k1;
+  const mgx_status fs = build_adj_fx(a);
+  if (fs != MGX_OK) {
+    mgx_adjoint_destroy(reinterpret_cast<mgx_adjoint*>(a));
+    return fs;
+  }
   *out = reinterpret_cast<mgx_adjoint*>(a);
   return MGX_OK;
 }
@@ -623,6 +781,7 @@ mgx_status mgx_adjoint_destroy(mgx_adjoint* aa) {
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
   if (!a) return MGX_OK;
   drop_adj_graphs(a);
+  if (a->fx_block) cudaFree(a->fx_block);
   if (a->cap_stream) cudaStreamDestroy(a->cap_stream);
   cudaFree(a->d_step);
   cudaFree(a->own_seg);
@@ -632,6 +791,7 @@ mgx_status mgx_adjoint_destroy(mgx_adjoint* aa) {
   cudaFree(a->d.PG);
   cudaFree(a->d.PA);
   cudaFree(a->d.PB);
+  cudaFree(a->PH);
   cudaFree(a->grads);
   cudaFree(a->sub);
   delete a;
@@ -653,8 +813,9 @@ mgx_status mgx_adjoint_sync_models(mgx_adjoint* aa) {
   if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_sync_models: null argument");
   a->d.F = a->fwd->d;
   a->d.R = a->rev->d;
+  a->d.PH = has_higher_onsite(a->fwd->d) ? a->PH : nullptr;
   drop_adj_graphs(a);
-  return MGX_OK;
+  return build_adj_fx(a);
 }
 
 int64_t mgx_adjoint_storage_doubles(const mgx_adjoint* aa) {
@@ -740,6 +901,7 @@ mgx_status mgx_adjoint_zero_grads(mgx_adjoint* aa, void* stream) {
   MGX_CUDA_TRY(cudaMemsetAsync(a->d.PG, 0, sizeof(double) * 9 * (size_t)a->d.ngroups * N, st));
   MGX_CUDA_TRY(cudaMemsetAsync(a->d.PA, 0, sizeof(double) * 9 * (size_t)N, st));
   MGX_CUDA_TRY(cudaMemsetAsync(a->d.PB, 0, sizeof(double) * 3 * (size_t)N, st));
+  MGX_CUDA_TRY(cudaMemsetAsync(a->PH, 0, sizeof(double) * 3 * (size_t)N, st));
   return MGX_OK;
 }
 
@@ -753,6 +915,15 @@ mgx_status mgx_adjoint_grads(mgx_adjoint* aa, double* out, void* stream) {
   k_sum_rows<<<9 * G, 256, 0, st>>>(a->d.PG, N, N, out);
   k_sum_rows<<<9 * ns, 256, 0, st>>>(a->d.PA, L.ncell, L.ncell, out + 9 * G);   // rows (component k, sublattice s)
   k_sum_rows<<<3, 256, 0, st>>>(a->d.PB, N, N, out + 9 * G + 9 * ns);
+  MGX_CUDA_TRY(cudaGetLastError());
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_grads_onsite_higher(mgx_adjoint* aa, double* out, void* stream) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a || !out) return set_error(MGX_ERR_INVALID, "mgx_adjoint_grads_onsite_higher: null argument");
+  const long long N = a->fwd->d.N;
+  k_sum_rows<<<3, 256, 0, (cudaStream_t)stream>>>(a->PH, N, N, out);
   MGX_CUDA_TRY(cudaGetLastError());
   return MGX_OK;
 }

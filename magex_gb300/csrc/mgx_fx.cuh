@@ -17,9 +17,10 @@ __device__ __forceinline__ int2 fx_halves(long long v) {
   return make_int2((int)hi, (int)(v - (hi << LIMB)));
 }
 
+// round(x 2^(2 LIMB)) (ties to even) in two halves, on the integer pipes
 template <int LIMB>
 __device__ __forceinline__ int2 fx_split(double x) {
-  return fx_halves<LIMB>(__double2ll_rn(x * (double)(1LL << (2 * LIMB))));
+  return fx_halves<LIMB>(double_to_ll_scaled(x, 2 * LIMB));
 }
 
 __device__ __forceinline__ long long mad_wide(int a, int b, long long c) {

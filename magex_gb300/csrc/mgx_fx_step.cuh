@@ -25,14 +25,16 @@ __device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, c
   }
 }
 
-// 56-bit form: field in FP64, (hh + x 2^-28) 2^(sigma - 56) with one final rounding
+// 56-bit form: field in FP64 = (hh + x 2^-28) 2^(sigma - 56): x rounded to units of 2^(sigma - 56)
+// in integer arithmetic (|t| < 2^58), then t converted to FP64 and scaled by the power of two in one
+// rounding, all on the integer pipes
 __device__ __forceinline__ void fx_gather64(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
                                             long long q, int s, int c0, int c1, int c2, double h[3]) {
   FxAcc a;
   fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
-  const double sc = F.scale[s];
+  const int e2 = F.scale_exp[s];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) h[c] = fma((double)a.x[c], 3.7252902984619141e-9, (double)a.hh[c]) * sc;
+  for (int c = 0; c < 3; ++c) h[c] = ll_to_double_scaled(a.hh[c] + ((a.x[c] + (1LL << 27)) >> 28), e2);
 }
 
 // spin of the site as a (hi, lo) float pair from its fixed-point halves (exact)
@@ -113,11 +115,13 @@ __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P,
 }
 
 // Predictor of site q (0 <= q < L.N) of the fixed-point forms: writes P.ep, P.k1 and the split F.eps at q.
-// HIGHER: the 56-bit form with the model's cubic / higher-uniaxial terms.
+// HIGHER: the 56-bit form with the model's cubic / higher-uniaxial terms.  The adjoint's recomputation
+// (56-bit Heun form) also stores the total field (Hout) and the inverse norm of the predictor (rout).
 template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
 __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 const double* __restrict__ e, const double* __restrict__ noise,
-                                                long long q, uint64_t step) {
+                                                long long q, uint64_t step, double* __restrict__ Hout = nullptr,
+                                                double* __restrict__ rout = nullptr) {
   constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   const long long N = L.N;
   const double ex = e[q], ey = e[N + q], ez = e[2 * N + q];
@@ -125,6 +129,9 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
     P.ep[q] = ex; P.ep[N + q] = ey; P.ep[2 * N + q] = ez;
     P.k1[q] = 0.0; P.k1[N + q] = 0.0; P.k1[2 * N + q] = 0.0;
     F.eps[q] = F.es[q]; F.eps[N + q] = F.es[N + q]; F.eps[2 * N + q] = F.es[2 * N + q];
+    if (Hout) {
+      Hout[q] = 0.0; Hout[N + q] = 0.0; Hout[2 * N + q] = 0.0;
+    }
     return;
   }
   int s, c0, c1, c2;
@@ -134,6 +141,9 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
     if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
       double bx, by, bz;
       fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
+      if (Hout) {
+        Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
+      }
       llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
               f[2]);
     } else {
@@ -143,6 +153,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
     y = fma(P.dt, f[1], ey);
     z = fma(P.dt, f[2], ez);
     const double r = rsqrt(x * x + y * y + z * z);
+    if (rout) rout[q] = r;
     x *= r; y *= r; z *= r;
   } else {
     double bx, by, bz;
@@ -158,13 +169,24 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
   F.eps[q] = fx_split<LIMB>(x); F.eps[N + q] = fx_split<LIMB>(y); F.eps[2 * N + q] = fx_split<LIMB>(z);
 }
 
-// Corrector of site q: reads the neighbours' F.eps, P.k1 and e at q, writes e and its split F.es at q.
+// Corrector of site q: reads the neighbours' F.eps, P.k1 and e at q, writes e and its split F.es at q
+// (the new spins to eout instead of e when given; Hout and rout as in fx_predict_site).
 template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
 __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 double* __restrict__ e, const double* __restrict__ noise, long long q,
-                                                uint64_t step) {
+                                                uint64_t step, double* __restrict__ Hout = nullptr,
+                                                double* __restrict__ eout = nullptr,
+                                                double* __restrict__ rout = nullptr) {
   constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
-  if (L.pinned && L.pinned[q]) return;                 // e and its split stay as they are
+  if (L.pinned && L.pinned[q]) {                       // e and its split stay as they are
+    if (eout) {
+      eout[q] = e[q]; eout[L.N + q] = e[L.N + q]; eout[2 * L.N + q] = e[2 * L.N + q];
+    }
+    if (Hout) {
+      Hout[q] = 0.0; Hout[L.N + q] = 0.0; Hout[2 * L.N + q] = 0.0;
+    }
+    return;
+  }
   const long long N = L.N;
   int s, c0, c1, c2;
   site_coords(L, q, s, c0, c1, c2);
@@ -176,6 +198,9 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
       const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
       double bx, by, bz;
       fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
+      if (Hout) {
+        Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
+      }
       llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, f[0], f[1],
               f[2]);
     } else {
@@ -194,8 +219,10 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
     rotate(x, y, z, P.half_dt * (k1x + wx), P.half_dt * (k1y + wy), P.half_dt * (k1z + wz));
   }
   const double r = rsqrt(x * x + y * y + z * z);
+  if (rout) rout[q] = r;
   x *= r; y *= r; z *= r;
-  e[q] = x; e[N + q] = y; e[2 * N + q] = z;
+  double* o = eout ? eout : e;
+  o[q] = x; o[N + q] = y; o[2 * N + q] = z;
   F.es[q] = fx_split<LIMB>(x); F.es[N + q] = fx_split<LIMB>(y); F.es[2 * N + q] = fx_split<LIMB>(z);
 }
 

@@ -138,6 +138,7 @@ struct DevFX {
   const int2* lin;               // [nbond] (linear offset of the neighbour of an interior cell, signed R2)
   int4 reach[MGX_MAX_SUBLATTICES];
   double scale[MGX_MAX_SUBLATTICES];  // 2^(sigma_s - 2 limb): value of one unit of the accumulator
+  int scale_exp[MGX_MAX_SUBLATTICES];  // sigma_s - 2 limb (the same scale as a power of two)
   float2 alpha[MGX_MAX_SUBLATTICES], pre[MGX_MAX_SUBLATTICES], sig[MGX_MAX_SUBLATTICES];
   float2 B[3];                   // (hi, lo) split of the external field, refreshed at every launch
   int2* es;                      // [3][N] fixed-point split of e
@@ -181,10 +182,13 @@ struct LLGPlan {
   unsigned long long* d_step = nullptr;
   // step on host buffers (mgx_llg_step_host): device copies of the spins, the copy stream and a
   // second compute stream (consecutive slabs run on alternate streams so each fills the other's tail)
-  cudaStream_t copy_stream = nullptr, aux_stream = nullptr;
+  // (and a pack stream: the copies in run back to back on the copy stream while each landed slab is
+  // packed into the lattice layout on the pack stream)
+  cudaStream_t copy_stream = nullptr, aux_stream = nullptr, pack_stream = nullptr;
   double* host_lat = nullptr;    // [3][N] lattice layout
   double* host_aos = nullptr;    // [N][3] magex order (staging of the copies)
-  cudaEvent_t host_ev[2 * MGX_HOST_CHUNKS + 4] = {};  // in[c] | out[c] | start | done | joined aux | joined main
+  // in[c] (packed) | out[c] (unpacked) | copied[c] | start | done | joined aux | joined main
+  cudaEvent_t host_ev[3 * MGX_HOST_CHUNKS + 4] = {};
   // the slab pipeline of a host-buffer step captured as a graph (step index from d_step), for the
   // last two (input, output) buffer pairs: replaying it costs one launch instead of ~250 API calls
   LLGGraph host_graphs[2];
@@ -432,6 +436,65 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
 
 // Three N(0,1) draws for (site, step) by Box-Muller on one Philox block.  The draws are computed
 // in fp32 (their statistical quality, not their rounding, matters) and widened to fp64.
+// ------------------------------------------------------------------ exact conversions on the integer pipes
+// GB300 runs FP64-width conversions (I2F.F64, F2I.F64, F2F.F64) on its FP64 pipe, 16 cycles per warp
+// instruction like a DFMA.  These do the same conversions with integer instructions on the bit
+// patterns (IEEE 754 binary32 / binary64), with the same rounding (to nearest, ties to even).
+
+// float -> double, exactly (normal floats by moving exponent and mantissa; zero and subnormals, which
+// a Box-Muller draw almost never yields, through the hardware conversion)
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int ex = (b >> 23) & 0xFFu;
+  if (ex == 0u || ex == 0xFFu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(b >> 31) << 63) | ((unsigned long long)(ex + 896u) << 52) |
+                                  ((unsigned long long)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// (double)t * 2^e2 rounded to nearest even, for |t| < 2^63 and a normal result
+__device__ __forceinline__ double ll_to_double_scaled(long long t, int e2) {
+  if (t == 0) return 0.0;
+  const unsigned long long sgn = t < 0 ? (1ULL << 63) : 0ULL;
+  const unsigned long long a = t < 0 ? 0ULL - (unsigned long long)t : (unsigned long long)t;
+  int msb = 63 - __clzll((long long)a);
+  unsigned long long m;
+  if (msb <= 52) {
+    m = a << (52 - msb);
+  } else {
+    const int sh = msb - 52;
+    m = a >> sh;
+    const unsigned long long rem = a & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+    m += (rem > half || (rem == half && (m & 1ULL))) ? 1ULL : 0ULL;
+    if (m >> 53) {
+      m >>= 1;
+      ++msb;
+    }
+  }
+  return __longlong_as_double(
+      (long long)(sgn | ((unsigned long long)(msb + e2 + 1023) << 52) | (m & ((1ULL << 52) - 1))));
+}
+
+// round(x * 2^k) to nearest even, for |x 2^k| < 2^62 (the fixed-point spins: |x| <= 1 + 2^-52)
+__device__ __forceinline__ long long double_to_ll_scaled(double x, int k) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((u >> 52) & 0x7FF);
+  if (E == 0) return 0;                                  // zero or subnormal: |x 2^k| < 1/2
+  const unsigned long long m = (u & ((1ULL << 52) - 1)) | (1ULL << 52);
+  const int sh = E - 1075 + k;                           // |x 2^k| = m 2^sh
+  unsigned long long v;
+  if (sh >= 0) {
+    v = m << sh;
+  } else if (sh < -54) {
+    v = 0;
+  } else {
+    const int r = -sh;
+    const unsigned long long q = m >> r, rem = m & ((1ULL << r) - 1), half = 1ULL << (r - 1);
+    v = q + ((rem > half || (rem == half && (q & 1ULL))) ? 1ULL : 0ULL);
+  }
+  return (u >> 63) ? -(long long)v : (long long)v;
+}
+
 __device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uint64_t step, double& g0, double& g1,
                                                double& g2) {
   const uint4 r = philox4x32_10(make_uint4((uint32_t)site, (uint32_t)(site >> 32), (uint32_t)step,
@@ -445,9 +508,9 @@ __device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uin
   const float m3 = sqrtf(-2.0f * logf(u3));
   float s1, c1;
   sincospif(2.0f * v1, &s1, &c1);
-  g0 = (double)(m1 * c1);
-  g1 = (double)(m1 * s1);
-  g2 = (double)(m3 * cospif(2.0f * v3));
+  g0 = f32_to_f64(m1 * c1);
+  g1 = f32_to_f64(m1 * s1);
+  g2 = f32_to_f64(m3 * cospif(2.0f * v3));
 }
 
 }  // namespace mgx

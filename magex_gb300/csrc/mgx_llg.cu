@@ -217,7 +217,8 @@ static void drop_host_buffers(LLGPlan* pl) {
   }
   if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
   if (pl->aux_stream) cudaStreamDestroy(pl->aux_stream);
-  pl->copy_stream = pl->aux_stream = nullptr;
+  if (pl->pack_stream) cudaStreamDestroy(pl->pack_stream);
+  pl->copy_stream = pl->aux_stream = pl->pack_stream = nullptr;
 }
 
 }  // namespace mgx
@@ -434,22 +435,32 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
   const DevLattice& L = m->d;
   const long long N = L.N;
   const bool fx = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER || pl->precision == MGX_PRECISION_INT48_GATHER;
-  cudaStream_t cs = pl->copy_stream;
+  cudaStream_t cs = pl->copy_stream, ps = pl->pack_stream;
   cudaEvent_t* ev_in = pl->host_ev;
   cudaEvent_t* ev_out = pl->host_ev + MGX_HOST_CHUNKS;
-  cudaEvent_t ev_start = pl->host_ev[2 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[2 * MGX_HOST_CHUNKS + 1];
-  cudaEvent_t ev_join_aux = pl->host_ev[2 * MGX_HOST_CHUNKS + 2], ev_join_main = pl->host_ev[2 * MGX_HOST_CHUNKS + 3];
+  cudaEvent_t* ev_copied = pl->host_ev + 2 * MGX_HOST_CHUNKS;
+  cudaEvent_t ev_start = pl->host_ev[3 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[3 * MGX_HOST_CHUNKS + 1];
+  cudaEvent_t ev_join_aux = pl->host_ev[3 * MGX_HOST_CHUNKS + 2], ev_join_main = pl->host_ev[3 * MGX_HOST_CHUNKS + 3];
   const long long layer = (long long)L.L1 * L.L2;
   auto cell0 = [&](int c) { return (long long)L.L0 * c / nc * layer; };    // first cell of slab c
   MGX_CUDA_TRY(cudaEventRecord(ev_start, ms));
   MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_start, 0));
+  if (nc > 1) MGX_CUDA_TRY(cudaStreamWaitEvent(ps, ev_start, 0));
   for (int c = 0; c < nc; ++c) {
     const long long sb = (nc == 1 ? 0 : cell0(c) * L.ns), se = (nc == 1 ? N : cell0(c + 1) * L.ns);
     MGX_CUDA_TRY(cudaMemcpyAsync(pl->host_aos + 3 * sb, e_in + 3 * sb, sizeof(double) * 3 * (se - sb),
                                  cudaMemcpyDefault, cs));
-    enqueue_pack(m, pl->host_aos, pl->host_lat, sb, se - sb, cs);
-    if (fx && nc > 1) enqueue_fx_split_cells(pl, pl->host_lat, cs, cell0(c), cell0(c + 1) - cell0(c));
-    MGX_CUDA_TRY(cudaEventRecord(ev_in[c], cs));
+    if (nc == 1) {
+      enqueue_pack(m, pl->host_aos, pl->host_lat, sb, se - sb, cs);
+      MGX_CUDA_TRY(cudaEventRecord(ev_in[c], cs));
+      continue;
+    }
+    // slabs: the next copy does not wait for this slab's packing (pack stream)
+    MGX_CUDA_TRY(cudaEventRecord(ev_copied[c], cs));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(ps, ev_copied[c], 0));
+    enqueue_pack(m, pl->host_aos, pl->host_lat, sb, se - sb, ps);
+    if (fx) enqueue_fx_split_cells(pl, pl->host_lat, ps, cell0(c), cell0(c + 1) - cell0(c));
+    MGX_CUDA_TRY(cudaEventRecord(ev_in[c], ps));
   }
   double* lat = pl->host_lat;
   if (nc == 1) {
@@ -494,7 +505,12 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
                                    cudaMemcpyDefault, cs));
     }
   }
-  // the copy stream waited for every slab of both compute streams: `ms` continues after all of it
+  // the copy stream waited for every slab of both compute streams (and, below, for the pack stream):
+  // `ms` continues after all of it
+  if (nc > 1) {
+    MGX_CUDA_TRY(cudaEventRecord(ev_copied[0], ps));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_copied[0], 0));
+  }
   MGX_CUDA_TRY(cudaEventRecord(ev_done, cs));
   MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_done, 0));
   return MGX_OK;
@@ -528,6 +544,7 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
     for (cudaEvent_t& ev : pl->host_ev)
       if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->aux_stream, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->pack_stream, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
     if (err != cudaSuccess) {
       drop_host_buffers(pl);

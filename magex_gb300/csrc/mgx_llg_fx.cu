@@ -201,7 +201,10 @@ mgx_status fx_build(const Model* m, int limb, bool field_scaled, int ncopies, De
         return set_error(MGX_ERR_UNSUPPORTED, "sublattice %d has %d couplings: the 56-bit fixed-point sum takes at "
                          "most 127 couplings per site (plus the on-site term)", s, off[s + 1] - off[s]);
   std::vector<int> sigma(ns, 0);
-  for (int s = 0; s < MGX_MAX_SUBLATTICES; ++s) fx->scale[s] = 0.0;
+  for (int s = 0; s < MGX_MAX_SUBLATTICES; ++s) {
+    fx->scale[s] = 0.0;
+    fx->scale_exp[s] = 0;
+  }
   for (int s = 0; s < ns; ++s) {
     double mx = 0.0, sum = 0.0;
     for (int b = off[s]; b < off[s + 1]; ++b)
@@ -221,6 +224,7 @@ mgx_status fx_build(const Model* m, int limb, bool field_scaled, int ncopies, De
                        "fixed-point gather", s, e);
     sigma[s] = e;
     fx->scale[s] = std::ldexp(1.0, e - 2 * limb);
+    fx->scale_exp[s] = e - 2 * limb;
   }
   std::vector<int2> Jq((size_t)std::max(nb, 1) * 10, make_int2(0, 0)), Aq((size_t)ns * 10, make_int2(0, 0));
   for (int s = 0; s < ns; ++s) {

@@ -15,7 +15,8 @@ fixed-point spins and couplings (INT32 pipe): its only extra error, the 2^-57 qu
 inputs, is below the rounding of an FP64 multiply-add chain, and it is 3.5x faster on GB300, whose
 FP64 units run at 1/61 of its FP32 rate.  "auto" (default) is "fp64_fixed" for the models that form
 supports (lattice stencils with per-sublattice moments and single-ion tensors, uniform damping and
-temperature, no spin-orbit torque) and "fp64" otherwise; a
+temperature, no spin-orbit torque) where it is faster (at least 2^15 sites, couplings beyond
+isotropic numbers) and "fp64" otherwise; a
 solver on "auto" moves to an FP64 plan when field hooks (field_func, extra_field) are first used.
 Two reduced forms keep the spins, the integration and the renormalisation in FP64 and move the rest
 off the FP64 pipe (Heun: field and right-hand side on compensated FP32 pairs): "df32" evaluates the
@@ -69,6 +70,12 @@ PRECISIONS = {"fp64": _lib.PRECISION_FP64, "df32": _lib.PRECISION_DF32_GATHER, "
               "fp64_fixed": _lib.PRECISION_FP64_FIXED_GATHER}
 
 
+#: below this many sites a step is bound by the latency of one thread's dependent chain, which the
+#: longer integer gather lengthens: "auto" keeps the FP64 plan there (measured on GB300: the FP64 step
+#: is faster up to ~16k sites for two-site bcc and triangular films)
+AUTO_FIXED_MIN_SITES = 1 << 15
+
+
 def fixed_point_eligible(sc, alpha=0.1, sot=None):
     """True when the exact fixed-point sum form (fp64_fixed) supports the system: a lattice stencil
     of fewer than 2^31 sites with per-sublattice moments and single-ion tensors, uniform damping and
@@ -84,6 +91,15 @@ def fixed_point_eligible(sc, alpha=0.1, sot=None):
     if len(sc.bond_src) and np.bincount(np.asarray(sc.bond_src)).max() > 127:
         return False                     # the 56-bit accumulators take at most 127 couplings per site
     return not sc.has_higher
+
+
+def auto_fixed(sc, alpha=0.1, sot=None):
+    """What precision="auto" picks: the fixed-point sum form where it is supported and faster, i.e.
+    for lattices of at least AUTO_FIXED_MIN_SITES sites whose couplings are not plain isotropic
+    numbers (an isotropic stencil costs the FP64 gather one multiply-add per component and neighbour,
+    the fixed-point sum always nine products of a full tensor; measured: FP64 stays faster for the
+    isotropic simple-cubic model up to 262k sites)."""
+    return fixed_point_eligible(sc, alpha, sot) and sc.N >= AUTO_FIXED_MIN_SITES and int(sc.width) != 1
 
 class GB300LLG:
     """Stochastic Heun / Depondt LLG on one GB300, with the API of magex ``LLGSolver``."""
@@ -112,7 +128,7 @@ class GB300LLG:
         self.sc = supercell_from_system(system)
         self.auto_precision = precision == "auto"
         if self.auto_precision:
-            precision = "fp64_fixed" if fixed_point_eligible(self.sc, alpha, sot) else "fp64"
+            precision = "fp64_fixed" if auto_fixed(self.sc, alpha, sot) else "fp64"
         self.precision = precision
         self.model = DeviceModel(self.sc, device)
         if system is not self.sc:

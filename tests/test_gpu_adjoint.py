@@ -28,11 +28,11 @@ def _params(theta, S):
     return T, A, B
 
 
-def _setup(L, nsteps, seg):
+def _setup(L, nsteps, seg, precision="auto"):
     from magex_gb300.adjoint import AdjointLLG
     from magex_gb300.workloads import film_parameter_basis, triangular_film
     sc = triangular_film(L=L, field=(0, 0, BZ))
-    adj = AdjointLLG(sc, alpha=ALPHA, dt=DT, seg_steps=seg)
+    adj = AdjointLLG(sc, alpha=ALPHA, dt=DT, seg_steps=seg, precision=precision)
     S = torch.as_tensor(group_basis(adj, film_parameter_basis(sc)), dtype=torch.float64)
     assert adj.groups.ngroups == 3                      # 6 nearest neighbours = 3 reverse pairs
     assert np.allclose(adj.T0, (J1 * np.eye(3)[None] + D * S.numpy()), atol=1e-15)
@@ -76,12 +76,15 @@ def _target(adj, S, sc, nsteps):
         return llg_trajectory(adj, e1, T, A, B, nsteps).detach()
 
 
-def test_adjoint_matches_torch_autograd_16x16(cuda):
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fixed"])
+def test_adjoint_matches_torch_autograd_16x16(cuda, precision):
     """Gradient w.r.t. e(0), J1, D, K, B_z of a 300-step trajectory (checkpoints every 40 steps)
-    equals torch autograd through the dense FP64 restatement on a 16 x 16 film."""
+    equals torch autograd through the dense FP64 restatement on a 16 x 16 film, with the forward and
+    its recomputation in the FP64 form and in the form with the exact fixed-point exchange sum."""
     from torch_reference import coupling_index, heun_trajectory
     nsteps = 300
-    sc, adj, S = _setup(16, nsteps, 40)
+    sc, adj, S = _setup(16, nsteps, 40, precision)
+    assert adj.precision == precision
     target = _target(adj, S, sc, nsteps)
     e0 = sc.init_spins("random", seed=1)
     theta0 = [J1, D, K, BZ]
@@ -100,12 +103,14 @@ def test_adjoint_matches_torch_autograd_16x16(cuda):
     assert np.abs(ge_gpu - ge_ref).max() <= 1e-8 * np.abs(ge_ref).max()
 
 
-def test_adjoint_matches_central_differences_128x128(cuda):
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fixed"])
+def test_adjoint_matches_central_differences_128x128(cuda, precision):
     """The differentiable-LLG workload: 128 x 128 film, 2000 Heun steps, checkpoints every 100 steps;
-    dL/d(J1, D, K, B_z) and three components of dL/de(0) against central differences, h = 1e-6."""
+    dL/d(J1, D, K, B_z) and three components of dL/de(0) against central differences, h = 1e-6, with
+    the forward in either form."""
     from magex_gb300.adjoint import llg_trajectory
     nsteps = 2000
-    sc, adj, S = _setup(128, nsteps, 100)
+    sc, adj, S = _setup(128, nsteps, 100, precision)
     target = _target(adj, S, sc, nsteps)
     e0 = sc.init_spins("random", seed=1)
     theta0 = np.array([J1, D, K, BZ])
@@ -238,8 +243,10 @@ def test_adjoint_per_bond_groups_equal_pair_groups(cuda):
     assert np.allclose(grads[0], grads[1], rtol=1e-10, atol=1e-12)
 
 
-def test_adjoint_resident_segments_equal_recompute(cuda):
-    """Keeping segments resident (no recomputation) gives the same gradient as recomputing them."""
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fixed"])
+def test_adjoint_resident_segments_equal_recompute(cuda, precision):
+    """Keeping segments resident (no recomputation) gives the same gradient as recomputing them
+    (bit for bit: the recomputation repeats the forward's arithmetic, in either form)."""
     from magex_gb300.adjoint import AdjointLLG, llg_trajectory
     from magex_gb300.workloads import film_parameter_basis, triangular_film, uniaxial_sia
     sc = triangular_film(L=24, field=(0, 0, BZ))
@@ -247,7 +254,7 @@ def test_adjoint_resident_segments_equal_recompute(cuda):
     target = torch.as_tensor(sc.init_spins("random", seed=2))
     out = []
     for cache in (0, 1 << 30, 3 * 8 * 14 * sc.N * 20):     # none, all, a part of the 5 segments
-        adj = AdjointLLG(sc, alpha=ALPHA, dt=DT, seg_steps=20, cache_bytes=cache)
+        adj = AdjointLLG(sc, alpha=ALPHA, dt=DT, seg_steps=20, cache_bytes=cache, precision=precision)
         S = torch.as_tensor(group_basis(adj, film_parameter_basis(sc)))
         theta = torch.tensor([J1, D], dtype=torch.float64, requires_grad=True)
         e = e0.clone().to(adj.device).requires_grad_(True)
@@ -259,3 +266,54 @@ def test_adjoint_resident_segments_equal_recompute(cuda):
         out.append((theta.grad.numpy().copy(), e.grad.cpu().numpy()))
     for g, ge in out[1:]:
         assert np.array_equal(g, out[0][0]) and np.array_equal(ge, out[0][1])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fixed"])
+@pytest.mark.parametrize("precision_fwd", ["recompute", "resident"])
+def test_adjoint_higher_onsite_terms_central_differences(cuda, golden_models, precision_fwd, precision):
+    """Cubic (rotated axes) and higher uniaxial anisotropy in the adjoint: the spins' adjoint through
+    the terms' Hessian and dL/dKc, dL/dK2, dL/dK3 (every site's constant moved together) against
+    central differences (h = 1e-6) of the same trajectory, with segments recomputed or resident.
+    Model: the sc system of the reference's sc_cubic fixture (Kc = 0.3, K2 = 0.2, K3 = 0.1 meV along
+    [111], DMI, SIA) at T = 0 plus a triangular film with rotated cubic axes and K2 at 8 K."""
+    from helpers import golden_supercell
+    from magex_gb300.adjoint import AdjointLLG, llg_trajectory
+    for tag, T_, nsteps in (("sc_cubic", 0.0, 60), ("tri_cubic_thermal", 8.0, 40)):
+        sc, meta = golden_supercell(golden_models, tag)
+        adj = AdjointLLG(sc, alpha=meta["alpha"], dt=meta["dt"], temperature=T_, seed=3, seg_steps=25,
+                         cache_bytes=0 if precision_fwd == "recompute" else "auto", precision=precision)
+        assert adj.has_higher
+        T0 = torch.as_tensor(adj.T0)
+        A0 = torch.as_tensor(np.asarray(sc.A_sub, float).reshape(sc.ns, 3, 3))
+        B0 = torch.as_tensor(np.asarray(sc.B, float))
+        H0 = adj.higher_params()
+        e0 = sc.init_spins("random", seed=5)
+        target = torch.as_tensor(sc.init_spins("random", seed=6), device=adj.device)
+        H = torch.tensor(H0, dtype=torch.float64, requires_grad=True)
+        e = torch.as_tensor(e0, device=adj.device).clone().requires_grad_(True)
+        eT = llg_trajectory(adj, e, T0, A0, B0, nsteps, H=H)
+        ((eT - target) ** 2).sum().backward()
+        gH, ge = H.grad.numpy(), e.grad.cpu().numpy()
+
+        def final(Hv, ev):
+            with torch.no_grad():
+                return llg_trajectory(adj, torch.as_tensor(ev, device=adj.device), T0, A0, B0, nsteps,
+                                      H=torch.as_tensor(Hv, dtype=torch.float64))
+
+        h = 1e-6
+        present = [sc.cubic is not None] + [sc.uniaxial_higher is not None] * 2
+        for k in range(3):
+            if not present[k]:
+                assert gH[k] == 0.0
+                continue
+            Hp, Hm = H0.copy(), H0.copy()
+            Hp[k] += h
+            Hm[k] -= h
+            fd = _central_difference(final(Hp, e0), final(Hm, e0), target, h)
+            assert abs(fd - gH[k]) <= 1e-6 * max(abs(fd), 1e-3), (tag, k, fd, gH[k])
+        for site, comp in [(0, 0), (7, 2), (sc.N - 1, 1)]:
+            ep, em = e0.copy(), e0.copy()
+            ep[site, comp] += h
+            em[site, comp] -= h
+            fd = _central_difference(final(H0, ep), final(H0, em), target, h)
+            assert abs(fd - ge[site, comp]) <= 1e-6 * max(abs(fd), 1e-3), (tag, site, comp, fd, ge[site, comp])
