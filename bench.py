@@ -265,10 +265,13 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
 
     def once(record):
-        theta = torch.tensor([1.0, 0.3], dtype=torch.float64, requires_grad=True)
+        # gradients w.r.t. e(0), J1, D, K and B_z (the differentiable-LLG workload's parameters)
+        theta = torch.tensor([1.0, 0.3, 0.05, 2.0], dtype=torch.float64, requires_grad=True)
         T = theta[0] * torch.eye(3, dtype=torch.float64)[None] + theta[1] * S
-        A = torch.as_tensor(uniaxial_sia(0.05))[None]
-        B = torch.tensor([0.0, 0.0, 2.0], dtype=torch.float64)
+        zz = torch.zeros((3, 3), dtype=torch.float64)
+        zz[2, 2] = 1.0
+        A = (-theta[2] * (zz - torch.eye(3, dtype=torch.float64) / 3.0))[None]
+        B = torch.stack([torch.zeros_like(theta[3]), torch.zeros_like(theta[3]), theta[3]])
         lat = plain.model.to_lattice(e0)
         e = torch.as_tensor(e0, device=adj.device).requires_grad_(True)
         torch.cuda.synchronize()
@@ -305,7 +308,7 @@ def bench_adjoint(L=128, nsteps=2000, seg=100, cache_bytes=0):
             "adjoint_over_forward": t_bwd / t_plain, "gradient_total_over_forward": (t_fwd + t_bwd) / t_plain,
             "default_forward": {"precision": default.precision, "ms": t_default,
                                 "adjoint_over_forward": t_bwd / t_default},
-            "grad_J1_D": [float(x) for x in g]}
+            "grad_J1_D_K_Bz": [float(x) for x in g]}
 
 
 def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0, precision="fp64"):

@@ -285,6 +285,11 @@ mgx_status mgx_adjoint_grads(mgx_adjoint* a, double* out, void* stream);
  * dL/dKc, dL/dK2, dL/dK3 (derivatives with respect to a change of every site's constant by the same
  * amount; zero when the model has none of those terms). */
 mgx_status mgx_adjoint_grads_onsite_higher(mgx_adjoint* a, double* out, void* stream);
+/* Which parameter gradients mgx_adjoint_backward accumulates (all three by default): the coupling
+ * groups, the single-ion tensors, the field (non-zero = accumulate).  The spins' adjoint and the
+ * cubic / higher-uniaxial gradients are always computed.  Skipping the ones a caller does not need
+ * saves their per-site reads and writes (torch.autograd asks only for the inputs that require grad). */
+mgx_status mgx_adjoint_set_needs(mgx_adjoint* a, int32_t couplings, int32_t onsite, int32_t field);
 
 /* ---------------------------------------------------------------- step without allocation
  * No counterpart in the reference.  One Heun / Depondt step like mgx_llg_step, for callers that

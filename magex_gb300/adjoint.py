@@ -283,8 +283,10 @@ class AdjointLLG:
             self.lib.mgx_adjoint_set_storage(self.handle, None)
         return cur, ckpts, cache
 
-    def backward(self, ckpts, ebar_T_lat, nsteps, cache=()):
-        """dL/de_0 (lattice layout) and (dL/dT, dL/dA, dL/dB) from dL/de_T."""
+    def backward(self, ckpts, ebar_T_lat, nsteps, cache=(), needs=(True, True, True)):
+        """dL/de_0 (lattice layout) and (dL/dT, dL/dA, dL/dB) from dL/de_T.  needs: which of the three
+        parameter gradients to accumulate (the others come back as zeros)."""
+        _lib.check(self.lib.mgx_adjoint_set_needs(self.handle, *(int(bool(x)) for x in needs)), "set_needs")
         ebar = ebar_T_lat.clone().contiguous()
         _lib.check(self.lib.mgx_adjoint_zero_grads(self.handle, stream_ptr()), "zero_grads")
         segs = self._segments(int(nsteps))
@@ -343,12 +345,14 @@ class _Trajectory(torch.autograd.Function):
         adj = ctx.adj
         _Trajectory._load(adj, ctx.params)           # the parameters may have changed since the forward
         ebar_T = adj.fwd.to_lattice(grad_eT.detach().contiguous())
-        ebar0, gT, gA, gB = adj.backward(ctx.ckpts, ebar_T, ctx.nsteps, ctx.cache)
+        needs = ctx.needs_input_grad[1:4]            # T, A, B: accumulate only what autograd asks for
+        ebar0, gT, gA, gB = adj.backward(ctx.ckpts, ebar_T, ctx.nsteps, ctx.cache, needs)
         ctx.cache = ()
         ge0 = adj.fwd.from_lattice(ebar0)
         d0, dT, dA, dB, dH = ctx.devs
         gH = None if dH is None else adj.last_grad_higher.to(dH)
-        return ge0.to(d0), gT.to(dT), gA.to(dA), gB.to(dB), gH, None, None
+        return (ge0.to(d0), gT.to(dT) if needs[0] else None, gA.to(dA) if needs[1] else None,
+                gB.to(dB) if needs[2] else None, gH, None, None)
 
 
 def llg_trajectory(adj, e0, T, A, B, nsteps, H=None):

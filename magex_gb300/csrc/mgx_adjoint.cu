@@ -41,6 +41,9 @@ struct AdjDev {
   double* PA;             // [9][N] single-ion gradients per site
   double* PB;             // [3][N] field gradients per site
   double* PH;             // [3][N] gradients w.r.t. the sites' Kc, K2, K3 (cubic / higher uniaxial), or nullptr
+  // which parameter gradients are accumulated (mgx_adjoint_set_needs): coupling groups (PG), single-ion
+  // tensors (PA), field (PB); the spins' adjoint is always computed
+  int need_G = 1, need_A = 1, need_B = 1;
 };
 
 struct AdjPlan {
@@ -149,10 +152,21 @@ __device__ __forceinline__ void store_cells(double* p, long long N, const double
   for (int k = 0; k < K; ++k) p[(long long)k * N] = v[k];
 }
 
-// PA -= g (x) v (single-ion gradient of one stage) and PB += Hbar (field gradient)
+// PA -= g (x) v (single-ion gradient of one stage) and PB += Hbar (field gradient), as far as requested
 __device__ __forceinline__ void accumulate_onsite(const AdjDev& A, long long N, long long q, bool hasA, double gx,
                                                   double gy, double gz, double vx, double vy, double vz, double Hbx,
                                                   double Hby, double Hbz) {
+  hasA = hasA && A.need_A;
+  if (!A.need_B) {
+    if (!hasA) return;
+    double pa[9];
+    load_cells<9>(A.PA + q, N, pa);
+    const double gv[3] = {gx, gy, gz}, v[3] = {vx, vy, vz};
+#pragma unroll
+    for (int k = 0; k < 9; ++k) pa[k] -= gv[k / 3] * v[k % 3];
+    store_cells<9>(A.PA + q, N, pa);
+    return;
+  }
   double pa[9], pb[3];
   if (hasA) load_cells<9>(A.PA + q, N, pa);
   load_cells<3>(A.PB + q, N, pb);
@@ -239,7 +253,7 @@ __device__ __forceinline__ void adjoint_gather(const AdjDev& A, const double* __
   double tx = 0.0, ty = 0.0, tz = 0.0;      // sum of g over couplings with tensor T_g^T
   const double vv[3] = {vx, vy, vz};
   auto flush = [&]() {
-    if (cur_g < 0) return;
+    if (cur_g < 0 || !A.need_G) return;
     double* P = A.PG + (long long)cur_g * 9 * N + q;
     const double gs[3] = {sx, sy, sz}, gt[3] = {tx, ty, tz};
     double acc[9];
@@ -916,6 +930,19 @@ mgx_status mgx_adjoint_grads(mgx_adjoint* aa, double* out, void* stream) {
   k_sum_rows<<<9 * ns, 256, 0, st>>>(a->d.PA, L.ncell, L.ncell, out + 9 * G);   // rows (component k, sublattice s)
   k_sum_rows<<<3, 256, 0, st>>>(a->d.PB, N, N, out + 9 * G + 9 * ns);
   MGX_CUDA_TRY(cudaGetLastError());
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_set_needs(mgx_adjoint* aa, int32_t couplings, int32_t onsite, int32_t field) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_set_needs: null adjoint");
+  const int g = couplings ? 1 : 0, o = onsite ? 1 : 0, f = field ? 1 : 0;
+  if (g != a->d.need_G || o != a->d.need_A || f != a->d.need_B) {
+    a->d.need_G = g;
+    a->d.need_A = o;
+    a->d.need_B = f;
+    drop_adj_graphs(a);                 // captured kernels hold the flags by value
+  }
   return MGX_OK;
 }
 

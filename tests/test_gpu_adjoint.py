@@ -317,3 +317,25 @@ def test_adjoint_higher_onsite_terms_central_differences(cuda, golden_models, pr
             em[site, comp] -= h
             fd = _central_difference(final(H0, ep), final(H0, em), target, h)
             assert abs(fd - ge[site, comp]) <= 1e-6 * max(abs(fd), 1e-3), (tag, site, comp, fd, ge[site, comp])
+
+
+def test_adjoint_accumulates_only_requested_gradients(cuda):
+    """autograd asks the adjoint only for the inputs that require grad (mgx_adjoint_set_needs): the
+    coupling gradient alone equals, bit for bit, the one computed together with the single-ion and
+    field gradients, and the spins' adjoint is unchanged."""
+    from magex_gb300.adjoint import llg_trajectory
+    sc, adj, S = _setup(24, 60, 20)
+    e0 = sc.init_spins("random", seed=1)
+    target = torch.as_tensor(sc.init_spins("random", seed=2), device=adj.device)
+    out = []
+    for all_params in (True, False):
+        theta = torch.tensor([J1, D, K, BZ], dtype=torch.float64, requires_grad=True)
+        T, A, B = _params(theta, S)
+        if not all_params:
+            A, B = A.detach(), B.detach()
+        e = torch.as_tensor(e0, device=adj.device).clone().requires_grad_(True)
+        ((llg_trajectory(adj, e, T, A, B, 60) - target) ** 2).sum().backward()
+        out.append((theta.grad.numpy().copy(), e.grad.cpu().numpy()))
+    assert np.array_equal(out[0][0][:2], out[1][0][:2])        # dL/dJ1, dL/dD through T
+    assert np.all(out[1][0][2:] == 0.0) and np.all(out[0][0][2:] != 0.0)
+    assert np.array_equal(out[0][1], out[1][1])
