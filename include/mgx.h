@@ -274,6 +274,11 @@ mgx_status mgx_adjoint_sync_models(mgx_adjoint* a);      /* after mgx_model_set_
  * 16-byte aligned; NULL = the own one), so that segments kept resident need no recomputation. */
 int64_t mgx_adjoint_storage_doubles(const mgx_adjoint* a);
 mgx_status mgx_adjoint_set_storage(mgx_adjoint* a, double* storage);
+/* The plan owns two storages (the second is allocated on first selection); selecting one makes it
+ * the current storage.  A caller can recompute one segment into one storage on a second stream
+ * while mgx_adjoint_backward runs through the other: the two share no device memory (ordering of
+ * the two calls on their streams, with events, is the caller's). */
+mgx_status mgx_adjoint_select_own_storage(mgx_adjoint* a, int32_t which);
 mgx_status mgx_adjoint_forward(mgx_adjoint* a, const double* e0, int32_t nsteps, uint64_t step0, double* e_out,
                                void* stream);
 /* nsteps: the length of the segment held by the current storage. */

@@ -134,6 +134,7 @@ SIGNATURES = {
     "mgx_adjoint_grads": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_adjoint_grads_onsite_higher": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_adjoint_set_needs": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    "mgx_adjoint_select_own_storage": (C.c_int32, [C.c_void_p, C.c_int32]),
     "mgx_observables": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mgx_observables_n": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "mgx_effective_field": (C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -291,6 +291,35 @@ class AdjointLLG:
         _lib.check(self.lib.mgx_adjoint_zero_grads(self.handle, stream_ptr()), "zero_grads")
         segs = self._segments(int(nsteps))
         first_cached = len(segs) - len(cache)
+        # Segments without resident states are recomputed from their checkpoints into the plan's two
+        # own storages, alternately, on a side stream: the recomputation of the next segment (earlier
+        # in time) runs while the backward pass goes through the current one.  A storage is reused once
+        # the backward pass through it has finished (event `free`), and a backward pass starts once its
+        # segment is recomputed (event `ready`).
+        main = torch.cuda.current_stream(self.device)
+        if not hasattr(self, "_side"):
+            self._side = torch.cuda.Stream(self.device)
+        side = self._side
+        free = [torch.cuda.Event(), torch.cuda.Event()]
+        for ev in free:
+            ev.record(main)
+        pending = [k for k in range(len(segs) - 1, -1, -1) if k < first_cached]
+        ready = {}
+
+        def recompute(k):
+            buf = k % 2
+            side.wait_event(free[buf])
+            _lib.check(self.lib.mgx_adjoint_select_own_storage(self.handle, buf), "select_own_storage")
+            n0, m = segs[k]
+            _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(ckpts[k].data_ptr()), m, n0, None,
+                                                    stream_ptr(side)), "mgx_adjoint_forward (recompute)")
+            ready[k] = torch.cuda.Event()
+            ready[k].record(side)
+
+        nxt = 0
+        if pending:
+            recompute(pending[0])
+            nxt = 1
         try:
             for k in range(len(segs) - 1, -1, -1):
                 n0, m = segs[k]
@@ -298,13 +327,18 @@ class AdjointLLG:
                     _lib.check(self.lib.mgx_adjoint_set_storage(self.handle, C.c_void_p(cache[k - first_cached].data_ptr())),
                                "set_storage")
                 else:
-                    _lib.check(self.lib.mgx_adjoint_set_storage(self.handle, None), "set_storage")
-                    _lib.check(self.lib.mgx_adjoint_forward(self.handle, C.c_void_p(ckpts[k].data_ptr()), m, n0, None,
-                                                            stream_ptr()), "mgx_adjoint_forward (recompute)")
-                _lib.check(self.lib.mgx_adjoint_backward(self.handle, C.c_void_p(ebar.data_ptr()), m, stream_ptr()),
+                    main.wait_event(ready.pop(k))
+                    if nxt < len(pending):
+                        recompute(pending[nxt])
+                        nxt += 1
+                    _lib.check(self.lib.mgx_adjoint_select_own_storage(self.handle, k % 2), "select_own_storage")
+                _lib.check(self.lib.mgx_adjoint_backward(self.handle, C.c_void_p(ebar.data_ptr()), m, stream_ptr(main)),
                            "mgx_adjoint_backward")
+                if k < first_cached:
+                    free[k % 2].record(main)
         finally:
             self.lib.mgx_adjoint_set_storage(self.handle, None)
+            main.wait_stream(side)
         _lib.check(self.lib.mgx_adjoint_grads(self.handle, C.c_void_p(self._grads.data_ptr()), stream_ptr()),
                    "mgx_adjoint_grads")
         G, ns = self.groups.ngroups, self.sc.ns

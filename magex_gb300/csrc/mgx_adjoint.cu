@@ -53,8 +53,10 @@ struct AdjPlan {
   DevLLG P;               // forward parameters; ep / k1 re-pointed per step
   int seg_cap = 0;
   int noise = MGX_NOISE_NONE;
-  double* seg = nullptr;  // current segment storage (own_seg or caller storage)
-  double* own_seg = nullptr;
+  double* seg = nullptr;  // current segment storage (one of own_seg or caller storage)
+  // two plan-owned storages: a caller may recompute one segment into one while the backward pass
+  // runs through the other (the second is allocated on first use)
+  double* own_seg[2] = {nullptr, nullptr};
   double* work = nullptr; // eacc | pbar | f1bar | g1 | g2 (5 x 3N)
   double* k1 = nullptr;
   double* grads = nullptr;  // reduction output on device
@@ -68,9 +70,10 @@ struct AdjPlan {
   // stencils, fields included, by value)
   cudaStream_t cap_stream = nullptr;
   unsigned long long* d_step = nullptr;
-  cudaGraphExec_t fwd_graph = nullptr, bwd_graph = nullptr;
-  int fwd_steps = 0, bwd_steps = 0;
-  const double* bwd_ebar = nullptr;
+  // (one pair per own storage)
+  cudaGraphExec_t fwd_graph[2] = {nullptr, nullptr}, bwd_graph[2] = {nullptr, nullptr};
+  int fwd_steps[2] = {0, 0}, bwd_steps[2] = {0, 0};
+  const double* bwd_ebar[2] = {nullptr, nullptr};
   // forward (and recomputation) with the exact 56-bit fixed-point exchange sum (MGX_PRECISION_FP64_FIXED_GATHER):
   // tables of the current couplings and the split copies of e / ep
   bool fixed = false;
@@ -656,11 +659,20 @@ static mgx_status build_adj_fx(AdjPlan* a) {
 }
 
 static void drop_adj_graphs(AdjPlan* a) {
-  if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
-  if (a->bwd_graph) cudaGraphExecDestroy(a->bwd_graph);
-  a->fwd_graph = a->bwd_graph = nullptr;
-  a->fwd_steps = a->bwd_steps = 0;
-  a->bwd_ebar = nullptr;
+  for (int k = 0; k < 2; ++k) {
+    if (a->fwd_graph[k]) cudaGraphExecDestroy(a->fwd_graph[k]);
+    if (a->bwd_graph[k]) cudaGraphExecDestroy(a->bwd_graph[k]);
+    a->fwd_graph[k] = a->bwd_graph[k] = nullptr;
+    a->fwd_steps[k] = a->bwd_steps[k] = 0;
+    a->bwd_ebar[k] = nullptr;
+  }
+}
+
+// Index of the current storage among the plan's own storages, or -1 for caller storage.
+static int own_index(const AdjPlan* a) {
+  for (int k = 0; k < 2; ++k)
+    if (a->own_seg[k] && a->seg == a->own_seg[k]) return k;
+  return -1;
 }
 
 // Capture the kernels that `enqueue` puts on a stream into *exec.
@@ -729,8 +741,8 @@ mgx_status mgx_adjoint_create(const mgx_model* fwd, const mgx_model* rev, const 
   const double gamma = 0.1760859630;
   const double pre = -gamma / (1.0 + p->alpha * p->alpha);
   const size_t n3 = 3 * (size_t)N;
-  cudaError_t err = cudaMalloc(&a->own_seg, sizeof(double) * seg_doubles(a));
-  a->seg = a->own_seg;
+  cudaError_t err = cudaMalloc(&a->own_seg[0], sizeof(double) * seg_doubles(a));
+  a->seg = a->own_seg[0];
   if (err == cudaSuccess) err = cudaMalloc(&a->work, sizeof(double) * n3 * 5);
   if (err == cudaSuccess) err = cudaMalloc(&a->k1, sizeof(double) * n3);
   if (err == cudaSuccess) err = cudaMalloc(&a->d_group, sizeof(int2) * grp.size());
@@ -798,7 +810,8 @@ mgx_status mgx_adjoint_destroy(mgx_adjoint* aa) {
   if (a->fx_block) cudaFree(a->fx_block);
   if (a->cap_stream) cudaStreamDestroy(a->cap_stream);
   cudaFree(a->d_step);
-  cudaFree(a->own_seg);
+  cudaFree(a->own_seg[0]);
+  cudaFree(a->own_seg[1]);
   cudaFree(a->work);
   cudaFree(a->k1);
   cudaFree(a->d_group);
@@ -841,7 +854,7 @@ mgx_status mgx_adjoint_set_storage(mgx_adjoint* aa, double* storage) {
   AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
   if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_set_storage: null adjoint");
   if (storage && ((uintptr_t)storage % 16) != 0) return set_error(MGX_ERR_INVALID, "storage must be 16-byte aligned");
-  a->seg = storage ? storage : a->own_seg;
+  a->seg = storage ? storage : a->own_seg[0];
   return MGX_OK;
 }
 
@@ -856,21 +869,22 @@ mgx_status mgx_adjoint_forward(mgx_adjoint* aa, const double* e0, int32_t nsteps
   const long long N = a->fwd->d.N;
   if (e0 != seg_ptr(a, 0, SEG_E))
     MGX_CUDA_TRY(cudaMemcpyAsync(seg_ptr(a, 0, SEG_E), e0, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, st));
-  if (a->seg == a->own_seg && N <= kAdjGraphMaxSites) {
+  const int own = own_index(a);
+  if (own >= 0 && N <= kAdjGraphMaxSites) {
     // recomputed segments of a small lattice: one graph replay (the step index from the counter)
-    if (!a->fwd_graph || a->fwd_steps != nsteps) {
-      if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
-      a->fwd_graph = nullptr;
+    if (!a->fwd_graph[own] || a->fwd_steps[own] != nsteps) {
+      if (a->fwd_graph[own]) cudaGraphExecDestroy(a->fwd_graph[own]);
+      a->fwd_graph[own] = nullptr;
       DevLLG P = a->P;
       P.step_base = a->d_step;
-      const mgx_status cs = capture_adj(a, &a->fwd_graph, [&](cudaStream_t cst) {
+      const mgx_status cs = capture_adj(a, &a->fwd_graph[own], [&](cudaStream_t cst) {
         enqueue_adj_forward(a, P, nsteps, 0, cst);
       });
       if (cs != MGX_OK) return cs;
-      a->fwd_steps = nsteps;
+      a->fwd_steps[own] = nsteps;
     }
     k_adj_step_set<<<1, 1, 0, st>>>(a->d_step, (unsigned long long)step0);
-    MGX_CUDA_TRY(cudaGraphLaunch(a->fwd_graph, st));
+    MGX_CUDA_TRY(cudaGraphLaunch(a->fwd_graph[own], st));
   } else {
     enqueue_adj_forward(a, a->P, nsteps, step0, st);
   }
@@ -888,18 +902,19 @@ mgx_status mgx_adjoint_backward(mgx_adjoint* aa, double* ebar, int32_t nsteps, v
     return set_error(MGX_ERR_INVALID, "nsteps = %d outside 1..%d (segment capacity)", nsteps, a->seg_cap);
   cudaStream_t st = (cudaStream_t)stream;
   const long long N = a->fwd->d.N;
-  if (a->seg == a->own_seg && N <= kAdjGraphMaxSites) {
-    if (!a->bwd_graph || a->bwd_steps != nsteps || a->bwd_ebar != ebar) {
-      if (a->bwd_graph) cudaGraphExecDestroy(a->bwd_graph);
-      a->bwd_graph = nullptr;
-      const mgx_status cs = capture_adj(a, &a->bwd_graph, [&](cudaStream_t cst) {
+  const int own = own_index(a);
+  if (own >= 0 && N <= kAdjGraphMaxSites) {
+    if (!a->bwd_graph[own] || a->bwd_steps[own] != nsteps || a->bwd_ebar[own] != ebar) {
+      if (a->bwd_graph[own]) cudaGraphExecDestroy(a->bwd_graph[own]);
+      a->bwd_graph[own] = nullptr;
+      const mgx_status cs = capture_adj(a, &a->bwd_graph[own], [&](cudaStream_t cst) {
         enqueue_adj_backward(a, ebar, nsteps, cst);
       });
       if (cs != MGX_OK) return cs;
-      a->bwd_steps = nsteps;
-      a->bwd_ebar = ebar;
+      a->bwd_steps[own] = nsteps;
+      a->bwd_ebar[own] = ebar;
     }
-    MGX_CUDA_TRY(cudaGraphLaunch(a->bwd_graph, st));
+    MGX_CUDA_TRY(cudaGraphLaunch(a->bwd_graph[own], st));
   } else {
     enqueue_adj_backward(a, ebar, nsteps, st);
   }
@@ -930,6 +945,15 @@ mgx_status mgx_adjoint_grads(mgx_adjoint* aa, double* out, void* stream) {
   k_sum_rows<<<9 * ns, 256, 0, st>>>(a->d.PA, L.ncell, L.ncell, out + 9 * G);   // rows (component k, sublattice s)
   k_sum_rows<<<3, 256, 0, st>>>(a->d.PB, N, N, out + 9 * G + 9 * ns);
   MGX_CUDA_TRY(cudaGetLastError());
+  return MGX_OK;
+}
+
+mgx_status mgx_adjoint_select_own_storage(mgx_adjoint* aa, int32_t which) {
+  AdjPlan* a = reinterpret_cast<AdjPlan*>(aa);
+  if (!a) return set_error(MGX_ERR_INVALID, "mgx_adjoint_select_own_storage: null adjoint");
+  if (which != 0 && which != 1) return set_error(MGX_ERR_INVALID, "own storage %d is not 0 or 1", which);
+  if (!a->own_seg[which]) MGX_CUDA_TRY(cudaMalloc(&a->own_seg[which], sizeof(double) * seg_doubles(a)));
+  a->seg = a->own_seg[which];
   return MGX_OK;
 }
 
