@@ -184,11 +184,14 @@ struct LLGPlan {
   // second compute stream (consecutive slabs run on alternate streams so each fills the other's tail)
   // (and a pack stream: the copies in run back to back on the copy stream while each landed slab is
   // packed into the lattice layout on the pack stream)
+  // and two corrector streams: the corrector of a slab starts once the predictors of the slabs it
+  // gathers from are done, while the predictors of later slabs still run)
   cudaStream_t copy_stream = nullptr, aux_stream = nullptr, pack_stream = nullptr;
+  cudaStream_t corr_stream[2] = {nullptr, nullptr};
   double* host_lat = nullptr;    // [3][N] lattice layout
   double* host_aos = nullptr;    // [N][3] magex order (staging of the copies)
-  // in[c] (packed) | out[c] (unpacked) | copied[c] | start | done | joined aux | joined main
-  cudaEvent_t host_ev[3 * MGX_HOST_CHUNKS + 4] = {};
+  // in[c] (packed) | out[c] (unpacked) | copied[c] | predicted[c] | start | done | joined aux | joined main
+  cudaEvent_t host_ev[4 * MGX_HOST_CHUNKS + 4] = {};
   // the slab pipeline of a host-buffer step captured as a graph (step index from d_step), for the
   // last two (input, output) buffer pairs: replaying it costs one launch instead of ~250 API calls
   LLGGraph host_graphs[2];

@@ -219,6 +219,10 @@ static void drop_host_buffers(LLGPlan* pl) {
   if (pl->aux_stream) cudaStreamDestroy(pl->aux_stream);
   if (pl->pack_stream) cudaStreamDestroy(pl->pack_stream);
   pl->copy_stream = pl->aux_stream = pl->pack_stream = nullptr;
+  for (cudaStream_t& cst : pl->corr_stream) {
+    if (cst) cudaStreamDestroy(cst);
+    cst = nullptr;
+  }
 }
 
 }  // namespace mgx
@@ -439,8 +443,9 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
   cudaEvent_t* ev_in = pl->host_ev;
   cudaEvent_t* ev_out = pl->host_ev + MGX_HOST_CHUNKS;
   cudaEvent_t* ev_copied = pl->host_ev + 2 * MGX_HOST_CHUNKS;
-  cudaEvent_t ev_start = pl->host_ev[3 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[3 * MGX_HOST_CHUNKS + 1];
-  cudaEvent_t ev_join_aux = pl->host_ev[3 * MGX_HOST_CHUNKS + 2], ev_join_main = pl->host_ev[3 * MGX_HOST_CHUNKS + 3];
+  cudaEvent_t* ev_pred = pl->host_ev + 3 * MGX_HOST_CHUNKS;
+  cudaEvent_t ev_start = pl->host_ev[4 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[4 * MGX_HOST_CHUNKS + 1];
+  cudaEvent_t ev_join_aux = pl->host_ev[4 * MGX_HOST_CHUNKS + 2];
   const long long layer = (long long)L.L1 * L.L2;
   auto cell0 = [&](int c) { return (long long)L.L0 * c / nc * layer; };    // first cell of slab c
   MGX_CUDA_TRY(cudaEventRecord(ev_start, ms));
@@ -485,14 +490,19 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
         enqueue_fx_range(pl, lat, noise, step, st, 1, cell0(c), cell0(c + 1) - cell0(c));
       else
         enqueue_fp64_range(pl, lat, noise, step, st, 1, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
+      MGX_CUDA_TRY(cudaEventRecord(ev_pred[c], st));
     }
-    // every corrector gathers the predicted spins of its neighbours: both streams pass all predictors
-    MGX_CUDA_TRY(cudaEventRecord(ev_join_aux, run[1]));
-    MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_join_aux, 0));
-    MGX_CUDA_TRY(cudaEventRecord(ev_join_main, ms));
-    MGX_CUDA_TRY(cudaStreamWaitEvent(run[1], ev_join_main, 0));
-    for (int c = 0; c < nc; ++c) {
-      cudaStream_t st = run[c & 1];
+    // the corrector of slab c gathers the predicted spins of slabs c-1 .. c+1 and overwrites the spins
+    // (and their fixed-point copy) of slab c, which the predictors of c-1 and c+1 read: it waits for
+    // those three predictors only, on streams of its own, so it overlaps the later predictors
+    for (int k = 0; k < nc; ++k) {
+      const int c = ring ? (k + 2) % nc : k;
+      cudaStream_t st = pl->corr_stream[k & 1];
+      for (int d = -1; d <= 1; ++d) {
+        const int n = c + d;
+        if (n >= 0 && n < nc) MGX_CUDA_TRY(cudaStreamWaitEvent(st, ev_pred[n], 0));
+        else if (ring) MGX_CUDA_TRY(cudaStreamWaitEvent(st, ev_pred[(n + nc) % nc], 0));
+      }
       if (fx)
         enqueue_fx_range(pl, lat, noise, step, st, 2, cell0(c), cell0(c + 1) - cell0(c));
       else
@@ -505,11 +515,13 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
                                    cudaMemcpyDefault, cs));
     }
   }
-  // the copy stream waited for every slab of both compute streams (and, below, for the pack stream):
-  // `ms` continues after all of it
+  // the copy stream waited for every slab of the corrector streams (and, below, for the pack and the
+  // second predictor stream): `ms` continues after all of it
   if (nc > 1) {
     MGX_CUDA_TRY(cudaEventRecord(ev_copied[0], ps));
     MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_copied[0], 0));
+    MGX_CUDA_TRY(cudaEventRecord(ev_join_aux, pl->aux_stream));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_join_aux, 0));
   }
   MGX_CUDA_TRY(cudaEventRecord(ev_done, cs));
   MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_done, 0));
@@ -545,6 +557,8 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
       if (err == cudaSuccess) err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->aux_stream, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->pack_stream, cudaStreamNonBlocking);
+    for (cudaStream_t& cst : pl->corr_stream)
+      if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
     if (err != cudaSuccess) {
       drop_host_buffers(pl);
