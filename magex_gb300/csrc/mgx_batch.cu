@@ -81,10 +81,10 @@ constexpr int BATCH_MAX_THREADS = 512;
 
 // HIGHER: a separate instantiation for batches with cubic / higher-uniaxial terms (in any system), so
 // that the plain stage kernels keep their registers.
-template <int STAGE, int NOISE, int INTEG, bool FIXED, bool HIGHER>
 // At least two CTAs of the largest tile per SM, i.e. at most 64 registers: the fixed-point-sum bodies
 // otherwise take 86-98 registers, and the occupancy lost costs more than the few spills (measured on
 // the 256-film ensemble: 1.26 against 1.68 ms per step; the FP64 bodies use 64 either way).
+template <int STAGE, int NOISE, int INTEG, bool FIXED, bool HIGHER>
 __global__ void __launch_bounds__(BATCH_MAX_THREADS, 2) k_batch_stage(const BatchSys* __restrict__ sys,
                                                                    const int2* __restrict__ tiles, int ntiles,
                                                                    double* __restrict__ e,
