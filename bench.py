@@ -367,11 +367,12 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0, precision="fp64")
     free, _ = torch.cuda.mem_get_info()
     cache = int(0.6 * free)
     adj = AdjointLLG(sc, groups, alpha=ALPHA, dt=DT, temperature=300.0, seed=77, seg_steps=100, cache_bytes=cache)
-    plain = GB300LLG(sc, ALPHA, DT, 300.0, 77)
+    plain = GB300LLG(sc, ALPHA, DT, 300.0, 77, precision="fp64")     # the all-FP64 forward
+    default = GB300LLG(sc, ALPHA, DT, 300.0, 77)                      # the default solver ("auto")
     A0 = torch.as_tensor(np.stack([uniaxial_sia(0.01)] * sc.ns))
     B0 = torch.tensor(FIELD, dtype=torch.float64)
     e0 = torch.as_tensor(sc.init_spins("random", seed=5), device=adj.device)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(7)]
 
     def once(record):
         T = torch.as_tensor(adj.T0).clone().requires_grad_(True)
@@ -391,12 +392,17 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0, precision="fp64")
         loss.backward()
         if record:
             ev[4].record(stream)
+            lat2 = default.model.to_lattice(e0)
+            ev[5].record(stream)
+            default.run_lattice(lat2, adj_steps)
+            ev[6].record(stream)
         torch.cuda.synchronize()
         return float(loss.detach()), T.grad
 
     once(False)
     loss, g = once(True)
     t = [ev[0].elapsed_time(ev[k]) for k in range(1, 5)]
+    t_default = ev[5].elapsed_time(ev[6])
     return {**head,
             "adjoint": {"system": f"one {L}^3 system ({sc.N:,} spins) at 300 K", "steps": adj_steps,
                         "loss": "mean energy per spin after the trajectory (meV)",
@@ -405,6 +411,9 @@ def bench_config5(nsys=64, L=64, K=10, adj_steps=1000, seed=0, precision="fp64")
                         "forward_plain_ms": t[0], "forward_checkpointed_ms": t[1] - t[0],
                         "loss_ms": t[2] - t[1], "backward_ms": t[3] - t[2],
                         "adjoint_over_forward": (t[3] - t[2]) / t[0], "loss_value": loss,
+                        "forward_precision": adj.precision,
+                        "default_forward": {"precision": default.precision, "ms": t_default,
+                                            "adjoint_over_forward": (t[3] - t[2]) / t_default},
                         "grad_norm_per_shell": [float(x) for x in g.reshape(4, -1).norm(dim=1)]}}
 
 
@@ -796,8 +805,10 @@ def north_star_summary(line):
                 out[key + "_bwd_over_default_fwd"] = _r(d["adjoint_over_forward"], 3)
     c5 = line.get("large_batched_adjoint")
     if c5:
+        a5 = c5.get("adjoint", {})
         out["config5"] = {"batched_value": _r(c5["batched_value"]), "speedup_vs_plain": _r(c5["speedup_vs_plain"], 3),
-                          "adjoint_bwd_over_fwd": _r(c5.get("adjoint", {}).get("adjoint_over_forward"), 3)}
+                          "adjoint_bwd_over_fwd": _r(a5.get("adjoint_over_forward"), 3),
+                          "adjoint_bwd_over_default_fwd": _r(a5.get("default_forward", {}).get("adjoint_over_forward"), 3)}
     c5f = line.get("large_batched_fp64_fixed")
     if c5f:
         out["config5_fp64_fixed"] = {"batched_value": _r(c5f["batched_value"]),
