@@ -44,6 +44,13 @@ struct AdjDev {
   // which parameter gradients are accumulated (mgx_adjoint_set_needs): coupling groups (PG), single-ion
   // tensors (PA), field (PB); the spins' adjoint is always computed
   int need_G = 1, need_A = 1, need_B = 1;
+  // fixed-point transposed gathers (the plan's forward uses the fixed-point sum): the reverse
+  // couplings as 56-bit fixed-point tensors, and per stage (0: g1, 1: g2) each site's g as 56-bit
+  // fixed point at a power-of-two scale of its own (block floating point: gs = round(g 2^(56 - ge)))
+  int fixed = 0;
+  DevFX RF;
+  int2* gs[2] = {nullptr, nullptr};   // [3][N] each
+  int* ge[2] = {nullptr, nullptr};    // [N] each
 };
 
 struct AdjPlan {
@@ -79,6 +86,8 @@ struct AdjPlan {
   bool fixed = false;
   DevFX fx{};
   void* fx_block = nullptr;
+  void* rfx_block = nullptr;       // fixed-point tables of the reverse stencil (transposed gathers)
+  void* gsplit_block = nullptr;    // g1 / g2 in block floating point
 };
 
 // Lattices up to this size replay captured graphs for recomputed segments (larger ones are bound by
@@ -358,6 +367,120 @@ __global__ void __launch_bounds__(256, 4) k_fwd_corr_fx(const DevLattice L, cons
 
 __global__ void k_adj_step_set(unsigned long long* c, unsigned long long v) { *c = v; }
 
+// ---------------------------------------------------------------- fixed-point transposed gather
+// g of site q in block floating point: the exponent tau with max_c |g_c| < 2^tau (from the bit pattern
+// of the largest component) and round(g_c 2^(56 - tau)) in balanced 28-bit halves, all on the integer
+// pipes.
+__device__ __forceinline__ void store_g_split(const AdjDev& A, int which, long long N, long long q, double gx,
+                                              double gy, double gz) {
+  const unsigned long long mask = 0x7FFFFFFFFFFFFFFFULL;
+  const unsigned long long ax = (unsigned long long)__double_as_longlong(gx) & mask;
+  const unsigned long long ay = (unsigned long long)__double_as_longlong(gy) & mask;
+  const unsigned long long az = (unsigned long long)__double_as_longlong(gz) & mask;
+  const unsigned long long m = ax > ay ? (ax > az ? ax : az) : (ay > az ? ay : az);
+  const int E = (int)(m >> 52);
+  const int tau = (E == 0 ? 1 : E) - 1022;
+  int2* gs = A.gs[which];
+  gs[q] = fx_halves<28>(double_to_ll_scaled(gx, 56 - tau));
+  gs[N + q] = fx_halves<28>(double_to_ll_scaled(gy, 56 - tau));
+  gs[2 * N + q] = fx_halves<28>(double_to_ll_scaled(gz, 56 - tau));
+  A.ge[which][q] = tau;
+}
+
+// a 56-bit fixed-point value (two halves) at exponent tau_j, re-expressed at exponent tau_j + d
+// (rounded, d >= 0)
+__device__ __forceinline__ long long fx_align(int2 h, int d) {
+  const long long v = ((long long)h.x << 28) + (long long)h.y;
+  if (d <= 0) return v;
+  if (d > 62) return 0;
+  return (v + (1LL << (d - 1))) >> d;
+}
+
+// t 2^e2 as FP64 (ll_to_double_scaled, with a plain fallback where the result would leave the normal
+// range: the adjoint field of a site whose neighbours' g are all tiny)
+__device__ __forceinline__ double fx_to_double(long long t, int e2) {
+  if (t == 0) return 0.0;
+  const unsigned long long a = t < 0 ? 0ULL - (unsigned long long)t : (unsigned long long)t;
+  const int msb = 63 - __clzll((long long)a);
+  if (msb + e2 + 1023 < 2 || msb + e2 + 1023 > 2045) return ldexp((double)t, e2);
+  return ll_to_double_scaled(t, e2);
+}
+
+// The transposed gather of adjoint_gather on the integer pipes: the neighbours' g (block floating
+// point, stage `which`) are aligned to the largest exponent among them and multiplied by the
+// fixed-point J^T exactly (the sum of products is exact; each aligned term is rounded to 2^-57 of the
+// largest); the group sums for the parameter gradients are exact integer sums too.  The coupling
+// gradients' outer products stay FP64.
+__device__ __forceinline__ void adjoint_gather_fx(const AdjDev& A, int which, long long q, int s, int c0, int c1,
+                                                  int c2, double vx, double vy, double vz, double& ox, double& oy,
+                                                  double& oz) {
+  const DevLattice& L = A.R;
+  const long long N = L.N;
+  const int2* __restrict__ gs = A.gs[which];
+  const int* __restrict__ ge = A.ge[which];
+  const int b0 = __ldg(L.bond_off + s), b1 = __ldg(L.bond_off + s + 1);
+  auto nbr = [&](int b) -> long long {
+    const int4 geo = __ldg(L.bond_geo + b);
+    int n0 = c0 + geo.y, n1 = c1 + geo.z, n2 = c2 + geo.w;
+    bool ok = true;
+    if (L.pbc0) { n0 -= (n0 >= L.L0) ? L.L0 : 0; } else { ok &= (unsigned)n0 < (unsigned)L.L0; }
+    if (L.pbc1) { n1 -= (n1 >= L.L1) ? L.L1 : 0; } else { ok &= (unsigned)n1 < (unsigned)L.L1; }
+    if (L.pbc2) { n2 -= (n2 >= L.L2) ? L.L2 : 0; } else { ok &= (unsigned)n2 < (unsigned)L.L2; }
+    return ok ? (long long)geo.x * L.ncell + ((long long)n0 * L.L1 + n1) * L.L2 + n2 : -1LL;
+  };
+  int tmax = -2000;
+  for (int b = b0; b < b1; ++b) {
+    const long long j = nbr(b);
+    if (j >= 0) tmax = max(tmax, __ldg(ge + j));
+  }
+  FxAcc acc;
+  long long ss[3] = {0, 0, 0}, tt[3] = {0, 0, 0};   // exact sums of g over plain / transposed couplings
+  int cur_g = -1;
+  const double vv[3] = {vx, vy, vz};
+  auto flush = [&]() {
+    if (cur_g < 0 || !A.need_G) return;
+    double* P = A.PG + (long long)cur_g * 9 * N + q;
+    double gsd[3], gtd[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      gsd[c] = fx_to_double(ss[c], tmax - 56);
+      gtd[c] = fx_to_double(tt[c], tmax - 56);
+    }
+    double accp[9];
+    load_cells<9>(P, N, accp);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) accp[3 * a + b] = fma(vv[a], gtd[b], fma(gsd[a], vv[b], accp[3 * a + b]));
+    store_cells<9>(P, N, accp);
+  };
+  for (int b = b0; b < b1; ++b) {
+    const int2 gr = __ldg(A.group + b);
+    if (gr.x != cur_g) {
+      flush();
+      cur_g = gr.x;
+      ss[0] = ss[1] = ss[2] = 0;
+      tt[0] = tt[1] = tt[2] = 0;
+    }
+    const long long j = nbr(b);
+    if (j < 0) continue;
+    const int d = tmax - __ldg(ge + j);
+    const long long v0 = fx_align(__ldg(gs + j), d), v1 = fx_align(__ldg(gs + N + j), d),
+                    v2 = fx_align(__ldg(gs + 2 * N + j), d);
+    fx_mat(A.RF.J + 5 * b, fx_halves<28>(v0), fx_halves<28>(v1), fx_halves<28>(v2), acc);
+    if (gr.y) {
+      tt[0] += v0; tt[1] += v1; tt[2] += v2;
+    } else {
+      ss[0] += v0; ss[1] += v1; ss[2] += v2;
+    }
+  }
+  flush();
+  const int e2 = A.RF.scale_exp[s] + tmax;
+  ox = fx_to_double(acc.hh[0] + ((acc.x[0] + (1LL << 27)) >> 28), e2);
+  oy = fx_to_double(acc.hh[1] + ((acc.x[1] + (1LL << 27)) >> 28), e2);
+  oz = fx_to_double(acc.hh[2] + ((acc.x[2] + (1LL << 27)) >> 28), e2);
+}
+
 // ---------------------------------------------------------------- backward kernels
 // Site-local part of the backward step (first kernel body of step n): ybar from zbar = dL/de' through
 // the corrector normalisation (e' = y |y|^-1 and |y|^-1 are stored), the rhs adjoint at (p, H2), g2
@@ -374,6 +497,7 @@ __device__ __forceinline__ void adj_local_site(const AdjDev& A, long long q, con
     store3(pbar, N, q, 0.0, 0.0, 0.0);
     store3(f1bar, N, q, 0.0, 0.0, 0.0);
     store3(g2, N, q, 0.0, 0.0, 0.0);
+    if (A.fixed) store_g_split(A, 1, N, q, 0.0, 0.0, 0.0);
     return;
   }
   const int s = (int)(q / L.ncell);
@@ -409,6 +533,7 @@ __device__ __forceinline__ void adj_local_site(const AdjDev& A, long long q, con
   store3(pbar, N, q, pbx, pby, pbz);
   store3(f1bar, N, q, fbx, fby, fbz);
   store3(g2, N, q, gx, gy, gz);
+  if (A.fixed) store_g_split(A, 1, N, q, gx, gy, gz);
 }
 
 __global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double* __restrict__ Z,
@@ -426,6 +551,7 @@ __global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double*
 // Second kernel of step n: pbar += sum_rev J^T g2, xbar through the predictor normalisation
 // (p = x |x|^-1, both stored), the rhs adjoint at (e, H1), g1; stage-2 coupling and stage-1 single-ion
 // and field gradients.
+template <bool FX>
 __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* __restrict__ E,
                                                  const double* __restrict__ Pp, const double* __restrict__ H1,
                                                  const double* __restrict__ R, double* __restrict__ eacc,
@@ -440,7 +566,10 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
   double px, py, pz;
   load3(Pp, N, q, px, py, pz);
   double tx, ty, tz;
-  adjoint_gather(A, g2, q, s, c0, c1, c2, px, py, pz, tx, ty, tz);
+  if (FX)
+    adjoint_gather_fx(A, 1, q, s, c0, c1, c2, px, py, pz, tx, ty, tz);
+  else
+    adjoint_gather(A, g2, q, s, c0, c1, c2, px, py, pz, tx, ty, tz);
   double pbx, pby, pbz;
   load3(pbar, N, q, pbx, pby, pbz);
   pbx += tx;
@@ -451,6 +580,7 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
   if (L.pinned && L.pinned[q]) {          // p = e on pinned sites
     store3(eacc, N, q, ax + pbx, ay + pby, az + pbz);
     store3(g1, N, q, 0.0, 0.0, 0.0);
+    if (FX) store_g_split(A, 0, N, q, 0.0, 0.0, 0.0);
     return;
   }
   double ex, ey, ez, h1x, h1y, h1z;
@@ -492,12 +622,13 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
   accumulate_onsite(A, N, q, L.has_A != 0, gx, gy, gz, ex, ey, ez, Hbx, Hby, Hbz);
   store3(eacc, N, q, ax, ay, az);
   store3(g1, N, q, gx, gy, gz);
+  if (FX) store_g_split(A, 0, N, q, gx, gy, gz);
 }
 
 // Last kernel of step n: ebar_n = acc + sum_rev J^T g1 (and the stage-1 coupling gradients).  With
 // FUSE the site-local body of step n - 1 follows in the same thread on ebar_n, which is then never
 // stored; otherwise ebar_n is written out.
-template <bool FUSE>
+template <bool FUSE, bool FX>
 __global__ void __launch_bounds__(256) k_adj_final(const AdjDev A, const double* __restrict__ E,
                                                    double* __restrict__ eacc, const double* __restrict__ g1,
                                                    double* __restrict__ ebar, const double* __restrict__ Pprev,
@@ -513,7 +644,10 @@ __global__ void __launch_bounds__(256) k_adj_final(const AdjDev A, const double*
   double ex, ey, ez;
   load3(E, N, q, ex, ey, ez);
   double tx, ty, tz;
-  adjoint_gather(A, g1, q, s, c0, c1, c2, ex, ey, ez, tx, ty, tz);
+  if (FX)
+    adjoint_gather_fx(A, 0, q, s, c0, c1, c2, ex, ey, ez, tx, ty, tz);
+  else
+    adjoint_gather(A, g1, q, s, c0, c1, c2, ex, ey, ez, tx, ty, tz);
   double ax, ay, az;
   load3(eacc, N, q, ax, ay, az);
   if (FUSE) {
@@ -637,14 +771,28 @@ static void enqueue_adj_backward(const AdjPlan* a, double* ebar, int nsteps, cud
   k_adj_local<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, last + 1, SEG_E), seg_ptr(a, last, SEG_P),
                                     seg_ptr(a, last, SEG_H2), seg_ptr(a, last, SEG_R), ebar, eacc, pbar, f1bar, g2);
   for (int n = last; n >= 0; --n) {
-    k_adj_mid<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
-                                    seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
+    if (a->d.fixed)
+      k_adj_mid<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
+                                            seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
+    else
+      k_adj_mid<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
+                                             seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
     if (n > 0) {
-      k_adj_final<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr, seg_ptr(a, n - 1, SEG_P),
-                                              seg_ptr(a, n - 1, SEG_H2), seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
+      if (a->d.fixed)
+        k_adj_final<true, true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr,
+                                                      seg_ptr(a, n - 1, SEG_P), seg_ptr(a, n - 1, SEG_H2),
+                                                      seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
+      else
+        k_adj_final<true, false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr,
+                                                       seg_ptr(a, n - 1, SEG_P), seg_ptr(a, n - 1, SEG_H2),
+                                                       seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
     } else {
-      k_adj_final<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr, nullptr,
-                                               nullptr, nullptr, nullptr);
+      if (a->d.fixed)
+        k_adj_final<false, true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr,
+                                                       nullptr, nullptr, nullptr, nullptr);
+      else
+        k_adj_final<false, false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr,
+                                                        nullptr, nullptr, nullptr, nullptr);
     }
   }
 }
@@ -654,8 +802,26 @@ static void enqueue_adj_backward(const AdjPlan* a, double* ebar, int nsteps, cud
 static mgx_status build_adj_fx(AdjPlan* a) {
   if (!a->fixed) return MGX_OK;
   if (a->fx_block) cudaFree(a->fx_block);
-  a->fx_block = nullptr;
-  return fx_build(a->fwd, 28, true, 2, &a->fx, &a->fx_block);
+  if (a->rfx_block) cudaFree(a->rfx_block);
+  a->fx_block = a->rfx_block = nullptr;
+  mgx_status st = fx_build(a->fwd, 28, true, 2, &a->fx, &a->fx_block);
+  if (st == MGX_OK) st = fx_build(a->rev, 28, false, 0, &a->d.RF, &a->rfx_block);
+  if (st != MGX_OK) return st;
+  if (!a->gsplit_block) {
+    const size_t N = (size_t)a->fwd->d.N;
+    MGX_CUDA_TRY(cudaMalloc(&a->gsplit_block, 2 * (sizeof(int2) * 3 * N + sizeof(int) * N)));
+    char* p = (char*)a->gsplit_block;
+    for (int k = 0; k < 2; ++k) {
+      a->d.gs[k] = (int2*)p;
+      p += sizeof(int2) * 3 * N;
+    }
+    for (int k = 0; k < 2; ++k) {
+      a->d.ge[k] = (int*)p;
+      p += sizeof(int) * N;
+    }
+  }
+  a->d.fixed = 1;
+  return MGX_OK;
 }
 
 static void drop_adj_graphs(AdjPlan* a) {
@@ -808,6 +974,8 @@ mgx_status mgx_adjoint_destroy(mgx_adjoint* aa) {
   if (!a) return MGX_OK;
   drop_adj_graphs(a);
   if (a->fx_block) cudaFree(a->fx_block);
+  if (a->rfx_block) cudaFree(a->rfx_block);
+  if (a->gsplit_block) cudaFree(a->gsplit_block);
   if (a->cap_stream) cudaStreamDestroy(a->cap_stream);
   cudaFree(a->d_step);
   cudaFree(a->own_seg[0]);

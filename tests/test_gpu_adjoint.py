@@ -339,3 +339,29 @@ def test_adjoint_accumulates_only_requested_gradients(cuda):
     assert np.array_equal(out[0][0][:2], out[1][0][:2])        # dL/dJ1, dL/dD through T
     assert np.all(out[1][0][2:] == 0.0) and np.all(out[0][0][2:] != 0.0)
     assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_fixed_point_adjoint_equals_fp64_adjoint(cuda):
+    """The adjoint with the forward and the transposed gathers in exact 56-bit fixed point (the
+    neighbours' g in block floating point, aligned to the largest exponent) gives the gradients of
+    the all-FP64 adjoint to rounding: two-site bcc with four shells of full per-shell tensors (50
+    couplings per site), 300 K, d(mean energy after 30 steps)/d(shell tensors) and d/de(0)."""
+    from magex_gb300.adjoint import AdjointLLG, CouplingGroups, energy_per_site, llg_trajectory
+    from magex_gb300.workloads import bcc_two_site, uniaxial_sia
+    sc = bcc_two_site(L=6, J=(20.0, 10.0, -1.0, 1.0), dmi_frac=0.05, per="shell", seed=1, field=(0, 0, 0.3))
+    groups = CouplingGroups.per_shell(sc)
+    A0 = torch.as_tensor(np.stack([uniaxial_sia(0.01)] * 2))
+    B0 = torch.tensor([0.0, 0.0, 0.3], dtype=torch.float64)
+    out = {}
+    for precision in ("fp64", "fp64_fixed"):
+        adj = AdjointLLG(sc, groups, alpha=0.05, dt=1e-4, temperature=300.0, seed=4, seg_steps=10,
+                         cache_bytes=0, precision=precision)
+        T = torch.as_tensor(adj.T0).clone().requires_grad_(True)
+        e = torch.as_tensor(sc.init_spins("random", seed=7), device=adj.device).requires_grad_(True)
+        eT = llg_trajectory(adj, e, T, A0, B0, 30)
+        energy_per_site(sc, groups, eT, T, A0, B0).mean().backward()
+        out[precision] = (T.grad.numpy().copy(), e.grad.cpu().numpy())
+    gT64, ge64 = out["fp64"]
+    gTfx, gefx = out["fp64_fixed"]
+    assert np.abs(gTfx - gT64).max() <= 1e-10 * np.abs(gT64).max()
+    assert np.abs(gefx - ge64).max() <= 1e-10 * np.abs(ge64).max()
