@@ -20,6 +20,8 @@ kernels in oracle/, all host threads, its own ziggurat noise) on the same worklo
 from __future__ import annotations
 
 import argparse
+import atexit
+import datetime
 import json
 import os
 import statistics
@@ -53,55 +55,81 @@ def dist_env():
 
 # ------------------------------------------------------------------------------------ clocks
 class ClockSampler:
-    """nvidia-smi clock / throttle samples during the timed region (200 ms period)."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+    """nvidia-smi clock / throttle samples (50 ms period, each with nvidia-smi's own timestamp).
 
-    def __init__(self, index):
-        self.index = index
-        self.proc = None
+    Started well before the timed region (nvidia-smi needs a few hundred ms to come up); `summary`
+    keeps the samples whose timestamps fall between `mark_start` and `mark_end`.  A region shorter
+    than the period may hold none: then the last sample before it and the first after it stand in,
+    and the record says so (`window`)."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
-    def __enter__(self):
+    def __init__(self, index, period_ms=50):
+        self.index, self.period_ms = index, period_ms
+        self.proc, self.out, self.stopped = None, "", False
+        self.t0 = self.t1 = None
+
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self.proc = None
+        atexit.register(self.stop)          # never leave the sampler running after an error
         return self
 
-    def __exit__(self, *a):
-        self.out = ""
-        if self.proc is not None:
-            self.proc.terminate()
-            try:
-                self.out, _ = self.proc.communicate(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
-                self.out, _ = self.proc.communicate()
+    def mark_start(self):
+        self.t0 = datetime.datetime.now()
 
-    def summary(self):
-        if self.proc is None:
-            return None
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.out.strip().splitlines():
+    def mark_end(self):
+        self.t1 = datetime.datetime.now()
+
+    def stop(self):
+        if self.proc is None or self.stopped:
+            return
+        self.stopped = True
+        if self.proc.poll() is None:
+            self.proc.terminate()
+        try:
+            self.out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            self.out, _ = self.proc.communicate()
+
+    @classmethod
+    def parse(cls, text):
+        rows = []
+        for line in text.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 9:
+            if len(f) < 10:
                 continue
             try:
-                sm.append(float(f[1]))
-                smax.append(float(f[2]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f")
+                sm, smax = float(f[2]), float(f[3])
             except ValueError:
                 continue
-            for name, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        if not sm:
+            rows.append((ts, sm, smax, {n for n, v in zip(cls.NAMES, f[6:10]) if v.lower() == "active"}))
+        return rows
+
+    def summary(self):
+        if self.proc is None or self.t0 is None or self.t1 is None:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        rows = self.parse(self.out)
+        inside = [r for r in rows if self.t0 <= r[0] <= self.t1]
+        window = "timed region"
+        if not inside:
+            before = [r for r in rows if r[0] < self.t0]
+            after = [r for r in rows if r[0] > self.t1]
+            inside = before[-1:] + after[:1]
+            window = f"bracketing samples (timed region shorter than the {self.period_ms} ms period)"
+        if not inside:
+            return None
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": max(r[2] for r in inside),
+                "reasons": sorted(set().union(*(r[3] for r in inside))), "samples": len(inside),
+                "window": window, "period_ms": self.period_ms}
 
 
 # ------------------------------------------------------------------------------------ CPU (oracle) timing
@@ -835,6 +863,7 @@ def run_gb300(args):
     import ctypes as C
 
     lib = _lib.load()
+    clk = ClockSampler(local).start()   # running well before the timed region
     peak64 = C.c_double()
     _lib.check(lib.mgx_measure_fp64_peak(C.byref(peak64)), "fp64 peak")
 
@@ -869,13 +898,15 @@ def run_gb300(args):
     if ws > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        a_ev.record(stream)
-        sol.run_lattice(lat, K)
-        b_ev.record(stream)
-        torch.cuda.synchronize()
-        if ws > 1:
-            dist.barrier()
+    clk.mark_start()
+    a_ev.record(stream)
+    sol.run_lattice(lat, K)
+    b_ev.record(stream)
+    torch.cuda.synchronize()
+    clk.mark_end()
+    if ws > 1:
+        dist.barrier()
+    clk.stop()
     total_ms = a_ev.elapsed_time(b_ev)
     norm_err = float((torch.linalg.vector_norm(lat, dim=0) - 1).abs().max())
     if not (norm_err < 1e-12):
