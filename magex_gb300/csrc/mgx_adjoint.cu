@@ -548,15 +548,20 @@ __global__ void __launch_bounds__(256) k_adj_local(const AdjDev A, const double*
   adj_local_site(A, q, Z, Pp, H2, R, zbx, zby, zbz, eacc, pbar, f1bar, g2);
 }
 
+// Resident blocks per SM asked of the adjoint kernels in the fixed-point form: their FP64 work is
+// about two thirds of the all-FP64 form's, so occupancy (80 registers, a few spills) pays there; the
+// FP64 instantiations keep their registers (about 126) and stay bound by the FP64 pipe.  Measured on
+// the 1024^2 film (200 steps, fixed-point form): backward 213.5 -> 190.2 ms.
+constexpr int kAdjFxBlocks = 3;
+
 // Second kernel of step n: pbar += sum_rev J^T g2, xbar through the predictor normalisation
 // (p = x |x|^-1, both stored), the rhs adjoint at (e, H1), g1; stage-2 coupling and stage-1 single-ion
 // and field gradients.
 template <bool FX>
-__global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* __restrict__ E,
-                                                 const double* __restrict__ Pp, const double* __restrict__ H1,
-                                                 const double* __restrict__ R, double* __restrict__ eacc,
-                                                 const double* __restrict__ pbar, const double* __restrict__ f1bar,
-                                                 const double* __restrict__ g2, double* __restrict__ g1) {
+__device__ __forceinline__ void adj_mid_site(
+    const AdjDev& A, const double* __restrict__ E, const double* __restrict__ Pp, const double* __restrict__ H1,
+    const double* __restrict__ R, double* __restrict__ eacc, const double* __restrict__ pbar,
+    const double* __restrict__ f1bar, const double* __restrict__ g2, double* __restrict__ g1) {
   const DevLattice& L = A.F;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
@@ -629,12 +634,10 @@ __global__ void __launch_bounds__(256) k_adj_mid(const AdjDev A, const double* _
 // FUSE the site-local body of step n - 1 follows in the same thread on ebar_n, which is then never
 // stored; otherwise ebar_n is written out.
 template <bool FUSE, bool FX>
-__global__ void __launch_bounds__(256) k_adj_final(const AdjDev A, const double* __restrict__ E,
-                                                   double* __restrict__ eacc, const double* __restrict__ g1,
-                                                   double* __restrict__ ebar, const double* __restrict__ Pprev,
-                                                   const double* __restrict__ H2prev, const double* __restrict__ Rprev,
-                                                   double* __restrict__ pbar, double* __restrict__ f1bar,
-                                                   double* __restrict__ g2) {
+__device__ __forceinline__ void adj_final_site(
+    const AdjDev& A, const double* __restrict__ E, double* __restrict__ eacc, const double* __restrict__ g1,
+    double* __restrict__ ebar, const double* __restrict__ Pprev, const double* __restrict__ H2prev,
+    const double* __restrict__ Rprev, double* __restrict__ pbar, double* __restrict__ f1bar, double* __restrict__ g2) {
   const DevLattice& L = A.F;
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= L.N) return;
@@ -657,6 +660,34 @@ __global__ void __launch_bounds__(256) k_adj_final(const AdjDev A, const double*
     store3(ebar, N, q, ax + tx, ay + ty, az + tz);
   }
 }
+
+// The adjoint kernels: the FP64 form unbounded in registers, the fixed-point form at kAdjFxBlocks
+// blocks per SM.
+#define MGX_MID_PARAMS                                                                                          \
+  const AdjDev A, const double* __restrict__ E, const double* __restrict__ Pp, const double* __restrict__ H1,    \
+      const double* __restrict__ R, double* __restrict__ eacc, const double* __restrict__ pbar,                 \
+      const double* __restrict__ f1bar, const double* __restrict__ g2, double* __restrict__ g1
+#define MGX_FINAL_PARAMS                                                                                        \
+  const AdjDev A, const double* __restrict__ E, double* __restrict__ eacc, const double* __restrict__ g1,        \
+      double* __restrict__ ebar, const double* __restrict__ Pprev, const double* __restrict__ H2prev,           \
+      const double* __restrict__ Rprev, double* __restrict__ pbar, double* __restrict__ f1bar,                  \
+      double* __restrict__ g2
+__global__ void __launch_bounds__(256) k_adj_mid(MGX_MID_PARAMS) {
+  adj_mid_site<false>(A, E, Pp, H1, R, eacc, pbar, f1bar, g2, g1);
+}
+__global__ void __launch_bounds__(256, kAdjFxBlocks) k_adj_mid_fx(MGX_MID_PARAMS) {
+  adj_mid_site<true>(A, E, Pp, H1, R, eacc, pbar, f1bar, g2, g1);
+}
+template <bool FUSE>
+__global__ void __launch_bounds__(256) k_adj_final(MGX_FINAL_PARAMS) {
+  adj_final_site<FUSE, false>(A, E, eacc, g1, ebar, Pprev, H2prev, Rprev, pbar, f1bar, g2);
+}
+template <bool FUSE>
+__global__ void __launch_bounds__(256, kAdjFxBlocks) k_adj_final_fx(MGX_FINAL_PARAMS) {
+  adj_final_site<FUSE, true>(A, E, eacc, g1, ebar, Pprev, H2prev, Rprev, pbar, f1bar, g2);
+}
+#undef MGX_MID_PARAMS
+#undef MGX_FINAL_PARAMS
 
 // out[r] = sum of x[r*stride .. r*stride + len)  (one block per row, fixed-order tree)
 __global__ void __launch_bounds__(256) k_sum_rows(const double* __restrict__ x, long long len, long long stride,
@@ -772,26 +803,26 @@ static void enqueue_adj_backward(const AdjPlan* a, double* ebar, int nsteps, cud
                                     seg_ptr(a, last, SEG_H2), seg_ptr(a, last, SEG_R), ebar, eacc, pbar, f1bar, g2);
   for (int n = last; n >= 0; --n) {
     if (a->d.fixed)
-      k_adj_mid<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
+      k_adj_mid_fx<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
                                             seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
     else
-      k_adj_mid<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
+      k_adj_mid<<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), seg_ptr(a, n, SEG_P), seg_ptr(a, n, SEG_H1),
                                              seg_ptr(a, n, SEG_R), eacc, pbar, f1bar, g2, g1);
     if (n > 0) {
       if (a->d.fixed)
-        k_adj_final<true, true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr,
+        k_adj_final_fx<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr,
                                                       seg_ptr(a, n - 1, SEG_P), seg_ptr(a, n - 1, SEG_H2),
                                                       seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
       else
-        k_adj_final<true, false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr,
+        k_adj_final<true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, n, SEG_E), eacc, g1, nullptr,
                                                        seg_ptr(a, n - 1, SEG_P), seg_ptr(a, n - 1, SEG_H2),
                                                        seg_ptr(a, n - 1, SEG_R), pbar, f1bar, g2);
     } else {
       if (a->d.fixed)
-        k_adj_final<false, true><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr,
+        k_adj_final_fx<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr,
                                                        nullptr, nullptr, nullptr, nullptr);
       else
-        k_adj_final<false, false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr,
+        k_adj_final<false><<<grid, tpb, 0, st>>>(a->d, seg_ptr(a, 0, SEG_E), eacc, g1, ebar, nullptr, nullptr,
                                                         nullptr, nullptr, nullptr, nullptr);
     }
   }
