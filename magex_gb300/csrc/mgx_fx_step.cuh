@@ -169,16 +169,27 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
   F.eps[q] = fx_split<LIMB>(x); F.eps[N + q] = fx_split<LIMB>(y); F.eps[2 * N + q] = fx_split<LIMB>(z);
 }
 
+// the new spins of lattice site q (stencil layout) as row cell*ns + s of a magex-order (N, 3) array
+__device__ __forceinline__ void store_site_row(const DevLattice& L, double* __restrict__ rows, long long q, int s,
+                                               double x, double y, double z) {
+  double* r = rows + 3 * ((q - (long long)s * L.ncell) * L.ns + s);
+  r[0] = x; r[1] = y; r[2] = z;
+}
+
 // Corrector of site q: reads the neighbours' F.eps, P.k1 and e at q, writes e and its split F.es at q
-// (the new spins to eout instead of e when given; Hout and rout as in fx_predict_site).
-template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
+// (the new spins to eout instead of e when given; Hout and rout as in fx_predict_site).  ROWS (the
+// last stage of a step on host buffers, stencil layout): the new spins go to the magex-order rows
+// `rows` only, and neither e nor its split is written.
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false, bool ROWS = false>
 __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 double* __restrict__ e, const double* __restrict__ noise, long long q,
                                                 uint64_t step, double* __restrict__ Hout = nullptr,
                                                 double* __restrict__ eout = nullptr,
-                                                double* __restrict__ rout = nullptr) {
+                                                double* __restrict__ rout = nullptr,
+                                                double* __restrict__ rows = nullptr) {
   constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   if (L.pinned && L.pinned[q]) {                       // e and its split stay as they are
+    if (ROWS) store_site_row(L, rows, q, (int)(q / L.ncell), e[q], e[L.N + q], e[2 * L.N + q]);
     if (eout) {
       eout[q] = e[q]; eout[L.N + q] = e[L.N + q]; eout[2 * L.N + q] = e[2 * L.N + q];
     }
@@ -221,6 +232,10 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
   const double r = rsqrt(x * x + y * y + z * z);
   if (rout) rout[q] = r;
   x *= r; y *= r; z *= r;
+  if (ROWS) {
+    store_site_row(L, rows, q, s, x, y, z);
+    return;
+  }
   double* o = eout ? eout : e;
   o[q] = x; o[N + q] = y; o[2 * N + q] = z;
   F.es[q] = fx_split<LIMB>(x); F.es[N + q] = fx_split<LIMB>(y); F.es[2 * N + q] = fx_split<LIMB>(z);

@@ -180,17 +180,18 @@ struct LLGPlan {
   unsigned long long graph_clock = 0;
   long long last_tail = -1;      // step count of the previous call's ungraphed tail
   unsigned long long* d_step = nullptr;
-  // step on host buffers (mgx_llg_step_host): device copies of the spins, the copy stream and a
-  // second compute stream (consecutive slabs run on alternate streams so each fills the other's tail)
-  // (and a pack stream: the copies in run back to back on the copy stream while each landed slab is
-  // packed into the lattice layout on the pack stream)
-  // and two corrector streams: the corrector of a slab starts once the predictors of the slabs it
-  // gathers from are done, while the predictors of later slabs still run)
-  cudaStream_t copy_stream = nullptr, aux_stream = nullptr, pack_stream = nullptr;
+  // step on host buffers (mgx_llg_step_host): device copies of the spins, the copy stream (copies in)
+  // and a second compute stream (consecutive slabs run on alternate streams so each fills the other's
+  // tail), a pack stream (the copies in run back to back on the copy stream while each landed slab is
+  // packed into the lattice layout), two corrector streams (the corrector of a slab starts once the
+  // predictors of the slabs it gathers from are done, while the predictors of later slabs still run)
+  // and an out stream (each finished slab goes back to the host while the copies in still run: the
+  // two directions overlap)
+  cudaStream_t copy_stream = nullptr, aux_stream = nullptr, pack_stream = nullptr, out_stream = nullptr;
   cudaStream_t corr_stream[2] = {nullptr, nullptr};
   double* host_lat = nullptr;    // [3][N] lattice layout
   double* host_aos = nullptr;    // [N][3] magex order (staging of the copies)
-  // in[c] (packed) | out[c] (unpacked) | copied[c] | predicted[c] | start | done | joined aux | joined main
+  // in[c] (packed) | out[c] (corrected) | copied[c] | predicted[c] | start | done | joined aux | joined out
   cudaEvent_t host_ev[4 * MGX_HOST_CHUNKS + 4] = {};
   // the slab pipeline of a host-buffer step captured as a graph (step index from d_step), for the
   // last two (input, output) buffer pairs: replaying it costs one launch instead of ~250 API calls
@@ -228,11 +229,13 @@ void enqueue_df_step(const LLGPlan* pl, double* e, const double* noise, uint64_t
 mgx_status build_fx_tables(LLGPlan* pl);
 void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st);
 void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages);
-// The same stages on cells [cb, cb + cn) of every sublattice, and the split of those cells only
-// (the slabs of mgx_llg_step_host).
+// The same stages on cells [cb, cb + cn) of every sublattice (the slabs of mgx_llg_step_host); with
+// `rows` the corrector writes the new spins of those cells to the magex-order (N, 3) rows only.  The
+// fused packing of magex-order rows [begin, begin + count) into e and its fixed-point split.
 void enqueue_fx_range(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages,
-                      long long cb, long long cn);
-void enqueue_fx_split_cells(const LLGPlan* pl, const double* e, cudaStream_t st, long long cb, long long cn);
+                      long long cb, long long cn, double* rows = nullptr);
+void enqueue_fx_pack_split(const LLGPlan* pl, const double* rows, double* lat, long long begin, long long count,
+                           cudaStream_t st);
 
 // Host-side NVTX range over one library call (named in profiler timelines; a no-op without a tool).
 struct NvtxRange {

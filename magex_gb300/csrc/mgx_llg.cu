@@ -218,7 +218,8 @@ static void drop_host_buffers(LLGPlan* pl) {
   if (pl->copy_stream) cudaStreamDestroy(pl->copy_stream);
   if (pl->aux_stream) cudaStreamDestroy(pl->aux_stream);
   if (pl->pack_stream) cudaStreamDestroy(pl->pack_stream);
-  pl->copy_stream = pl->aux_stream = pl->pack_stream = nullptr;
+  if (pl->out_stream) cudaStreamDestroy(pl->out_stream);
+  pl->copy_stream = pl->aux_stream = pl->pack_stream = pl->out_stream = nullptr;
   for (cudaStream_t& cst : pl->corr_stream) {
     if (cst) cudaStreamDestroy(cst);
     cst = nullptr;
@@ -445,7 +446,7 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
   cudaEvent_t* ev_copied = pl->host_ev + 2 * MGX_HOST_CHUNKS;
   cudaEvent_t* ev_pred = pl->host_ev + 3 * MGX_HOST_CHUNKS;
   cudaEvent_t ev_start = pl->host_ev[4 * MGX_HOST_CHUNKS], ev_done = pl->host_ev[4 * MGX_HOST_CHUNKS + 1];
-  cudaEvent_t ev_join_aux = pl->host_ev[4 * MGX_HOST_CHUNKS + 2];
+  cudaEvent_t ev_join_aux = pl->host_ev[4 * MGX_HOST_CHUNKS + 2], ev_join_out = pl->host_ev[4 * MGX_HOST_CHUNKS + 3];
   const long long layer = (long long)L.L1 * L.L2;
   auto cell0 = [&](int c) { return (long long)L.L0 * c / nc * layer; };    // first cell of slab c
   MGX_CUDA_TRY(cudaEventRecord(ev_start, ms));
@@ -463,8 +464,10 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
     // slabs: the next copy does not wait for this slab's packing (pack stream)
     MGX_CUDA_TRY(cudaEventRecord(ev_copied[c], cs));
     MGX_CUDA_TRY(cudaStreamWaitEvent(ps, ev_copied[c], 0));
-    enqueue_pack(m, pl->host_aos, pl->host_lat, sb, se - sb, ps);
-    if (fx) enqueue_fx_split_cells(pl, pl->host_lat, ps, cell0(c), cell0(c + 1) - cell0(c));
+    if (fx)
+      enqueue_fx_pack_split(pl, pl->host_aos, pl->host_lat, sb, se - sb, ps);
+    else
+      enqueue_pack(m, pl->host_aos, pl->host_lat, sb, se - sb, ps);
     MGX_CUDA_TRY(cudaEventRecord(ev_in[c], ps));
   }
   double* lat = pl->host_lat;
@@ -477,8 +480,9 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
     MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_out[0], 0));
     MGX_CUDA_TRY(cudaMemcpyAsync(e_out, pl->host_aos, sizeof(double) * 3 * N, cudaMemcpyDefault, cs));
   } else {
-    cudaStream_t run[2] = {ms, pl->aux_stream};
+    cudaStream_t run[2] = {ms, pl->aux_stream}, os = pl->out_stream;
     MGX_CUDA_TRY(cudaStreamWaitEvent(run[1], ev_start, 0));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(os, ev_start, 0));
     // predictors: slab c gathers from slabs c-1 .. c+1 (cyclically when axis 0 is periodic); the
     // copies land in slab order, so waiting for the last slab needed is enough
     const bool ring = L.pbc0 != 0;
@@ -503,25 +507,29 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
         if (n >= 0 && n < nc) MGX_CUDA_TRY(cudaStreamWaitEvent(st, ev_pred[n], 0));
         else if (ring) MGX_CUDA_TRY(cudaStreamWaitEvent(st, ev_pred[(n + nc) % nc], 0));
       }
-      if (fx)
-        enqueue_fx_range(pl, lat, noise, step, st, 2, cell0(c), cell0(c + 1) - cell0(c));
-      else
-        enqueue_fp64_range(pl, lat, noise, step, st, 2, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
       const long long sb = cell0(c) * L.ns, se = cell0(c + 1) * L.ns;
-      enqueue_unpack(m, lat, pl->host_aos, sb, se - sb, st);
+      if (fx) {
+        // the corrector writes the slab's new spins straight into the (N, 3) staging rows
+        enqueue_fx_range(pl, lat, noise, step, st, 2, cell0(c), cell0(c + 1) - cell0(c), pl->host_aos);
+      } else {
+        enqueue_fp64_range(pl, lat, noise, step, st, 2, CellRange{cell0(c), cell0(c + 1) - cell0(c)});
+        enqueue_unpack(m, lat, pl->host_aos, sb, se - sb, st);
+      }
       MGX_CUDA_TRY(cudaEventRecord(ev_out[c], st));
-      MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_out[c], 0));
+      MGX_CUDA_TRY(cudaStreamWaitEvent(os, ev_out[c], 0));
       MGX_CUDA_TRY(cudaMemcpyAsync(e_out + 3 * sb, pl->host_aos + 3 * sb, sizeof(double) * 3 * (se - sb),
-                                   cudaMemcpyDefault, cs));
+                                   cudaMemcpyDefault, os));
     }
   }
-  // the copy stream waited for every slab of the corrector streams (and, below, for the pack and the
-  // second predictor stream): `ms` continues after all of it
+  // the out stream waited for every slab of the corrector streams; the copy stream joins it, the pack
+  // stream and the second predictor stream: `ms` continues after all of it
   if (nc > 1) {
     MGX_CUDA_TRY(cudaEventRecord(ev_copied[0], ps));
     MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_copied[0], 0));
     MGX_CUDA_TRY(cudaEventRecord(ev_join_aux, pl->aux_stream));
     MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_join_aux, 0));
+    MGX_CUDA_TRY(cudaEventRecord(ev_join_out, pl->out_stream));
+    MGX_CUDA_TRY(cudaStreamWaitEvent(cs, ev_join_out, 0));
   }
   MGX_CUDA_TRY(cudaEventRecord(ev_done, cs));
   MGX_CUDA_TRY(cudaStreamWaitEvent(ms, ev_done, 0));
@@ -531,10 +539,11 @@ static mgx_status enqueue_host_step(LLGPlan* pl, const double* e_in, double* e_o
 
 // Copies of host buffers inside one step.  The input goes to the device in axis-0 slabs on the plan's
 // copy stream (each packed into the lattice layout as it lands, and for the fixed-point-gather forms
-// split into its fixed-point copy); the predictor of a slab starts once
+// split into its fixed-point copy in the same pass); the predictor of a slab starts once
 // the slabs it gathers from (its own and its neighbours', every slab at least as thick as the
-// couplings' reach) are in; the corrector runs slab by slab and each finished slab goes back to the
-// host while the next ones are computed.  Consecutive slabs alternate between the caller's stream and
+// couplings' reach) are in; the corrector runs slab by slab (the fixed-point forms' corrector writes
+// the new spins straight into the (N, 3) staging rows) and each finished slab goes back to the host on
+// the out stream while the next ones are computed.  Consecutive slabs alternate between the caller's stream and
 // a second compute stream, so the blocks of one slab fill the tail of the previous one.  The
 // predictor and corrector kernels, and so the result, are those of mgx_llg_step: only the launch grid
 // is split.
@@ -559,6 +568,7 @@ mgx_status mgx_llg_step_host(mgx_llg* pp, const double* e_in, double* e_out, con
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->pack_stream, cudaStreamNonBlocking);
     for (cudaStream_t& cst : pl->corr_stream)
       if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->out_stream, cudaStreamNonBlocking);
     if (err == cudaSuccess) err = cudaStreamCreateWithFlags(&pl->copy_stream, cudaStreamNonBlocking);
     if (err != cudaSuccess) {
       drop_host_buffers(pl);

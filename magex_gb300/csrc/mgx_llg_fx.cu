@@ -31,16 +31,6 @@ __global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, 
   if (i < n) xs[i] = fx_split<PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24>(x[i]);
 }
 
-// The split of cells [cb, cb + cn) of every sublattice (blockIdx.y) and component (blockIdx.z).
-template <int PREC>
-__global__ void __launch_bounds__(256) k_fx_split_cells(const double* __restrict__ x, int2* __restrict__ xs,
-                                                        long long N, int ncell, long long cb, long long cn) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= cn) return;
-  const long long q = (long long)blockIdx.z * N + (long long)blockIdx.y * ncell + cb + i;
-  xs[q] = fx_split<PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24>(x[q]);
-}
-
 // Sites begin + i (i < count) of sublattice blockIdx.y: the whole lattice is one row of N sites
 // (gridDim.y = 1, begin = 0), a range of cells one row of `count` cells per sublattice.
 template <int NOISE, int INTEG, int PREC, bool HIGHER>
@@ -53,19 +43,41 @@ __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const
                                                 P.step_base ? *P.step_base + step : step);
 }
 
-template <int NOISE, int INTEG, int PREC, bool HIGHER>
+template <int NOISE, int INTEG, int PREC, bool HIGHER, bool ROWS = false>
 __global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                        double* __restrict__ e, const double* __restrict__ noise,
-                                                       uint64_t step, long long begin, long long count) {
+                                                       uint64_t step, long long begin, long long count,
+                                                       double* __restrict__ rows = nullptr) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
-    fx_correct_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
-                                                P.step_base ? *P.step_base + step : step);
+    fx_correct_site<NOISE, INTEG, PREC, HIGHER, ROWS>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+                                                      P.step_base ? *P.step_base + step : step, nullptr, nullptr,
+                                                      nullptr, rows);
+}
+
+// Magex-order rows [begin, begin + count) of an (N, 3) array -> lattice layout (3, N) and its fixed-point
+// split, in one pass (the input slabs of a step on host buffers)
+template <int LIMB>
+__global__ void __launch_bounds__(256) k_pack_split(const double* __restrict__ rows, double* __restrict__ lat,
+                                                    int2* __restrict__ xs, int ns, int ncell, long long N,
+                                                    long long begin, long long count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const long long site = begin + i;
+  const long long cell = site / ns;
+  const int s = (int)(site - cell * ns);
+  const long long q = (long long)s * ncell + cell;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double v = rows[3 * site + c];
+    lat[c * N + q] = v;
+    xs[c * N + q] = fx_split<LIMB>(v);
+  }
 }
 
 template <int NOISE, int INTEG, int PREC>
 static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st,
-                      long long cb, long long cn) {
+                      long long cb, long long cn, double* rows) {
   const DevLattice& L = pl->model->d;
   DevFX F = pl->fx;
   F.B[0] = split_host(L.B0);
@@ -80,39 +92,56 @@ static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_
   constexpr bool H = PREC == MGX_PRECISION_FP64_FIXED_GATHER;
   if (H && has_higher_onsite(L)) {
     if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
-    if (stages & 2) k_correct_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+    if ((stages & 2) && rows)
+      k_correct_fx<NOISE, INTEG, PREC, H, true><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
+    else if (stages & 2)
+      k_correct_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
   } else {
     if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
-    if (stages & 2) k_correct_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+    if ((stages & 2) && rows)
+      k_correct_fx<NOISE, INTEG, PREC, false, true><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
+    else if (stages & 2)
+      k_correct_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
   }
 }
 
 template <int NOISE, int PREC>
 static void fx_integ(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st,
-                     long long cb, long long cn) {
+                     long long cb, long long cn, double* rows) {
   if (pl->p.integrator == MGX_INTEGRATOR_DEPONDT)
-    launch_fx<NOISE, MGX_INTEGRATOR_DEPONDT, PREC>(pl, e, noise, step, stages, st, cb, cn);
+    launch_fx<NOISE, MGX_INTEGRATOR_DEPONDT, PREC>(pl, e, noise, step, stages, st, cb, cn, rows);
   else
-    launch_fx<NOISE, MGX_INTEGRATOR_HEUN, PREC>(pl, e, noise, step, stages, st, cb, cn);
+    launch_fx<NOISE, MGX_INTEGRATOR_HEUN, PREC>(pl, e, noise, step, stages, st, cb, cn, rows);
 }
 
 template <int PREC>
 static void fx_noise(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st,
-                     long long cb, long long cn) {
+                     long long cb, long long cn, double* rows) {
   const int mode = pl->sigma_zero ? MGX_NOISE_NONE : pl->p.noise;
   switch (mode) {
-    case MGX_NOISE_HOST: fx_integ<MGX_NOISE_HOST, PREC>(pl, e, noise, step, stages, st, cb, cn); break;
-    case MGX_NOISE_PHILOX: fx_integ<MGX_NOISE_PHILOX, PREC>(pl, e, noise, step, stages, st, cb, cn); break;
-    default: fx_integ<MGX_NOISE_NONE, PREC>(pl, e, noise, step, stages, st, cb, cn); break;
+    case MGX_NOISE_HOST: fx_integ<MGX_NOISE_HOST, PREC>(pl, e, noise, step, stages, st, cb, cn, rows); break;
+    case MGX_NOISE_PHILOX: fx_integ<MGX_NOISE_PHILOX, PREC>(pl, e, noise, step, stages, st, cb, cn, rows); break;
+    default: fx_integ<MGX_NOISE_NONE, PREC>(pl, e, noise, step, stages, st, cb, cn, rows); break;
   }
 }
 
 void enqueue_fx_range(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages,
-                      long long cb, long long cn) {
+                      long long cb, long long cn, double* rows) {
   if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
-    fx_noise<MGX_PRECISION_FP64_FIXED_GATHER>(pl, e, noise, step, stages, st, cb, cn);
+    fx_noise<MGX_PRECISION_FP64_FIXED_GATHER>(pl, e, noise, step, stages, st, cb, cn, rows);
   else
-    fx_noise<MGX_PRECISION_INT48_GATHER>(pl, e, noise, step, stages, st, cb, cn);
+    fx_noise<MGX_PRECISION_INT48_GATHER>(pl, e, noise, step, stages, st, cb, cn, rows);
+}
+
+void enqueue_fx_pack_split(const LLGPlan* pl, const double* rows, double* lat, long long begin, long long count,
+                           cudaStream_t st) {
+  const DevLattice& L = pl->model->d;
+  if (count <= 0) return;
+  const unsigned grid = (unsigned)((count + 255) / 256);
+  if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
+    k_pack_split<28><<<grid, 256, 0, st>>>(rows, lat, pl->fx.es, L.ns, L.ncell, L.N, begin, count);
+  else
+    k_pack_split<24><<<grid, 256, 0, st>>>(rows, lat, pl->fx.es, L.ns, L.ncell, L.N, begin, count);
 }
 
 void enqueue_fx_step(const LLGPlan* pl, double* e, const double* noise, uint64_t step, cudaStream_t st, int stages) {
@@ -128,15 +157,6 @@ void enqueue_fx_split(const LLGPlan* pl, const double* e, cudaStream_t st) {
     k_fx_split<MGX_PRECISION_INT48_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, n);
 }
 
-void enqueue_fx_split_cells(const LLGPlan* pl, const double* e, cudaStream_t st, long long cb, long long cn) {
-  const DevLattice& L = pl->model->d;
-  if (cn <= 0) return;
-  const dim3 grid((unsigned)((cn + 255) / 256), (unsigned)L.ns, 3u);
-  if (pl->precision == MGX_PRECISION_FP64_FIXED_GATHER)
-    k_fx_split_cells<MGX_PRECISION_FP64_FIXED_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, L.N, L.ncell, cb, cn);
-  else
-    k_fx_split_cells<MGX_PRECISION_INT48_GATHER><<<grid, 256, 0, st>>>(e, pl->fx.es, L.N, L.ncell, cb, cn);
-}
 
 // balanced (hi, lo) int32 halves of round(v 2^(2 limb - sigma)), |v| <= 2^sigma
 static int2 fx_host(double v, int sigma, int limb) {

@@ -263,30 +263,42 @@ def test_graph_replayed_run_equals_direct_launches(cuda, precision):
         assert torch.equal(la, lb), n
 
 
-@pytest.mark.parametrize("shells,pbc0,noise,precision,L", [
-    ((20.0, 10.0, -1.0), True, "philox", "fp64", (96, 76, 76)),
-    ((20.0, 10.0, -1.0, 1.0), True, "philox", "fp64", (96, 76, 76)),   # 4th shell: couplings reach 2 layers
-    ((20.0, 10.0, -1.0), False, "philox", "fp64", (96, 76, 76)),        # open along the slab axis
-    ((20.0, 10.0, -1.0), True, "host", "fp64", (96, 76, 76)),
-    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76)),  # slabs, each split as it lands
-    ((20.0, 10.0, -1.0, 1.0), False, "host", "fp64_fixed", (96, 76, 76)),  # open axis 0, reach 2, host noise
-    ((20.0, 10.0, -1.0), True, "philox", "int48", (96, 76, 76)),
-    ((20.0, 10.0, -1.0), True, "philox", "df32", (96, 76, 76)),        # one piece (reduced split refreshed)
-    ((20.0, 10.0, -1.0), True, "philox", "fp64", (4, 512, 256)),      # four slabs of one layer
-    ((20.0, 10.0, -1.0), False, "philox", "fp64", (2, 512, 512)),     # too thin to split: one piece
+@pytest.mark.parametrize("shells,pbc0,noise,precision,L,extra", [
+    ((20.0, 10.0, -1.0), True, "philox", "fp64", (96, 76, 76), None),
+    ((20.0, 10.0, -1.0, 1.0), True, "philox", "fp64", (96, 76, 76), None),   # 4th shell: couplings reach 2 layers
+    ((20.0, 10.0, -1.0), False, "philox", "fp64", (96, 76, 76), None),        # open along the slab axis
+    ((20.0, 10.0, -1.0), True, "host", "fp64", (96, 76, 76), None),
+    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76), None),  # slabs, each split as it lands
+    ((20.0, 10.0, -1.0, 1.0), False, "host", "fp64_fixed", (96, 76, 76), None),  # open axis 0, reach 2, host noise
+    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76), "pinned"),   # pinned sites keep their spins
+    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76), "depondt"),
+    ((20.0, 10.0, -1.0), True, "philox", "fp64_fixed", (96, 76, 76), "higher"),   # cubic + higher uniaxial
+    ((20.0, 10.0, -1.0), True, "philox", "int48", (96, 76, 76), None),
+    ((20.0, 10.0, -1.0), True, "philox", "df32", (96, 76, 76), None),        # one piece (reduced split refreshed)
+    ((20.0, 10.0, -1.0), True, "philox", "fp64", (4, 512, 256), None),      # four slabs of one layer
+    ((20.0, 10.0, -1.0), False, "philox", "fp64", (2, 512, 512), None),     # too thin to split: one piece
 ])
-def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precision, L):
+def test_host_buffer_step_equals_device_step(cuda, shells, pbc0, noise, precision, L, extra):
     """mgx_llg_step_host (pinned host buffers; copies in axis-0 slabs overlapping the stages for FP64
-    and fixed-point-gather plans of >= 2^20 sites) gives the same bits as the step on device spins:
-    also in place, and for pageable numpy input (one piece)."""
+    and fixed-point-gather plans of >= 2^20 sites; the fixed-point slabs packed and split in one pass
+    and their correctors writing the (N, 3) rows directly) gives the same bits as the step on device
+    spins: also in place, and for pageable numpy input (one piece)."""
     from magex_gb300.lattice import Supercell
     from magex_gb300.llg import GB300LLG
     from magex_gb300.spinmodel import load_results
     from magex_gb300.workloads import bcc_two_site_model
     sc = Supercell(load_results(bcc_two_site_model(J=shells)), L, (pbc0, True, True), (0.0, 0.0, 0.5))
     assert sc.N >= 1 << 20
-    a = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision)
-    b = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision)
+    rng = np.random.default_rng(9)
+    if extra == "pinned":
+        sc.pinned = rng.random(sc.N) < 0.05
+    if extra == "higher":
+        C = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+        sc.cubic = (rng.uniform(0.01, 0.05, sc.N), C)
+        sc.uniaxial_higher = (rng.uniform(0.0, 0.02, sc.N), rng.uniform(0.0, 0.01, sc.N), np.array([0.0, 0.6, 0.8]))
+    integ = "depondt" if extra == "depondt" else "heun"
+    a = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision, integrator=integ)
+    b = GB300LLG(sc, 0.05, 1e-4, 300.0, seed=5, noise=noise, precision=precision, integrator=integ)
     e0 = sc.init_spins("random", seed=3)
     h = torch.from_numpy(e0.copy()).pin_memory()
     out = torch.empty_like(h).pin_memory()
