@@ -23,9 +23,21 @@ __device__ __forceinline__ int2 fx_split(double x) {
   return fx_halves<LIMB>(double_to_ll_scaled(x, 2 * LIMB));
 }
 
+// c + a b exactly (64-bit two's complement), as a carry chain on the 32-bit halves: the low word of
+// the product added with carry out, then the signed high word with that carry in.  Timed against
+// `mad.wide.s32` on the bcc 128^3 step (CUDA events, 100 steps, identical spins): 1.089 against
+// 1.185 ms per step, with fewer spilled registers.
 __device__ __forceinline__ long long mad_wide(int a, int b, long long c) {
   long long d;
-  asm("mad.wide.s32 %0, %1, %2, %3;" : "=l"(d) : "r"(a), "r"(b), "l"(c));
+  asm("{\n\t"
+      ".reg .u32 lo, hi;\n\t"
+      "mov.b64 {lo, hi}, %3;\n\t"
+      "mad.lo.cc.u32 lo, %1, %2, lo;\n\t"
+      "madc.hi.s32 hi, %1, %2, hi;\n\t"
+      "mov.b64 %0, {lo, hi};\n\t"
+      "}"
+      : "=l"(d)
+      : "r"(a), "r"(b), "l"(c));
   return d;
 }
 
