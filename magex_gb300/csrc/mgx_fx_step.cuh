@@ -33,8 +33,12 @@ __device__ __forceinline__ void fx_gather64(const DevLattice& L, const DevFX& F,
   FxAcc a;
   fx_accumulate(L, F, xs, q, s, c0, c1, c2, a);
   const int e2 = F.scale_exp[s];
+  const double sc = F.scale[s];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) h[c] = ll_to_double_scaled(a.hh[c] + ((a.x[c] + (1LL << 27)) >> 28), e2);
+  for (int c = 0; c < 3; ++c) {
+    const long long t = a.hh[c] + ((a.x[c] + (1LL << 27)) >> 28);
+    h[c] = F.hw_convert ? __ll2double_rn(t) * sc : ll_to_double_scaled(t, e2);   // the same rounding
+  }
 }
 
 // spin of the site as a (hi, lo) float pair from its fixed-point halves (exact)
@@ -111,7 +115,7 @@ __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P,
   by = h[1] + L.B1;
   bz = h[2] + L.B2;
   if (HIGHER) add_higher_onsite(L, q, s, sx, sy, sz, bx, by, bz);
-  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz);
+  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz, PREC == MGX_PRECISION_FP64_FIXED_GATHER && F.hw_convert);
 }
 
 // Predictor of site q (0 <= q < L.N) of the fixed-point forms: writes P.ep, P.k1 and the split F.eps at q.
@@ -166,7 +170,8 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
   }
   P.ep[q] = x; P.ep[N + q] = y; P.ep[2 * N + q] = z;
   P.k1[q] = f[0]; P.k1[N + q] = f[1]; P.k1[2 * N + q] = f[2];
-  F.eps[q] = fx_split<LIMB>(x); F.eps[N + q] = fx_split<LIMB>(y); F.eps[2 * N + q] = fx_split<LIMB>(z);
+  F.eps[q] = fx_split<LIMB>(x, F.hw_convert); F.eps[N + q] = fx_split<LIMB>(y, F.hw_convert);
+  F.eps[2 * N + q] = fx_split<LIMB>(z, F.hw_convert);
 }
 
 // the new spins of lattice site q (stencil layout) as row cell*ns + s of a magex-order (N, 3) array
@@ -177,10 +182,10 @@ __device__ __forceinline__ void store_site_row(const DevLattice& L, double* __re
 }
 
 // Corrector of site q: reads the neighbours' F.eps, P.k1 and e at q, writes e and its split F.es at q
-// (the new spins to eout instead of e when given; Hout and rout as in fx_predict_site).  ROWS (the
-// last stage of a step on host buffers, stencil layout): the new spins go to the magex-order rows
+// (the new spins to eout instead of e when given; Hout and rout as in fx_predict_site).  With rows
+// (the last stage of a step on host buffers, stencil layout) the new spins go to the magex-order rows
 // `rows` only, and neither e nor its split is written.
-template <int NOISE, int INTEG, int PREC, bool HIGHER = false, bool ROWS = false>
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
 __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 double* __restrict__ e, const double* __restrict__ noise, long long q,
                                                 uint64_t step, double* __restrict__ Hout = nullptr,
@@ -189,7 +194,7 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
                                                 double* __restrict__ rows = nullptr) {
   constexpr int LIMB = PREC == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   if (L.pinned && L.pinned[q]) {                       // e and its split stay as they are
-    if (ROWS) store_site_row(L, rows, q, (int)(q / L.ncell), e[q], e[L.N + q], e[2 * L.N + q]);
+    if (rows) store_site_row(L, rows, q, (int)(q / L.ncell), e[q], e[L.N + q], e[2 * L.N + q]);
     if (eout) {
       eout[q] = e[q]; eout[L.N + q] = e[L.N + q]; eout[2 * L.N + q] = e[2 * L.N + q];
     }
@@ -232,13 +237,14 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
   const double r = rsqrt(x * x + y * y + z * z);
   if (rout) rout[q] = r;
   x *= r; y *= r; z *= r;
-  if (ROWS) {
+  if (rows) {
     store_site_row(L, rows, q, s, x, y, z);
     return;
   }
   double* o = eout ? eout : e;
   o[q] = x; o[N + q] = y; o[2 * N + q] = z;
-  F.es[q] = fx_split<LIMB>(x); F.es[N + q] = fx_split<LIMB>(y); F.es[2 * N + q] = fx_split<LIMB>(z);
+  F.es[q] = fx_split<LIMB>(x, F.hw_convert); F.es[N + q] = fx_split<LIMB>(y, F.hw_convert);
+  F.es[2 * N + q] = fx_split<LIMB>(z, F.hw_convert);
 }
 
 }  // namespace mgx

@@ -141,6 +141,12 @@ struct DevFX {
   int scale_exp[MGX_MAX_SUBLATTICES];  // sigma_s - 2 limb (the same scale as a power of two)
   float2 alpha[MGX_MAX_SUBLATTICES], pre[MGX_MAX_SUBLATTICES], sig[MGX_MAX_SUBLATTICES];
   float2 B[3];                   // (hi, lo) split of the external field, refreshed at every launch
+  // 1: the conversions between the fixed-point values and FP64 (and of the FP32 noise draws) use the
+  // hardware converters, which run on the FP64 pipe; 0: exact bit manipulation on the integer pipes.
+  // Set by fx_build from the couplings per site: where there are many, the integer pipes are the
+  // busier side and the FP64 pipe has room (bcc 128^3, 26 couplings: 1.089 -> 1.047 ms per step);
+  // where there are few, the FP64 pipe is (triangular film 2048^2, 6 couplings: 0.697 -> 0.840 ms).
+  int hw_convert;
   int2* es;                      // [3][N] fixed-point split of e
   int2* eps;                     // [3][N] fixed-point split of ep
 };
@@ -501,8 +507,9 @@ __device__ __forceinline__ long long double_to_ll_scaled(double x, int k) {
   return (u >> 63) ? -(long long)v : (long long)v;
 }
 
+// (hw: the FP32 draws widened by the hardware conversion instead of on the integer pipes; same values)
 __device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uint64_t step, double& g0, double& g1,
-                                               double& g2) {
+                                               double& g2, bool hw = false) {
   const uint4 r = philox4x32_10(make_uint4((uint32_t)site, (uint32_t)(site >> 32), (uint32_t)step,
                                            (uint32_t)(step >> 32)),
                                 make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
@@ -514,9 +521,10 @@ __device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uin
   const float m3 = sqrtf(-2.0f * logf(u3));
   float s1, c1;
   sincospif(2.0f * v1, &s1, &c1);
-  g0 = f32_to_f64(m1 * c1);
-  g1 = f32_to_f64(m1 * s1);
-  g2 = f32_to_f64(m3 * cospif(2.0f * v3));
+  const float f0 = m1 * c1, f1 = m1 * s1, f2 = m3 * cospif(2.0f * v3);
+  g0 = hw ? (double)f0 : f32_to_f64(f0);
+  g1 = hw ? (double)f1 : f32_to_f64(f1);
+  g2 = hw ? (double)f2 : f32_to_f64(f2);
 }
 
 }  // namespace mgx

@@ -43,16 +43,19 @@ __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const
                                                 P.step_base ? *P.step_base + step : step);
 }
 
-template <int NOISE, int INTEG, int PREC, bool HIGHER, bool ROWS = false>
+// rows != nullptr (the slabs of a step on host buffers): the new spins go to those magex-order rows
+// only.  A run-time choice, so that the host-buffer step runs the very kernel of the device step and
+// gives its bits whatever the compiler makes of either.
+template <int NOISE, int INTEG, int PREC, bool HIGHER>
 __global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                        double* __restrict__ e, const double* __restrict__ noise,
                                                        uint64_t step, long long begin, long long count,
-                                                       double* __restrict__ rows = nullptr) {
+                                                       double* __restrict__ rows) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
-    fx_correct_site<NOISE, INTEG, PREC, HIGHER, ROWS>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
-                                                      P.step_base ? *P.step_base + step : step, nullptr, nullptr,
-                                                      nullptr, rows);
+    fx_correct_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
+                                                P.step_base ? *P.step_base + step : step, nullptr, nullptr,
+                                                nullptr, rows);
 }
 
 // Magex-order rows [begin, begin + count) of an (N, 3) array -> lattice layout (3, N) and its fixed-point
@@ -92,16 +95,11 @@ static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_
   constexpr bool H = PREC == MGX_PRECISION_FP64_FIXED_GATHER;
   if (H && has_higher_onsite(L)) {
     if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
-    if ((stages & 2) && rows)
-      k_correct_fx<NOISE, INTEG, PREC, H, true><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
-    else if (stages & 2)
-      k_correct_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+    if (stages & 2) k_correct_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
   } else {
     if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
-    if ((stages & 2) && rows)
-      k_correct_fx<NOISE, INTEG, PREC, false, true><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
-    else if (stages & 2)
-      k_correct_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+    if (stages & 2)
+      k_correct_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
   }
 }
 
@@ -176,6 +174,10 @@ mgx_status fx_build(const Model* m, int limb, bool field_scaled, int ncopies, De
   std::vector<double> J((size_t)std::max(nb, 1) * W), A(9 * ns), inv(ns);
   std::vector<int4> geo((size_t)std::max(nb, 1));
   MGX_CUDA_TRY(cudaMemcpy(off.data(), d.bond_off, sizeof(int) * (ns + 1), cudaMemcpyDeviceToHost));
+  // conversions on the hardware converters for stencils of at least 16 couplings per site (see DevFX)
+  int zmax = 0;
+  for (int s = 0; s < ns; ++s) zmax = std::max(zmax, off[s + 1] - off[s]);
+  fx->hw_convert = zmax >= 16 ? 1 : 0;
   if (nb > 0) {
     MGX_CUDA_TRY(cudaMemcpy(J.data(), d.bond_J, sizeof(double) * nb * W, cudaMemcpyDeviceToHost));
     MGX_CUDA_TRY(cudaMemcpy(geo.data(), d.bond_geo, sizeof(int4) * nb, cudaMemcpyDeviceToHost));

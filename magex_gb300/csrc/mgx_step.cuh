@@ -55,7 +55,8 @@ __device__ __forceinline__ void add_sot(const DevLLG& P, double x, double y, dou
 
 template <int NOISE>
 __device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P, const double* __restrict__ noise,
-                                            long long q, int s, uint64_t step, double& bx, double& by, double& bz) {
+                                            long long q, int s, uint64_t step, double& bx, double& by, double& bz,
+                                            bool hw_convert = false) {
   if (NOISE == MGX_NOISE_NONE) return;
   const double sig = P.sigma_site ? __ldg(P.sigma_site + q) : __ldg(P.sigma_sub + s);
   double g0, g1, g2;
@@ -64,7 +65,7 @@ __device__ __forceinline__ void add_thermal(const DevLattice& L, const DevLLG& P
     g1 = __ldg(noise + L.N + q);
     g2 = __ldg(noise + 2 * L.N + q);
   } else {
-    philox_normal3(P.seed, magex_site(L, q, s), step, g0, g1, g2);
+    philox_normal3(P.seed, magex_site(L, q, s), step, g0, g1, g2, hw_convert);
   }
   bx = fma(sig, g0, bx);
   by = fma(sig, g1, by);
