@@ -377,25 +377,31 @@ __device__ __forceinline__ double uniaxial_higher_energy(const DevLattice& L, lo
 // dE/de of the higher on-site terms at site q (magex/fast.py:39-64 order: cubic, then uniaxial)
 __device__ __forceinline__ void higher_onsite_grad(const DevLattice& L, long long q, double x, double y, double z,
                                                    double& gx, double& gy, double& gz) {
+  // every rounding explicit (fma, or __dmul_rn / __dadd_rn where nothing may be fused), so that each
+  // kernel that inlines this gives the same bits whatever the compiler fuses around it
   gx = gy = gz = 0.0;
+  const double* C = L.C;
   if (L.Kc_site) {
-    const double a1 = L.C[0] * x + L.C[1] * y + L.C[2] * z;
-    const double a2 = L.C[3] * x + L.C[4] * y + L.C[5] * z;
-    const double a3 = L.C[6] * x + L.C[7] * y + L.C[8] * z;
-    const double q1 = a1 * a1, q2 = a2 * a2, q3 = a3 * a3;
-    const double kc = L.Kc_site[q];
-    const double d1 = 2.0 * a1 * (q2 + q3) * kc, d2 = 2.0 * a2 * (q1 + q3) * kc, d3 = 2.0 * a3 * (q1 + q2) * kc;
-    gx += d1 * L.C[0] + d2 * L.C[3] + d3 * L.C[6];
-    gy += d1 * L.C[1] + d2 * L.C[4] + d3 * L.C[7];
-    gz += d1 * L.C[2] + d2 * L.C[5] + d3 * L.C[8];
+    const double a1 = fma(C[0], x, fma(C[1], y, __dmul_rn(C[2], z)));
+    const double a2 = fma(C[3], x, fma(C[4], y, __dmul_rn(C[5], z)));
+    const double a3 = fma(C[6], x, fma(C[7], y, __dmul_rn(C[8], z)));
+    const double q1 = __dmul_rn(a1, a1), q2 = __dmul_rn(a2, a2), q3 = __dmul_rn(a3, a3);
+    const double kc2 = __dmul_rn(2.0, L.Kc_site[q]);
+    const double d1 = __dmul_rn(__dmul_rn(kc2, a1), __dadd_rn(q2, q3));
+    const double d2 = __dmul_rn(__dmul_rn(kc2, a2), __dadd_rn(q1, q3));
+    const double d3 = __dmul_rn(__dmul_rn(kc2, a3), __dadd_rn(q1, q2));
+    gx = fma(d3, C[6], fma(d2, C[3], __dmul_rn(d1, C[0])));
+    gy = fma(d3, C[7], fma(d2, C[4], __dmul_rn(d1, C[1])));
+    gz = fma(d3, C[8], fma(d2, C[5], __dmul_rn(d1, C[2])));
   }
   if (L.K2_site) {
-    const double c = x * L.u[0] + y * L.u[1] + z * L.u[2];
-    const double c2 = c * c;
-    const double f = -4.0 * L.K2_site[q] * c2 * c - 6.0 * L.K3_site[q] * c2 * c2 * c;
-    gx += f * L.u[0];
-    gy += f * L.u[1];
-    gz += f * L.u[2];
+    const double* u = L.u;
+    const double c = fma(x, u[0], fma(y, u[1], __dmul_rn(z, u[2])));
+    const double c2 = __dmul_rn(c, c), c3 = __dmul_rn(c2, c);
+    const double f = fma(__dmul_rn(-4.0, L.K2_site[q]), c3, __dmul_rn(__dmul_rn(-6.0, L.K3_site[q]), __dmul_rn(c2, c3)));
+    gx = fma(f, u[0], gx);
+    gy = fma(f, u[1], gy);
+    gz = fma(f, u[2], gz);
   }
 }
 
@@ -406,9 +412,9 @@ __device__ __forceinline__ void add_higher_onsite(const DevLattice& L, long long
   double gx, gy, gz;
   higher_onsite_grad(L, q, x, y, z, gx, gy, gz);
   const double inv = L.inv_mu_site ? L.inv_mu_site[q] : L.inv_mu_sub[s];
-  bx -= gx * inv;
-  by -= gy * inv;
-  bz -= gz * inv;
+  bx = fma(-gx, inv, bx);
+  by = fma(-gy, inv, by);
+  bz = fma(-gz, inv, bz);
 }
 
 // LLG right-hand side f = pre [e x B + alpha e x (e x B)], pre = -gamma / (1 + alpha^2)
