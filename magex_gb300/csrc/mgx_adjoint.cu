@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(256, 4) k_fwd_pred_fx(const DevLattice L, cons
                                                         double* __restrict__ H1, double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < L.N)
-    fx_predict_site<NOISE, MGX_INTEGRATOR_HEUN, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(
+    fx_predict_site<NOISE, MGX_INTEGRATOR_HEUN, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER, 0>(
         L, P, F, e, nullptr, q, P.step_base ? *P.step_base + step : step, H1, R);
 }
 
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(256, 4) k_fwd_corr_fx(const DevLattice L, cons
                                                         double* __restrict__ eout, double* __restrict__ R) {
   const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (q < L.N)
-    fx_correct_site<NOISE, MGX_INTEGRATOR_HEUN, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(
+    fx_correct_site<NOISE, MGX_INTEGRATOR_HEUN, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER, 0>(
         L, P, F, e, nullptr, q, P.step_base ? *P.step_base + step : step, H2, eout, R + L.N);
 }
 

@@ -99,9 +99,9 @@ __global__ void __launch_bounds__(BATCH_MAX_THREADS, 2) k_batch_stage(const Batc
     const double* ns = noise ? noise + S.off3 : nullptr;
     if (FIXED) {
       if (STAGE == 0)
-        fx_predict_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(S.L, S.P, S.F, es, ns, q, st);
+        fx_predict_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER, 0>(S.L, S.P, S.F, es, ns, q, st);
       else
-        fx_correct_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER>(S.L, S.P, S.F, es, ns, q, st);
+        fx_correct_site<NOISE, INTEG, MGX_PRECISION_FP64_FIXED_GATHER, HIGHER, 0>(S.L, S.P, S.F, es, ns, q, st);
       continue;
     }
     // the EXTRA bodies add the higher on-site fields (the spin-orbit torque and per-site extra field

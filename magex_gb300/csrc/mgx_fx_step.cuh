@@ -25,9 +25,19 @@ __device__ __forceinline__ void fx_gather(const DevLattice& L, const DevFX& F, c
   }
 }
 
+// Where the conversions of the fixed-point forms run (DevFX::hw_convert): HWC = 2 reads the plan's
+// flag at run time; 0 / 1 fix the integer pipes / the hardware converters at compile time (kernels
+// that carry no branch for it: the batched stages and the adjoint's recomputation, capped at few
+// registers, keep the integer pipes).
+template <int HWC>
+__device__ __forceinline__ bool fx_hw(const DevFX& F) {
+  return HWC == 2 ? F.hw_convert != 0 : HWC == 1;
+}
+
 // 56-bit form: field in FP64 = (hh + x 2^-28) 2^(sigma - 56): x rounded to units of 2^(sigma - 56)
 // in integer arithmetic (|t| < 2^58), then t converted to FP64 and scaled by the power of two in one
-// rounding, all on the integer pipes
+// rounding, on the integer pipes or the hardware converter (the same value)
+template <int HWC = 2>
 __device__ __forceinline__ void fx_gather64(const DevLattice& L, const DevFX& F, const int2* __restrict__ xs,
                                             long long q, int s, int c0, int c1, int c2, double h[3]) {
   FxAcc a;
@@ -37,7 +47,7 @@ __device__ __forceinline__ void fx_gather64(const DevLattice& L, const DevFX& F,
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const long long t = a.hh[c] + ((a.x[c] + (1LL << 27)) >> 28);
-    h[c] = F.hw_convert ? __ll2double_rn(t) * sc : ll_to_double_scaled(t, e2);   // the same rounding
+    h[c] = fx_hw<HWC>(F) ? __ll2double_rn(t) * sc : ll_to_double_scaled(t, e2);   // the same rounding
   }
 }
 
@@ -95,7 +105,7 @@ __device__ __forceinline__ void fx_rhs(const DevLattice& L, const DevLLG& P, con
 // the field of the Depondt integrator for both forms.  HIGHER (56-bit form only, a separate
 // instantiation) adds the cubic and higher-uniaxial fields at the site's FP64 spin (sx, sy, sz), in the
 // place the FP64 kernels add them: after the effective field, before the thermal field.
-template <int NOISE, int PREC, bool HIGHER = false>
+template <int NOISE, int PREC, bool HIGHER = false, int HWC = 2>
 __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                            const int2* __restrict__ xs, const double* __restrict__ noise,
                                            long long q, int s, int c0, int c1, int c2, uint64_t step, double& bx,
@@ -103,7 +113,7 @@ __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P,
                                            double sz = 0.0) {
   double h[3];
   if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
-    fx_gather64(L, F, xs, q, s, c0, c1, c2, h);
+    fx_gather64<HWC>(L, F, xs, q, s, c0, c1, c2, h);
   } else {
     dfp hp[3];
     fx_gather(L, F, xs, q, s, c0, c1, c2, hp);
@@ -115,13 +125,13 @@ __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P,
   by = h[1] + L.B1;
   bz = h[2] + L.B2;
   if (HIGHER) add_higher_onsite(L, q, s, sx, sy, sz, bx, by, bz);
-  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz, PREC == MGX_PRECISION_FP64_FIXED_GATHER && F.hw_convert);
+  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz, PREC == MGX_PRECISION_FP64_FIXED_GATHER && fx_hw<HWC>(F));
 }
 
 // Predictor of site q (0 <= q < L.N) of the fixed-point forms: writes P.ep, P.k1 and the split F.eps at q.
 // HIGHER: the 56-bit form with the model's cubic / higher-uniaxial terms.  The adjoint's recomputation
 // (56-bit Heun form) also stores the total field (Hout) and the inverse norm of the predictor (rout).
-template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false, int HWC = 2>
 __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 const double* __restrict__ e, const double* __restrict__ noise,
                                                 long long q, uint64_t step, double* __restrict__ Hout = nullptr,
@@ -144,7 +154,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
   if (INTEG == MGX_INTEGRATOR_HEUN) {
     if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
       double bx, by, bz;
-      fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
+      fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
       if (Hout) {
         Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
       }
@@ -161,7 +171,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
     x *= r; y *= r; z *= r;
   } else {
     double bx, by, bz;
-    fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
+    fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
     double fx, fy, fz;
     llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     f[0] = ey * fz - ez * fy; f[1] = ez * fx - ex * fz; f[2] = ex * fy - ey * fx;
@@ -170,8 +180,8 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
   }
   P.ep[q] = x; P.ep[N + q] = y; P.ep[2 * N + q] = z;
   P.k1[q] = f[0]; P.k1[N + q] = f[1]; P.k1[2 * N + q] = f[2];
-  F.eps[q] = fx_split<LIMB>(x, F.hw_convert); F.eps[N + q] = fx_split<LIMB>(y, F.hw_convert);
-  F.eps[2 * N + q] = fx_split<LIMB>(z, F.hw_convert);
+  F.eps[q] = fx_split<LIMB>(x, fx_hw<HWC>(F)); F.eps[N + q] = fx_split<LIMB>(y, fx_hw<HWC>(F));
+  F.eps[2 * N + q] = fx_split<LIMB>(z, fx_hw<HWC>(F));
 }
 
 // the new spins of lattice site q (stencil layout) as row cell*ns + s of a magex-order (N, 3) array
@@ -185,7 +195,7 @@ __device__ __forceinline__ void store_site_row(const DevLattice& L, double* __re
 // (the new spins to eout instead of e when given; Hout and rout as in fx_predict_site).  With rows
 // (the last stage of a step on host buffers, stencil layout) the new spins go to the magex-order rows
 // `rows` only, and neither e nor its split is written.
-template <int NOISE, int INTEG, int PREC, bool HIGHER = false>
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false, int HWC = 2>
 __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 double* __restrict__ e, const double* __restrict__ noise, long long q,
                                                 uint64_t step, double* __restrict__ Hout = nullptr,
@@ -213,7 +223,7 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
     if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
       const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
       double bx, by, bz;
-      fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
+      fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
       if (Hout) {
         Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
       }
@@ -228,7 +238,7 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
   } else {
     const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
     double bx, by, bz;
-    fx_field64<NOISE, PREC, HIGHER>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
+    fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
     double fx, fy, fz;
     llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     const double wx = py * fz - pz * fy, wy = pz * fx - px * fz, wz = px * fy - py * fx;
@@ -243,8 +253,8 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
   }
   double* o = eout ? eout : e;
   o[q] = x; o[N + q] = y; o[2 * N + q] = z;
-  F.es[q] = fx_split<LIMB>(x, F.hw_convert); F.es[N + q] = fx_split<LIMB>(y, F.hw_convert);
-  F.es[2 * N + q] = fx_split<LIMB>(z, F.hw_convert);
+  F.es[q] = fx_split<LIMB>(x, fx_hw<HWC>(F)); F.es[N + q] = fx_split<LIMB>(y, fx_hw<HWC>(F));
+  F.es[2 * N + q] = fx_split<LIMB>(z, fx_hw<HWC>(F));
 }
 
 }  // namespace mgx

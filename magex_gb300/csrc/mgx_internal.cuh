@@ -144,8 +144,10 @@ struct DevFX {
   // 1: the conversions between the fixed-point values and FP64 (and of the FP32 noise draws) use the
   // hardware converters, which run on the FP64 pipe; 0: exact bit manipulation on the integer pipes.
   // Set by fx_build from the couplings per site: where there are many, the integer pipes are the
-  // busier side and the FP64 pipe has room (bcc 128^3, 26 couplings: 1.089 -> 1.047 ms per step);
-  // where there are few, the FP64 pipe is (triangular film 2048^2, 6 couplings: 0.697 -> 0.840 ms).
+  // busier side and the FP64 pipe has room (bcc 128^3, 26 couplings: 1.089 -> 1.071 ms per step);
+  // where there are few, the FP64 pipe is (triangular film 2048^2, 6 couplings: 0.697 -> 0.840 ms
+  // with every conversion on the hardware), and so it is with the cubic / higher-uniaxial terms.
+  // Read at run time by the single-lattice kernels only (fx_hw<2>).
   int hw_convert;
   int2* es;                      // [3][N] fixed-point split of e
   int2* eps;                     // [3][N] fixed-point split of ep

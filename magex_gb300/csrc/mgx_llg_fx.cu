@@ -87,6 +87,10 @@ static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_
   F.B[1] = split_host(L.B1);
   F.B[2] = split_host(L.B2);
   const bool whole = cb == 0 && cn == L.ncell;
+  // the slabs of a step on host buffers keep the conversions on the integer pipes: there the slab
+  // kernels share the GPU with each other and with the packing (bcc 128^3: 1.343 ms per call against
+  // 1.352 with the hardware converters; the same kernel, so the same values either way)
+  if (!whole) F.hw_convert = 0;
   const long long count = whole ? L.N : cn;
   const int tpb = site_block_size(whole ? L.N : cn * L.ns);
   const dim3 grid((unsigned)((count + tpb - 1) / tpb), whole ? 1u : (unsigned)L.ns);
@@ -179,10 +183,11 @@ mgx_status fx_build(const Model* m, int limb, bool field_scaled, int ncopies, De
   std::vector<double> J((size_t)std::max(nb, 1) * W), A(9 * ns), inv(ns);
   std::vector<int4> geo((size_t)std::max(nb, 1));
   MGX_CUDA_TRY(cudaMemcpy(off.data(), d.bond_off, sizeof(int) * (ns + 1), cudaMemcpyDeviceToHost));
-  // conversions on the hardware converters for stencils of at least 16 couplings per site (see DevFX)
+  // conversions on the hardware converters for stencils of at least 16 couplings per site without the
+  // cubic / higher-uniaxial terms, whose FP64 work makes the FP64 pipe the busier side (see DevFX)
   int zmax = 0;
   for (int s = 0; s < ns; ++s) zmax = std::max(zmax, off[s + 1] - off[s]);
-  fx->hw_convert = zmax >= 16 ? 1 : 0;
+  fx->hw_convert = zmax >= 16 && !has_higher_onsite(d) ? 1 : 0;
   if (nb > 0) {
     MGX_CUDA_TRY(cudaMemcpy(J.data(), d.bond_J, sizeof(double) * nb * W, cudaMemcpyDeviceToHost));
     MGX_CUDA_TRY(cudaMemcpy(geo.data(), d.bond_geo, sizeof(int4) * nb, cudaMemcpyDeviceToHost));
