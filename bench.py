@@ -957,7 +957,11 @@ def run_gb300(args):
     else:
         hbm_peak, peak_src = 6800.0, "fallback"
     achieved = bytes_per_spin * N / (dom_ms * 1e-3) / 1e9
-    traffic = read_ncu_traffic().get(dominant.split(" + ")[-1])
+    # measured DRAM bytes per spin of every kernel of the timed pair (the split and the predictor for
+    # the fixed-point plan), None unless all of them were captured
+    per_kernel = read_ncu_traffic()
+    parts = [per_kernel.get(k) for k in dominant.split(" + ")]
+    traffic = None if any(v is None for v in parts) else sum(parts)
     flops_step = fp64_flops_per_spin_step(z)
     clocks = clk.summary()
     # the all-FP64 plan on the same workload, beside the default
