@@ -33,8 +33,14 @@ __global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, 
 
 // Sites begin + i (i < count) of sublattice blockIdx.y: the whole lattice is one row of N sites
 // (gridDim.y = 1, begin = 0), a range of cells one row of `count` cells per sublattice.
+// Resident blocks per SM of the stage kernels: 5 (48 registers and ~100 B of spills per thread) for
+// the plain bodies, 4 (64 registers) with the cubic / higher-uniaxial terms.  Timed on bcc 128^3
+// (CUDA events, 100 steps): 1.046 ms per step at 5 blocks, 1.076 at 4, 1.124 at 6; the triangular
+// film 2048^2 (6 couplings) 0.704 against 0.698 ms.
+constexpr int kFxBlocks = 5;
+
 template <int NOISE, int INTEG, int PREC, bool HIGHER>
-__global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
+__global__ void __launch_bounds__(256, HIGHER ? 4 : kFxBlocks) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                        const double* __restrict__ e, const double* __restrict__ noise,
                                                        uint64_t step, long long begin, long long count) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -47,7 +53,7 @@ __global__ void __launch_bounds__(256, 4) k_predict_fx(const DevLattice L, const
 // A separate instantiation: the device step's corrector carries no branch for it (a run-time pointer
 // cost 2.3 % of the bcc 128^3 step).
 template <int NOISE, int INTEG, int PREC, bool HIGHER, bool ROWS = false>
-__global__ void __launch_bounds__(256, 4) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
+__global__ void __launch_bounds__(256, HIGHER ? 4 : kFxBlocks) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
                                                        double* __restrict__ e, const double* __restrict__ noise,
                                                        uint64_t step, long long begin, long long count,
                                                        double* __restrict__ rows) {
