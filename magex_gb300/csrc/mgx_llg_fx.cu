@@ -33,16 +33,16 @@ __global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, 
 
 // Sites begin + i (i < count) of sublattice blockIdx.y: the whole lattice is one row of N sites
 // (gridDim.y = 1, begin = 0), a range of cells one row of `count` cells per sublattice.
-// Resident blocks per SM of the stage kernels: 5 (48 registers and ~100 B of spills per thread) for
-// the plain bodies, 4 (64 registers) with the cubic / higher-uniaxial terms.  Timed on bcc 128^3
-// (CUDA events, 100 steps): 1.046 ms per step at 5 blocks, 1.076 at 4, 1.124 at 6; the triangular
-// film 2048^2 (6 couplings) 0.704 against 0.698 ms.
-constexpr int kFxBlocks = 5;
-
-template <int NOISE, int INTEG, int PREC, bool HIGHER>
-__global__ void __launch_bounds__(256, HIGHER ? 4 : kFxBlocks) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
-                                                       const double* __restrict__ e, const double* __restrict__ noise,
-                                                       uint64_t step, long long begin, long long count) {
+// BLK: resident blocks per SM of the stage kernels.  5 (48 registers, ~100 B of spills per thread)
+// for stencils of at least 16 couplings per site without the higher on-site terms (the plans whose
+// conversions run on the hardware converters, DevFX::hw_convert), 4 (64 registers) otherwise.  Timed
+// with CUDA events over 100 steps: bcc 128^3 (26 couplings) 1.046 ms per step at 5, 1.076 at 4,
+// 1.124 at 6; the triangular film 2048^2 (6 couplings) 0.698 ms at 4, 0.704 at 5, and small films,
+// whose plans are launch- and latency-bound, about 8 % slower at 5.
+template <int NOISE, int INTEG, int PREC, bool HIGHER, int BLK>
+__global__ void __launch_bounds__(256, BLK) k_predict_fx(const DevLattice L, const DevLLG P, const DevFX F,
+                                                         const double* __restrict__ e, const double* __restrict__ noise,
+                                                         uint64_t step, long long begin, long long count) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
     fx_predict_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
@@ -52,11 +52,11 @@ __global__ void __launch_bounds__(256, HIGHER ? 4 : kFxBlocks) k_predict_fx(cons
 // ROWS (the slabs of a step on host buffers): the new spins go to the magex-order rows `rows` only.
 // A separate instantiation: the device step's corrector carries no branch for it (a run-time pointer
 // cost 2.3 % of the bcc 128^3 step).
-template <int NOISE, int INTEG, int PREC, bool HIGHER, bool ROWS = false>
-__global__ void __launch_bounds__(256, HIGHER ? 4 : kFxBlocks) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
-                                                       double* __restrict__ e, const double* __restrict__ noise,
-                                                       uint64_t step, long long begin, long long count,
-                                                       double* __restrict__ rows) {
+template <int NOISE, int INTEG, int PREC, bool HIGHER, int BLK, bool ROWS = false>
+__global__ void __launch_bounds__(256, BLK) k_correct_fx(const DevLattice L, const DevLLG P, const DevFX F,
+                                                         double* __restrict__ e, const double* __restrict__ noise,
+                                                         uint64_t step, long long begin, long long count,
+                                                         double* __restrict__ rows) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
     fx_correct_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
@@ -84,6 +84,21 @@ __global__ void __launch_bounds__(256) k_pack_split(const double* __restrict__ r
   }
 }
 
+template <int NOISE, int INTEG, int PREC, bool HIGHER, int BLK>
+static void launch_stages(const LLGPlan* pl, const DevFX& F, double* e, const double* noise, uint64_t step,
+                          int stages, cudaStream_t st, dim3 grid, int tpb, long long cb, long long count,
+                          double* rows) {
+  const DevLattice& L = pl->model->d;
+  if (stages & 1)
+    k_predict_fx<NOISE, INTEG, PREC, HIGHER, BLK><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
+  if ((stages & 2) && rows)
+    k_correct_fx<NOISE, INTEG, PREC, HIGHER, BLK, true><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count,
+                                                                              rows);
+  else if (stages & 2)
+    k_correct_fx<NOISE, INTEG, PREC, HIGHER, BLK><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count,
+                                                                        nullptr);
+}
+
 template <int NOISE, int INTEG, int PREC>
 static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_t step, int stages, cudaStream_t st,
                       long long cb, long long cn, double* rows) {
@@ -101,20 +116,17 @@ static void launch_fx(const LLGPlan* pl, double* e, const double* noise, uint64_
   const int tpb = site_block_size(whole ? L.N : cn * L.ns);
   const dim3 grid((unsigned)((count + tpb - 1) / tpb), whole ? 1u : (unsigned)L.ns);
   // cubic / higher-uniaxial terms (56-bit form only): a separate instantiation, so that the plain
-  // kernels keep their registers
-  constexpr bool H = PREC == MGX_PRECISION_FP64_FIXED_GATHER;
-  if (H && has_higher_onsite(L)) {
-    if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
-    if ((stages & 2) && rows)
-      k_correct_fx<NOISE, INTEG, PREC, H, true><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
-    else if (stages & 2)
-      k_correct_fx<NOISE, INTEG, PREC, H><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, nullptr);
+  // kernels keep their registers; five blocks per SM for the stencils with many couplings (BLK above,
+  // chosen from the plan's tables: the slabs of a host-buffer step run the device step's kernels)
+  if constexpr (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
+    if (has_higher_onsite(L))
+      launch_stages<NOISE, INTEG, PREC, true, 4>(pl, F, e, noise, step, stages, st, grid, tpb, cb, count, rows);
+    else if (pl->fx.hw_convert)
+      launch_stages<NOISE, INTEG, PREC, false, 5>(pl, F, e, noise, step, stages, st, grid, tpb, cb, count, rows);
+    else
+      launch_stages<NOISE, INTEG, PREC, false, 4>(pl, F, e, noise, step, stages, st, grid, tpb, cb, count, rows);
   } else {
-    if (stages & 1) k_predict_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count);
-    if ((stages & 2) && rows)
-      k_correct_fx<NOISE, INTEG, PREC, false, true><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, rows);
-    else if (stages & 2)
-      k_correct_fx<NOISE, INTEG, PREC, false><<<grid, tpb, 0, st>>>(L, pl->p, F, e, noise, step, cb, count, nullptr);
+    launch_stages<NOISE, INTEG, PREC, false, 4>(pl, F, e, noise, step, stages, st, grid, tpb, cb, count, rows);
   }
 }
 
