@@ -105,7 +105,9 @@ __device__ __forceinline__ void fx_rhs(const DevLattice& L, const DevLLG& P, con
 // the field of the Depondt integrator for both forms.  HIGHER (56-bit form only, a separate
 // instantiation) adds the cubic and higher-uniaxial fields at the site's FP64 spin (sx, sy, sz), in the
 // place the FP64 kernels add them: after the effective field, before the thermal field.
-template <int NOISE, int PREC, bool HIGHER = false, int HWC = 2>
+// NC (Philox noise of the 56-bit form): 1 draws the normals and stores them in F.nz, 2 reads them
+// back from F.nz (the corrector of the same step), 0 draws them.
+template <int NOISE, int PREC, bool HIGHER = false, int HWC = 2, int NC = 0>
 __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                            const int2* __restrict__ xs, const double* __restrict__ noise,
                                            long long q, int s, int c0, int c1, int c2, uint64_t step, double& bx,
@@ -125,13 +127,29 @@ __device__ __forceinline__ void fx_field64(const DevLattice& L, const DevLLG& P,
   by = h[1] + L.B1;
   bz = h[2] + L.B2;
   if (HIGHER) add_higher_onsite(L, q, s, sx, sy, sz, bx, by, bz);
-  add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz, PREC == MGX_PRECISION_FP64_FIXED_GATHER && fx_hw<HWC>(F));
+  if (NOISE == MGX_NOISE_PHILOX && NC != 0) {
+    const long long N = L.N;
+    float f0, f1, f2;
+    if (NC == 1) {
+      philox_normal3f(P.seed, magex_site(L, q, s), step, f0, f1, f2);
+      F.nz[q] = f0; F.nz[N + q] = f1; F.nz[2 * N + q] = f2;
+    } else {
+      f0 = F.nz[q]; f1 = F.nz[N + q]; f2 = F.nz[2 * N + q];
+    }
+    const bool hw = fx_hw<HWC>(F);
+    const double sig = P.sigma_site ? __ldg(P.sigma_site + q) : __ldg(P.sigma_sub + s);
+    bx = fma(sig, hw ? (double)f0 : f32_to_f64(f0), bx);
+    by = fma(sig, hw ? (double)f1 : f32_to_f64(f1), by);
+    bz = fma(sig, hw ? (double)f2 : f32_to_f64(f2), bz);
+  } else {
+    add_thermal<NOISE>(L, P, noise, q, s, step, bx, by, bz, PREC == MGX_PRECISION_FP64_FIXED_GATHER && fx_hw<HWC>(F));
+  }
 }
 
 // Predictor of site q (0 <= q < L.N) of the fixed-point forms: writes P.ep, P.k1 and the split F.eps at q.
 // HIGHER: the 56-bit form with the model's cubic / higher-uniaxial terms.  The adjoint's recomputation
 // (56-bit Heun form) also stores the total field (Hout) and the inverse norm of the predictor (rout).
-template <int NOISE, int INTEG, int PREC, bool HIGHER = false, int HWC = 2>
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false, int HWC = 2, bool NCACHE = false>
 __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 const double* __restrict__ e, const double* __restrict__ noise,
                                                 long long q, uint64_t step, double* __restrict__ Hout = nullptr,
@@ -154,7 +172,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
   if (INTEG == MGX_INTEGRATOR_HEUN) {
     if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
       double bx, by, bz;
-      fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
+      fx_field64<NOISE, PREC, HIGHER, HWC, NCACHE ? 1 : 0>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
       if (Hout) {
         Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
       }
@@ -171,7 +189,7 @@ __device__ __forceinline__ void fx_predict_site(const DevLattice& L, const DevLL
     x *= r; y *= r; z *= r;
   } else {
     double bx, by, bz;
-    fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
+    fx_field64<NOISE, PREC, HIGHER, HWC, NCACHE ? 1 : 0>(L, P, F, F.es, noise, q, s, c0, c1, c2, step, bx, by, bz, ex, ey, ez);
     double fx, fy, fz;
     llg_rhs(ex, ey, ez, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     f[0] = ey * fz - ez * fy; f[1] = ez * fx - ex * fz; f[2] = ex * fy - ey * fx;
@@ -195,7 +213,7 @@ __device__ __forceinline__ void store_site_row(const DevLattice& L, double* __re
 // (the new spins to eout instead of e when given; Hout and rout as in fx_predict_site).  With rows
 // (the last stage of a step on host buffers, stencil layout) the new spins go to the magex-order rows
 // `rows` only, and neither e nor its split is written.
-template <int NOISE, int INTEG, int PREC, bool HIGHER = false, int HWC = 2>
+template <int NOISE, int INTEG, int PREC, bool HIGHER = false, int HWC = 2, bool NCACHE = false>
 __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLLG& P, const DevFX& F,
                                                 double* __restrict__ e, const double* __restrict__ noise, long long q,
                                                 uint64_t step, double* __restrict__ Hout = nullptr,
@@ -223,7 +241,7 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
     if (PREC == MGX_PRECISION_FP64_FIXED_GATHER) {
       const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
       double bx, by, bz;
-      fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
+      fx_field64<NOISE, PREC, HIGHER, HWC, NCACHE ? 2 : 0>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
       if (Hout) {
         Hout[q] = bx; Hout[N + q] = by; Hout[2 * N + q] = bz;
       }
@@ -238,7 +256,7 @@ __device__ __forceinline__ void fx_correct_site(const DevLattice& L, const DevLL
   } else {
     const double px = P.ep[q], py = P.ep[N + q], pz = P.ep[2 * N + q];
     double bx, by, bz;
-    fx_field64<NOISE, PREC, HIGHER, HWC>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
+    fx_field64<NOISE, PREC, HIGHER, HWC, NCACHE ? 2 : 0>(L, P, F, F.eps, noise, q, s, c0, c1, c2, step, bx, by, bz, px, py, pz);
     double fx, fy, fz;
     llg_rhs(px, py, pz, bx, by, bz, __ldg(P.alpha_sub + s), __ldg(P.pre_sub + s), P.precession != 0, fx, fy, fz);
     const double wx = py * fz - pz * fy, wy = pz * fx - px * fz, wz = px * fy - py * fx;

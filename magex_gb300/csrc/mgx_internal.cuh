@@ -149,6 +149,9 @@ struct DevFX {
   // with every conversion on the hardware), and so it is with the cubic / higher-uniaxial terms.
   // Read at run time by the single-lattice kernels only (fx_hw<2>).
   int hw_convert;
+  // [3][N] the FP32 normal draws of the current step (Philox noise, the five-block single-lattice stage
+  // kernels): the predictor stores them and the corrector reads them back instead of drawing them again
+  float* nz;
   int2* es;                      // [3][N] fixed-point split of e
   int2* eps;                     // [3][N] fixed-point split of ep
 };
@@ -177,6 +180,7 @@ struct LLGPlan {
   void* df_block = nullptr;
   DevFX fx{};
   void* fx_block = nullptr;
+  float* fx_noise = nullptr;     // DevFX::nz of the 56-bit plans
   void* sub_block = nullptr;     // alpha_sub | pre_sub | sigma_sub
   double* site_block = nullptr;  // alpha_site | pre_site
   double* sigma_site = nullptr;
@@ -515,9 +519,9 @@ __device__ __forceinline__ long long double_to_ll_scaled(double x, int k) {
   return (u >> 63) ? -(long long)v : (long long)v;
 }
 
-// (hw: the FP32 draws widened by the hardware conversion instead of on the integer pipes; same values)
-__device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uint64_t step, double& g0, double& g1,
-                                               double& g2, bool hw = false) {
+// three standard normal FP32 draws of (seed, site, step): one Philox block, Box-Muller in FP32
+__device__ __forceinline__ void philox_normal3f(uint64_t seed, uint64_t site, uint64_t step, float& f0, float& f1,
+                                                float& f2) {
   const uint4 r = philox4x32_10(make_uint4((uint32_t)site, (uint32_t)(site >> 32), (uint32_t)step,
                                            (uint32_t)(step >> 32)),
                                 make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
@@ -529,7 +533,17 @@ __device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uin
   const float m3 = sqrtf(-2.0f * logf(u3));
   float s1, c1;
   sincospif(2.0f * v1, &s1, &c1);
-  const float f0 = m1 * c1, f1 = m1 * s1, f2 = m3 * cospif(2.0f * v3);
+  f0 = m1 * c1;
+  f1 = m1 * s1;
+  f2 = m3 * cospif(2.0f * v3);
+}
+
+// the same draws in FP64 (exact); hw: widened by the hardware conversion instead of on the integer
+// pipes (the same values)
+__device__ __forceinline__ void philox_normal3(uint64_t seed, uint64_t site, uint64_t step, double& g0, double& g1,
+                                               double& g2, bool hw = false) {
+  float f0, f1, f2;
+  philox_normal3f(seed, site, step, f0, f1, f2);
   g0 = hw ? (double)f0 : f32_to_f64(f0);
   g1 = hw ? (double)f1 : f32_to_f64(f1);
   g2 = hw ? (double)f2 : f32_to_f64(f2);

@@ -364,6 +364,7 @@ mgx_status mgx_llg_destroy(mgx_llg* pp) {
   cudaFree(pl->scratch);
   cudaFree(pl->df_block);
   cudaFree(pl->fx_block);
+  cudaFree(pl->fx_noise);
   drop_llg_graph(pl);
   if (pl->cap_stream) cudaStreamDestroy(pl->cap_stream);
   cudaFree(pl->d_step);

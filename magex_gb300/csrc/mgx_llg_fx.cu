@@ -33,6 +33,14 @@ __global__ void __launch_bounds__(256) k_fx_split(const double* __restrict__ x, 
 
 // Sites begin + i (i < count) of sublattice blockIdx.y: the whole lattice is one row of N sites
 // (gridDim.y = 1, begin = 0), a range of cells one row of `count` cells per sublattice.
+// Philox noise of the 56-bit form in the five-block kernels (the plans of many couplings per site): the
+// predictor stores its normal draws (DevFX::nz) and the corrector of the same step reads them back, 12 B
+// per site each way instead of a second Philox block and Box-Muller per site.  bcc 128^3: 1.047 ->
+// 1.029 ms per step; on the triangular film 2048^2 (FP64-bound, four blocks) it cost 6.8 %, so the
+// four-block kernels draw the normals in both stages.
+template <int NOISE, int PREC, int BLK>
+constexpr bool kNoiseCache = NOISE == MGX_NOISE_PHILOX && PREC == MGX_PRECISION_FP64_FIXED_GATHER && BLK == 5;
+
 // BLK: resident blocks per SM of the stage kernels.  5 (48 registers, ~100 B of spills per thread)
 // for stencils of at least 16 couplings per site without the higher on-site terms (the plans whose
 // conversions run on the hardware converters, DevFX::hw_convert), 4 (64 registers) otherwise.  Timed
@@ -45,8 +53,8 @@ __global__ void __launch_bounds__(256, BLK) k_predict_fx(const DevLattice L, con
                                                          uint64_t step, long long begin, long long count) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
-    fx_predict_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
-                                                P.step_base ? *P.step_base + step : step);
+    fx_predict_site<NOISE, INTEG, PREC, HIGHER, 2, kNoiseCache<NOISE, PREC, BLK>>(
+        L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i, P.step_base ? *P.step_base + step : step);
 }
 
 // ROWS (the slabs of a step on host buffers): the new spins go to the magex-order rows `rows` only.
@@ -59,9 +67,9 @@ __global__ void __launch_bounds__(256, BLK) k_correct_fx(const DevLattice L, con
                                                          double* __restrict__ rows) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count)
-    fx_correct_site<NOISE, INTEG, PREC, HIGHER>(L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i,
-                                                P.step_base ? *P.step_base + step : step, nullptr, nullptr,
-                                                nullptr, ROWS ? rows : nullptr);
+    fx_correct_site<NOISE, INTEG, PREC, HIGHER, 2, kNoiseCache<NOISE, PREC, BLK>>(
+        L, P, F, e, noise, (long long)blockIdx.y * L.ncell + begin + i, P.step_base ? *P.step_base + step : step,
+        nullptr, nullptr, nullptr, ROWS ? rows : nullptr);
 }
 
 // Magex-order rows [begin, begin + count) of an (N, 3) array -> lattice layout (3, N) and its fixed-point
@@ -206,6 +214,7 @@ mgx_status fx_build(const Model* m, int limb, bool field_scaled, int ncopies, De
   int zmax = 0;
   for (int s = 0; s < ns; ++s) zmax = std::max(zmax, off[s + 1] - off[s]);
   fx->hw_convert = zmax >= 16 && !has_higher_onsite(d) ? 1 : 0;
+  fx->nz = nullptr;
   if (nb > 0) {
     MGX_CUDA_TRY(cudaMemcpy(J.data(), d.bond_J, sizeof(double) * nb * W, cudaMemcpyDeviceToHost));
     MGX_CUDA_TRY(cudaMemcpy(geo.data(), d.bond_geo, sizeof(int4) * nb, cudaMemcpyDeviceToHost));
@@ -319,6 +328,11 @@ mgx_status build_fx_tables(LLGPlan* pl) {
   const int limb = pl->precision == MGX_PRECISION_FP64_FIXED_GATHER ? 28 : 24;
   const mgx_status st = fx_build(pl->model, limb, true, 2, &pl->fx, &pl->fx_block);
   if (st != MGX_OK) return st;
+  // the normal-draw cache of the five-block kernels (the plans whose stages run five blocks per SM)
+  if (limb == 28 && pl->fx.hw_convert && !has_higher_onsite(pl->model->d)) {
+    MGX_CUDA_TRY(cudaMalloc(&pl->fx_noise, sizeof(float) * 3 * (size_t)pl->model->d.N));
+    pl->fx.nz = pl->fx_noise;
+  }
   const int ns = pl->model->d.ns;
   std::vector<double> ap(2 * ns);
   MGX_CUDA_TRY(cudaMemcpy(ap.data(), pl->p.alpha_sub, sizeof(double) * ns, cudaMemcpyDeviceToHost));
