@@ -66,6 +66,25 @@ def test_reduced_full_size_bcc_against_fp64(cuda, precision):
     assert float((torch.linalg.vector_norm(out[1], dim=0) - 1).abs().max()) < 1e-14
 
 
+@pytest.mark.parametrize("integrator", ["heun", "depondt"])
+def test_fixed_point_philox_draws_read_back_match_fp64(cuda, integrator):
+    """bcc 48^3 (221,184 spins, 26 couplings: the plan runs its stages at five blocks per SM and its
+    corrector reads back the predictor's Philox draws), 300 K: 20 steps stay within 1e-12 per step of
+    the FP64 plan, which draws the normals in both stages, for both integrators."""
+    from magex_gb300.llg import GB300LLG
+    from magex_gb300.workloads import bcc_two_site
+    sc = bcc_two_site(L=48)
+    e0 = sc.init_spins("random", seed=6)
+    out = []
+    for prec in ("fp64", "fp64_fixed"):
+        sol = GB300LLG(sc, 0.05, 1e-4, 300.0, 91, integrator=integrator, precision=prec)
+        lat = sol.model.to_lattice(e0)
+        sol.run_lattice(lat, 20)
+        out.append(lat)
+    err = float((out[0] - out[1]).abs().max())
+    assert err <= 1e-12 * 20, err
+
+
 @pytest.mark.parametrize("precision", PRECISIONS)
 def test_reduced_refuses_unsupported_layouts(cuda, golden, golden_models, precision):
     from helpers import golden_irregular
