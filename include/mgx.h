@@ -210,11 +210,15 @@ mgx_status mgx_llg_stage(mgx_llg* plan, int32_t stage, double* e, const double* 
 /* One step of mgx_llg_step on host buffers: e_in and e_out are (N, 3) float64 spins in magex site
  * order (the arrays magex's LLGSolver.step takes and returns, magex/llg.py:216-227; e_out may equal
  * e_in).  Replaces the copy in, step and copy out that a Python caller would make, with the copies
- * overlapping the stages when both buffers are page-locked (pinned) and the plan is an FP64
- * stencil plan of at least 2^20 sites: the copies then run in axis-0 slabs on a copy stream of the
- * plan, and the slabs' stages alternate between `stream` and a second stream of the plan.  Work
- * enqueued on `stream` after this call, and a synchronisation of `stream`, follow all of it.  noise as for mgx_llg_step (device, lattice layout).  The plan keeps two device copies of
- * the spins for this (6 N doubles) from the first call on. */
+ * overlapping the stages when both buffers are page-locked (pinned) and the plan is an FP64 or
+ * fixed-point-sum stencil plan of at least 2^20 sites: the input then goes to the device in axis-0
+ * slabs on a copy stream of the plan, each slab is packed (and split) as it lands, the slabs'
+ * predictors and correctors run on streams of the plan as soon as the slabs they gather from are
+ * ready, and each finished slab goes back on an out stream while the rest is computed; the whole
+ * pipeline is replayed as a CUDA graph per (e_in, e_out) pair.  Work enqueued on `stream` after
+ * this call, and a synchronisation of `stream`, follow all of it.  noise as for mgx_llg_step
+ * (device, lattice layout).  The plan keeps two device copies of the spins for this (6 N doubles)
+ * from the first call on. */
 mgx_status mgx_llg_step_host(mgx_llg* plan, const double* e_in, double* e_out, const double* noise, uint64_t step,
                              void* stream);
 
